@@ -1,0 +1,158 @@
+/* pdgpu.h — C ABI of the GB300 nonbonded / Generalised-Born / LCPO path for PD.
+ *
+ * Plain C types only: pointers, sizes, doubles and ints.  The library owns all
+ * device memory of a context; host arrays passed in are borrowed for the
+ * duration of the call.  No function throws; every function returns a status
+ * (PDGPU_OK == 0, negative on error, see pdgpu_error_string()).
+ *
+ * Units are PD's WorkSpace units throughout: positions in Angstrom, energies in
+ * J per molecule, forces in N, velocities in m/s, masses in kg, per-atom LJ
+ * epsilon stored as sqrt(J) and LJ radius as Rmin/2 in Angstrom
+ * (PD src/mmlib/system/fundamentals.h:191-197).
+ *
+ * The reference interfaces each entry point replaces are cited beside it
+ * (paths inside the PD project).  A context is bound to one CUDA device and one
+ * stream and is not re-entrant; distinct contexts may be used concurrently.
+ */
+#ifndef PDGPU_H
+#define PDGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------- */
+#define PDGPU_OK 0
+#define PDGPU_ERR_ARG (-1)            /* invalid argument (PD: ProcedureException)          */
+#define PDGPU_ERR_CUDA (-2)           /* CUDA runtime error                                  */
+#define PDGPU_ERR_LIST_OVERFLOW (-3)  /* an LCPO overlap list exceeded its capacity          */
+#define PDGPU_ERR_FIXED_OVERFLOW (-4) /* a fixed-point accumulator left its range            */
+#define PDGPU_ERR_NAN (-5)            /* NaN energy or force (PD: assertStability)           */
+#define PDGPU_ERR_TIMEOUT (-6)        /* a device wait exceeded its iteration limit          */
+#define PDGPU_ERR_UNSUPPORTED (-7)    /* option not supported (e.g. GB in a periodic box)    */
+#define PDGPU_ERR_STALE_LIST (-8)     /* an atom moved more than Padding/2 since the rebuild */
+#define PDGPU_ERR_STATE (-9)          /* call sequence error (e.g. compute before positions) */
+
+/* ---- what to compute ------------------------------------------------------ */
+#define PDGPU_NB 1u      /* FF_NonBonded: LJ + Coulomb with PD's switching     */
+#define PDGPU_GB 2u      /* FF_GeneralizedBorn_Still, FastMode (incl. vacuum LJ/Coulomb) */
+#define PDGPU_SA 4u      /* FF_SASA_LCPO                                        */
+#define PDGPU_BONDED 8u  /* FF_Bonded: bonds, angles, torsions, impropers       */
+
+/* Per-system energies in J per molecule; the fields mirror PD's Hamiltonian
+ * (src/mmlib/workspace/hamiltonian.h:43-66). */
+typedef struct {
+    double epot, vdw, elec, pol, pol_self, pol_cross, surf, virial;
+    double bond, angle, torsion, improper;
+} pdgpu_energies;
+
+/* Static description of one or more independent systems (a batch).  All
+ * per-atom arrays are concatenated over systems in system order; index arrays
+ * use these global atom indices.  Optional arrays may be NULL. */
+typedef struct {
+    int nsystems;
+    const int *natoms;           /* [nsystems] */
+    const double *box;           /* [nsystems*3]; all zero => infinite space */
+    const double *charge;        /* [N] e */
+    const double *radius;        /* [N] LJ Rmin/2, Angstrom */
+    const double *epsilon;       /* [N] sqrt(eps [J]) */
+    const double *mass;          /* [N] kg (needed only for dynamics) */
+    /* Still GB (optional): raw type radius, Vj, terms123 as set up by
+     * FF_GeneralizedBorn_Still::calcFixedBornRadiiTerms (gbff.cpp:324-398) */
+    const double *gb_radius, *gb_vj, *gb_terms123;
+    /* LCPO (optional): radius (+1.4 probe), P1..P4 [N*4], sigma (J/A^2), use flag */
+    const double *lcpo_radius, *lcpo_p, *lcpo_sigma;
+    const int *lcpo_use;
+    /* bonded pairs as PD's neighbour list classifies them: (i, j, bondorder),
+     * bondorder 0..3 (1-2 = 1, 1-3 = 2, 1-4 = 3); pairs not listed are ordinary */
+    int nexcl;
+    const int *excl;
+    /* FF_Bonded terms (optional), PD units: bond (i,j)+(l,k); angle (i,a,j)+(theta0,k);
+     * torsion/improper (i,a,b,j,terms)+(Vn,n,gamma)x4 */
+    int nbond;  const int *bond_idx;  const double *bond_par;
+    int nangle; const int *angle_idx; const double *angle_par;
+    int ntors;  const int *tors_idx;  const double *tors_par;
+    int nimpr;  const int *impr_idx;  const double *impr_par;
+} pdgpu_system_desc;
+
+/* FF_NonBonded public parameters (src/mmlib/forcefields/nonbonded.h:62-231). */
+typedef struct {
+    double Cutoff, InnerCutoff, VdwCutoff, VdwInnerCutoff;
+    double Vdw14Scaling, Elec14Scaling, Dielectric;
+    int EnergySwitch, ForceSwitch, DoVdw, DoElec;
+} pdgpu_nb_params;
+
+/* FF_GeneralizedBorn_Still public parameters (src/mmlib/forcefields/gbff.h:123-203). */
+typedef struct {
+    double Cutoff, InnerCutoff, VdwCutoff, VdwInnerCutoff;
+    double Vdw14Scaling, Elec14Scaling;
+    double DielectricSolute, DielectricSolvent, GbsaStillCutoff, ExpApproxThreshold, BornRadiusOffset;
+    double P4, P5;
+} pdgpu_gb_params;
+
+/* NeighbourList settings (src/mmlib/workspace/neighbourlist.h:54-126). */
+typedef struct {
+    double Padding;      /* list skin, Angstrom (PD default 0.5) */
+    int check_skin;      /* 1: flag PDGPU_ERR_STALE_LIST when an atom moved > Padding/2 */
+} pdgpu_list_params;
+
+typedef struct pdgpu_ctx pdgpu_ctx;
+
+/* ---- life cycle ----------------------------------------------------------- */
+/* Replaces the setup() of FF_NonBonded / FF_GeneralizedBorn_Still / FF_SASA_LCPO
+ * (nonbonded.cpp:1025-1053, gbff.cpp:57-104, lcpo.cpp:33-127): copies every
+ * parameter to the device.  Returns NULL and sets *status on failure. */
+pdgpu_ctx *pdgpu_create(int device, const pdgpu_system_desc *desc, int *status);
+int pdgpu_destroy(pdgpu_ctx *ctx);
+const char *pdgpu_error_string(int status);
+
+int pdgpu_set_nb_params(pdgpu_ctx *ctx, const pdgpu_nb_params *p);
+int pdgpu_set_gb_params(pdgpu_ctx *ctx, const pdgpu_gb_params *p);
+int pdgpu_set_list_params(pdgpu_ctx *ctx, const pdgpu_list_params *p);
+/* Per-atom charges / LJ radius / sqrt(eps) / GB Vj, terms123 (all optional, NULL keeps) —
+ * the parameter update after FF re-setup. */
+int pdgpu_update_params(pdgpu_ctx *ctx, const double *charge, const double *radius, const double *epsilon,
+                        const double *gb_vj, const double *gb_terms123);
+
+/* ---- state ---------------------------------------------------------------- */
+/* Upload positions (Angstrom).  stride_bytes is the distance between atoms;
+ * 24 for packed xyz, 72 for PD's SnapShotAtom {p, f, v} (snapshot.h:33-39). */
+int pdgpu_set_positions(pdgpu_ctx *ctx, const double *xyz, size_t stride_bytes);
+/* Same from device memory already on this context's device (packed xyz). */
+int pdgpu_set_positions_device(pdgpu_ctx *ctx, const double *d_xyz);
+int pdgpu_get_positions(pdgpu_ctx *ctx, double *xyz, size_t stride_bytes);
+
+/* ---- neighbour list ------------------------------------------------------- */
+/* Replaces NeighbourList::calcNewList (neighbourlist.cpp:222-439): cell-grid
+ * sort, block bounding boxes and the tile list at radius max(cutoffs)+Padding. */
+int pdgpu_rebuild_list(pdgpu_ctx *ctx);
+
+/* ---- evaluation ----------------------------------------------------------- */
+/* Replaces ForcefieldBase::calcForces of the selected components
+ * (nonbonded.cpp:1222-1246, gbff.cpp:185-197, lcpo.cpp:193-206).  Energies for
+ * each system are written to out[0..nsystems) (may be NULL).  Forces in N are
+ * ADDED into f (may be NULL) at stride_bytes per atom, as PD components add
+ * into WorkSpace::cur.atom[i].f. */
+int pdgpu_compute(pdgpu_ctx *ctx, unsigned what, pdgpu_energies *out, double *f, size_t stride_bytes);
+/* Device variant: forces in N written (not added) to d_f (packed xyz, device
+ * memory) without any host synchronisation; energies stay on the device until
+ * pdgpu_get_energies(). */
+int pdgpu_compute_device(pdgpu_ctx *ctx, unsigned what, double *d_f);
+int pdgpu_get_energies(pdgpu_ctx *ctx, pdgpu_energies *out);
+/* Born radii (Angstrom, original atom order) and LCPO per-atom SASA (A^2) from
+ * the last evaluation that computed them. */
+int pdgpu_get_born_radii(pdgpu_ctx *ctx, double *born);
+int pdgpu_get_sasa(pdgpu_ctx *ctx, double *sasa);
+
+/* ---- diagnostics ---------------------------------------------------------- */
+/* Tile / pair counts of the current list: ntiles, nmasked tiles, slots. */
+int pdgpu_list_stats(pdgpu_ctx *ctx, long long *ntiles, long long *nmasked, long long *nslots);
+/* Stream the context launches on (cudaStream_t as void*), for event timing. */
+void *pdgpu_stream(pdgpu_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PDGPU_H */

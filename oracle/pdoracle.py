@@ -59,7 +59,13 @@ def lib():
     if _lib is None:
         if not os.path.exists(LIB_PATH):
             build()
-        L = ctypes.CDLL(LIB_PATH)
+        try:
+            L = ctypes.CDLL(LIB_PATH)
+        except OSError:
+            # built for another CPU architecture: rebuild from source here
+            os.remove(LIB_PATH)
+            build()
+            L = ctypes.CDLL(LIB_PATH)
         L.pdo_nonbonded.argtypes = [ctypes.POINTER(System), ctypes.POINTER(NBParams), ctypes.c_int,
                                     ctypes.POINTER(Energies), _dp]
         L.pdo_list_checksums.argtypes = [ctypes.POINTER(System), ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,

@@ -1,0 +1,413 @@
+// k_list.cu — cell-grid sort, blocks, tile list, exclusion masks and the
+// per-evaluation position pack.  Replaces NeighbourList::calcNewList
+// (PD src/mmlib/workspace/neighbourlist.cpp:222-439): PD scans all j < i at
+// minimum image; here atoms are binned on a 32^3 grid ordered along a Hilbert
+// curve, grouped into 32-atom blocks, and block pairs whose bounding boxes come
+// within max(cutoffs)+Padding form the tile list.  The bond order PD packs into
+// each list entry (neighbourlist.cpp:398-422, 179-220) becomes a per-tile
+// exclusion / 1-4 bit mask.
+#include <cstdio>
+
+#include "pdgpu_context.cuh"
+
+namespace pdgpu {
+
+// ---------------------------------------------------------------------------
+// 3-D Hilbert index of a cell (J. Skilling, "Programming the Hilbert curve",
+// AIP Conf. Proc. 707, 2004: axes -> transposed form, then bit interleave).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int hilbert3(unsigned x0, unsigned x1, unsigned x2) {
+  unsigned X[3] = {x0, x1, x2};
+  const unsigned M = 1u << (kHilbertBits - 1);
+  for (unsigned Q = M; Q > 1; Q >>= 1) {
+    unsigned P = Q - 1;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      if (X[i] & Q) {
+        X[0] ^= P;
+      } else {
+        unsigned t = (X[0] ^ X[i]) & P;
+        X[0] ^= t;
+        X[i] ^= t;
+      }
+    }
+  }
+  X[1] ^= X[0];
+  X[2] ^= X[1];
+  unsigned t = 0;
+  for (unsigned Q = M; Q > 1; Q >>= 1)
+    if (X[2] & Q) t ^= Q - 1;
+  X[0] ^= t; X[1] ^= t; X[2] ^= t;
+  int h = 0;
+  for (int b = kHilbertBits - 1; b >= 0; b--) {
+    h = (h << 3) | (((X[0] >> b) & 1) << 2) | (((X[1] >> b) & 1) << 1) | ((X[2] >> b) & 1);
+  }
+  return h;
+}
+
+// order-preserving float <-> int for atomic min / max
+__device__ __forceinline__ int f2ord(float f) {
+  int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+__global__ void k_bbox_init(int* lo, int* hi, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    lo[i] = f2ord(3.0e38f);
+    hi[i] = f2ord(-3.0e38f);
+  }
+}
+
+__global__ void k_bbox(DevView v, const int* atom_sys, int* lo, int* hi) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= v.natom) return;
+  int s = atom_sys[a];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    float x = (float)v.pos[3 * a + c];
+    atomicMin(&lo[3 * s + c], f2ord(x));
+    atomicMax(&hi[3 * s + c], f2ord(x));
+  }
+}
+
+__device__ __forceinline__ double wrap_coord(double x, double L) { return x - L * floor(x / L); }
+
+__global__ void k_keys(DevView v, const int* atom_sys, const int* lo, const int* hi, int* bucket, int* count) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= v.natom) return;
+  int s = atom_sys[a];
+  const SystemInfo& S = v.sys[s];
+  unsigned q[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    double x = v.pos[3 * a + c];
+    double f;
+    if (S.periodic) {
+      f = wrap_coord(x, S.box[c]) / S.box[c];
+    } else {
+      double l = ord2f(lo[3 * s + c]), h = ord2f(hi[3 * s + c]);
+      f = (x - l) / (h - l + 1e-3);
+    }
+    int qi = (int)(f * (1 << kHilbertBits));
+    qi = qi < 0 ? 0 : (qi > (1 << kHilbertBits) - 1 ? (1 << kHilbertBits) - 1 : qi);
+    q[c] = (unsigned)qi;
+  }
+  int b = s * kCellsPerSystem + hilbert3(q[0], q[1], q[2]);
+  bucket[a] = b;
+  atomicAdd(&count[b], 1);
+}
+
+// --- exclusive scan (three-phase, 1024 elements per block) -----------------
+__global__ void k_scan_block(const int* in, int* out, int* block_sums, int n) {
+  __shared__ int sh[1024];
+  int tid = threadIdx.x;
+  int i = blockIdx.x * 1024 + tid;
+  int x = i < n ? in[i] : 0;
+  sh[tid] = x;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    int y = tid >= o ? sh[tid - o] : 0;
+    __syncthreads();
+    sh[tid] += y;
+    __syncthreads();
+  }
+  if (i < n) out[i] = sh[tid] - x;
+  if (tid == 1023) block_sums[blockIdx.x] = sh[1023];
+}
+
+__global__ void k_scan_sums(int* sums, int nb) {
+  // single block: sequential chunks, inclusive -> exclusive
+  __shared__ int sh[1024];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += 1024) {
+    int i = base + threadIdx.x;
+    int x = i < nb ? sums[i] : 0;
+    sh[threadIdx.x] = x;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      int y = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+      __syncthreads();
+      sh[threadIdx.x] += y;
+      __syncthreads();
+    }
+    if (i < nb) sums[i] = sh[threadIdx.x] - x + carry;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += sh[1023];
+    __syncthreads();
+  }
+}
+
+__global__ void k_scan_add(int* out, const int* sums, int n) {
+  int i = blockIdx.x * 1024 + threadIdx.x;
+  if (i < n) out[i] += sums[blockIdx.x];
+}
+
+__global__ void k_scatter(int natom, const int* bucket, const int* offset, int* cursor, int* tmp) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= natom) return;
+  int b = bucket[a];
+  tmp[offset[b] + atomicAdd(&cursor[b], 1)] = a;
+}
+
+// insertion sort inside each non-empty cell so the order is deterministic
+__global__ void k_cell_sort(int ncells, const int* offset, const int* count, int* tmp) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= ncells) return;
+  int n = count[b];
+  if (n < 2) return;
+  int* p = tmp + offset[b];
+  for (int i = 1; i < n; i++) {
+    int x = p[i];
+    int j = i - 1;
+    while (j >= 0 && p[j] > x) {
+      p[j + 1] = p[j];
+      j--;
+    }
+    p[j + 1] = x;
+  }
+}
+
+__global__ void k_to_slots(DevView v, const int* atom_sys, const int* tmp, int* sorted_atom, int* slot_of) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= v.natom) return;
+  int a = tmp[k];
+  int s = atom_sys[a];
+  const SystemInfo& S = v.sys[s];
+  int slot = S.pad_start + (k - S.atom_start);
+  sorted_atom[slot] = a;
+  slot_of[a] = slot;
+}
+
+// block bounding boxes; one warp per block
+__global__ void k_blocks(DevView v) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= v.nblocks) return;
+  int slot = warp * 32 + lane;
+  int a = v.sorted_atom[slot];
+  const SystemInfo& S = v.sys[v.slot_sys[warp]];
+  double lo[3], hi[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    double x = 0;
+    if (a >= 0) {
+      x = v.pos[3 * a + c];
+      if (S.periodic) x = wrap_coord(x, S.box[c]);
+    }
+    lo[c] = a >= 0 ? x : 1e300;
+    hi[c] = a >= 0 ? x : -1e300;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[c] = fmin(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+      hi[c] = fmax(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+    }
+  }
+  if (lane == 0) {
+    float4 h;
+    for (int c = 0; c < 3; c++) v.center[3 * warp + c] = 0.5 * (lo[c] + hi[c]);
+    h.x = (float)(0.5 * (hi[0] - lo[0])) + 1e-4f;
+    h.y = (float)(0.5 * (hi[1] - lo[1])) + 1e-4f;
+    h.z = (float)(0.5 * (hi[2] - lo[2])) + 1e-4f;
+    h.w = 0.f;
+    v.half[warp] = h;
+  }
+}
+
+// static per-slot parameters (LJ radius, sqrt eps, GB radius, Vj)
+__global__ void k_slot_params(DevView v, const double* radius, const double* sqeps, const double* gbR,
+                              const double* gbVj, const double* lcR, const int* lcUse, float4* lc_par) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= v.nslots) return;
+  int a = v.sorted_atom[s];
+  float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 l = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (a >= 0) {
+    p.x = (float)radius[a];
+    p.y = (float)sqeps[a];
+    if (gbR) {
+      p.z = (float)gbR[a];
+      p.w = (float)gbVj[a];
+    }
+    if (lcR) {
+      l.x = (float)lcR[a];
+      l.y = lcUse[a] ? 1.f : 0.f;
+    }
+  }
+  v.par[s] = p;
+  if (lc_par) lc_par[s] = l;
+}
+
+// candidate block pairs -> tiles
+__global__ void k_tiles(DevView v, long long ncand, float R, float margin) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncand) return;
+  // system by binary search over cand_start
+  int lo = 0, hi = v.nsys - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (v.sys[mid].cand_start <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  const SystemInfo& S = v.sys[lo];
+  long long l = t - S.cand_start;
+  long long nb = S.nblocks;
+  // row bi starts at bi*nb - bi*(bi-1)/2 and holds nb-bi entries
+  double fb = (2.0 * nb + 1.0 - sqrt((2.0 * nb + 1.0) * (2.0 * nb + 1.0) - 8.0 * (double)l)) * 0.5;
+  long long bi = (long long)fb;
+  if (bi < 0) bi = 0;
+  if (bi > nb - 1) bi = nb - 1;
+  while (bi > 0 && bi * nb - bi * (bi - 1) / 2 > l) bi--;
+  while (bi + 1 < nb && (bi + 1) * nb - (bi + 1) * bi / 2 <= l) bi++;
+  long long bj = bi + (l - (bi * nb - bi * (bi - 1) / 2));
+  int gi = S.block_start + (int)bi, gj = S.block_start + (int)bj;
+  float4 hi4 = v.half[gi], hj4 = v.half[gj];
+  float hs[3] = {hi4.x + hj4.x, hi4.y + hj4.y, hi4.z + hj4.z};
+  double dist2 = 0;
+  bool need_mi = false;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    double d = v.center[3 * gj + c] - v.center[3 * gi + c];
+    if (S.periodic) {
+      d -= S.box[c] * rint(d / S.box[c]);
+      if (fabs(d) + hs[c] + margin >= 0.5 * S.box[c]) need_mi = true;
+    }
+    double g = fabs(d) - hs[c];
+    if (g > 0) dist2 += g * g;
+  }
+  if (dist2 > (double)R * R) return;
+  int idx = atomicAdd(v.ntiles, 1);
+  Tile T;
+  T.bi = gi;
+  T.bj = gj;
+  T.mask = -1;
+  T.flags = (need_mi ? 1 : 0) | (gi == gj ? 2 : 0);
+  v.tiles[idx] = T;
+}
+
+// bond order of an atom pair as PD's list stores it; 7 when not bonded
+__device__ __forceinline__ int pair_bondorder(const DevView& v, int a, int b) {
+  int lo = a < b ? a : b, hi = a < b ? b : a;
+  int d = hi - lo;
+  if (d == 0) return 0;
+  if (d <= kBandWidth) {
+    unsigned long long bit = 1ull << (d - 1);
+    if (v.band_excl[lo] & bit) return 2;  // 1-1/1-2/1-3: all treated alike (excluded)
+    if (v.band_14[lo] & bit) return 3;
+    return 7;
+  }
+  int best = 7;
+  for (int k = v.far_start[lo]; k < v.far_start[lo + 1]; k++)
+    if (v.far_idx[k] == hi && v.far_bo[k] < best) best = v.far_bo[k];
+  return best;
+}
+
+// exclusion masks in rotation order (bit k <-> j slot (lane+k)&31); one warp per tile
+__global__ void k_masks(DevView v) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  int nt = *v.ntiles;
+  if (warp >= nt) return;
+  Tile T = v.tiles[warp];
+  int ai = v.sorted_atom[T.bi * 32 + lane];
+  int aj0 = v.sorted_atom[T.bj * 32 + lane];
+  bool diag = T.flags & 2;
+  unsigned ex = 0, m14 = 0;
+  for (int k = 0; k < 32; k++) {
+    int aj = __shfl_sync(0xffffffffu, aj0, (lane + k) & 31);
+    if (ai < 0 || aj < 0 || (diag && k == 0)) {
+      ex |= 1u << k;
+      continue;
+    }
+    int bo = pair_bondorder(v, ai, aj);
+    if (bo <= 2) ex |= 1u << k;
+    else if (bo == 3) m14 |= 1u << k;
+  }
+  bool any = __any_sync(0xffffffffu, (ex | m14) != 0);
+  if (!any) return;
+  int idx = 0;
+  if (lane == 0) idx = atomicAdd(v.nmasks, 1);
+  idx = __shfl_sync(0xffffffffu, idx, 0);
+  v.masks[idx * 32 + lane] = make_uint2(ex, m14);
+  if (lane == 0) v.tiles[warp].mask = idx;
+}
+
+// per-evaluation pack: FP64 positions -> float offsets from the block centre
+__global__ void k_pack(DevView v, const double* charge, float check2, int store_ref) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= v.nslots) return;
+  int a = v.sorted_atom[s];
+  int b = s >> 5;
+  float4 o;
+  if (a < 0) {
+    // padding slot: zero parameters, parked far away from everything and each other
+    o = make_float4(1.0e6f * (float)(1 + (s & 31)), 1.0e6f * (float)(1 + (s >> 5)), -1.0e6f, 0.f);
+  } else {
+    const SystemInfo& S = v.sys[v.slot_sys[b]];
+    double r[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      double d = v.pos[3 * a + c] - v.center[3 * b + c];
+      if (S.periodic) d -= S.box[c] * rint(d / S.box[c]);
+      r[c] = d;
+    }
+    o = make_float4((float)r[0], (float)r[1], (float)r[2], (float)charge[a]);
+    if (store_ref) {
+      v.rel0[s] = o;
+    } else if (check2 > 0.f) {
+      float4 q = v.rel0[s];
+      float dx = o.x - q.x, dy = o.y - q.y, dz = o.z - q.z;
+      if (dx * dx + dy * dy + dz * dz > check2) atomicOr(v.status, (unsigned)ST_STALE_LIST);
+    }
+  }
+  v.xq[s] = o;
+}
+
+static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+int launch_list_build(Context& c, float list_radius) {
+  DevView v = c.view();
+  cudaStream_t st = c.stream;
+  int ncells = c.nsys * kCellsPerSystem;
+  int* lo = reinterpret_cast<int*>(c.d_sys_lo.p);
+  int* hi = reinterpret_cast<int*>(c.d_sys_hi.p);
+  k_bbox_init<<<nblk(3 * c.nsys, 128), 128, 0, st>>>(lo, hi, 3 * c.nsys);
+  k_bbox<<<nblk(c.natom, 256), 256, 0, st>>>(v, c.d_atom_sys.p, lo, hi);
+  cudaMemsetAsync(c.d_count.p, 0, sizeof(int) * ncells, st);
+  cudaMemsetAsync(c.d_cursor.p, 0, sizeof(int) * ncells, st);
+  k_keys<<<nblk(c.natom, 256), 256, 0, st>>>(v, c.d_atom_sys.p, lo, hi, c.d_bucket.p, c.d_count.p);
+  int nsb = nblk(ncells, 1024);
+  k_scan_block<<<nsb, 1024, 0, st>>>(c.d_count.p, c.d_offset.p, c.d_scan_tmp.p, ncells);
+  k_scan_sums<<<1, 1024, 0, st>>>(c.d_scan_tmp.p, nsb);
+  k_scan_add<<<nsb, 1024, 0, st>>>(c.d_offset.p, c.d_scan_tmp.p, ncells);
+  k_scatter<<<nblk(c.natom, 256), 256, 0, st>>>(c.natom, c.d_bucket.p, c.d_offset.p, c.d_cursor.p,
+                                                 c.d_tmp_sorted.p);
+  k_cell_sort<<<nblk(ncells, 256), 256, 0, st>>>(ncells, c.d_offset.p, c.d_count.p, c.d_tmp_sorted.p);
+  cudaMemsetAsync(c.d_sorted_atom.p, 0xff, sizeof(int) * c.nslots, st);
+  k_to_slots<<<nblk(c.natom, 256), 256, 0, st>>>(v, c.d_atom_sys.p, c.d_tmp_sorted.p, c.d_sorted_atom.p,
+                                                  c.d_slot_of.p);
+  k_blocks<<<nblk((long long)c.nblocks * 32, 256), 256, 0, st>>>(v);
+  k_slot_params<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_radius.p, c.d_sqeps.p, c.has_gb ? c.d_gbR.p : nullptr,
+                                                      c.has_gb ? c.d_gbVj.p : nullptr,
+                                                      c.has_sa ? c.d_lcpoR.p : nullptr,
+                                                      c.has_sa ? c.d_lcpoUse.p : nullptr,
+                                                      c.has_sa ? c.d_lc_par.p : nullptr);
+  cudaMemsetAsync(c.d_counters.p, 0, sizeof(int) * 2, st);
+  k_tiles<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, list_radius, (float)c.lp.Padding);
+  // masks: launched over the worst case; warps beyond *ntiles return at once
+  k_masks<<<nblk(c.ncand * 32, 256), 256, 0, st>>>(v);
+  k_pack<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_charge.p, 0.f, 1);
+  return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
+}
+
+int launch_pack(Context& c, float check_disp) {
+  DevView v = c.view();
+  float c2 = check_disp > 0 ? check_disp * check_disp : 0.f;
+  k_pack<<<nblk(c.nslots, 256), 256, 0, c.stream>>>(v, c.d_charge.p, c2, 0);
+  return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
+}
+
+}  // namespace pdgpu

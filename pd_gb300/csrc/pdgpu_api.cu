@@ -1,0 +1,602 @@
+// pdgpu_api.cu — the C ABI declared in include/pdgpu.h.
+//
+// Host orchestration only: validation, parameter conversion to the internal
+// units (kcal/mol, Angstrom), buffer management and the launch sequence of one
+// evaluation.  No function throws; errors come back as status codes.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "pdgpu_context.cuh"
+
+using namespace pdgpu;
+
+struct pdgpu_ctx {
+  Context c;
+};
+
+namespace {
+
+int cuda_status(cudaError_t e, Context* c = nullptr, const char* what = "") {
+  if (e == cudaSuccess) return PDGPU_OK;
+  if (c) {
+    c->last_error = PDGPU_ERR_CUDA;
+    c->last_msg = std::string(what) + ": " + cudaGetErrorString(e);
+  }
+  return PDGPU_ERR_CUDA;
+}
+
+#define CK(expr)                                              \
+  do {                                                        \
+    cudaError_t _e = (expr);                                  \
+    if (_e != cudaSuccess) return cuda_status(_e, &c, #expr); \
+  } while (0)
+
+template <typename T>
+cudaError_t upload(DBuf<T>& b, const T* h, size_t n) {
+  cudaError_t e = b.alloc(n);
+  if (e != cudaSuccess || n == 0) return e;
+  return cudaMemcpy(b.p, h, n * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+double list_radius(const Context& c) {
+  double r = 0;
+  if (c.nb_set) r = std::max(r, std::max(c.nb.Cutoff, c.nb.VdwCutoff));
+  if (c.gb_set) r = std::max(r, std::max(c.gb.Cutoff, c.gb.VdwCutoff));
+  if (c.has_sa) r = std::max(r, 7.0);  // FF_SASA_LCPO::setup requests 7 A (lcpo.cpp:37)
+  return r + c.lp.Padding;
+}
+
+int read_status(Context& c) {
+  unsigned st = 0;
+  cudaError_t e = cudaMemcpyAsync(&st, c.d_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  if (e != cudaSuccess) return cuda_status(e, &c, "status");
+  if (st & ST_NAN) return PDGPU_ERR_NAN;
+  if (st & ST_FIXED_OVERFLOW) return PDGPU_ERR_FIXED_OVERFLOW;
+  if (st & ST_LCPO_OVERFLOW) return PDGPU_ERR_LIST_OVERFLOW;
+  if (st & ST_STALE_LIST) return PDGPU_ERR_STALE_LIST;
+  return PDGPU_OK;
+}
+
+NBConst make_nb_const(const pdgpu_nb_params& p) {
+  NBConst k{};
+  double C = p.Cutoff, I = p.InnerCutoff;
+  k.cut2 = (float)(C * C);
+  k.vdwcut = (float)p.VdwCutoff;
+  k.vdwinner = (float)p.VdwInnerCutoff;
+  k.inner = (float)I;
+  double vw = p.VdwCutoff - p.VdwInnerCutoff, w = C - I;
+  k.vdwinvw2 = vw > 0 ? (float)(1.0 / (vw * vw)) : 0.f;
+  k.invw2 = w > 0 ? (float)(1.0 / (w * w)) : 0.f;
+  k.econv_diel = (float)(econv_kcal() / p.Dielectric);
+  k.vdw14 = (float)p.Vdw14Scaling;
+  k.elec14 = (float)p.Elec14Scaling;
+  // Steinbach-Brooks force-switch constants (nonbonded.cpp:620-636)
+  double C2 = C * C, I2 = I * I;
+  double sA = 1.0 / ((C2 - I2) * (C2 - I2) * (C2 - I2));
+  double sB = -(C2 * C2 * C2 - 3.0 * C2 * C2 * I2);
+  double sC = 6.0 * C2 * I2, sD = -(C2 + I2), sE = 2.0 / 5.0;
+  double innerV = sA * (sB / I + sC * I + sD * I * I * I + sE * I * I * I * I * I);
+  double cutV = sA * (sB / C + sC * C + sD * C * C * C + sE * C * C * C * C * C);
+  k.sA = (float)sA; k.sB = (float)sB; k.sC = (float)sC; k.sD = (float)sD; k.sE = (float)sE;
+  k.fsw_cutV = (float)cutV;
+  k.eshift = (float)(I < C ? 1.0 / I + (innerV - cutV) : 0.0);
+  k.cut2_d = (float)C2;
+  k.inner2 = (float)I2;
+  k.elecmode = 1;
+  if (p.EnergySwitch) k.elecmode = 3;
+  if (p.ForceSwitch) k.elecmode = 4;
+  if (!p.DoElec) k.elecmode = 0;
+  k.dovdw = p.DoVdw ? 1 : 0;
+  return k;
+}
+
+GBConst make_gb_const(const pdgpu_gb_params& p, double listR) {
+  GBConst k{};
+  double C = p.Cutoff, I = p.InnerCutoff;
+  k.cut2 = (float)(C * C);
+  k.inner = (float)I;
+  double w = C - I, vw = p.VdwCutoff - p.VdwInnerCutoff;
+  k.invw2 = w > 0 ? (float)(1.0 / (w * w)) : 0.f;
+  k.vdwcut = (float)p.VdwCutoff;
+  k.vdwinner = (float)p.VdwInnerCutoff;
+  k.vdwinvw2 = vw > 0 ? (float)(1.0 / (vw * vw)) : 0.f;
+  double still = std::min(p.GbsaStillCutoff, listR);
+  k.still2 = (float)(still * still);
+  double ec = econv_kcal();
+  k.econv_in = (float)(ec / p.DielectricSolute);
+  k.econv_out = (float)(ec / p.DielectricSolvent);
+  k.premul = (float)(-0.5 * ec * (1.0 / p.DielectricSolute - 1.0 / p.DielectricSolvent));
+  k.vdw14 = (float)p.Vdw14Scaling;
+  k.elec14 = (float)p.Elec14Scaling;
+  k.thresh = (float)p.ExpApproxThreshold;
+  k.P4 = (float)p.P4;
+  k.P5 = (float)p.P5;
+  k.invP5 = (float)(1.0 / p.P5);
+  return k;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pdgpu_error_string(int status) {
+  switch (status) {
+    case PDGPU_OK: return "ok";
+    case PDGPU_ERR_ARG: return "invalid argument";
+    case PDGPU_ERR_CUDA: return "CUDA runtime error";
+    case PDGPU_ERR_LIST_OVERFLOW: return "LCPO overlap list overflow";
+    case PDGPU_ERR_FIXED_OVERFLOW: return "fixed-point accumulator overflow";
+    case PDGPU_ERR_NAN: return "NaN energy or force";
+    case PDGPU_ERR_TIMEOUT: return "device wait timed out";
+    case PDGPU_ERR_UNSUPPORTED: return "unsupported option";
+    case PDGPU_ERR_STALE_LIST: return "an atom moved more than Padding/2 since the list was built";
+    case PDGPU_ERR_STATE: return "call sequence error";
+    default: return "unknown status";
+  }
+}
+
+pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
+  auto fail = [&](int st) -> pdgpu_ctx* {
+    if (status) *status = st;
+    return nullptr;
+  };
+  if (!d || d->nsystems < 1 || !d->natoms || !d->box || !d->charge || !d->radius || !d->epsilon)
+    return fail(PDGPU_ERR_ARG);
+  if (cudaSetDevice(device) != cudaSuccess) return fail(PDGPU_ERR_CUDA);
+  pdgpu_ctx* h = new (std::nothrow) pdgpu_ctx();
+  if (!h) return fail(PDGPU_ERR_ARG);
+  Context& c = h->c;
+  c.device = device;
+  auto bad = [&](int st) -> pdgpu_ctx* {
+    delete h;
+    return fail(st);
+  };
+  if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) return bad(PDGPU_ERR_CUDA);
+
+  // systems and padded layout
+  c.nsys = d->nsystems;
+  int atom = 0, slot = 0, block = 0;
+  long long cand = 0;
+  c.any_periodic = false;
+  c.all_periodic = true;
+  for (int s = 0; s < c.nsys; s++) {
+    if (d->natoms[s] < 1) return bad(PDGPU_ERR_ARG);
+    SystemInfo S{};
+    S.atom_start = atom;
+    S.natom = d->natoms[s];
+    S.pad_start = slot;
+    S.npad = (S.natom + 31) / 32 * 32;
+    S.block_start = block;
+    S.nblocks = S.npad / 32;
+    S.cand_start = cand;
+    int per = 0;
+    for (int k = 0; k < 3; k++) {
+      S.box[k] = d->box[3 * s + k];
+      if (S.box[k] > 0) per++;
+    }
+    if (per != 0 && per != 3) return bad(PDGPU_ERR_ARG);
+    S.periodic = per == 3;
+    c.any_periodic |= S.periodic;
+    c.all_periodic &= S.periodic;
+    c.sys.push_back(S);
+    atom += S.natom;
+    slot += S.npad;
+    block += S.nblocks;
+    cand += (long long)S.nblocks * (S.nblocks + 1) / 2;
+  }
+  c.natom = atom;
+  c.nslots = slot;
+  c.nblocks = block;
+  c.ncand = cand;
+  const int N = c.natom;
+
+  c.h_atom_sys.resize(N);
+  std::vector<int> block_sys(c.nblocks);
+  for (int s = 0; s < c.nsys; s++) {
+    for (int a = 0; a < c.sys[s].natom; a++) c.h_atom_sys[c.sys[s].atom_start + a] = s;
+    for (int b = 0; b < c.sys[s].nblocks; b++) block_sys[c.sys[s].block_start + b] = s;
+  }
+
+  // per-atom parameters in internal units
+  const double sq = std::sqrt(kNa / kKcal2J);  // sqrt(J) -> sqrt(kcal/mol)
+  std::vector<double> sqeps(N);
+  for (int a = 0; a < N; a++) sqeps[a] = d->epsilon[a] * sq;
+
+  // bonded pairs: band masks (|i-j| <= 64) and a far list
+  std::vector<unsigned long long> bex(N, 0ull), b14(N, 0ull);
+  std::vector<std::vector<std::pair<int, int>>> far(N);
+  for (int k = 0; k < d->nexcl; k++) {
+    int i = d->excl[3 * k], j = d->excl[3 * k + 1], bo = d->excl[3 * k + 2];
+    if (i < 0 || j < 0 || i >= N || j >= N || c.h_atom_sys[i] != c.h_atom_sys[j]) return bad(PDGPU_ERR_ARG);
+    int lo = std::min(i, j), hi = std::max(i, j), dd = hi - lo;
+    if (dd == 0 || bo > 3) continue;
+    if (dd <= kBandWidth) {
+      unsigned long long bit = 1ull << (dd - 1);
+      if (bo <= 2) bex[lo] |= bit;
+      else b14[lo] |= bit;
+    } else {
+      far[lo].push_back(std::make_pair(hi, bo));
+    }
+  }
+  std::vector<int> fstart(N + 1, 0), fidx, fbo;
+  for (int a = 0; a < N; a++) {
+    fstart[a + 1] = fstart[a] + (int)far[a].size();
+    for (auto& p : far[a]) {
+      fidx.push_back(p.first);
+      fbo.push_back(p.second);
+    }
+  }
+  if (fidx.empty()) {
+    fidx.push_back(-1);
+    fbo.push_back(7);
+  }
+
+  cudaError_t e = cudaSuccess;
+#define UP(buf, ptr, n) \
+  if (e == cudaSuccess) e = upload(buf, ptr, n)
+  UP(c.d_sys, c.sys.data(), c.sys.size());
+  UP(c.d_atom_sys, c.h_atom_sys.data(), (size_t)N);
+  UP(c.d_block_sys, block_sys.data(), block_sys.size());
+  UP(c.d_charge, d->charge, (size_t)N);
+  UP(c.d_radius, d->radius, (size_t)N);
+  UP(c.d_sqeps, sqeps.data(), (size_t)N);
+  UP(c.d_band_excl, bex.data(), (size_t)N);
+  UP(c.d_band_14, b14.data(), (size_t)N);
+  UP(c.d_far_start, fstart.data(), fstart.size());
+  UP(c.d_far_idx, fidx.data(), fidx.size());
+  UP(c.d_far_bo, fbo.data(), fbo.size());
+  if (d->mass) {
+    UP(c.d_mass, d->mass, (size_t)N);
+    c.has_mass = true;
+  }
+  if (d->gb_radius && d->gb_vj && d->gb_terms123) {
+    c.has_gb = true;
+    UP(c.d_gbR, d->gb_radius, (size_t)N);
+    UP(c.d_gbVj, d->gb_vj, (size_t)N);
+    UP(c.d_gbT, d->gb_terms123, (size_t)N);
+  }
+  if (d->lcpo_radius && d->lcpo_p && d->lcpo_sigma && d->lcpo_use) {
+    c.has_sa = true;
+    std::vector<double> sig(N);
+    for (int a = 0; a < N; a++) sig[a] = d->lcpo_sigma[a] * (kNa / kKcal2J);
+    UP(c.d_lcpoR, d->lcpo_radius, (size_t)N);
+    UP(c.d_lcpoP, d->lcpo_p, (size_t)N * 4);
+    UP(c.d_lcpoSig, sig.data(), (size_t)N);
+    UP(c.d_lcpoUse, d->lcpo_use, (size_t)N);
+  }
+  // bonded terms, energies converted from J to kcal/mol
+  const double J2k = kNa / kKcal2J;
+  c.nbond = std::max(0, d->nbond);
+  c.nangle = std::max(0, d->nangle);
+  c.ntors = std::max(0, d->ntors);
+  c.nimpr = std::max(0, d->nimpr);
+  if (c.nbond && (!d->bond_idx || !d->bond_par)) return bad(PDGPU_ERR_ARG);
+  if (c.nangle && (!d->angle_idx || !d->angle_par)) return bad(PDGPU_ERR_ARG);
+  if (c.ntors && (!d->tors_idx || !d->tors_par)) return bad(PDGPU_ERR_ARG);
+  if (c.nimpr && (!d->impr_idx || !d->impr_par)) return bad(PDGPU_ERR_ARG);
+  {
+    std::vector<double> bp(2 * (size_t)c.nbond), ap(2 * (size_t)c.nangle), tp(12 * (size_t)c.ntors),
+        ip(12 * (size_t)c.nimpr);
+    for (int k = 0; k < c.nbond; k++) {
+      bp[2 * k] = d->bond_par[2 * k];
+      bp[2 * k + 1] = d->bond_par[2 * k + 1] * J2k;
+    }
+    for (int k = 0; k < c.nangle; k++) {
+      ap[2 * k] = d->angle_par[2 * k];
+      ap[2 * k + 1] = d->angle_par[2 * k + 1] * J2k;
+    }
+    for (int k = 0; k < c.ntors; k++)
+      for (int t = 0; t < 4; t++) {
+        tp[12 * k + 3 * t] = d->tors_par[12 * k + 3 * t] * J2k;
+        tp[12 * k + 3 * t + 1] = d->tors_par[12 * k + 3 * t + 1];
+        tp[12 * k + 3 * t + 2] = d->tors_par[12 * k + 3 * t + 2];
+      }
+    for (int k = 0; k < c.nimpr; k++)
+      for (int t = 0; t < 4; t++) {
+        ip[12 * k + 3 * t] = d->impr_par[12 * k + 3 * t] * J2k;
+        ip[12 * k + 3 * t + 1] = d->impr_par[12 * k + 3 * t + 1];
+        ip[12 * k + 3 * t + 2] = d->impr_par[12 * k + 3 * t + 2];
+      }
+    UP(c.d_bidx, d->bond_idx, 2 * (size_t)c.nbond);
+    UP(c.d_bpar, bp.data(), bp.size());
+    UP(c.d_aidx, d->angle_idx, 3 * (size_t)c.nangle);
+    UP(c.d_apar, ap.data(), ap.size());
+    UP(c.d_tidx, d->tors_idx, 5 * (size_t)c.ntors);
+    UP(c.d_tpar, tp.data(), tp.size());
+    UP(c.d_iidx, d->impr_idx, 5 * (size_t)c.nimpr);
+    UP(c.d_ipar, ip.data(), ip.size());
+    c.has_bonded = c.nbond + c.nangle + c.ntors + c.nimpr > 0;
+  }
+#undef UP
+
+  // dynamic buffers
+  const size_t ncells = (size_t)c.nsys * kCellsPerSystem;
+  const size_t nsb = (ncells + 1023) / 1024;
+  if (e == cudaSuccess) e = c.d_pos.alloc(3 * (size_t)N);
+  if (e == cudaSuccess) e = c.d_fout.alloc(3 * (size_t)N);
+  if (e == cudaSuccess) e = c.d_bucket.alloc(N);
+  if (e == cudaSuccess) e = c.d_count.alloc(ncells);
+  if (e == cudaSuccess) e = c.d_offset.alloc(ncells);
+  if (e == cudaSuccess) e = c.d_cursor.alloc(ncells);
+  if (e == cudaSuccess) e = c.d_scan_tmp.alloc(nsb + 1);
+  if (e == cudaSuccess) e = c.d_tmp_sorted.alloc(N);
+  if (e == cudaSuccess) e = c.d_sys_lo.alloc(3 * (size_t)c.nsys);
+  if (e == cudaSuccess) e = c.d_sys_hi.alloc(3 * (size_t)c.nsys);
+  if (e == cudaSuccess) e = c.d_sorted_atom.alloc(c.nslots);
+  if (e == cudaSuccess) e = c.d_slot_of.alloc(N);
+  if (e == cudaSuccess) e = c.d_center.alloc(3 * (size_t)c.nblocks);
+  if (e == cudaSuccess) e = c.d_half.alloc(c.nblocks);
+  if (e == cudaSuccess) e = c.d_tiles.alloc(c.ncand);
+  if (e == cudaSuccess) e = c.d_counters.alloc(2);
+  if (e == cudaSuccess) e = c.d_masks.alloc((size_t)c.ncand * 32);
+  if (e == cudaSuccess) e = c.d_xq.alloc(c.nslots);
+  if (e == cudaSuccess) e = c.d_par.alloc(c.nslots);
+  if (e == cudaSuccess) e = c.d_rel0.alloc(c.nslots);
+  if (e == cudaSuccess) e = c.d_facc.alloc(3 * (size_t)c.nslots);
+  if (e == cudaSuccess) e = c.d_eacc.alloc((size_t)c.nsys * E_NSLOTS);
+  if (e == cudaSuccess) e = c.d_status.alloc(1);
+  if (c.has_gb) {
+    if (e == cudaSuccess) e = c.d_gpol.alloc(c.nslots);
+    if (e == cudaSuccess) e = c.d_deda.alloc(c.nslots);
+    if (e == cudaSuccess) e = c.d_born_f.alloc(c.nslots);
+    if (e == cudaSuccess) e = c.d_chain_f.alloc(c.nslots);
+    if (e == cudaSuccess) e = c.d_born_d.alloc(N);
+  }
+  if (c.has_sa) {
+    if (e == cudaSuccess) e = c.d_lc_ncand.alloc(c.nslots);
+    if (e == cudaSuccess) e = c.d_lc_cand.alloc((size_t)c.nslots * kLcpoCand);
+    if (e == cudaSuccess) e = c.d_lc_n.alloc(c.nslots);
+    if (e == cudaSuccess) e = c.d_lc_idx.alloc((size_t)c.nslots * kLcpoMax);
+    if (e == cudaSuccess) e = c.d_lc_s.alloc((size_t)c.nslots * kLcpoMax);
+    if (e == cudaSuccess) e = c.d_sasa.alloc(N);
+    if (e == cudaSuccess) e = c.d_lc_par.alloc(c.nslots);
+  }
+  if (e == cudaSuccess) e = cudaMemset(c.d_status.p, 0, sizeof(unsigned));
+  if (e != cudaSuccess) return bad(PDGPU_ERR_CUDA);
+  c.h_eacc.resize((size_t)c.nsys * E_NSLOTS);
+
+  // PD defaults: FF_NonBonded::settodefault (nonbonded.cpp:985-1021),
+  // FF_GeneralizedBorn_Still constructor (gbff.cpp:33-55), NeighbourList Padding 0.5
+  c.nb = pdgpu_nb_params{15.0, 12.0, 15.0, 12.0, 1.0, 1.0, 1.0, 0, 1, 1, 1};
+  c.gb = pdgpu_gb_params{15.0, 12.0, 15.0, 12.0, 1.0, 1.0, 1.0, 80.0, 10.0, -4.0, 0.0, 15.236, 1.254};
+  c.lp = pdgpu_list_params{0.5, 1};
+  if (status) *status = PDGPU_OK;
+  return h;
+}
+
+int pdgpu_destroy(pdgpu_ctx* h) {
+  if (!h) return PDGPU_ERR_ARG;
+  cudaSetDevice(h->c.device);
+  if (h->c.stream) cudaStreamSynchronize(h->c.stream);
+  cudaStream_t st = h->c.stream;
+  delete h;
+  if (st) cudaStreamDestroy(st);
+  return PDGPU_OK;
+}
+
+int pdgpu_set_nb_params(pdgpu_ctx* h, const pdgpu_nb_params* p) {
+  if (!h || !p || p->Cutoff <= 0 || p->InnerCutoff > p->Cutoff || p->VdwInnerCutoff > p->VdwCutoff ||
+      p->Dielectric == 0)
+    return PDGPU_ERR_ARG;
+  h->c.nb = *p;
+  h->c.nb_set = true;
+  h->c.list_built = false;
+  return PDGPU_OK;
+}
+
+int pdgpu_set_gb_params(pdgpu_ctx* h, const pdgpu_gb_params* p) {
+  if (!h || !p || p->Cutoff <= 0 || p->InnerCutoff > p->Cutoff || p->DielectricSolute == 0 ||
+      p->DielectricSolvent == 0 || p->P5 == 0)
+    return PDGPU_ERR_ARG;
+  h->c.gb = *p;
+  h->c.gb_set = true;
+  h->c.list_built = false;
+  return PDGPU_OK;
+}
+
+int pdgpu_set_list_params(pdgpu_ctx* h, const pdgpu_list_params* p) {
+  if (!h || !p || p->Padding < 0) return PDGPU_ERR_ARG;
+  h->c.lp = *p;
+  h->c.list_built = false;
+  return PDGPU_OK;
+}
+
+int pdgpu_update_params(pdgpu_ctx* h, const double* charge, const double* radius, const double* epsilon,
+                        const double* gb_vj, const double* gb_terms123) {
+  if (!h) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  CK(cudaSetDevice(c.device));
+  const size_t N = c.natom;
+  if (charge) CK(cudaMemcpyAsync(c.d_charge.p, charge, N * 8, cudaMemcpyHostToDevice, c.stream));
+  if (radius) CK(cudaMemcpyAsync(c.d_radius.p, radius, N * 8, cudaMemcpyHostToDevice, c.stream));
+  if (epsilon) {
+    std::vector<double> sq(N);
+    const double f = std::sqrt(kNa / kKcal2J);
+    for (size_t a = 0; a < N; a++) sq[a] = epsilon[a] * f;
+    CK(cudaMemcpyAsync(c.d_sqeps.p, sq.data(), N * 8, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+  }
+  if ((gb_vj || gb_terms123) && !c.has_gb) return PDGPU_ERR_STATE;
+  if (gb_vj) CK(cudaMemcpyAsync(c.d_gbVj.p, gb_vj, N * 8, cudaMemcpyHostToDevice, c.stream));
+  if (gb_terms123) CK(cudaMemcpyAsync(c.d_gbT.p, gb_terms123, N * 8, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  // slot parameters are refreshed at the next list build
+  c.list_built = false;
+  return PDGPU_OK;
+}
+
+int pdgpu_set_positions(pdgpu_ctx* h, const double* xyz, size_t stride) {
+  if (!h || !xyz || stride < 24 || stride % 8) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  CK(cudaSetDevice(c.device));
+  CK(cudaMemcpy2DAsync(c.d_pos.p, 24, xyz, stride, 24, c.natom, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  c.positions_set = true;
+  return PDGPU_OK;
+}
+
+int pdgpu_set_positions_device(pdgpu_ctx* h, const double* d_xyz) {
+  if (!h || !d_xyz) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  CK(cudaSetDevice(c.device));
+  CK(cudaMemcpyAsync(c.d_pos.p, d_xyz, 24 * (size_t)c.natom, cudaMemcpyDeviceToDevice, c.stream));
+  c.positions_set = true;
+  return PDGPU_OK;
+}
+
+int pdgpu_get_positions(pdgpu_ctx* h, double* xyz, size_t stride) {
+  if (!h || !xyz || stride < 24 || stride % 8) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  CK(cudaSetDevice(c.device));
+  CK(cudaMemcpy2DAsync(xyz, stride, c.d_pos.p, 24, 24, c.natom, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return PDGPU_OK;
+}
+
+static int rebuild_list(Context& c) {
+  if (!c.positions_set) return PDGPU_ERR_STATE;
+  if (!c.nb_set && !c.gb_set && !c.has_sa) return PDGPU_ERR_STATE;
+  CK(cudaSetDevice(c.device));
+  CK(cudaMemsetAsync(c.d_status.p, 0, sizeof(unsigned), c.stream));
+  float R = (float)list_radius(c);
+  int st = launch_list_build(c, R);
+  if (st != PDGPU_OK) return st;
+  c.list_radius_built = R;
+  c.list_built = true;
+  return PDGPU_OK;
+}
+
+int pdgpu_rebuild_list(pdgpu_ctx* h) {
+  if (!h) return PDGPU_ERR_ARG;
+  return rebuild_list(h->c);
+}
+
+static int enqueue_compute(Context& c, unsigned what) {
+  if (!c.positions_set) return PDGPU_ERR_STATE;
+  if ((what & PDGPU_NB) && !c.nb_set) return PDGPU_ERR_STATE;
+  if ((what & PDGPU_GB) && (!c.has_gb || !c.gb_set)) return PDGPU_ERR_STATE;
+  if ((what & PDGPU_SA) && !c.has_sa) return PDGPU_ERR_STATE;
+  if ((what & (PDGPU_GB | PDGPU_SA)) && c.any_periodic) return PDGPU_ERR_UNSUPPORTED;
+  CK(cudaMemsetAsync(c.d_status.p, 0, sizeof(unsigned), c.stream));
+  if (!c.list_built) {
+    int st = rebuild_list(c);
+    if (st != PDGPU_OK) return st;
+  } else {
+    int st = launch_pack(c, c.lp.check_skin ? (float)(0.5 * c.lp.Padding) : 0.f);
+    if (st != PDGPU_OK) return st;
+  }
+  CK(cudaMemsetAsync(c.d_facc.p, 0, sizeof(long long) * 3 * c.nslots, c.stream));
+  CK(cudaMemsetAsync(c.d_eacc.p, 0, sizeof(long long) * E_NSLOTS * c.nsys, c.stream));
+  int st = PDGPU_OK;
+  if (what & PDGPU_NB) st = launch_nb(c, make_nb_const(c.nb), true);
+  if (st == PDGPU_OK && (what & PDGPU_GB)) {
+    GBConst k = make_gb_const(c.gb, c.list_radius_built);
+    double ec = econv_kcal();
+    double premul = -0.5 * ec * (1.0 / c.gb.DielectricSolute - 1.0 / c.gb.DielectricSolvent);
+    st = launch_gb(c, k, 0.5 * ec, c.gb.BornRadiusOffset, premul);
+  }
+  if (st == PDGPU_OK && (what & PDGPU_SA)) st = launch_lcpo(c);
+  if (st == PDGPU_OK && (what & PDGPU_BONDED)) st = launch_bonded(c);
+  return st;
+}
+
+int pdgpu_get_energies(pdgpu_ctx* h, pdgpu_energies* out) {
+  if (!h || !out) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  CK(cudaSetDevice(c.device));
+  CK(cudaMemcpyAsync(c.h_eacc.data(), c.d_eacc.p, sizeof(long long) * E_NSLOTS * c.nsys, cudaMemcpyDeviceToHost,
+                     c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  for (int s = 0; s < c.nsys; s++) {
+    const long long* E = &c.h_eacc[(size_t)s * E_NSLOTS];
+    auto J = [&](int k) { return (double)E[k] / kEnergyScale * kKcalMolToJ; };
+    pdgpu_energies& o = out[s];
+    o.vdw = J(E_VDW);
+    o.elec = J(E_ELEC);
+    o.pol_cross = J(E_POL_CROSS);
+    o.pol_self = J(E_POL_SELF);
+    o.pol = o.pol_cross + o.pol_self;
+    o.surf = J(E_SURF);
+    o.virial = J(E_VIRIAL);
+    o.bond = J(E_BOND);
+    o.angle = J(E_ANGLE);
+    o.torsion = J(E_TORS);
+    o.improper = J(E_IMPR);
+    o.epot = o.vdw + o.elec + o.pol + o.surf + o.bond + o.angle + o.torsion + o.improper;
+  }
+  return PDGPU_OK;
+}
+
+int pdgpu_compute(pdgpu_ctx* h, unsigned what, pdgpu_energies* out, double* f, size_t stride) {
+  if (!h || (f && (stride < 24 || stride % 8))) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  CK(cudaSetDevice(c.device));
+  int st = enqueue_compute(c, what);
+  if (st != PDGPU_OK) return st;
+  if (f) {
+    st = launch_finalize_forces(c, c.d_fout.p, 3, false, kForceToN);
+    if (st != PDGPU_OK) return st;
+    c.h_stage.resize(3 * (size_t)c.natom);
+    CK(cudaMemcpyAsync(c.h_stage.data(), c.d_fout.p, 24 * (size_t)c.natom, cudaMemcpyDeviceToHost, c.stream));
+  }
+  st = read_status(c);
+  if (st != PDGPU_OK) return st;
+  if (f) {
+    const size_t sd = stride / 8;
+    for (int a = 0; a < c.natom; a++)
+      for (int k = 0; k < 3; k++) f[a * sd + k] += c.h_stage[3 * (size_t)a + k];
+  }
+  if (out) return pdgpu_get_energies(h, out);
+  return PDGPU_OK;
+}
+
+int pdgpu_compute_device(pdgpu_ctx* h, unsigned what, double* d_f) {
+  if (!h) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  CK(cudaSetDevice(c.device));
+  int st = enqueue_compute(c, what);
+  if (st != PDGPU_OK) return st;
+  if (d_f) st = launch_finalize_forces(c, d_f, 3, false, kForceToN);
+  return st;
+}
+
+int pdgpu_get_born_radii(pdgpu_ctx* h, double* born) {
+  if (!h || !born) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.has_gb) return PDGPU_ERR_STATE;
+  CK(cudaSetDevice(c.device));
+  CK(cudaMemcpyAsync(born, c.d_born_d.p, 8 * (size_t)c.natom, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return PDGPU_OK;
+}
+
+int pdgpu_get_sasa(pdgpu_ctx* h, double* sasa) {
+  if (!h || !sasa) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.has_sa) return PDGPU_ERR_STATE;
+  CK(cudaSetDevice(c.device));
+  CK(cudaMemcpyAsync(sasa, c.d_sasa.p, 8 * (size_t)c.natom, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  return PDGPU_OK;
+}
+
+int pdgpu_list_stats(pdgpu_ctx* h, long long* ntiles, long long* nmasked, long long* nslots) {
+  if (!h) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  int cnt[2] = {0, 0};
+  CK(cudaSetDevice(c.device));
+  CK(cudaMemcpyAsync(cnt, c.d_counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  if (ntiles) *ntiles = cnt[0];
+  if (nmasked) *nmasked = cnt[1];
+  if (nslots) *nslots = c.nslots;
+  return PDGPU_OK;
+}
+
+void* pdgpu_stream(pdgpu_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
+
+}  // extern "C"

@@ -1,0 +1,145 @@
+// pdgpu_common.cuh — shared definitions for the GB300 nonbonded / GB / LCPO path.
+//
+// Layout (one context may hold several independent systems, "a batch"):
+//   * original order  : atoms as the host numbers them, systems concatenated.
+//   * sorted order    : per system, atoms ordered along a 3-D Hilbert curve of a
+//                       32^3 cell grid, padded to a multiple of 32; slot s holds
+//                       original atom sorted_atom[s] (or -1 for padding).
+//   * blocks          : 32 consecutive sorted slots of one system.
+//   * tiles           : block pairs (bi <= bj) of one system whose bounding boxes
+//                       come within the list radius; one warp evaluates the
+//                       32x32 interactions of a tile by shuffle rotation.
+// Forces, Born-radius sums, dE/da and energies are accumulated in 64-bit fixed
+// point, so results are bit-identical run to run whatever the tile order.
+// Internal units: Angstrom, kcal/mol, e; conversion to PD units (J, N) happens
+// once per atom / per energy at the end.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/pdgpu.h"
+
+namespace pdgpu {
+
+constexpr int kWarp = 32;
+constexpr int kHilbertBits = 5;                       // 32 cells per dimension
+constexpr int kCellsPerSystem = 1 << (3 * kHilbertBits);
+constexpr int kBandWidth = 64;                        // bonded partners within +-64 indices use the band masks
+constexpr int kLcpoMax = 80;                          // PD caps an atom's LCPO overlap list at 80 (lcpo.h:24)
+constexpr int kLcpoCand = 160;                        // candidate capacity before the cap is applied
+
+// fixed-point scales
+constexpr double kForceScale = 4294967296.0;          // 2^32 per kcal/mol/A
+constexpr double kEnergyScale = 16777216.0;           // 2^24 per kcal/mol
+constexpr double kSumScale = 4294967296.0;            // 2^32 per unit (Born sums, dE/da)
+
+// per-system energy slots (fixed point)
+enum EnergySlot { E_VDW = 0, E_ELEC, E_POL_CROSS, E_POL_SELF, E_SURF, E_VIRIAL, E_BOND, E_ANGLE, E_TORS, E_IMPR, E_NSLOTS };
+
+// status bits set by kernels
+enum StatusBits : unsigned {
+  ST_LCPO_OVERFLOW = 1u,
+  ST_FIXED_OVERFLOW = 2u,
+  ST_NAN = 4u,
+  ST_STALE_LIST = 8u,
+};
+
+struct SystemInfo {
+  int atom_start;   // first atom (original order)
+  int natom;
+  int pad_start;    // first slot (sorted order)
+  int npad;         // multiple of 32
+  int block_start;
+  int nblocks;
+  long long cand_start;  // first candidate block pair of this system
+  int periodic;
+  double box[3];
+};
+
+struct Tile {
+  int bi, bj;
+  int mask;    // index into the exclusion-mask table or -1
+  int flags;   // bit0: per-pair minimum image needed, bit1: diagonal tile
+};
+
+// Pair-law constants for the LJ + Coulomb kernel (FF_NonBonded)
+struct NBConst {
+  float cut2, vdwcut, vdwinner, inner, vdwinvw2, invw2;
+  float econv_diel;        // econv * (1/Dielectric) in kcal A / mol / e^2
+  float vdw14, elec14;
+  float sA, sB, sC, sD, sE, fsw_cutV, eshift, cut2_d, inner2;
+  int elecmode;            // 0 none, 1 plain, 3 energy switch, 4 force switch
+  int dovdw;
+};
+
+// Constants for the GB fast path (FF_GeneralizedBorn_Still::calcForcesIncludingVacuo)
+struct GBConst {
+  float cut2, inner, invw2, vdwcut, vdwinner, vdwinvw2;
+  float still2;            // min(GbsaStillCutoff, list radius)^2
+  float econv_in, econv_out, premul;  // kcal units
+  float vdw14, elec14, thresh;
+  float P4, P5, invP5;
+};
+
+// Device-side view of a context, passed by value to kernels.
+struct DevView {
+  int nsys, natom, nslots, nblocks;
+  const SystemInfo* sys;
+  const int* slot_sys;       // [nblocks] system of each block
+  // original order
+  const double* pos;         // natom*3
+  // sorted order
+  const int* sorted_atom;    // [nslots]
+  float4* xq;                // rel pos + charge
+  float4* par;               // LJ radius, sqrt(eps kcal), GB R (raw), GB Vj
+  float4* rel0;              // rel pos at list build (displacement check)
+  double* center;            // [nblocks*3]
+  float4* half;              // [nblocks] half extents
+  unsigned long long* band_excl;   // [natom*2]? (see below) per atom: bit d-1 => partner i+d excluded (bo<=2)
+  unsigned long long* band_14;     // per atom: bit d-1 => partner i+d is a 1-4 pair
+  const int* far_start;      // CSR of partners beyond the band, per atom
+  const int* far_idx;
+  const int* far_bo;
+  Tile* tiles;
+  int* ntiles;
+  uint2* masks;              // [nmask*32] per lane: (excluded bits, 1-4 bits) in rotation order
+  int* nmasks;
+  long long* facc;           // [nslots*3]
+  long long* eacc;           // [nsys*E_NSLOTS]
+  unsigned* status;
+};
+
+// ---------------------------------------------------------------------------
+// fixed point helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long fix_force(float x) { return __float2ll_rn(x * 4294967296.0f); }
+__device__ __forceinline__ long long fix_energy(float x) { return __float2ll_rn(x * 16777216.0f); }
+__device__ __forceinline__ long long fix_energy_d(double x) { return __double2ll_rn(x * 16777216.0); }
+__device__ __forceinline__ long long fix_sum(float x) { return __float2ll_rn(x * 4294967296.0f); }
+__device__ __forceinline__ void atomic_add_ll(long long* p, long long v) {
+  atomicAdd(reinterpret_cast<unsigned long long*>(p), static_cast<unsigned long long>(v));
+}
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers (defined in the .cu files)
+// ---------------------------------------------------------------------------
+struct Context;
+int launch_list_build(Context& c, float list_radius);
+int launch_pack(Context& c, float check_disp);
+int launch_nb(Context& c, const NBConst& k, bool need_virial);
+int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset, double premul);
+int launch_lcpo(Context& c);
+int launch_bonded(Context& c);
+int launch_finalize_forces(Context& c, double* out, size_t stride_doubles, bool add, double scale);
+
+}  // namespace pdgpu

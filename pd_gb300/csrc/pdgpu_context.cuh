@@ -1,0 +1,149 @@
+// pdgpu_context.cuh — host-side context: device buffers, parameters, stream.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "pdgpu_common.cuh"
+
+namespace pdgpu {
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    release();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DBuf() { release(); }
+};
+
+struct Context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int nsys = 0, natom = 0, nslots = 0, nblocks = 0;
+  long long ncand = 0;
+  bool any_periodic = false, all_periodic = true;
+  bool has_gb = false, has_sa = false, has_bonded = false, has_mass = false;
+  bool positions_set = false, list_built = false;
+  std::vector<SystemInfo> sys;
+  std::vector<int> h_atom_sys;
+
+  // parameters
+  pdgpu_nb_params nb{};
+  pdgpu_gb_params gb{};
+  pdgpu_list_params lp{};
+  bool nb_set = false, gb_set = false;
+  float list_radius_built = 0.f;
+
+  // static per-atom data (original order)
+  DBuf<SystemInfo> d_sys;
+  DBuf<int> d_atom_sys;        // [natom]
+  DBuf<int> d_block_sys;       // [nblocks]
+  DBuf<double> d_charge, d_radius, d_sqeps;   // sqeps in sqrt(kcal/mol)
+  DBuf<double> d_gbR, d_gbVj, d_gbT;          // GB raw radius, Vj, terms123
+  DBuf<double> d_lcpoR, d_lcpoP, d_lcpoSig;   // lcpo radius, P1..P4, sigma (kcal/mol/A^2)
+  DBuf<int> d_lcpoUse;
+  DBuf<unsigned long long> d_band_excl, d_band_14;
+  DBuf<int> d_far_start, d_far_idx, d_far_bo;
+  DBuf<double> d_mass;                         // kg
+
+  // dynamic state
+  DBuf<double> d_pos;          // [natom*3] Angstrom
+  DBuf<double> d_fout;         // [natom*3] N (device-side output buffer)
+
+  // list build scratch
+  DBuf<int> d_bucket;          // [natom]
+  DBuf<int> d_count, d_offset, d_cursor;      // [nsys*kCellsPerSystem]
+  DBuf<int> d_scan_tmp;
+  DBuf<int> d_tmp_sorted;      // [natom]
+  DBuf<float> d_sys_lo, d_sys_hi;              // [nsys*3]
+  DBuf<int> d_sorted_atom;     // [nslots]
+  DBuf<int> d_slot_of;         // [natom] sorted slot of each atom
+  DBuf<double> d_center;       // [nblocks*3]
+  DBuf<float4> d_half;         // [nblocks]
+  DBuf<Tile> d_tiles;          // [ncand]
+  DBuf<int> d_counters;        // [0] ntiles, [1] nmasks
+  DBuf<uint2> d_masks;         // [ncand*32] worst case
+  DBuf<float4> d_xq, d_par, d_rel0;  // [nslots]
+
+  // accumulators
+  DBuf<long long> d_facc;      // [nslots*3]
+  DBuf<long long> d_eacc;      // [nsys*E_NSLOTS]
+  DBuf<unsigned> d_status;
+
+  // GB
+  DBuf<long long> d_gpol, d_deda;   // [nslots]
+  DBuf<float> d_born_f;             // [nslots]
+  DBuf<float> d_chain_f;            // [nslots] a^2/166 * dE/da * P4
+  DBuf<double> d_born_d;            // [natom] original order
+  // LCPO
+  DBuf<int> d_lc_ncand;             // [nslots]
+  DBuf<int> d_lc_cand;              // [nslots*kLcpoCand]
+  DBuf<int> d_lc_n;                 // [nslots]
+  DBuf<int> d_lc_idx;               // [nslots*kLcpoMax] slot indices, ascending original index
+  DBuf<float> d_lc_s;               // [nslots*kLcpoMax] overlap s_ij
+  DBuf<double> d_sasa;              // [natom]
+  DBuf<float4> d_lc_par;            // [nslots] (radius, use, -, -)
+
+  // bonded
+  int nbond = 0, nangle = 0, ntors = 0, nimpr = 0;
+  DBuf<int> d_bidx, d_aidx, d_tidx, d_iidx;
+  DBuf<double> d_bpar, d_apar, d_tpar, d_ipar;
+
+  // host staging
+  std::vector<long long> h_eacc;
+  std::vector<double> h_stage;
+  int last_error = 0;
+  std::string last_msg;
+
+  DevView view() const {
+    DevView v;
+    v.nsys = nsys;
+    v.natom = natom;
+    v.nslots = nslots;
+    v.nblocks = nblocks;
+    v.sys = d_sys.p;
+    v.slot_sys = d_block_sys.p;
+    v.pos = d_pos.p;
+    v.sorted_atom = d_sorted_atom.p;
+    v.xq = d_xq.p;
+    v.par = d_par.p;
+    v.rel0 = d_rel0.p;
+    v.center = d_center.p;
+    v.half = d_half.p;
+    v.band_excl = d_band_excl.p;
+    v.band_14 = d_band_14.p;
+    v.far_start = d_far_start.p;
+    v.far_idx = d_far_idx.p;
+    v.far_bo = d_far_bo.p;
+    v.tiles = d_tiles.p;
+    v.ntiles = d_counters.p;
+    v.masks = d_masks.p;
+    v.nmasks = d_counters.p + 1;
+    v.facc = d_facc.p;
+    v.eacc = d_eacc.p;
+    v.status = d_status.p;
+    return v;
+  }
+};
+
+// unit conversions (PD PhysicsConst, src/mmlib/forcefields/forcefield.cpp:35-55)
+constexpr double kKcal2J = 4184.0;
+constexpr double kNa = 6.0221418E23;
+constexpr double kAngstrom = 1E-10;
+constexpr double kKcalMolToJ = kKcal2J / kNa;                  // kcal/mol -> J per molecule
+constexpr double kForceToN = kKcalMolToJ / kAngstrom;           // kcal/mol/A -> N
+inline double econv_kcal() {
+  const double e = 1.60217645E-19, e0 = 8.854187817E-12, pi = 3.14159265358979323846;
+  return ((1.0 / kKcal2J) * kNa * e * e) / (4.0 * pi * e0 * kAngstrom);
+}
+
+}  // namespace pdgpu

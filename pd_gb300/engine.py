@@ -1,0 +1,152 @@
+"""Python handle on one libpdgpu context (the C ABI in include/pdgpu.h)."""
+import ctypes
+
+import numpy as np
+
+from . import ffi
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def _pd(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _pi(a):
+    return None if a is None else a.ctypes.data_as(_ip)
+
+
+class DeviceContext:
+    """Owns a pdgpu context for a SystemImage; every call raises PDGPUError on failure."""
+
+    def __init__(self, image, device=0):
+        self.lib = ffi.load()
+        self.image = image
+        im = image
+        self._keep = []
+
+        def keep(a, dtype):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=dtype)
+            self._keep.append(a)
+            return a
+
+        d = ffi.SystemDesc()
+        d.nsystems = im.nsystems
+        d.natoms = _pi(keep(im.natoms, np.int32))
+        d.box = _pd(keep(im.box, np.float64))
+        d.charge = _pd(keep(im.charge, np.float64))
+        d.radius = _pd(keep(im.radius, np.float64))
+        d.epsilon = _pd(keep(im.epsilon, np.float64))
+        d.mass = _pd(keep(im.mass, np.float64))
+        if im.has_gb:
+            d.gb_radius = _pd(keep(im.gb_radius, np.float64))
+            d.gb_vj = _pd(keep(im.gb_vj, np.float64))
+            d.gb_terms123 = _pd(keep(im.gb_terms123, np.float64))
+        if im.has_sa:
+            d.lcpo_radius = _pd(keep(im.lcpo_radius, np.float64))
+            d.lcpo_p = _pd(keep(im.lcpo_p, np.float64))
+            d.lcpo_sigma = _pd(keep(im.lcpo_sigma, np.float64))
+            d.lcpo_use = _pi(keep(im.lcpo_use, np.int32))
+        ex = keep(im.excl, np.int32)
+        d.nexcl = len(ex)
+        d.excl = _pi(ex)
+        for name, (idx, par) in (("bond", im.bonds), ("angle", im.angles), ("tors", im.torsions),
+                                 ("impr", im.impropers)):
+            i = keep(idx, np.int32)
+            p = keep(par, np.float64)
+            setattr(d, "n" + name, len(i))
+            setattr(d, name + "_idx", _pi(i) if len(i) else None)
+            setattr(d, name + "_par", _pd(p) if len(i) else None)
+        st = ctypes.c_int(0)
+        h = self.lib.pdgpu_create(int(device), ctypes.byref(d), ctypes.byref(st))
+        if not h:
+            raise ffi.PDGPUError(st.value, "pdgpu_create")
+        self.h = ctypes.c_void_p(h)
+        self.natom = im.natom
+        self.nsystems = im.nsystems
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pdgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- parameters --------------------------------------------------------
+    def set_nb(self, **kw):
+        p = ffi.NBParams(**kw)
+        ffi.check(self.lib.pdgpu_set_nb_params(self.h, ctypes.byref(p)), "pdgpu_set_nb_params")
+
+    def set_gb(self, **kw):
+        p = ffi.GBParams(**kw)
+        ffi.check(self.lib.pdgpu_set_gb_params(self.h, ctypes.byref(p)), "pdgpu_set_gb_params")
+
+    def set_list(self, padding, check_skin=True):
+        p = ffi.ListParams(float(padding), int(check_skin))
+        ffi.check(self.lib.pdgpu_set_list_params(self.h, ctypes.byref(p)), "pdgpu_set_list_params")
+
+    def update_params(self, charge=None, radius=None, epsilon=None, gb_vj=None, gb_terms123=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float64) for a in
+                (charge, radius, epsilon, gb_vj, gb_terms123)]
+        ffi.check(self.lib.pdgpu_update_params(self.h, *[_pd(a) for a in arrs]), "pdgpu_update_params")
+
+    # -- state / evaluation ------------------------------------------------
+    def set_positions(self, pos, stride=24):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        ffi.check(self.lib.pdgpu_set_positions(self.h, _pd(pos), stride), "pdgpu_set_positions")
+
+    def set_positions_device(self, ptr):
+        ffi.check(self.lib.pdgpu_set_positions_device(self.h, ctypes.c_void_p(ptr)), "pdgpu_set_positions_device")
+
+    def get_positions(self):
+        out = np.zeros((self.natom, 3))
+        ffi.check(self.lib.pdgpu_get_positions(self.h, _pd(out), 24), "pdgpu_get_positions")
+        return out
+
+    def rebuild_list(self):
+        ffi.check(self.lib.pdgpu_rebuild_list(self.h), "pdgpu_rebuild_list")
+
+    def compute(self, what, forces=None):
+        """Energies (list of dicts, one per system, J) and forces ADDED into `forces` (N)."""
+        E = (ffi.Energies * self.nsystems)()
+        fp = None
+        if forces is not None:
+            assert forces.dtype == np.float64 and forces.flags.c_contiguous and forces.shape == (self.natom, 3)
+            fp = _pd(forces)
+        ffi.check(self.lib.pdgpu_compute(self.h, what, E, fp, 24), "pdgpu_compute")
+        return [e.as_dict() for e in E]
+
+    def compute_device(self, what, dptr=None):
+        ffi.check(self.lib.pdgpu_compute_device(self.h, what, None if dptr is None else ctypes.c_void_p(dptr)),
+                  "pdgpu_compute_device")
+
+    def energies(self):
+        E = (ffi.Energies * self.nsystems)()
+        ffi.check(self.lib.pdgpu_get_energies(self.h, E), "pdgpu_get_energies")
+        return [e.as_dict() for e in E]
+
+    def born_radii(self):
+        out = np.zeros(self.natom)
+        ffi.check(self.lib.pdgpu_get_born_radii(self.h, _pd(out)), "pdgpu_get_born_radii")
+        return out
+
+    def sasa(self):
+        out = np.zeros(self.natom)
+        ffi.check(self.lib.pdgpu_get_sasa(self.h, _pd(out)), "pdgpu_get_sasa")
+        return out
+
+    def list_stats(self):
+        a, b, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        ffi.check(self.lib.pdgpu_list_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+                  "pdgpu_list_stats")
+        return {"tiles": a.value, "masked_tiles": b.value, "slots": c.value}
+
+    def stream(self):
+        return self.lib.pdgpu_stream(self.h)

@@ -1,0 +1,127 @@
+"""ctypes binding to libpdgpu.so (include/pdgpu.h).
+
+The library is built in-tree (pd_gb300/_build/libpdgpu.so) by pd_gb300.build.
+There is no fallback: if the library cannot be loaded, every entry point raises.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+OK = 0
+ERRORS = {
+    -1: "invalid argument", -2: "CUDA runtime error", -3: "LCPO overlap list overflow",
+    -4: "fixed-point accumulator overflow", -5: "NaN energy or force", -6: "device wait timed out",
+    -7: "unsupported option", -8: "stale neighbour list", -9: "call sequence error",
+}
+NB, GB, SA, BONDED = 1, 2, 4, 8
+
+
+class PDGPUError(RuntimeError):
+    """Raised for a non-zero pdgpu status (PD raises ProcedureException / RuntimeError)."""
+
+    def __init__(self, status, where=""):
+        self.status = status
+        super().__init__("%s: pdgpu status %d (%s)" % (where, status, ERRORS.get(status, "unknown")))
+
+
+class Energies(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in ("epot", "vdw", "elec", "pol", "pol_self", "pol_cross", "surf",
+                                                "virial", "bond", "angle", "torsion", "improper")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class SystemDesc(ctypes.Structure):
+    _fields_ = [("nsystems", ctypes.c_int), ("natoms", _ip), ("box", _dp), ("charge", _dp), ("radius", _dp),
+                ("epsilon", _dp), ("mass", _dp), ("gb_radius", _dp), ("gb_vj", _dp), ("gb_terms123", _dp),
+                ("lcpo_radius", _dp), ("lcpo_p", _dp), ("lcpo_sigma", _dp), ("lcpo_use", _ip),
+                ("nexcl", ctypes.c_int), ("excl", _ip),
+                ("nbond", ctypes.c_int), ("bond_idx", _ip), ("bond_par", _dp),
+                ("nangle", ctypes.c_int), ("angle_idx", _ip), ("angle_par", _dp),
+                ("ntors", ctypes.c_int), ("tors_idx", _ip), ("tors_par", _dp),
+                ("nimpr", ctypes.c_int), ("impr_idx", _ip), ("impr_par", _dp)]
+
+
+class NBParams(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in ("Cutoff", "InnerCutoff", "VdwCutoff", "VdwInnerCutoff",
+                                                "Vdw14Scaling", "Elec14Scaling", "Dielectric")] + \
+               [(k, ctypes.c_int) for k in ("EnergySwitch", "ForceSwitch", "DoVdw", "DoElec")]
+
+
+class GBParams(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in (
+        "Cutoff", "InnerCutoff", "VdwCutoff", "VdwInnerCutoff", "Vdw14Scaling", "Elec14Scaling",
+        "DielectricSolute", "DielectricSolvent", "GbsaStillCutoff", "ExpApproxThreshold", "BornRadiusOffset",
+        "P4", "P5")]
+
+
+class ListParams(ctypes.Structure):
+    _fields_ = [("Padding", ctypes.c_double), ("check_skin", ctypes.c_int)]
+
+
+# every symbol include/pdgpu.h declares, with its ctypes signature
+SIGNATURES = {
+    "pdgpu_create": ([ctypes.c_int, ctypes.POINTER(SystemDesc), _ip], ctypes.c_void_p),
+    "pdgpu_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "pdgpu_error_string": ([ctypes.c_int], ctypes.c_char_p),
+    "pdgpu_set_nb_params": ([ctypes.c_void_p, ctypes.POINTER(NBParams)], ctypes.c_int),
+    "pdgpu_set_gb_params": ([ctypes.c_void_p, ctypes.POINTER(GBParams)], ctypes.c_int),
+    "pdgpu_set_list_params": ([ctypes.c_void_p, ctypes.POINTER(ListParams)], ctypes.c_int),
+    "pdgpu_update_params": ([ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
+    "pdgpu_set_positions": ([ctypes.c_void_p, _dp, ctypes.c_size_t], ctypes.c_int),
+    "pdgpu_set_positions_device": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "pdgpu_get_positions": ([ctypes.c_void_p, _dp, ctypes.c_size_t], ctypes.c_int),
+    "pdgpu_rebuild_list": ([ctypes.c_void_p], ctypes.c_int),
+    "pdgpu_compute": ([ctypes.c_void_p, ctypes.c_uint, ctypes.POINTER(Energies), _dp, ctypes.c_size_t],
+                      ctypes.c_int),
+    "pdgpu_compute_device": ([ctypes.c_void_p, ctypes.c_uint, ctypes.c_void_p], ctypes.c_int),
+    "pdgpu_get_energies": ([ctypes.c_void_p, ctypes.POINTER(Energies)], ctypes.c_int),
+    "pdgpu_get_born_radii": ([ctypes.c_void_p, _dp], ctypes.c_int),
+    "pdgpu_get_sasa": ([ctypes.c_void_p, _dp], ctypes.c_int),
+    "pdgpu_list_stats": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                          ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+    "pdgpu_stream": ([ctypes.c_void_p], ctypes.c_void_p),
+}
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libpdgpu.so (building it first if allowed).  Raises if it cannot be loaded."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise OSError("libpdgpu.so is not built (%s); run pd_gb300.build.build()" % path)
+        _build.build()
+    try:
+        L = ctypes.CDLL(path)
+    except OSError:
+        if not build_if_missing:
+            raise
+        # a library built for another machine (e.g. another CPU architecture): rebuild here
+        _build.build(force=True)
+        L = ctypes.CDLL(path)
+    for name, (args, res) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def check(status, where):
+    if status != OK:
+        raise PDGPUError(status, where)
+    return status

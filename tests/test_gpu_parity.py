@@ -1,0 +1,176 @@
+"""CUDA path (through the C ABI) against the oracle and PD's own FP64 outputs.
+
+Tolerances (FP32 pair math, 64-bit fixed-point accumulation vs FP64):
+  energies  |dE| / |E| <= 1e-6
+  forces    sqrt(mean |dF|^2) / sqrt(mean |F|^2) <= 1e-5
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err, rel_rms
+from helpers import gb_kwargs, gb_params, list_cutoff, nb_kwargs, nb_params, oracle_system, ref_energy
+
+pytestmark = pytest.mark.gpu
+
+E_TOL = 1e-6
+F_TOL = 1e-5
+
+
+def make_ctx(d, padding=None):
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.workspace import SystemImage
+    im = SystemImage._from_fixture(d)
+    ctx = DeviceContext(im)
+    ctx.set_list(float(d["cfg_padding"][0]) if padding is None else padding)
+    ctx.set_positions(d["pos"])
+    return ctx
+
+
+NB_CASES = [("water_c1", "nb"), ("water_c1", "nbfswitch"), ("water_c1", "nbnormal"), ("water_c1", "nbvdwsplit"),
+            ("peptide30", "nb"), ("peptide30_ap", "nb"), ("peptide120", "nb")]
+
+
+@pytest.mark.parametrize("name,tag", NB_CASES)
+def test_nb_matches_pd(goldens, name, tag):
+    from pd_gb300 import ffi
+    d = goldens[name]
+    ctx = make_ctx(d)
+    ctx.set_nb(**nb_kwargs(d, tag))
+    f = np.zeros((len(d["pos"]), 3))
+    e = ctx.compute(ffi.NB, f)[0]
+    ref_f = d[tag + "_f"]
+    for k in ("vdw", "elec", "epot"):
+        assert rel_err(e[k], ref_energy(d, tag, k)) <= E_TOL, (k, e[k], ref_energy(d, tag, k))
+    assert rel_err(e["virial"], ref_energy(d, tag, "virial")) <= 1e-5
+    assert rel_rms(f, ref_f) <= F_TOL
+
+
+@pytest.mark.parametrize("name", ["peptide30", "peptide30_ap", "peptide120"])
+def test_gb_matches_pd(goldens, name):
+    from pd_gb300 import ffi
+    d = goldens[name]
+    ctx = make_ctx(d)
+    ctx.set_gb(**gb_kwargs(d))
+    f = np.zeros((len(d["pos"]), 3))
+    e = ctx.compute(ffi.GB, f)[0]
+    born = ctx.born_radii()
+    assert np.max(np.abs(born / d["gb_born"] - 1)) < 1e-6
+    for k in ("vdw", "elec", "pol", "pol_self", "pol_cross", "epot"):
+        assert rel_err(e[k], ref_energy(d, "gb", k)) <= E_TOL, (k, e[k], ref_energy(d, "gb", k))
+    assert rel_rms(f, d["gb_f"]) <= F_TOL
+
+
+@pytest.mark.parametrize("name", ["peptide30", "peptide120"])
+def test_lcpo_matches_pd(goldens, name):
+    from pd_gb300 import ffi
+    d = goldens[name]
+    ctx = make_ctx(d)
+    ctx.set_gb(**gb_kwargs(d))   # list radius as in the fixture (GB + LCPO requests)
+    f = np.zeros((len(d["pos"]), 3))
+    e = ctx.compute(ffi.SA, f)[0]
+    assert rel_err(e["surf"], ref_energy(d, "sasa", "surf")) <= E_TOL
+    sa = ctx.sasa()
+    assert np.max(np.abs(sa - d["lcpo_sasa"])) <= 1e-4 * max(1.0, np.max(d["lcpo_sasa"]))
+    assert rel_rms(f, d["sasa_f"]) <= F_TOL
+
+
+@pytest.mark.parametrize("name", ["water_c1", "peptide30", "peptide120"])
+def test_bonded_matches_pd(goldens, name):
+    from pd_gb300 import ffi
+    d = goldens[name]
+    ctx = make_ctx(d)
+    ctx.set_nb(**nb_kwargs(d, "nb"))
+    f = np.zeros((len(d["pos"]), 3))
+    e = ctx.compute(ffi.BONDED, f)[0]
+    tot = e["bond"] + e["angle"] + e["torsion"] + e["improper"]
+    assert rel_err(tot, ref_energy(d, "bonded", "epot")) <= 1e-5
+    assert rel_rms(f, d["bonded_f"]) <= 1e-5
+
+
+def test_deterministic_and_forces_add(goldens):
+    from pd_gb300 import ffi
+    d = goldens["peptide120"]
+    ctx = make_ctx(d)
+    ctx.set_gb(**gb_kwargs(d))
+    f1 = np.zeros((len(d["pos"]), 3))
+    e1 = ctx.compute(ffi.GB | ffi.SA, f1)
+    f2 = np.zeros((len(d["pos"]), 3))
+    e2 = ctx.compute(ffi.GB | ffi.SA, f2)
+    assert np.array_equal(f1, f2) and e1 == e2
+    ctx.compute(ffi.GB | ffi.SA, f2)          # forces are ADDED, as PD components add into atom[i].f
+    assert np.array_equal(f2, 2 * f1)
+
+
+def test_batch_equals_separate_systems(goldens):
+    """Several systems in one context give each system's own result (tiles never cross systems)."""
+    from pd_gb300 import ffi
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.workspace import SystemImage
+    names = ["peptide30", "peptide120", "peptide30_ap"]
+    ims = [SystemImage._from_fixture(goldens[n]) for n in names]
+    batch = SystemImage.concat(ims)
+    ctx = DeviceContext(batch)
+    ctx.set_list(2.0)
+    ctx.set_gb(**gb_kwargs(goldens["peptide30"]))
+    ctx.set_positions(np.concatenate([goldens[n]["pos"] for n in names]))
+    f = np.zeros((batch.natom, 3))
+    eb = ctx.compute(ffi.GB, f)
+    o = batch.offsets
+    for k, n in enumerate(names):
+        c1 = make_ctx(goldens[n])
+        c1.set_gb(**gb_kwargs(goldens["peptide30"]))
+        f1 = np.zeros((len(goldens[n]["pos"]), 3))
+        e1 = c1.compute(ffi.GB, f1)[0]
+        assert np.array_equal(f[o[k]:o[k + 1]], f1)
+        assert eb[k] == e1
+
+
+def test_stale_list_is_reported(goldens):
+    from pd_gb300 import ffi
+    d = goldens["water_c1"]
+    ctx = make_ctx(d)
+    ctx.set_nb(**nb_kwargs(d, "nb"))
+    ctx.compute(ffi.NB)
+    p = d["pos"].copy()
+    p[0] += 1.5          # further than Padding/2 = 1 A
+    ctx.set_positions(p)
+    with pytest.raises(ffi.PDGPUError) as ei:
+        ctx.compute(ffi.NB)
+    assert ei.value.status == -8
+    ctx.rebuild_list()
+    ctx.compute(ffi.NB)
+
+
+def test_nan_is_reported(goldens):
+    from pd_gb300 import ffi
+    d = goldens["peptide30"]
+    ctx = make_ctx(d)
+    ctx.set_nb(**nb_kwargs(d, "nb"))
+    p = d["pos"].copy()
+    p[5] = p[40]        # two non-bonded atoms on top of each other
+    ctx.set_positions(p)
+    ctx.rebuild_list()
+    with pytest.raises(ffi.PDGPUError):
+        ctx.compute(ffi.NB)
+
+
+def test_forcefield_mirror_matches_pd(goldens):
+    """PD-style use: WorkSpace + Forcefield.add(...) + calcForces, results in wspace.ene / cur.f."""
+    import pd_gb300 as pdg
+    d = goldens["peptide30"]
+    ws = pdg.WorkSpace(pdg.SystemImage._from_fixture(d))
+    ws.Padding = 2.0
+    ff = pdg.Forcefield(ws)
+    gb = pdg.FF_GeneralizedBorn_Still_GPU(ws)
+    gb.Cutoff, gb.InnerCutoff = 12.0, 9.0
+    gb.VdwCutoff, gb.VdwInnerCutoff = 12.0, 9.0
+    sasa = pdg.FF_SASA_LCPO_GPU(ws)
+    sasa.GlobalASP = 0.005
+    ff.add(gb)
+    ff.add(sasa)
+    ff.calcForces()
+    ref = ref_energy(d, "gb", "epot") + ref_energy(d, "sasa", "epot")
+    assert rel_err(ws.ene.epot, ref) <= E_TOL
+    assert rel_rms(ws.cur.f, d["gb_f"] + d["sasa_f"]) <= F_TOL
+    assert rel_err(ws.ene.epot_pol, ref_energy(d, "gb", "pol")) <= E_TOL
+    assert rel_err(ws.ene.epot_surf, ref_energy(d, "sasa", "surf")) <= E_TOL

@@ -1,0 +1,88 @@
+"""The FP64 C restatement (oracle/) against PD's own outputs (tests/golden/)."""
+import numpy as np
+import pytest
+
+from conftest import rel_err, rel_rms
+from helpers import gb_params, list_cutoff, nb_params, oracle_system, ref_energy
+from oracle import pdoracle as O
+
+NB_TAGS = [("water_c1", "nb"), ("water_c1", "nbfswitch"), ("water_c1", "nbnormal"), ("water_c1", "nbvdwsplit"),
+           ("peptide30", "nb"), ("peptide30_ap", "nb"), ("peptide120", "nb")]
+
+
+@pytest.mark.parametrize("name,tag", NB_TAGS)
+def test_nonbonded_matches_pd(goldens, name, tag):
+    d = goldens[name]
+    e, f = O.nonbonded(oracle_system(d), nb_params(d, tag))
+    for i, k in enumerate(("epot", "vdw", "elec")):
+        assert rel_err(e[i], ref_energy(d, tag, k)) < 1e-12
+    assert rel_err(e[7], ref_energy(d, tag, "virial")) < 1e-12
+    assert rel_rms(f, d[tag + "_f"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["water_c1", "peptide30", "peptide120"])
+def test_list_checksums_match_pd(goldens, name):
+    d = goldens[name]
+    c, s1, s2 = O.list_checksums(oracle_system(d), list_cutoff(d))
+    assert np.array_equal(c, d["nl_n"]) and np.array_equal(s1, d["nl_sumj"]) and np.array_equal(s2, d["nl_sumj2"])
+
+
+@pytest.mark.parametrize("name", ["peptide30", "peptide30_ap", "peptide120"])
+def test_gb_matches_pd(goldens, name):
+    d = goldens[name]
+    p = gb_params(d)
+    vj, t = O.gb_fixed_terms(d["gb_radius"], d["cov12"], d["cov12d"], d["cov13"], d["cov13d"], p)
+    assert np.max(np.abs(vj - d["gb_vj"])) <= 1e-12 * np.max(np.abs(d["gb_vj"]))
+    assert np.max(np.abs(t - d["gb_terms123"])) <= 1e-12 * np.max(np.abs(d["gb_terms123"]))
+    e, f, born = O.gb_forces(oracle_system(d), p, d["gb_radius"], d["gb_vj"], d["gb_terms123"])
+    assert np.max(np.abs(born / d["gb_born"] - 1)) < 1e-12
+    for i, k in enumerate(("epot", "vdw", "elec", "pol", "pol_self", "pol_cross")):
+        assert rel_err(e[i], ref_energy(d, "gb", k)) < 1e-12, k
+    assert rel_rms(f, d["gb_f"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["peptide30", "peptide120"])
+def test_lcpo_matches_pd(goldens, name):
+    d = goldens[name]
+    e, f, sa = O.lcpo_forces(oracle_system(d), list_cutoff(d), d["lcpo_radius"], d["lcpo_P"], d["lcpo_sigma"],
+                             d["lcpo_use"])
+    assert rel_err(e[6], ref_energy(d, "sasa", "surf")) < 1e-12
+    assert np.max(np.abs(sa - d["lcpo_sasa"])) < 1e-9
+    assert rel_rms(f, d["sasa_f"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["water_c1", "peptide30", "peptide120"])
+def test_bonded_matches_pd(goldens, name):
+    d = goldens[name]
+    ene, f = O.bonded(d["pos"], d["bond_idx"], d["bond_par"], d["angle_idx"], d["angle_par"], d["torsion_idx"],
+                      d["torsion_par"], d["improper_idx"], d["improper_par"])
+    assert rel_err(ene.sum(), ref_energy(d, "bonded", "epot")) < 1e-10
+    assert rel_rms(f, d["bonded_f"]) < 1e-9
+
+
+@pytest.mark.parametrize("mode", ["eswitch", "fswitch", "normal"])
+def test_pair_law_scan(goldens, mode):
+    """FF_NonBonded::calc_LJ_Coulomb_Force r-scan (nonbonded.cpp:400-534)."""
+    scan = goldens["water_c1"]["scan_" + mode]
+    p = O.nb_params(Cutoff=12, InnerCutoff=9, VdwCutoff=12, VdwInnerCutoff=9, EnergySwitch=int(mode == "eswitch"),
+                    ForceSwitch=int(mode == "fswitch"))
+    eps = 1.0 / (1 / 4184.0 * 6.0221418e23)
+    for r, vp, vf, ep, ef in scan[::7]:
+        got = O.pair_law(p, r, 3.0, eps, 1.0, 1.0)
+        for g, ref in zip(got, (vp, vf, ep, ef)):
+            assert abs(g - ref) <= 1e-12 * max(abs(ref), 1e-30) + 1e-300
+
+
+def test_oracle_threads_agree(goldens):
+    d = goldens["peptide120"]
+    s = oracle_system(d)
+    e1, f1, _ = O.gb_forces(s, gb_params(d), d["gb_radius"], d["gb_vj"], d["gb_terms123"], nthreads=1)
+    e4, f4, _ = O.gb_forces(s, gb_params(d), d["gb_radius"], d["gb_vj"], d["gb_terms123"], nthreads=4)
+    assert np.allclose(e1, e4, rtol=1e-12) and rel_rms(f4, f1) < 1e-12
+
+
+def test_langevin_coefficients_branches():
+    """Taylor branch (gamma*dt <= 0.05) and exponential branch agree near the switch point."""
+    a = O.langevin_coeffs(1e13, 0.0499e-14)
+    b = O.langevin_coeffs(1e13, 0.0501e-14)
+    assert np.allclose(a[:3], b[:3], rtol=1e-2)
