@@ -40,6 +40,7 @@ extern "C" {
 #define PDGPU_GB 2u      /* FF_GeneralizedBorn_Still, FastMode (incl. vacuum LJ/Coulomb) */
 #define PDGPU_SA 4u      /* FF_SASA_LCPO                                        */
 #define PDGPU_BONDED 8u  /* FF_Bonded: bonds, angles, torsions, impropers       */
+#define PDGPU_ENERGY 0x100u /* pdgpu_compute_device: also form the energies (in FP64) */
 
 /* Per-system energies in J per molecule; the fields mirror PD's Hamiltonian
  * (src/mmlib/workspace/hamiltonian.h:43-66). */
@@ -137,8 +138,10 @@ int pdgpu_rebuild_list(pdgpu_ctx *ctx);
  * into WorkSpace::cur.atom[i].f. */
 int pdgpu_compute(pdgpu_ctx *ctx, unsigned what, pdgpu_energies *out, double *f, size_t stride_bytes);
 /* Device variant: forces in N written (not added) to d_f (packed xyz, device
- * memory) without any host synchronisation; energies stay on the device until
- * pdgpu_get_energies(). */
+ * memory) without any host synchronisation.  Energies are formed only when
+ * `what` includes PDGPU_ENERGY and stay on the device until pdgpu_get_energies().
+ * Forces are FP32 pair math with 64-bit fixed-point sums; energies, when
+ * requested, are formed per pair in FP64. */
 int pdgpu_compute_device(pdgpu_ctx *ctx, unsigned what, double *d_f);
 int pdgpu_get_energies(pdgpu_ctx *ctx, pdgpu_energies *out);
 /* Born radii (Angstrom, original atom order) and LCPO per-atom SASA (A^2) from

@@ -39,6 +39,39 @@ __device__ __forceinline__ float3 cross(float3 a, float3 b) {
 }
 __device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 
+// PD's dihedral energy in FP64 (energy evaluations only)
+__device__ double dihedral_energy_d(const BondedView& b, const int* idx, const double* par) {
+  int ti = idx[0], ta = idx[1], tb = idx[2], tj = idx[3], terms = idx[4];
+  double v1[3], v2[3], v3[3];
+  for (int c = 0; c < 3; c++) {
+    v1[c] = b.pos[3 * ti + c] - b.pos[3 * ta + c];
+    v2[c] = b.pos[3 * ta + c] - b.pos[3 * tb + c];
+    v3[c] = b.pos[3 * tb + c] - b.pos[3 * tj + c];
+  }
+  double n1[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2], v1[0] * v2[1] - v1[1] * v2[0]};
+  double n2[3] = {v2[1] * v3[2] - v2[2] * v3[1], v2[2] * v3[0] - v2[0] * v3[2], v2[0] * v3[1] - v2[1] * v3[0]};
+  double n3[3] = {v2[1] * n1[2] - v2[2] * n1[1], v2[2] * n1[0] - v2[0] * n1[2], v2[0] * n1[1] - v2[1] * n1[0]};
+  double m1 = sqrt(n1[0] * n1[0] + n1[1] * n1[1] + n1[2] * n1[2]);
+  double m2 = sqrt(n2[0] * n2[0] + n2[1] * n2[1] + n2[2] * n2[2]);
+  double m3 = sqrt(n3[0] * n3[0] + n3[1] * n3[1] + n3[2] * n3[2]);
+  double cphi = (n1[0] * n2[0] + n1[1] * n2[1] + n1[2] * n2[2]) / (m1 * m2);
+  double sphi = (n3[0] * n2[0] + n3[1] * n2[1] + n3[2] * n2[2]) / (m3 * m2);
+  double phi = -atan2(sphi, cphi);
+  double E = 0;
+  for (int t = 0; t < terms; t++) {
+    double k = par[3 * t], n = par[3 * t + 1], g = par[3 * t + 2];
+    if (n > 0) {
+      E += k * (1.0 + cos(n * phi + g));
+    } else {
+      double diff = phi - g;
+      if (diff < -3.14159265358979323846) diff += 2 * 3.14159265358979323846;
+      else if (diff > 3.14159265358979323846) diff -= 2 * 3.14159265358979323846;
+      E += k * diff * diff;
+    }
+  }
+  return E;
+}
+
 __device__ float dihedral(const BondedView& b, const int* idx, const double* par) {
   int ti = idx[0], ta = idx[1], tb = idx[2], tj = idx[3], terms = idx[4];
   float3 v1 = dvec(b.pos, ti, ta), v2 = dvec(b.pos, ta, tb), v3 = dvec(b.pos, tb, tj);
@@ -81,11 +114,12 @@ __device__ float dihedral(const BondedView& b, const int* idx, const double* par
   return E;
 }
 
+template <bool ENERGY>
 __global__ void k_bonded(BondedView b) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   int total = b.nbond + b.nangle + b.ntors + b.nimpr;
   if (t >= total) return;
-  float E = 0.f;
+  double E = 0.0;
   int slot, sys;
   if (t < b.nbond) {
     int i = b.bidx[2 * t], j = b.bidx[2 * t + 1];
@@ -93,7 +127,7 @@ __global__ void k_bonded(BondedView b) {
     double vx = b.pos[3 * i] - b.pos[3 * j], vy = b.pos[3 * i + 1] - b.pos[3 * j + 1], vz = b.pos[3 * i + 2] - b.pos[3 * j + 2];
     double d = sqrt(vx * vx + vy * vy + vz * vz);
     double dl = d - l;
-    E = (float)(k * dl * dl);
+    E = k * dl * dl;
     float f = (float)(2.0 * k * dl / d);
     add_force(b, i, -f * (float)vx, -f * (float)vy, -f * (float)vz);
     add_force(b, j, f * (float)vx, f * (float)vy, f * (float)vz);
@@ -112,7 +146,17 @@ __global__ void k_bonded(BondedView b) {
       ct = fminf(1.f, fmaxf(-1.f, ct));
       float th = acosf(ct);
       float st = sinf(th);
-      E = k * (th - theta0) * (th - theta0);
+      if (ENERGY) {
+        double ud[3], wd[3];
+        for (int c = 0; c < 3; c++) {
+          ud[c] = b.pos[3 * i + c] - b.pos[3 * a + c];
+          wd[c] = b.pos[3 * j + c] - b.pos[3 * a + c];
+        }
+        double cd = (ud[0] * wd[0] + ud[1] * wd[1] + ud[2] * wd[2]) /
+                    sqrt((ud[0] * ud[0] + ud[1] * ud[1] + ud[2] * ud[2]) * (wd[0] * wd[0] + wd[1] * wd[1] + wd[2] * wd[2]));
+        double thd = acos(fmin(1.0, fmax(-1.0, cd)));
+        E = b.apar[2 * q + 1] * (thd - b.apar[2 * q]) * (thd - b.apar[2 * q]);
+      }
       float dEdth = 2.f * k * (th - theta0);
       float3 gi, gj;
       gi.x = (ct * u.x / lu - w.x / lw) / (lu * st);
@@ -127,19 +171,21 @@ __global__ void k_bonded(BondedView b) {
     }
   } else if (t < b.nbond + b.nangle + b.ntors) {
     int q = t - b.nbond - b.nangle;
-    E = dihedral(b, b.tidx + 5 * q, b.tpar + 12 * q);
+    dihedral(b, b.tidx + 5 * q, b.tpar + 12 * q);
+    if (ENERGY) E = dihedral_energy_d(b, b.tidx + 5 * q, b.tpar + 12 * q);
     slot = E_TORS;
     sys = b.atom_sys[b.tidx[5 * q]];
   } else {
     int q = t - b.nbond - b.nangle - b.ntors;
-    E = dihedral(b, b.iidx + 5 * q, b.ipar + 12 * q);
+    dihedral(b, b.iidx + 5 * q, b.ipar + 12 * q);
+    if (ENERGY) E = dihedral_energy_d(b, b.iidx + 5 * q, b.ipar + 12 * q);
     slot = E_IMPR;
     sys = b.atom_sys[b.iidx[5 * q]];
   }
-  atomic_add_ll(&b.eacc[(size_t)sys * E_NSLOTS + slot], fix_energy(E));
+  if (ENERGY) atomic_add_ll(&b.eacc[(size_t)sys * E_NSLOTS + slot], fix_energy_d(E));
 }
 
-int launch_bonded(Context& c) {
+int launch_bonded(Context& c, bool energy) {
   BondedView b;
   b.slot_of = c.d_slot_of.p;
   b.atom_sys = c.d_atom_sys.p;
@@ -151,7 +197,8 @@ int launch_bonded(Context& c) {
   b.bpar = c.d_bpar.p; b.apar = c.d_apar.p; b.tpar = c.d_tpar.p; b.ipar = c.d_ipar.p;
   int total = c.nbond + c.nangle + c.ntors + c.nimpr;
   if (total == 0) return PDGPU_OK;
-  k_bonded<<<(total + 255) / 256, 256, 0, c.stream>>>(b);
+  if (energy) k_bonded<true><<<(total + 255) / 256, 256, 0, c.stream>>>(b);
+  else k_bonded<false><<<(total + 255) / 256, 256, 0, c.stream>>>(b);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

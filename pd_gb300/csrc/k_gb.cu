@@ -33,6 +33,16 @@ __device__ __forceinline__ unsigned diag_exclusion(int lane) {
 
 #define ROT(x) x = __shfl_sync(0xffffffffu, x, (lane + 1) & 31)
 
+// FP64 squared distance of two sorted slots from the original positions
+__device__ __forceinline__ double r2_slots_fp64(const DevView& v, int sa, int sb) {
+  int a = v.sorted_atom[sa], b = v.sorted_atom[sb];
+  if (a < 0 || b < 0) return 1e300;
+  double dx = v.pos[3 * b] - v.pos[3 * a], dy = v.pos[3 * b + 1] - v.pos[3 * a + 1],
+         dz = v.pos[3 * b + 2] - v.pos[3 * a + 2];
+  return dx * dx + dy * dy + dz * dz;
+}
+
+
 // ---------------------------------------------------------------------------
 // pass 1: Born-radius pair sums  Gpol_i += P4 Vj CCF / r^4  (bond order > 2)
 // ---------------------------------------------------------------------------
@@ -53,7 +63,10 @@ __global__ void __launch_bounds__(256) k_gb_born(DevView v, GBConst k, long long
     for (int kk = 0; kk < 32; kk++) {
       float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
       float r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 <= k.still2 && !((ex >> kk) & 1u)) {
+      bool in = r2 <= k.still2;
+      if (fabsf(r2 - k.still2) <= 2e-6f * k.still2)
+        in = r2_slots_fp64(v, T.bi * 32 + lane, T.bj * 32 + ((lane + kk) & 31)) <= k.still2_d;
+      if (in && !((ex >> kk) & 1u)) {
         float rs = pi.z + pj.z;
         float rdivR = r2 / (rs * rs);
         float ccf = 1.f;
@@ -88,9 +101,53 @@ __global__ void k_gb_radii(DevView v, const double* terms123, const long long* g
   born_d[a] = r;
 }
 
+// Energies of one loop-1 pair (gbff.cpp:1546-1746) in FP64.
+__device__ __forceinline__ void gb_pair_energy(const GBConst& k, const DevView& v, int a, int b, double r2, bool excl,
+                                               bool is14, double& evdw, double& eel, double& epol) {
+  if (r2 > k.cut2_d) return;
+  double r = sqrt(r2), invr = 1.0 / r;
+  double qiqj = v.charge[a] * v.charge[b];
+  double aiaj = v.born[a] * v.born[b];
+  double u = -0.25 * r2 / aiaj;
+  double s14 = is14 ? k.elec14_d : 1.0;
+  double S = 1.0;
+  if (r >= k.inner_d) {
+    double w = r - k.inner_d;
+    double sw = 1.0 - w * w * k.invw2_d;
+    S = sw * sw;
+  }
+  double elec = 0.0;
+  if (u > k.thresh_d) {
+    double t = exp(u);
+    double ep = k.premul_d * qiqj / sqrt(r2 + t * aiaj);
+    if (!excl) elec = k.econv_in_d * s14 * qiqj * invr;
+    epol += 2.0 * ep * S;
+  } else if (!excl) {
+    elec = k.econv_out_d * s14 * qiqj * invr;
+  }
+  if (excl) return;
+  eel += elec * S;
+  if (r < k.vdwcut_d) {
+    double t = (v.radius[a] + v.radius[b]) * invr;
+    double B = t * t;
+    B = B * B * B;
+    double A = B * B;
+    double eps = v.sqeps[a] * v.sqeps[b] * (is14 ? k.vdw14_d : 1.0);
+    double Ev = eps * (A - 2.0 * B);
+    if (r > k.vdwinner_d) {
+      double w = r - k.vdwinner_d;
+      double sw = 1.0 - w * w * k.vdwinvw2_d;
+      Ev *= sw * sw;
+    }
+    evdw += Ev;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // pass 2: GB cross term fused with vacuum LJ + Coulomb, i > j pairs within Cutoff
+// (forces, dE/da in FP32; with ENERGY the pair energies are formed in FP64)
 // ---------------------------------------------------------------------------
+template <bool ENERGY>
 __global__ void __launch_bounds__(256) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -101,29 +158,46 @@ __global__ void __launch_bounds__(256) k_gb_pair(DevView v, GBConst k, const flo
     unsigned ex, m14;
     tile_setup(v, T, lane, xi, xj, ex, m14);
     const unsigned dmask = (T.flags & 2) ? diag_exclusion(lane) : 0u;
-    const float4 pi = v.par[T.bi * 32 + lane];
-    float4 pj = v.par[T.bj * 32 + lane];
-    const float ai = born[T.bi * 32 + lane];
-    float aj = born[T.bj * 32 + lane];
+    const int si = T.bi * 32 + lane, sj = T.bj * 32 + lane;
+    const float4 pi = v.par[si];
+    float4 pj = v.par[sj];
+    const float ai = born[si];
+    float aj = born[sj];
     float fix = 0.f, fiy = 0.f, fiz = 0.f, fjx = 0.f, fjy = 0.f, fjz = 0.f;
     float dai = 0.f, daj = 0.f;
-    float evdw = 0.f, eel = 0.f, epol = 0.f;
+    double evdw = 0.0, eel = 0.0, epol = 0.0;
+    const int atom_i = v.sorted_atom[si];
 #pragma unroll 2
     for (int kk = 0; kk < 32; kk++) {
       float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
       float r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 <= k.cut2 && !((dmask >> kk) & 1u)) {
-        const bool excl = (ex >> kk) & 1u;      // bond order <= 2: GB only
-        const bool is14 = (m14 >> kk) & 1u;
+      const bool pair = !((dmask >> kk) & 1u);
+      const bool excl = (ex >> kk) & 1u;      // bond order <= 2: GB only
+      const bool is14 = (m14 >> kk) & 1u;
+      if (ENERGY && pair) {
+        const int sjk = T.bj * 32 + ((lane + kk) & 31);
+        const int atom_j = v.sorted_atom[sjk];
+        if (atom_i >= 0 && atom_j >= 0)
+          gb_pair_energy(k, v, atom_i, atom_j, r2_slots_fp64(v, si, sjk), excl, is14, evdw, eel, epol);
+      }
+      if (r2 <= k.cut2 && pair) {
         float invr = rsqrtf(r2);
         float r = r2 * invr;
         float qiqj = xi.w * xj.w;
         float aiaj = ai * aj;
         float u = -0.25f * r2 / aiaj;
+        bool gbon = u > k.thresh;
+        if (fabsf(u - k.thresh) <= 2e-6f * fabsf(k.thresh)) {
+          // the exp-approximation switch is discontinuous: decide it in FP64
+          const int sjk = T.bj * 32 + ((lane + kk) & 31);
+          const int atom_j = v.sorted_atom[sjk];
+          if (atom_i >= 0 && atom_j >= 0)
+            gbon = -0.25 * r2_slots_fp64(v, si, sjk) / (v.born[atom_i] * v.born[atom_j]) > k.thresh_d;
+        }
         float g = 0.f;           // scalar multiplying (xj - xi) in the force on i
         float elec = 0.f, delec = 0.f;
         const float s14 = is14 ? k.elec14 : 1.f;
-        if (u > k.thresh) {
+        if (gbon) {
           float tg = expf(u);
           float l = 1.f / (r2 + tg * aiaj);
           float fgb = sqrtf(l);
@@ -140,13 +214,10 @@ __global__ void __launch_bounds__(256) k_gb_pair(DevView v, GBConst k, const flo
             float dS = -4.f * k.invw2 * w * sw;
             float S = sw * sw;
             delec = S * delec + elec * dS;
-            elec *= S;
             dedr = S * dedr + dS * ep;
             dalpha *= S;
-            ep *= S;
           }
           g += 2.f * dedr * invr;
-          epol += ep;
           dai += dalpha * aj;
           daj += dalpha * ai;
         } else if (!excl) {
@@ -158,7 +229,6 @@ __global__ void __launch_bounds__(256) k_gb_pair(DevView v, GBConst k, const flo
             float dS = -4.f * k.invw2 * w * sw;
             float S = sw * sw;
             delec = S * delec + elec * dS;
-            elec *= S;
           }
         }
         if (!excl) {
@@ -177,11 +247,8 @@ __global__ void __launch_bounds__(256) k_gb_pair(DevView v, GBConst k, const flo
               float dS = -4.f * k.vdwinvw2 * w * sw;
               float S = sw * sw;
               dvdw = S * dvdw + Ev * dS;
-              Ev *= S;
             }
-            evdw += Ev;
           }
-          eel += elec;
           g += (dvdw + delec) * invr;
         }
         fix += g * dx; fiy += g * dy; fiz += g * dz;
@@ -193,7 +260,6 @@ __global__ void __launch_bounds__(256) k_gb_pair(DevView v, GBConst k, const flo
     if (!(fabsf(fix) + fabsf(fiy) + fabsf(fiz) + fabsf(fjx) + fabsf(fjy) + fabsf(fjz) + fabsf(dai) + fabsf(daj) <
           1.0e18f))
       atomicOr(v.status, (unsigned)ST_NAN);
-    const int si = T.bi * 32 + lane, sj = T.bj * 32 + lane;
     atomic_add_ll(&v.facc[3 * si], fix_force(fix));
     atomic_add_ll(&v.facc[3 * si + 1], fix_force(fiy));
     atomic_add_ll(&v.facc[3 * si + 2], fix_force(fiz));
@@ -202,9 +268,10 @@ __global__ void __launch_bounds__(256) k_gb_pair(DevView v, GBConst k, const flo
     atomic_add_ll(&v.facc[3 * sj + 2], fix_force(fjz));
     atomic_add_ll(&deda[si], fix_sum(dai));
     atomic_add_ll(&deda[sj], fix_sum(daj));
-    long long e0 = warp_sum_ll(fix_energy(evdw));
-    long long e1 = warp_sum_ll(fix_energy(eel));
-    long long e2 = warp_sum_ll(fix_energy(2.f * epol));
+    if (!ENERGY) continue;
+    long long e0 = warp_sum_ll(fix_energy_d(evdw));
+    long long e1 = warp_sum_ll(fix_energy_d(eel));
+    long long e2 = warp_sum_ll(fix_energy_d(epol));
     if (lane == 0) {
       long long* E = v.eacc + (size_t)v.slot_sys[T.bi] * E_NSLOTS;
       atomic_add_ll(&E[E_VDW], e0);
@@ -255,7 +322,10 @@ __global__ void __launch_bounds__(256) k_gb_chain(DevView v, GBConst k, const fl
     for (int kk = 0; kk < 32; kk++) {
       float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
       float r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 <= k.still2 && !((ex >> kk) & 1u)) {
+      bool in = r2 <= k.still2;
+      if (fabsf(r2 - k.still2) <= 2e-6f * k.still2)
+        in = r2_slots_fp64(v, T.bi * 32 + lane, T.bj * 32 + ((lane + kk) & 31)) <= k.still2_d;
+      if (in && !((ex >> kk) & 1u)) {
         float rs = pi.z + pj.z;
         float rdivR = r2 / (rs * rs);
         float ccf = 1.f, dccf = 0.f;
@@ -292,7 +362,7 @@ static int tile_grid(Context& c) {
   return (int)(want < g ? (want > 0 ? want : 1) : g);
 }
 
-int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset, double premul) {
+int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset, double premul, bool energy) {
   DevView v = c.view();
   cudaStream_t st = c.stream;
   int g = tile_grid(c);
@@ -301,7 +371,8 @@ int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset
   cudaMemsetAsync(c.d_deda.p, 0, sizeof(long long) * c.nslots, st);
   k_gb_born<<<g, 256, 0, st>>>(v, k, c.d_gpol.p);
   k_gb_radii<<<nb, 256, 0, st>>>(v, c.d_gbT.p, c.d_gpol.p, halfeconv, born_offset, c.d_born_f.p, c.d_born_d.p);
-  k_gb_pair<<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
+  if (energy) k_gb_pair<true><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
+  else k_gb_pair<false><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
   k_gb_self<<<nb, 256, 0, st>>>(v, c.d_charge.p, k, premul, c.d_deda.p, c.d_born_d.p, c.d_chain_f.p);
   k_gb_chain<<<g, 256, 0, st>>>(v, k, c.d_chain_f.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
@@ -398,7 +469,7 @@ __device__ __forceinline__ float3 rel_vec(const DevView& v, int a, int b) {
 // per atom i (one warp, lanes over i's overlap partners j): SASA_i and the
 // derivative terms collected on atom i (lcpo.cpp:781-949)
 __global__ void k_lcpo_main(DevView v, const float4* lc, const int* nl_n, const int* nl_idx, const float* nl_s,
-                            const double* P, const double* sigma, double* sasa_out) {
+                            const double* P, const double* sigma, double* sasa_out, int energy) {
   const int lane = threadIdx.x & 31;
   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (s >= v.nslots) return;
@@ -487,11 +558,11 @@ __global__ void k_lcpo_main(DevView v, const float4* lc, const int* nl_n, const 
     // PD adds SASAderiv / Angstrom; the derivative terms already hold d(sigma*SA)
     for (int c = 0; c < 3; c++) atomic_add_ll(&v.facc[3 * s + c], __double2ll_rn(f[c] * kForceScale));
     int sys = v.slot_sys[s >> 5];
-    atomic_add_ll(&v.eacc[(size_t)sys * E_NSLOTS + E_SURF], fix_energy_d(SA * sigma[a]));
+    if (energy) atomic_add_ll(&v.eacc[(size_t)sys * E_NSLOTS + E_SURF], fix_energy_d(SA * sigma[a]));
   }
 }
 
-int launch_lcpo(Context& c) {
+int launch_lcpo(Context& c, bool energy) {
   DevView v = c.view();
   cudaStream_t st = c.stream;
   int g = tile_grid(c);
@@ -501,7 +572,7 @@ int launch_lcpo(Context& c) {
   k_lcpo_sort<<<nw, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_ncand.p, c.d_lc_cand.p, c.d_lc_n.p, c.d_lc_idx.p,
                                    c.d_lc_s.p);
   k_lcpo_main<<<nw, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_n.p, c.d_lc_idx.p, c.d_lc_s.p, c.d_lcpoP.p,
-                                   c.d_lcpoSig.p, c.d_sasa.p);
+                                   c.d_lcpoSig.p, c.d_sasa.p, energy ? 1 : 0);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

@@ -9,24 +9,31 @@
 
 namespace pdgpu {
 
-template <int ELEC>
-__device__ __forceinline__ void nb_pair(const NBConst& k, float r2, float rsum, float eps, float qq, float& ev,
-                                        float& ee, float& dEdr_over_r, float& r_dEdr) {
-  float invr = rsqrtf(r2);
-  float r = r2 * invr;
-  float dv = 0.f, de = 0.f, Ev = 0.f, Ee = 0.f;
-  if (k.dovdw && r < k.vdwcut) {
-    float t = rsum * invr;
-    float B = t * t;
+// Pair law in arithmetic type T (float for forces, double for energies).
+template <typename T, int ELEC>
+__device__ __forceinline__ void nb_pair(const NBConst& k, T r2, T rsum, T eps, T qq, T& ev, T& ee, T& dEdr_over_r,
+                                        T& r_dEdr) {
+  T invr, r;
+  if (sizeof(T) == 4) {
+    invr = rsqrtf((float)r2);
+    r = r2 * invr;
+  } else {
+    r = sqrt((double)r2);
+    invr = (T)1 / r;
+  }
+  T dv = 0, de = 0, Ev = 0, Ee = 0;
+  if (k.dovdw && r < (T)k.vdwcut_d) {
+    T t = rsum * invr;
+    T B = t * t;
     B = B * B * B;
-    float A = B * B;
-    Ev = eps * (A - 2.f * B);
-    dv = -12.f * eps * invr * (A - B);
-    if (r > k.vdwinner) {
-      float u = r - k.vdwinner;
-      float sw = 1.f - u * u * k.vdwinvw2;
-      float dS = -4.f * k.vdwinvw2 * u * sw;
-      float S = sw * sw;
+    T A = B * B;
+    Ev = eps * (A - (T)2 * B);
+    dv = (T)-12 * eps * invr * (A - B);
+    if (r > (T)k.vdwinner_d) {
+      T u = r - (T)k.vdwinner_d;
+      T sw = (T)1 - u * u * (T)k.vdwinvw2_d;
+      T dS = (T)-4 * (T)k.vdwinvw2_d * u * sw;
+      T S = sw * sw;
       dv = S * dv + Ev * dS;
       Ev *= S;
     }
@@ -37,34 +44,50 @@ __device__ __forceinline__ void nb_pair(const NBConst& k, float r2, float rsum, 
   } else if (ELEC == 3) {
     Ee = qq * invr;
     de = -Ee * invr;
-    if (r > k.inner) {
-      float u = r - k.inner;
-      float sw = 1.f - u * u * k.invw2;
-      float dS = -4.f * k.invw2 * u * sw;
-      float S = sw * sw;
+    if (r > (T)k.inner_d) {
+      T u = r - (T)k.inner_d;
+      T sw = (T)1 - u * u * (T)k.invw2_d;
+      T dS = (T)-4 * (T)k.invw2_d * u * sw;
+      T S = sw * sw;
       de = S * de + Ee * dS;
       Ee *= S;
     }
   } else if (ELEC == 4) {
     // Steinbach & Brooks force switch, nonbonded.cpp:798-819
-    if (r > k.inner) {
-      float c2mr2 = k.cut2_d - r2;
-      de = -qq * k.sA * invr * invr * c2mr2 * c2mr2 * (k.cut2_d - 3.f * k.inner2 + 2.f * r2);
-      Ee = -qq * (k.sA * r * (k.sB * invr * invr + k.sC + k.sD * r2 + k.sE * r2 * r2) - k.fsw_cutV);
+    if (r > (T)k.inner_d) {
+      T c2mr2 = (T)k.cut2_d - r2;
+      de = -qq * (T)k.sA * invr * invr * c2mr2 * c2mr2 * ((T)k.cut2_d - (T)3 * (T)k.inner2_d + (T)2 * r2);
+      Ee = -qq * ((T)k.sA * r * ((T)k.sB * invr * invr + (T)k.sC + (T)k.sD * r2 + (T)k.sE * r2 * r2) - (T)k.fsw_cutV);
     } else {
       de = -qq * invr * invr;
-      Ee = qq * (invr - k.eshift);
+      Ee = qq * (invr - (T)k.eshift);
     }
   }
   ev += Ev;
   ee += Ee;
-  float d = dv + de;
+  T d = dv + de;
   dEdr_over_r = d * invr;
   r_dEdr = r * d;
 }
 
+// FP64 squared distance of two sorted slots from the original positions
+// (minimum image in a periodic box); used for energies and for pairs whose
+// FP32 distance lies within 2e-6 of a hard cutoff.
+__device__ __forceinline__ double r2_fp64(const DevView& v, const SystemInfo& S, int sa, int sb) {
+  int a = v.sorted_atom[sa], b = v.sorted_atom[sb];
+  if (a < 0 || b < 0) return 1e300;
+  double r2 = 0;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    double d = v.pos[3 * b + c] - v.pos[3 * a + c];
+    if (S.periodic) d -= S.box[c] * rint(d / S.box[c]);
+    r2 += d * d;
+  }
+  return r2;
+}
+
 // One warp per tile, grid-stride over tiles.
-template <int ELEC>
+template <int ELEC, bool ENERGY>
 __global__ void __launch_bounds__(256) k_nb_tiles(DevView v, NBConst k) {
   const int lane = threadIdx.x & 31;
   const int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -103,8 +126,9 @@ __global__ void __launch_bounds__(256) k_nb_tiles(DevView v, NBConst k) {
     }
     if (diag) ex |= ~((lane == 0) ? 0xffffffffu : ((1u << (32 - lane)) - 1u)) | 1u;  // keep only lane+k < 32, k > 0
     float fix = 0.f, fiy = 0.f, fiz = 0.f, fjx = 0.f, fjy = 0.f, fjz = 0.f;
-    float ev = 0.f, ee = 0.f, vir = 0.f;
+    double ev = 0.0, ee = 0.0, vir = 0.0;
     const float qi = xi.w * k.econv_diel;
+    const int ai = ENERGY ? v.sorted_atom[si] : 0;
 #pragma unroll 4
     for (int kk = 0; kk < 32; kk++) {
       float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
@@ -114,13 +138,29 @@ __global__ void __launch_bounds__(256) k_nb_tiles(DevView v, NBConst k) {
         dz -= Lz * rintf(dz / Lz);
       }
       float r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 <= k.cut2 && !((ex >> kk) & 1u)) {
+      const bool listed = !((ex >> kk) & 1u);
+      bool in = r2 <= k.cut2;
+      double r2d = 0.0;
+      if (listed && (ENERGY || fabsf(r2 - k.cut2) <= 2e-6f * k.cut2 || fabsf(r2 - k.vdwcut2) <= 2e-6f * k.vdwcut2)) {
+        r2d = r2_fp64(v, S, si, T.bj * 32 + ((lane + kk) & 31));
+        in = r2d <= k.cut2_dd;
+      }
+      if (listed && in) {
         bool is14 = (m14 >> kk) & 1u;
         float eps = pi.y * pj.y * (is14 ? k.vdw14 : 1.f);
         float qq = qi * xj.w * (is14 ? k.elec14 : 1.f);
-        float fs, rd;
-        nb_pair<ELEC>(k, r2, pi.x + pj.x, eps, qq, ev, ee, fs, rd);
-        vir += rd;
+        float fs, rd, evf = 0.f, eef = 0.f;
+        if (r2d > 0.0 && !ENERGY) r2 = (float)r2d;
+        nb_pair<float, ELEC>(k, r2, pi.x + pj.x, eps, qq, evf, eef, fs, rd);
+        if (ENERGY) {
+          // energy of this pair in FP64 from FP64 positions and parameters
+          const int aj = v.sorted_atom[T.bj * 32 + ((lane + kk) & 31)];
+          double fsd, rdd;
+          double epsd = v.sqeps[ai] * v.sqeps[aj] * (is14 ? k.vdw14_d : 1.0);
+          double qqd = v.charge[ai] * v.charge[aj] * k.econv_diel_d * (is14 ? k.elec14_d : 1.0);
+          nb_pair<double, ELEC>(k, r2d, v.radius[ai] + v.radius[aj], epsd, qqd, ev, ee, fsd, rdd);
+          vir += rdd;
+        }
         fix += fs * dx; fiy += fs * dy; fiz += fs * dz;
         fjx -= fs * dx; fjy -= fs * dy; fjz -= fs * dz;
       }
@@ -144,9 +184,10 @@ __global__ void __launch_bounds__(256) k_nb_tiles(DevView v, NBConst k) {
     atomic_add_ll(&v.facc[3 * sj], fix_force(fjx));
     atomic_add_ll(&v.facc[3 * sj + 1], fix_force(fjy));
     atomic_add_ll(&v.facc[3 * sj + 2], fix_force(fjz));
-    long long e0 = warp_sum_ll(fix_energy(ev));
-    long long e1 = warp_sum_ll(fix_energy(ee));
-    long long e2 = warp_sum_ll(fix_energy(vir));
+    if (!ENERGY) continue;
+    long long e0 = warp_sum_ll(fix_energy_d(ev));
+    long long e1 = warp_sum_ll(fix_energy_d(ee));
+    long long e2 = warp_sum_ll(fix_energy_d(vir));
     if (lane == 0) {
       long long* E = v.eacc + (size_t)sidx * E_NSLOTS;
       atomic_add_ll(&E[E_VDW], e0);
@@ -165,15 +206,21 @@ static int grid_for_tiles(Context& c) {
   return (int)(want < g ? (want > 0 ? want : 1) : g);
 }
 
-int launch_nb(Context& c, const NBConst& k, bool) {
+template <bool E>
+static void launch_nb_mode(Context& c, const NBConst& k, int g) {
   DevView v = c.view();
-  int g = grid_for_tiles(c);
   switch (k.elecmode) {
-    case 0: k_nb_tiles<0><<<g, 256, 0, c.stream>>>(v, k); break;
-    case 1: k_nb_tiles<1><<<g, 256, 0, c.stream>>>(v, k); break;
-    case 3: k_nb_tiles<3><<<g, 256, 0, c.stream>>>(v, k); break;
-    default: k_nb_tiles<4><<<g, 256, 0, c.stream>>>(v, k); break;
+    case 0: k_nb_tiles<0, E><<<g, 256, 0, c.stream>>>(v, k); break;
+    case 1: k_nb_tiles<1, E><<<g, 256, 0, c.stream>>>(v, k); break;
+    case 3: k_nb_tiles<3, E><<<g, 256, 0, c.stream>>>(v, k); break;
+    default: k_nb_tiles<4, E><<<g, 256, 0, c.stream>>>(v, k); break;
   }
+}
+
+int launch_nb(Context& c, const NBConst& k, bool energy) {
+  int g = grid_for_tiles(c);
+  if (energy) launch_nb_mode<true>(c, k, g);
+  else launch_nb_mode<false>(c, k, g);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

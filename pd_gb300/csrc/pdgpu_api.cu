@@ -65,27 +65,32 @@ NBConst make_nb_const(const pdgpu_nb_params& p) {
   NBConst k{};
   double C = p.Cutoff, I = p.InnerCutoff;
   k.cut2 = (float)(C * C);
-  k.vdwcut = (float)p.VdwCutoff;
-  k.vdwinner = (float)p.VdwInnerCutoff;
-  k.inner = (float)I;
+  k.cut2_dd = C * C;
+  k.vdwcut2 = (float)(p.VdwCutoff * p.VdwCutoff);
+  k.vdwcut_d = p.VdwCutoff;
+  k.vdwinner_d = p.VdwInnerCutoff;
+  k.inner_d = I;
   double vw = p.VdwCutoff - p.VdwInnerCutoff, w = C - I;
-  k.vdwinvw2 = vw > 0 ? (float)(1.0 / (vw * vw)) : 0.f;
-  k.invw2 = w > 0 ? (float)(1.0 / (w * w)) : 0.f;
-  k.econv_diel = (float)(econv_kcal() / p.Dielectric);
+  k.vdwinvw2_d = vw > 0 ? 1.0 / (vw * vw) : 0.0;
+  k.invw2_d = w > 0 ? 1.0 / (w * w) : 0.0;
+  k.econv_diel_d = econv_kcal() / p.Dielectric;
+  k.econv_diel = (float)k.econv_diel_d;
   k.vdw14 = (float)p.Vdw14Scaling;
   k.elec14 = (float)p.Elec14Scaling;
+  k.vdw14_d = p.Vdw14Scaling;
+  k.elec14_d = p.Elec14Scaling;
   // Steinbach-Brooks force-switch constants (nonbonded.cpp:620-636)
   double C2 = C * C, I2 = I * I;
-  double sA = 1.0 / ((C2 - I2) * (C2 - I2) * (C2 - I2));
-  double sB = -(C2 * C2 * C2 - 3.0 * C2 * C2 * I2);
-  double sC = 6.0 * C2 * I2, sD = -(C2 + I2), sE = 2.0 / 5.0;
-  double innerV = sA * (sB / I + sC * I + sD * I * I * I + sE * I * I * I * I * I);
-  double cutV = sA * (sB / C + sC * C + sD * C * C * C + sE * C * C * C * C * C);
-  k.sA = (float)sA; k.sB = (float)sB; k.sC = (float)sC; k.sD = (float)sD; k.sE = (float)sE;
-  k.fsw_cutV = (float)cutV;
-  k.eshift = (float)(I < C ? 1.0 / I + (innerV - cutV) : 0.0);
-  k.cut2_d = (float)C2;
-  k.inner2 = (float)I2;
+  k.sA = 1.0 / ((C2 - I2) * (C2 - I2) * (C2 - I2));
+  k.sB = -(C2 * C2 * C2 - 3.0 * C2 * C2 * I2);
+  k.sC = 6.0 * C2 * I2;
+  k.sD = -(C2 + I2);
+  k.sE = 2.0 / 5.0;
+  double innerV = k.sA * (k.sB / I + k.sC * I + k.sD * I * I * I + k.sE * I * I * I * I * I);
+  k.fsw_cutV = k.sA * (k.sB / C + k.sC * C + k.sD * C * C * C + k.sE * C * C * C * C * C);
+  k.eshift = I < C ? 1.0 / I + (innerV - k.fsw_cutV) : 0.0;
+  k.cut2_d = C2;
+  k.inner2_d = I2;
   k.elecmode = 1;
   if (p.EnergySwitch) k.elecmode = 3;
   if (p.ForceSwitch) k.elecmode = 4;
@@ -116,6 +121,19 @@ GBConst make_gb_const(const pdgpu_gb_params& p, double listR) {
   k.P4 = (float)p.P4;
   k.P5 = (float)p.P5;
   k.invP5 = (float)(1.0 / p.P5);
+  k.cut2_d = C * C;
+  k.inner_d = I;
+  k.invw2_d = w > 0 ? 1.0 / (w * w) : 0.0;
+  k.vdwcut_d = p.VdwCutoff;
+  k.vdwinner_d = p.VdwInnerCutoff;
+  k.vdwinvw2_d = vw > 0 ? 1.0 / (vw * vw) : 0.0;
+  k.still2_d = still * still;
+  k.econv_in_d = ec / p.DielectricSolute;
+  k.econv_out_d = ec / p.DielectricSolvent;
+  k.premul_d = -0.5 * ec * (1.0 / p.DielectricSolute - 1.0 / p.DielectricSolvent);
+  k.vdw14_d = p.Vdw14Scaling;
+  k.elec14_d = p.Elec14Scaling;
+  k.thresh_d = p.ExpApproxThreshold;
   return k;
 }
 
@@ -278,6 +296,22 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
   if (c.nangle && (!d->angle_idx || !d->angle_par)) return bad(PDGPU_ERR_ARG);
   if (c.ntors && (!d->tors_idx || !d->tors_par)) return bad(PDGPU_ERR_ARG);
   if (c.nimpr && (!d->impr_idx || !d->impr_par)) return bad(PDGPU_ERR_ARG);
+  {
+    // every bonded index must name an atom of this batch
+    auto in_range = [&](const int* idx, int count, int width, int used) {
+      for (int k = 0; k < count; k++)
+        for (int w = 0; w < used; w++)
+          if (idx[(size_t)k * width + w] < 0 || idx[(size_t)k * width + w] >= N) return false;
+      return true;
+    };
+    if (!in_range(d->bond_idx, c.nbond, 2, 2) || !in_range(d->angle_idx, c.nangle, 3, 3) ||
+        !in_range(d->tors_idx, c.ntors, 5, 4) || !in_range(d->impr_idx, c.nimpr, 5, 4))
+      return bad(PDGPU_ERR_ARG);
+    for (int k = 0; k < c.ntors; k++)
+      if (d->tors_idx[5 * k + 4] < 0 || d->tors_idx[5 * k + 4] > 4) return bad(PDGPU_ERR_ARG);
+    for (int k = 0; k < c.nimpr; k++)
+      if (d->impr_idx[5 * k + 4] < 0 || d->impr_idx[5 * k + 4] > 4) return bad(PDGPU_ERR_ARG);
+  }
   {
     std::vector<double> bp(2 * (size_t)c.nbond), ap(2 * (size_t)c.nangle), tp(12 * (size_t)c.ntors),
         ip(12 * (size_t)c.nimpr);
@@ -475,7 +509,7 @@ int pdgpu_rebuild_list(pdgpu_ctx* h) {
   return rebuild_list(h->c);
 }
 
-static int enqueue_compute(Context& c, unsigned what) {
+static int enqueue_compute(Context& c, unsigned what, bool energy) {
   if (!c.positions_set) return PDGPU_ERR_STATE;
   if ((what & PDGPU_NB) && !c.nb_set) return PDGPU_ERR_STATE;
   if ((what & PDGPU_GB) && (!c.has_gb || !c.gb_set)) return PDGPU_ERR_STATE;
@@ -492,15 +526,15 @@ static int enqueue_compute(Context& c, unsigned what) {
   CK(cudaMemsetAsync(c.d_facc.p, 0, sizeof(long long) * 3 * c.nslots, c.stream));
   CK(cudaMemsetAsync(c.d_eacc.p, 0, sizeof(long long) * E_NSLOTS * c.nsys, c.stream));
   int st = PDGPU_OK;
-  if (what & PDGPU_NB) st = launch_nb(c, make_nb_const(c.nb), true);
+  if (what & PDGPU_NB) st = launch_nb(c, make_nb_const(c.nb), energy);
   if (st == PDGPU_OK && (what & PDGPU_GB)) {
     GBConst k = make_gb_const(c.gb, c.list_radius_built);
     double ec = econv_kcal();
     double premul = -0.5 * ec * (1.0 / c.gb.DielectricSolute - 1.0 / c.gb.DielectricSolvent);
-    st = launch_gb(c, k, 0.5 * ec, c.gb.BornRadiusOffset, premul);
+    st = launch_gb(c, k, 0.5 * ec, c.gb.BornRadiusOffset, premul, energy);
   }
-  if (st == PDGPU_OK && (what & PDGPU_SA)) st = launch_lcpo(c);
-  if (st == PDGPU_OK && (what & PDGPU_BONDED)) st = launch_bonded(c);
+  if (st == PDGPU_OK && (what & PDGPU_SA)) st = launch_lcpo(c, energy);
+  if (st == PDGPU_OK && (what & PDGPU_BONDED)) st = launch_bonded(c, energy);
   return st;
 }
 
@@ -535,7 +569,7 @@ int pdgpu_compute(pdgpu_ctx* h, unsigned what, pdgpu_energies* out, double* f, s
   if (!h || (f && (stride < 24 || stride % 8))) return PDGPU_ERR_ARG;
   Context& c = h->c;
   CK(cudaSetDevice(c.device));
-  int st = enqueue_compute(c, what);
+  int st = enqueue_compute(c, what, out != nullptr);
   if (st != PDGPU_OK) return st;
   if (f) {
     st = launch_finalize_forces(c, c.d_fout.p, 3, false, kForceToN);
@@ -558,7 +592,7 @@ int pdgpu_compute_device(pdgpu_ctx* h, unsigned what, double* d_f) {
   if (!h) return PDGPU_ERR_ARG;
   Context& c = h->c;
   CK(cudaSetDevice(c.device));
-  int st = enqueue_compute(c, what);
+  int st = enqueue_compute(c, what, (what & PDGPU_ENERGY) != 0);
   if (st != PDGPU_OK) return st;
   if (d_f) st = launch_finalize_forces(c, d_f, 3, false, kForceToN);
   return st;

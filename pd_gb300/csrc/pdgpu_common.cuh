@@ -63,11 +63,11 @@ struct Tile {
 };
 
 // Pair-law constants for the LJ + Coulomb kernel (FF_NonBonded)
+// (the _d members are the same constants in FP64, for the energy arithmetic)
 struct NBConst {
-  float cut2, vdwcut, vdwinner, inner, vdwinvw2, invw2;
-  float econv_diel;        // econv * (1/Dielectric) in kcal A / mol / e^2
-  float vdw14, elec14;
-  float sA, sB, sC, sD, sE, fsw_cutV, eshift, cut2_d, inner2;
+  float cut2, vdwcut2, vdw14, elec14, econv_diel;
+  double cut2_dd, vdwcut_d, vdwinner_d, inner_d, vdwinvw2_d, invw2_d, econv_diel_d, vdw14_d, elec14_d;
+  double sA, sB, sC, sD, sE, fsw_cutV, eshift, cut2_d, inner2_d;
   int elecmode;            // 0 none, 1 plain, 3 energy switch, 4 force switch
   int dovdw;
 };
@@ -79,6 +79,9 @@ struct GBConst {
   float econv_in, econv_out, premul;  // kcal units
   float vdw14, elec14, thresh;
   float P4, P5, invP5;
+  // FP64 copies for the energy arithmetic
+  double cut2_d, inner_d, invw2_d, vdwcut_d, vdwinner_d, vdwinvw2_d, still2_d;
+  double econv_in_d, econv_out_d, premul_d, vdw14_d, elec14_d, thresh_d;
 };
 
 // Device-side view of a context, passed by value to kernels.
@@ -88,6 +91,10 @@ struct DevView {
   const int* slot_sys;       // [nblocks] system of each block
   // original order
   const double* pos;         // natom*3
+  const double* charge;      // natom, e
+  const double* radius;      // natom, LJ Rmin/2
+  const double* sqeps;       // natom, sqrt(kcal/mol)
+  const double* born;        // natom, Born radii of the last GB pass (FP64)
   // sorted order
   const int* sorted_atom;    // [nslots]
   float4* xq;                // rel pos + charge
@@ -137,9 +144,9 @@ struct Context;
 int launch_list_build(Context& c, float list_radius);
 int launch_pack(Context& c, float check_disp);
 int launch_nb(Context& c, const NBConst& k, bool need_virial);
-int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset, double premul);
-int launch_lcpo(Context& c);
-int launch_bonded(Context& c);
+int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset, double premul, bool energy);
+int launch_lcpo(Context& c, bool energy);
+int launch_bonded(Context& c, bool energy);
 int launch_finalize_forces(Context& c, double* out, size_t stride_doubles, bool add, double scale);
 
 }  // namespace pdgpu

@@ -113,6 +113,10 @@ struct Context {
     v.sys = d_sys.p;
     v.slot_sys = d_block_sys.p;
     v.pos = d_pos.p;
+    v.charge = d_charge.p;
+    v.radius = d_radius.p;
+    v.sqeps = d_sqeps.p;
+    v.born = d_born_d.p;
     v.sorted_atom = d_sorted_atom.p;
     v.xq = d_xq.p;
     v.par = d_par.p;

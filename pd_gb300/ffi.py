@@ -17,7 +17,7 @@ ERRORS = {
     -4: "fixed-point accumulator overflow", -5: "NaN energy or force", -6: "device wait timed out",
     -7: "unsupported option", -8: "stale neighbour list", -9: "call sequence error",
 }
-NB, GB, SA, BONDED = 1, 2, 4, 8
+NB, GB, SA, BONDED, ENERGY = 1, 2, 4, 8, 0x100
 
 
 class PDGPUError(RuntimeError):
