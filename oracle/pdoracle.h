@@ -2,7 +2,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path and
  * the timed CPU baseline; nothing in the product links or calls it.  Parity of
- * this restatement with PD itself is pinned by tests/golden/*.npz, which were
+ * this restatement with PD itself is pinned by the .npz files in tests/golden, which were
  * produced by the compiled PD reference (oracle/ref_driver.cpp).
  *
  * Units follow PD's WorkSpace: positions in Angstrom, energies in J per

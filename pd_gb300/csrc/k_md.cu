@@ -1,0 +1,200 @@
+// k_md.cu — FP64 integrators, kinetic energy and the REMD exchange, on device.
+//
+// PD src/mmlib/protocols/md.cpp:
+//   velocity Verlet (PD's variant)   applyForces_VelocityVerletIntegration :805-855
+//   Langevin                          applyForces_LangevinIntegration        :923-1063
+//   kinetic energy                    calcKineticEnergy                      :521-560
+// PD src/mmlib/protocols/remd.cpp:
+//   alternating-pair exchange + velocity rescale  :178-215, Metropolis :349-356
+//
+// Positions (A) and velocities (m/s) stay FP64 in original atom order.  The
+// force of atom a is read straight from the fixed-point accumulators of its
+// sorted slot (plus the cached LCPO share), so no separate force array is
+// written during dynamics.  Gaussian noise comes from Philox4x32-10
+// (Salmon et al., SC'11) keyed by the seed and counted by (step, atom), so a
+// trajectory is reproducible bit for bit.
+#include "pdgpu_md.cuh"
+
+namespace pdgpu {
+
+// ---- Philox4x32-10 ----------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32(uint4 ctr, uint2 key) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    unsigned hi0 = __umulhi(0xD2511F53u, ctr.x), lo0 = 0xD2511F53u * ctr.x;
+    unsigned hi1 = __umulhi(0xCD9E8D57u, ctr.z), lo1 = 0xCD9E8D57u * ctr.z;
+    ctr = make_uint4(hi1 ^ ctr.y ^ key.x, lo1, hi0 ^ ctr.w ^ key.y, lo0);
+    key.x += 0x9E3779B9u;
+    key.y += 0xBB67AE85u;
+  }
+  return ctr;
+}
+__device__ __forceinline__ double u01(unsigned x) { return ((double)x + 0.5) * (1.0 / 4294967296.0); }
+// two unit normals from two uniforms (Box-Muller)
+__device__ __forceinline__ void box_muller(unsigned a, unsigned b, double& n1, double& n2) {
+  double r = sqrt(-2.0 * log(u01(a)));
+  double s, c;
+  sincospi(2.0 * u01(b), &s, &c);
+  n1 = r * c;
+  n2 = r * s;
+}
+
+__device__ __forceinline__ void atom_force(const MDView& m, int a, double f[3]) {
+  int s = m.slot_of[a];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    long long q = m.facc[3 * s + c];
+    if (m.facc_sa) q += m.facc_sa[3 * s + c];
+    f[c] = (double)q * (1.0 / kForceScale) * kForceToN;
+  }
+}
+
+__device__ __forceinline__ void add_ke(const MDView& m, int a, const double v[3]) {
+  double ke = 0.5 * m.mass[a] * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  // J -> kcal/mol fixed point, per system
+  atomic_add_ll(&m.ke[m.atom_sys[a]], fix_energy_d(ke / kKcalMolToJ));
+}
+
+// PD velocity Verlet as written: half kick, (KE), half kick, drift t*(v+dv), kick
+__global__ void k_vv(MDView m, double dt) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= m.natom) return;
+  double f[3];
+  atom_force(m, a, f);
+  double tm = 0.5 * dt / m.mass[a];
+  double v[3], p[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    v[c] = m.vel[3 * a + c] + f[c] * tm;
+    p[c] = m.pos[3 * a + c];
+  }
+  add_ke(m, a, v);
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    double dv = f[c] * tm;
+    v[c] += dv;
+    p[c] += dt * (v[c] + dv) * (1.0 / kAngstrom);
+    v[c] += dv;
+    m.vel[3 * a + c] = v[c];
+    m.pos[3 * a + c] = p[c];
+  }
+}
+
+// PD Langevin step (gamma*dt > 1e-5 branch) with per-system target temperature
+__global__ void k_langevin(MDView m, LangevinCoeffs L, unsigned long long step, int first_step, int last_step) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= m.natom) return;
+  double f[3];
+  atom_force(m, a, f);
+  const double mass = m.mass[a];
+  const double tm = L.dt / mass;
+  double v[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    v[c] = m.vel[3 * a + c];
+    if (!first_step) v[c] += (1.0 - L.c0 / L.c1) * f[c] * tm / L.gt;
+  }
+  add_ke(m, a, v);
+  if (!last_step) {
+    const double T = m.temp[m.atom_sys[a]];
+    const double kTdivm = 1.38065E-23 * T / mass;
+    const double sigmav = sqrt(kTdivm * L.varv);
+    const double sigmar = sqrt(kTdivm * L.varr) / L.gamma;
+    // six normals, in PD's draw order n1x n2y | n2x n1z | n1y n2z (md.cpp:1017-1019)
+    uint2 key = make_uint2((unsigned)m.seed, (unsigned)(m.seed >> 32));
+    uint4 r0 = philox4x32(make_uint4((unsigned)step, (unsigned)(step >> 32), (unsigned)a, 0u), key);
+    uint4 r1 = philox4x32(make_uint4((unsigned)step, (unsigned)(step >> 32), (unsigned)a, 1u), key);
+    double n1x, n2y, n2x, n1z, n1y, n2z;
+    box_muller(r0.x, r0.y, n1x, n2y);
+    box_muller(r0.z, r0.w, n2x, n1z);
+    box_muller(r1.x, r1.y, n1y, n2z);
+    const double n1[3] = {n1x, n1y, n1z}, n2[3] = {n2x, n2y, n2z};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      double dvr = sigmav * (L.crv * n1[c] + L.sq1mcrv2 * n2[c]);
+      double drr = sigmar * n1[c];
+      double dr = L.dt * (L.c1 * v[c] + L.c2 * f[c] * tm) + drr;
+      double dv = (L.c0 * L.c2) * f[c] * tm / L.c1 + dvr;
+      m.pos[3 * a + c] += dr * (1.0 / kAngstrom);
+      v[c] = v[c] * L.c0 + dv;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) m.vel[3 * a + c] = v[c];
+}
+
+// REMD: one thread walks the temperature ladder (remd.cpp:178-215, 349-356).
+// temp_sys[r] = system holding temperature rung r; ladder[r] = temperature (K).
+__global__ void k_remd_exchange(const long long* eacc, int nsys, int parity, const double* ladder, int* temp_sys,
+                                double* temp, double* vscale, int* accepted, unsigned long long seed,
+                                unsigned long long round) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int s = 0; s < nsys; s++) vscale[s] = 1.0;
+  for (int r = parity; r < nsys - 1; r += 2) {
+    int lo = temp_sys[r], hi = temp_sys[r + 1];
+    double Tlo = ladder[r], Thi = ladder[r + 1];
+    double Elo = 0, Ehi = 0;
+    for (int k = 0; k < E_NSLOTS; k++) {
+      if (k == E_VIRIAL) continue;
+      Elo += (double)eacc[(size_t)lo * E_NSLOTS + k];
+      Ehi += (double)eacc[(size_t)hi * E_NSLOTS + k];
+    }
+    Elo = Elo / kEnergyScale * kKcalMolToJ;
+    Ehi = Ehi / kEnergyScale * kKcalMolToJ;
+    const double kB = 1.38065E-23;
+    double delta = (Elo - Ehi) * (1.0 / (kB * Thi) - 1.0 / (kB * Tlo));
+    uint4 rr = philox4x32(make_uint4((unsigned)round, (unsigned)(round >> 32), (unsigned)r, 7u),
+                          make_uint2((unsigned)seed ^ 0x5bd1e995u, (unsigned)(seed >> 32)));
+    bool acc = (delta <= 0) || (exp(-delta) > u01(rr.x));
+    accepted[r] = acc ? 1 : 0;
+    if (acc) {
+      // the structure at Tlo moves to Thi and vice versa; velocities follow sqrt(T'/T)
+      temp_sys[r] = hi;
+      temp_sys[r + 1] = lo;
+      temp[hi] = Tlo;
+      temp[lo] = Thi;
+      vscale[lo] *= sqrt(Thi / Tlo);
+      vscale[hi] *= sqrt(Tlo / Thi);
+    }
+  }
+}
+
+__global__ void k_scale_vel(MDView m, const double* vscale) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= m.natom) return;
+  double s = vscale[m.atom_sys[a]];
+  if (s != 1.0)
+    for (int c = 0; c < 3; c++) m.vel[3 * a + c] *= s;
+}
+
+// zero a fixed-point buffer (kernel form so it can sit inside a captured graph
+// and be skipped on steps that keep the cached LCPO forces)
+__global__ void k_zero_ll(long long* p, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0;
+}
+
+int launch_integrate(Context& c, MDState& md, unsigned long long step, bool first, bool last) {
+  MDView m = md_view(c, md);
+  int nb = (c.natom + 255) / 256;
+  cudaMemsetAsync(md.d_ke.p, 0, sizeof(long long) * c.nsys, c.stream);
+  if (md.p.Integrator == 0) k_vv<<<nb, 256, 0, c.stream>>>(m, md.p.Timestep);
+  else k_langevin<<<nb, 256, 0, c.stream>>>(m, md.L, step, first ? 1 : 0, last ? 1 : 0);
+  return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
+}
+
+int launch_remd(Context& c, MDState& md, int parity, unsigned long long round) {
+  MDView m = md_view(c, md);
+  k_remd_exchange<<<1, 32, 0, c.stream>>>(c.d_eacc.p, c.nsys, parity, md.d_ladder.p, md.d_temp_sys.p, md.d_temp.p,
+                                          md.d_vscale.p, md.d_accepted.p, md.p.seed, round);
+  k_scale_vel<<<(c.natom + 255) / 256, 256, 0, c.stream>>>(m, md.d_vscale.p);
+  return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
+}
+
+int launch_zero_ll(Context& c, long long* p, size_t n) {
+  if (n == 0) return PDGPU_OK;
+  k_zero_ll<<<(unsigned)((n + 255) / 256), 256, 0, c.stream>>>(p, n);
+  return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
+}
+
+}  // namespace pdgpu

@@ -1,0 +1,70 @@
+// pdgpu_md.cuh — device state of molecular dynamics / REMD on a context.
+#pragma once
+#include <map>
+
+#include "pdgpu_context.cuh"
+
+namespace pdgpu {
+
+// Langevin coefficients (md.cpp:941-1003), FP64
+struct LangevinCoeffs {
+  double dt, gamma, gt, c0, c1, c2, varv, varr, crv, sq1mcrv2;
+};
+
+struct MDState {
+  bool ready = false;
+  pdgpu_md_params p{};
+  LangevinCoeffs L{};
+  unsigned long long step = 0;        // global step counter (RNG counter, cadences)
+  unsigned long long exchange_round = 0;
+  bool trajectory_started = false;
+  DBuf<double> d_vel;                 // [natom*3] m/s
+  DBuf<double> d_temp;                // [nsys] target temperature of each system (K)
+  DBuf<double> d_ladder;              // [nsys] temperature of each rung (K)
+  DBuf<int> d_temp_sys;               // [nsys] system holding each rung
+  DBuf<double> d_vscale;              // [nsys]
+  DBuf<int> d_accepted;               // [nsys]
+  DBuf<long long> d_ke;               // [nsys] kinetic energy, fixed point kcal/mol
+  DBuf<long long> d_facc_sa;          // [nslots*3] cached LCPO forces
+  DBuf<long long> d_surf_cache;       // [nsys] cached LCPO energy
+  std::map<int, cudaGraphExec_t> graphs;
+  // autotuned launch shape of the tile kernels
+  int tile_ctas_per_sm = 8;
+  int tile_threads = 256;
+};
+
+struct MDView {
+  int natom;
+  const int* slot_of;
+  const int* atom_sys;
+  const double* mass;
+  double* pos;
+  double* vel;
+  const double* temp;
+  const long long* facc;
+  const long long* facc_sa;   // may be null
+  long long* ke;
+  unsigned long long seed;
+};
+
+inline MDView md_view(Context& c, MDState& md) {
+  MDView m;
+  m.natom = c.natom;
+  m.slot_of = c.d_slot_of.p;
+  m.atom_sys = c.d_atom_sys.p;
+  m.mass = c.d_mass.p;
+  m.pos = c.d_pos.p;
+  m.vel = md.d_vel.p;
+  m.temp = md.d_temp.p;
+  m.facc = c.d_facc.p;
+  m.facc_sa = (md.p.what & PDGPU_SA) ? md.d_facc_sa.p : nullptr;
+  m.ke = md.d_ke.p;
+  m.seed = md.p.seed;
+  return m;
+}
+
+int launch_integrate(Context& c, MDState& md, unsigned long long step, bool first, bool last);
+int launch_remd(Context& c, MDState& md, int parity, unsigned long long round);
+int launch_zero_ll(Context& c, long long* p, size_t n);
+
+}  // namespace pdgpu
