@@ -149,9 +149,54 @@ int pdgpu_get_energies(pdgpu_ctx *ctx, pdgpu_energies *out);
 int pdgpu_get_born_radii(pdgpu_ctx *ctx, double *born);
 int pdgpu_get_sasa(pdgpu_ctx *ctx, double *sasa);
 
+/* ---- dynamics: MolecularDynamics / REX_Local --------------------------------- */
+/* Integrator settings (PD src/mmlib/protocols/md.h, defaults md.cpp:60-86). */
+typedef struct {
+    int Integrator;              /* 0: PD velocity Verlet (md.cpp:805-855); 1: Langevin (md.cpp:923-1063) */
+    double Timestep;             /* s (PD default 1e-15) */
+    double FricCoeff;            /* Langevin friction, 1/s (PD default 1e13) */
+    int UpdateNList;             /* neighbour-list rebuild cadence in steps (PD default 10) */
+    int UpdateSasa;              /* LCPO recalculation cadence in steps (PD default 5, lcpo.cpp:193-206) */
+    unsigned what;               /* components: PDGPU_NB | PDGPU_GB | PDGPU_SA | PDGPU_BONDED */
+    unsigned long long seed;     /* Philox key of the Langevin noise and of the exchange draws */
+    int use_graph;               /* 1: replay captured CUDA graphs of the step */
+} pdgpu_md_params;
+
+/* Replaces MolecularDynamics::setup for every system of the batch; temps gives
+ * each system's target temperature (K).  Velocities start at zero. */
+int pdgpu_md_setup(pdgpu_ctx *ctx, const pdgpu_md_params *p, const double *temps);
+int pdgpu_set_velocities(pdgpu_ctx *ctx, const double *v, size_t stride_bytes);
+int pdgpu_get_velocities(pdgpu_ctx *ctx, double *v, size_t stride_bytes);
+/* Replaces MolecularDynamics::run_core (md.cpp:219-283) for nsteps steps of
+ * every system at once: list refresh on the UpdateNList cadence
+ * (protocolbase.cpp:135-144), forces, integrator; the trajectory continues
+ * across calls.  With energy_on_last the energies of the last step are formed
+ * (pdgpu_get_energies) — the exchange criterion needs them. */
+int pdgpu_md_run(pdgpu_ctx *ctx, int nsteps, int energy_on_last);
+/* Same without waiting: the steps are queued on the context stream and the
+ * device status (NaN, stale list, overflow) is collected by pdgpu_synchronize(). */
+int pdgpu_md_enqueue(pdgpu_ctx *ctx, int nsteps, int energy_on_last);
+int pdgpu_synchronize(pdgpu_ctx *ctx);
+/* Kinetic energy of each system after the last step (J), PD's calcKineticEnergy. */
+int pdgpu_get_kinetic(pdgpu_ctx *ctx, double *ekin);
+/* One REX_Local exchange sweep (remd.cpp:178-215): rungs (parity, parity+1),
+ * (parity+2, parity+3)... of the temperature ladder, Metropolis on the last
+ * energies (remd.cpp:349-356), accepted swaps exchange the systems' target
+ * temperatures and rescale their velocities by sqrt(T'/T).  accepted[r] (may be
+ * NULL) reports rung pair r; temps (may be NULL) returns each system's new
+ * target temperature. */
+int pdgpu_remd_exchange(pdgpu_ctx *ctx, int parity, int *accepted, double *temps);
+/* Project autotuner: times short trial runs (state restored afterwards) over
+ * list-rebuild cadences and tile-kernel launch shapes and keeps the fastest
+ * setting whose list never goes stale.  Outputs may be NULL. */
+int pdgpu_md_autotune(pdgpu_ctx *ctx, int trial_steps, int *update_nlist, int *ctas_per_sm);
+
 /* ---- diagnostics ---------------------------------------------------------- */
 /* Tile / pair counts of the current list: ntiles, nmasked tiles, slots. */
 int pdgpu_list_stats(pdgpu_ctx *ctx, long long *ntiles, long long *nmasked, long long *nslots);
+/* Number of kernels this context has launched so far (graph replays count
+ * every kernel node they run). */
+long long pdgpu_kernel_launches(pdgpu_ctx *ctx);
 /* Stream the context launches on (cudaStream_t as void*), for event timing. */
 void *pdgpu_stream(pdgpu_ctx *ctx);
 

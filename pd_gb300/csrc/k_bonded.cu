@@ -186,6 +186,7 @@ __global__ void k_bonded(BondedView b) {
 }
 
 int launch_bonded(Context& c, bool energy) {
+  c.kernel_launches += ((c.nbond + c.nangle + c.ntors + c.nimpr) > 0 ? 1 : 0);
   BondedView b;
   b.slot_of = c.d_slot_of.p;
   b.atom_sys = c.d_atom_sys.p;

@@ -358,11 +358,12 @@ static int tile_grid(Context& c) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
   long long want = (c.ncand + 7) / 8;
-  long long g = (long long)sms * 8;
+  long long g = (long long)sms * c.tile_ctas_per_sm;
   return (int)(want < g ? (want > 0 ? want : 1) : g);
 }
 
 int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset, double premul, bool energy) {
+  c.kernel_launches += 5;
   DevView v = c.view();
   cudaStream_t st = c.stream;
   int g = tile_grid(c);
@@ -469,7 +470,8 @@ __device__ __forceinline__ float3 rel_vec(const DevView& v, int a, int b) {
 // per atom i (one warp, lanes over i's overlap partners j): SASA_i and the
 // derivative terms collected on atom i (lcpo.cpp:781-949)
 __global__ void k_lcpo_main(DevView v, const float4* lc, const int* nl_n, const int* nl_idx, const float* nl_s,
-                            const double* P, const double* sigma, double* sasa_out, int energy) {
+                            const double* P, const double* sigma, double* sasa_out, long long* facc_out,
+                            long long* esurf_out, int esurf_stride) {
   const int lane = threadIdx.x & 31;
   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (s >= v.nslots) return;
@@ -556,13 +558,14 @@ __global__ void k_lcpo_main(DevView v, const float4* lc, const int* nl_n, const 
     }
     sasa_out[a] = SA;
     // PD adds SASAderiv / Angstrom; the derivative terms already hold d(sigma*SA)
-    for (int c = 0; c < 3; c++) atomic_add_ll(&v.facc[3 * s + c], __double2ll_rn(f[c] * kForceScale));
+    for (int c = 0; c < 3; c++) atomic_add_ll(&facc_out[3 * s + c], __double2ll_rn(f[c] * kForceScale));
     int sys = v.slot_sys[s >> 5];
-    if (energy) atomic_add_ll(&v.eacc[(size_t)sys * E_NSLOTS + E_SURF], fix_energy_d(SA * sigma[a]));
+    if (esurf_out) atomic_add_ll(&esurf_out[(size_t)sys * esurf_stride], fix_energy_d(SA * sigma[a]));
   }
 }
 
-int launch_lcpo(Context& c, bool energy) {
+int launch_lcpo(Context& c, long long* facc_out, long long* esurf_out, int esurf_stride) {
+  c.kernel_launches += 3;
   DevView v = c.view();
   cudaStream_t st = c.stream;
   int g = tile_grid(c);
@@ -572,7 +575,7 @@ int launch_lcpo(Context& c, bool energy) {
   k_lcpo_sort<<<nw, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_ncand.p, c.d_lc_cand.p, c.d_lc_n.p, c.d_lc_idx.p,
                                    c.d_lc_s.p);
   k_lcpo_main<<<nw, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_n.p, c.d_lc_idx.p, c.d_lc_s.p, c.d_lcpoP.p,
-                                   c.d_lcpoSig.p, c.d_sasa.p, energy ? 1 : 0);
+                                   c.d_lcpoSig.p, c.d_sasa.p, facc_out, esurf_out, esurf_stride);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

@@ -369,6 +369,7 @@ __global__ void k_pack(DevView v, const double* charge, float check2, int store_
 static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 int launch_list_build(Context& c, float list_radius) {
+  c.kernel_launches += 14;
   DevView v = c.view();
   cudaStream_t st = c.stream;
   int ncells = c.nsys * kCellsPerSystem;
@@ -404,6 +405,7 @@ int launch_list_build(Context& c, float list_radius) {
 }
 
 int launch_pack(Context& c, float check_disp) {
+  c.kernel_launches += 1;
   DevView v = c.view();
   float c2 = check_disp > 0 ? check_disp * check_disp : 0.f;
   k_pack<<<nblk(c.nslots, 256), 256, 0, c.stream>>>(v, c.d_charge.p, c2, 0);

@@ -81,9 +81,10 @@ __global__ void k_vv(MDView m, double dt) {
 }
 
 // PD Langevin step (gamma*dt > 1e-5 branch) with per-system target temperature
-__global__ void k_langevin(MDView m, LangevinCoeffs L, unsigned long long step, int first_step, int last_step) {
+__global__ void k_langevin(MDView m, LangevinCoeffs L, int first_step, int last_step) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= m.natom) return;
+  const unsigned long long step = *m.stepc;
   double f[3];
   atom_force(m, a, f);
   const double mass = m.mass[a];
@@ -174,16 +175,24 @@ __global__ void k_zero_ll(long long* p, size_t n) {
   if (i < n) p[i] = 0;
 }
 
-int launch_integrate(Context& c, MDState& md, unsigned long long step, bool first, bool last) {
+// advance the device-side step counter (kept on the device so captured graphs stay valid)
+__global__ void k_advance(unsigned long long* stepc) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *stepc += 1;
+}
+
+int launch_integrate(Context& c, MDState& md, bool first, bool last) {
+  c.kernel_launches += 2;
   MDView m = md_view(c, md);
   int nb = (c.natom + 255) / 256;
   cudaMemsetAsync(md.d_ke.p, 0, sizeof(long long) * c.nsys, c.stream);
   if (md.p.Integrator == 0) k_vv<<<nb, 256, 0, c.stream>>>(m, md.p.Timestep);
-  else k_langevin<<<nb, 256, 0, c.stream>>>(m, md.L, step, first ? 1 : 0, last ? 1 : 0);
+  else k_langevin<<<nb, 256, 0, c.stream>>>(m, md.L, first ? 1 : 0, last ? 1 : 0);
+  k_advance<<<1, 32, 0, c.stream>>>(md.d_step.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 
 int launch_remd(Context& c, MDState& md, int parity, unsigned long long round) {
+  c.kernel_launches += 2;
   MDView m = md_view(c, md);
   k_remd_exchange<<<1, 32, 0, c.stream>>>(c.d_eacc.p, c.nsys, parity, md.d_ladder.p, md.d_temp_sys.p, md.d_temp.p,
                                           md.d_vscale.p, md.d_accepted.p, md.p.seed, round);

@@ -202,7 +202,7 @@ static int grid_for_tiles(Context& c) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
   // persistent-style grid: 8 resident 256-thread CTAs per SM, grid-stride over tiles
   long long want = (c.ncand + 7) / 8;
-  long long g = (long long)sms * 8;
+  long long g = (long long)sms * c.tile_ctas_per_sm;
   return (int)(want < g ? (want > 0 ? want : 1) : g);
 }
 
@@ -218,6 +218,7 @@ static void launch_nb_mode(Context& c, const NBConst& k, int g) {
 }
 
 int launch_nb(Context& c, const NBConst& k, bool energy) {
+  c.kernel_launches += 1;
   int g = grid_for_tiles(c);
   if (energy) launch_nb_mode<true>(c, k, g);
   else launch_nb_mode<false>(c, k, g);
@@ -241,6 +242,7 @@ __global__ void k_finalize_forces(DevView v, double* out, size_t stride, int add
 }
 
 int launch_finalize_forces(Context& c, double* out, size_t stride_doubles, bool add, double scale) {
+  c.kernel_launches += 1;
   DevView v = c.view();
   k_finalize_forces<<<(c.nslots + 255) / 256, 256, 0, c.stream>>>(v, out, stride_doubles, add ? 1 : 0, scale);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;

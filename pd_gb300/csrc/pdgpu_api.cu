@@ -406,6 +406,7 @@ int pdgpu_destroy(pdgpu_ctx* h) {
   if (!h) return PDGPU_ERR_ARG;
   cudaSetDevice(h->c.device);
   if (h->c.stream) cudaStreamSynchronize(h->c.stream);
+  destroy_md(h->c);
   cudaStream_t st = h->c.stream;
   delete h;
   if (st) cudaStreamDestroy(st);
@@ -491,11 +492,12 @@ int pdgpu_get_positions(pdgpu_ctx* h, double* xyz, size_t stride) {
   return PDGPU_OK;
 }
 
-static int rebuild_list(Context& c) {
+}  // extern "C"
+
+int pdgpu::rebuild_list_impl(Context& c) {
   if (!c.positions_set) return PDGPU_ERR_STATE;
   if (!c.nb_set && !c.gb_set && !c.has_sa) return PDGPU_ERR_STATE;
   CK(cudaSetDevice(c.device));
-  CK(cudaMemsetAsync(c.d_status.p, 0, sizeof(unsigned), c.stream));
   float R = (float)list_radius(c);
   int st = launch_list_build(c, R);
   if (st != PDGPU_OK) return st;
@@ -504,27 +506,33 @@ static int rebuild_list(Context& c) {
   return PDGPU_OK;
 }
 
+extern "C" {
+
 int pdgpu_rebuild_list(pdgpu_ctx* h) {
   if (!h) return PDGPU_ERR_ARG;
-  return rebuild_list(h->c);
+  Context& c = h->c;
+  CK(cudaSetDevice(c.device));
+  CK(cudaMemsetAsync(c.d_status.p, 0, sizeof(unsigned), c.stream));
+  return rebuild_list_impl(c);
 }
 
-static int enqueue_compute(Context& c, unsigned what, bool energy) {
-  if (!c.positions_set) return PDGPU_ERR_STATE;
-  if ((what & PDGPU_NB) && !c.nb_set) return PDGPU_ERR_STATE;
-  if ((what & PDGPU_GB) && (!c.has_gb || !c.gb_set)) return PDGPU_ERR_STATE;
-  if ((what & PDGPU_SA) && !c.has_sa) return PDGPU_ERR_STATE;
-  if ((what & (PDGPU_GB | PDGPU_SA)) && c.any_periodic) return PDGPU_ERR_UNSUPPORTED;
-  CK(cudaMemsetAsync(c.d_status.p, 0, sizeof(unsigned), c.stream));
-  if (!c.list_built) {
-    int st = rebuild_list(c);
+}  // extern "C"
+
+// One force evaluation on the context stream (no host synchronisation).
+// rebuild: rebuild the list first (else pack the positions and check the skin).
+// LCPO forces go to lcpo_f and its energy to lcpo_e (stride lcpo_e_stride) when
+// run_lcpo; dynamics points them at the cached-LCPO buffers.
+int pdgpu::enqueue_forces(Context& c, unsigned what, bool energy, bool rebuild, long long* lcpo_f,
+                          long long* lcpo_e, int lcpo_e_stride, bool run_lcpo) {
+  if (rebuild || !c.list_built) {
+    int st = rebuild_list_impl(c);
     if (st != PDGPU_OK) return st;
   } else {
     int st = launch_pack(c, c.lp.check_skin ? (float)(0.5 * c.lp.Padding) : 0.f);
     if (st != PDGPU_OK) return st;
   }
   CK(cudaMemsetAsync(c.d_facc.p, 0, sizeof(long long) * 3 * c.nslots, c.stream));
-  CK(cudaMemsetAsync(c.d_eacc.p, 0, sizeof(long long) * E_NSLOTS * c.nsys, c.stream));
+  if (energy) CK(cudaMemsetAsync(c.d_eacc.p, 0, sizeof(long long) * E_NSLOTS * c.nsys, c.stream));
   int st = PDGPU_OK;
   if (what & PDGPU_NB) st = launch_nb(c, make_nb_const(c.nb), energy);
   if (st == PDGPU_OK && (what & PDGPU_GB)) {
@@ -533,9 +541,21 @@ static int enqueue_compute(Context& c, unsigned what, bool energy) {
     double premul = -0.5 * ec * (1.0 / c.gb.DielectricSolute - 1.0 / c.gb.DielectricSolvent);
     st = launch_gb(c, k, 0.5 * ec, c.gb.BornRadiusOffset, premul, energy);
   }
-  if (st == PDGPU_OK && (what & PDGPU_SA)) st = launch_lcpo(c, energy);
+  if (st == PDGPU_OK && (what & PDGPU_SA) && run_lcpo) st = launch_lcpo(c, lcpo_f, lcpo_e, lcpo_e_stride);
   if (st == PDGPU_OK && (what & PDGPU_BONDED)) st = launch_bonded(c, energy);
   return st;
+}
+
+extern "C" {
+
+static int enqueue_compute(Context& c, unsigned what, bool energy) {
+  if (!c.positions_set) return PDGPU_ERR_STATE;
+  if ((what & PDGPU_NB) && !c.nb_set) return PDGPU_ERR_STATE;
+  if ((what & PDGPU_GB) && (!c.has_gb || !c.gb_set)) return PDGPU_ERR_STATE;
+  if ((what & PDGPU_SA) && !c.has_sa) return PDGPU_ERR_STATE;
+  if ((what & (PDGPU_GB | PDGPU_SA)) && c.any_periodic) return PDGPU_ERR_UNSUPPORTED;
+  CK(cudaMemsetAsync(c.d_status.p, 0, sizeof(unsigned), c.stream));
+  return enqueue_forces(c, what, energy, false, c.d_facc.p, energy ? c.d_eacc.p + E_SURF : nullptr, E_NSLOTS, true);
 }
 
 int pdgpu_get_energies(pdgpu_ctx* h, pdgpu_energies* out) {

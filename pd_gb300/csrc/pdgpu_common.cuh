@@ -145,8 +145,14 @@ int launch_list_build(Context& c, float list_radius);
 int launch_pack(Context& c, float check_disp);
 int launch_nb(Context& c, const NBConst& k, bool need_virial);
 int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset, double premul, bool energy);
-int launch_lcpo(Context& c, bool energy);
+int launch_lcpo(Context& c, long long* facc_out, long long* esurf_out, int esurf_stride);
 int launch_bonded(Context& c, bool energy);
 int launch_finalize_forces(Context& c, double* out, size_t stride_doubles, bool add, double scale);
+// host-side orchestration shared by the evaluation and dynamics entry points
+int rebuild_list_impl(Context& c);
+int enqueue_forces(Context& c, unsigned what, bool energy, bool rebuild, long long* lcpo_f, long long* lcpo_e,
+                   int lcpo_e_stride, bool run_lcpo);
+struct MDState;
+void destroy_md(Context& c);
 
 }  // namespace pdgpu

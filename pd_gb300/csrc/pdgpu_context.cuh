@@ -42,6 +42,8 @@ struct Context {
   pdgpu_list_params lp{};
   bool nb_set = false, gb_set = false;
   float list_radius_built = 0.f;
+  int tile_ctas_per_sm = 8;    // launch shape of the tile kernels (autotuned)
+  long long kernel_launches = 0;  // kernels this context has put on its stream (graph replays included)
 
   // static per-atom data (original order)
   DBuf<SystemInfo> d_sys;
@@ -97,6 +99,9 @@ struct Context {
   int nbond = 0, nangle = 0, ntors = 0, nimpr = 0;
   DBuf<int> d_bidx, d_aidx, d_tidx, d_iidx;
   DBuf<double> d_bpar, d_apar, d_tpar, d_ipar;
+
+  // dynamics state (pdgpu_md_setup), owned by the context
+  MDState* md = nullptr;
 
   // host staging
   std::vector<long long> h_eacc;

@@ -19,6 +19,7 @@ struct MDState {
   unsigned long long exchange_round = 0;
   bool trajectory_started = false;
   DBuf<double> d_vel;                 // [natom*3] m/s
+  DBuf<unsigned long long> d_step;    // [1] device copy of the step counter
   DBuf<double> d_temp;                // [nsys] target temperature of each system (K)
   DBuf<double> d_ladder;              // [nsys] temperature of each rung (K)
   DBuf<int> d_temp_sys;               // [nsys] system holding each rung
@@ -28,9 +29,7 @@ struct MDState {
   DBuf<long long> d_facc_sa;          // [nslots*3] cached LCPO forces
   DBuf<long long> d_surf_cache;       // [nsys] cached LCPO energy
   std::map<int, cudaGraphExec_t> graphs;
-  // autotuned launch shape of the tile kernels
-  int tile_ctas_per_sm = 8;
-  int tile_threads = 256;
+  std::map<int, long long> graph_kernels;  // kernel nodes of each captured flavour
 };
 
 struct MDView {
@@ -45,6 +44,7 @@ struct MDView {
   const long long* facc_sa;   // may be null
   long long* ke;
   unsigned long long seed;
+  const unsigned long long* stepc;
 };
 
 inline MDView md_view(Context& c, MDState& md) {
@@ -60,10 +60,11 @@ inline MDView md_view(Context& c, MDState& md) {
   m.facc_sa = (md.p.what & PDGPU_SA) ? md.d_facc_sa.p : nullptr;
   m.ke = md.d_ke.p;
   m.seed = md.p.seed;
+  m.stepc = md.d_step.p;
   return m;
 }
 
-int launch_integrate(Context& c, MDState& md, unsigned long long step, bool first, bool last);
+int launch_integrate(Context& c, MDState& md, bool first, bool last);
 int launch_remd(Context& c, MDState& md, int parity, unsigned long long round);
 int launch_zero_ll(Context& c, long long* p, size_t n);
 

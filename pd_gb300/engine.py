@@ -150,3 +150,49 @@ class DeviceContext:
 
     def stream(self):
         return self.lib.pdgpu_stream(self.h)
+
+    # -- dynamics ----------------------------------------------------------
+    def md_setup(self, temps, integrator=1, timestep=2e-15, fric=1e13, update_nlist=10, update_sasa=5, what=0,
+                 seed=1, use_graph=True):
+        p = ffi.MDParams(int(integrator), float(timestep), float(fric), int(update_nlist), int(update_sasa),
+                         int(what), int(seed), int(bool(use_graph)))
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(temps, np.float64), (self.nsystems,)))
+        ffi.check(self.lib.pdgpu_md_setup(self.h, ctypes.byref(p), _pd(t)), "pdgpu_md_setup")
+
+    def set_velocities(self, v):
+        v = np.ascontiguousarray(v, np.float64)
+        ffi.check(self.lib.pdgpu_set_velocities(self.h, _pd(v), 24), "pdgpu_set_velocities")
+
+    def get_velocities(self):
+        out = np.zeros((self.natom, 3))
+        ffi.check(self.lib.pdgpu_get_velocities(self.h, _pd(out), 24), "pdgpu_get_velocities")
+        return out
+
+    def md_run(self, nsteps, energy_on_last=False):
+        ffi.check(self.lib.pdgpu_md_run(self.h, int(nsteps), int(bool(energy_on_last))), "pdgpu_md_run")
+
+    def md_enqueue(self, nsteps, energy_on_last=False):
+        ffi.check(self.lib.pdgpu_md_enqueue(self.h, int(nsteps), int(bool(energy_on_last))), "pdgpu_md_enqueue")
+
+    def synchronize(self):
+        ffi.check(self.lib.pdgpu_synchronize(self.h), "pdgpu_synchronize")
+
+    def kernel_launches(self):
+        return int(self.lib.pdgpu_kernel_launches(self.h))
+
+    def kinetic(self):
+        out = np.zeros(self.nsystems)
+        ffi.check(self.lib.pdgpu_get_kinetic(self.h, _pd(out)), "pdgpu_get_kinetic")
+        return out
+
+    def remd_exchange(self, parity):
+        acc = np.zeros(max(self.nsystems - 1, 1), np.int32)
+        temps = np.zeros(self.nsystems)
+        ffi.check(self.lib.pdgpu_remd_exchange(self.h, int(parity), _pi(acc), _pd(temps)), "pdgpu_remd_exchange")
+        return acc[:self.nsystems - 1], temps
+
+    def autotune(self, trial_steps=20):
+        a, b = ctypes.c_int(), ctypes.c_int()
+        ffi.check(self.lib.pdgpu_md_autotune(self.h, int(trial_steps), ctypes.byref(a), ctypes.byref(b)),
+                  "pdgpu_md_autotune")
+        return {"UpdateNList": a.value, "ctas_per_sm": b.value}

@@ -64,6 +64,12 @@ class ListParams(ctypes.Structure):
     _fields_ = [("Padding", ctypes.c_double), ("check_skin", ctypes.c_int)]
 
 
+class MDParams(ctypes.Structure):
+    _fields_ = [("Integrator", ctypes.c_int), ("Timestep", ctypes.c_double), ("FricCoeff", ctypes.c_double),
+                ("UpdateNList", ctypes.c_int), ("UpdateSasa", ctypes.c_int), ("what", ctypes.c_uint),
+                ("seed", ctypes.c_ulonglong), ("use_graph", ctypes.c_int)]
+
+
 # every symbol include/pdgpu.h declares, with its ctypes signature
 SIGNATURES = {
     "pdgpu_create": ([ctypes.c_int, ctypes.POINTER(SystemDesc), _ip], ctypes.c_void_p),
@@ -86,6 +92,16 @@ SIGNATURES = {
     "pdgpu_list_stats": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
                           ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
     "pdgpu_stream": ([ctypes.c_void_p], ctypes.c_void_p),
+    "pdgpu_md_setup": ([ctypes.c_void_p, ctypes.POINTER(MDParams), _dp], ctypes.c_int),
+    "pdgpu_set_velocities": ([ctypes.c_void_p, _dp, ctypes.c_size_t], ctypes.c_int),
+    "pdgpu_get_velocities": ([ctypes.c_void_p, _dp, ctypes.c_size_t], ctypes.c_int),
+    "pdgpu_md_run": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "pdgpu_get_kinetic": ([ctypes.c_void_p, _dp], ctypes.c_int),
+    "pdgpu_remd_exchange": ([ctypes.c_void_p, ctypes.c_int, _ip, _dp], ctypes.c_int),
+    "pdgpu_md_autotune": ([ctypes.c_void_p, ctypes.c_int, _ip, _ip], ctypes.c_int),
+    "pdgpu_md_enqueue": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "pdgpu_synchronize": ([ctypes.c_void_p], ctypes.c_int),
+    "pdgpu_kernel_launches": ([ctypes.c_void_p], ctypes.c_longlong),
 }
 
 _lib = None

@@ -1,0 +1,140 @@
+"""Device dynamics against the oracle's FP64 integrators (PD md.cpp) and REMD properties."""
+import numpy as np
+import pytest
+
+from conftest import rel_rms
+from helpers import gb_kwargs, nb_kwargs, nb_params, oracle_system
+from oracle import pdoracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def water_ctx(d, integrator, what, use_graph=True, temp=300.0):
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.workspace import SystemImage
+    ctx = DeviceContext(SystemImage._from_fixture(d))
+    ctx.set_list(2.0)
+    ctx.set_nb(**nb_kwargs(d, "nb"))
+    ctx.set_positions(d["pos"])
+    ctx.md_setup([temp], integrator=integrator, timestep=1e-15, fric=1e13, update_nlist=1, what=what,
+                 seed=7, use_graph=use_graph)
+    return ctx
+
+
+def oracle_forces(d, pos):
+    s = O.OracleSystem(pos, d["charge"], d["radius"], d["epsilon"], d["excl"], tuple(d["box"]))
+    _, f = O.nonbonded(s, nb_params(d, "nb"))
+    _, fb = O.bonded(pos, d["bond_idx"], d["bond_par"], d["angle_idx"], d["angle_par"], d["torsion_idx"],
+                     d["torsion_par"], d["improper_idx"], d["improper_par"])
+    return f + fb
+
+
+def test_velocity_verlet_steps_match_oracle(goldens):
+    from pd_gb300 import ffi
+    from pd_gb300.md import maxwell_boltzmann
+    d = goldens["water_c1"]
+    v0 = maxwell_boltzmann(d["mass"], 300.0, 3)
+    ctx = water_ctx(d, 0, ffi.NB | ffi.BONDED)
+    ctx.set_velocities(v0)
+    p, v = d["pos"].copy(), v0.copy()
+    for step in range(3):
+        ctx.md_run(1)
+        f = oracle_forces(d, p)
+        p, v, ek = O.vv_step(p, v, f, d["mass"], 1e-15)
+    gp, gv = ctx.get_positions(), ctx.get_velocities()
+    assert np.max(np.abs(gp - p)) < 1e-8
+    assert rel_rms(gv, v) < 1e-5
+
+
+def test_langevin_zero_temperature_matches_oracle(goldens):
+    """T = 0 removes the noise: the deterministic part of PD's Langevin step must agree."""
+    from pd_gb300 import ffi
+    from pd_gb300.md import maxwell_boltzmann
+    d = goldens["water_c1"]
+    v0 = maxwell_boltzmann(d["mass"], 300.0, 5)
+    ctx = water_ctx(d, 1, ffi.NB | ffi.BONDED, temp=0.0)
+    ctx.set_velocities(v0)
+    p, v = d["pos"].copy(), v0.copy()
+    noise = np.zeros((len(p), 6))
+    for step in range(3):
+        ctx.md_run(1)
+        f = oracle_forces(d, p)
+        p, v, _ = O.langevin_step(p, v, f, d["mass"], 1e-15, 1e13, 0.0, noise, first_step=(step == 0))
+    gp, gv = ctx.get_positions(), ctx.get_velocities()
+    assert np.max(np.abs(gp - p)) < 1e-8
+    assert rel_rms(gv, v) < 1e-5
+
+
+def test_graph_replay_is_bitwise_identical_to_direct_launches(goldens):
+    from pd_gb300 import ffi
+    d = goldens["water_c1"]
+    out = []
+    for g in (False, True):
+        ctx = water_ctx(d, 1, ffi.NB | ffi.BONDED, use_graph=g)
+        ctx.md_run(12, energy_on_last=True)
+        out.append((ctx.get_positions(), ctx.get_velocities(), ctx.energies()[0]["epot"]))
+        ctx.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+
+
+def test_langevin_thermalises_gb_peptide(goldens):
+    from pd_gb300 import ffi
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.workspace import SystemImage
+    d = goldens["peptide30"]
+    im = SystemImage._from_fixture(d)
+    ctx = DeviceContext(im)
+    ctx.set_list(2.0)
+    ctx.set_gb(**gb_kwargs(d))
+    ctx.set_positions(d["pos"])
+    ctx.md_setup([300.0], integrator=1, timestep=1e-15, fric=5e13, update_nlist=10, update_sasa=5,
+                 what=ffi.GB | ffi.SA | ffi.BONDED, seed=11)
+    temps = []
+    for _ in range(10):
+        ctx.md_run(200)
+        temps.append(2 * ctx.kinetic()[0] / (3 * im.natom * 1.38065e-23))
+    T = np.mean(temps[3:])
+    assert 250.0 < T < 350.0, temps
+
+
+def test_remd_exchange_swaps_temperatures_and_rescales(goldens):
+    """Equal energies and temperatures always accept (delta = 0); swapped
+    systems exchange target temperatures and velocities scale by sqrt(T'/T)."""
+    from pd_gb300 import ffi
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.workspace import SystemImage
+    d = goldens["peptide30"]
+    im = SystemImage.concat([SystemImage._from_fixture(d)] * 4)
+    ctx = DeviceContext(im)
+    ctx.set_list(2.0)
+    ctx.set_gb(**gb_kwargs(d))
+    ctx.set_positions(np.concatenate([d["pos"]] * 4))
+    ladder = np.array([300.0, 300.0, 400.0, 400.0])
+    ctx.md_setup(ladder, integrator=1, timestep=1e-15, what=ffi.GB | ffi.BONDED, seed=3)
+    ctx.md_run(1, energy_on_last=True)
+    v_before = ctx.get_velocities()
+    acc, temps = ctx.remd_exchange(0)       # rungs (0,1) and (2,3): equal T => delta = 0 => accept
+    assert acc[0] == 1 and acc[2] == 1
+    assert np.allclose(temps, [300, 300, 400, 400])
+    acc, temps = ctx.remd_exchange(1)       # rungs (1,2): 300 K <-> 400 K
+    n = im.natoms[0]
+    v_after = ctx.get_velocities()
+    if acc[1]:
+        lo, hi = 0, 3   # after the first sweep rung 1 holds system 0, rung 2 holds system 3
+        assert np.isclose(temps[lo], 400.0) and np.isclose(temps[hi], 300.0)
+        assert np.allclose(v_after[lo * n:(lo + 1) * n], v_before[lo * n:(lo + 1) * n] * np.sqrt(400 / 300.))
+    else:
+        assert np.array_equal(v_after, v_before)
+
+
+def test_md_is_deterministic(goldens):
+    from pd_gb300 import ffi
+    d = goldens["water_c1"]
+    res = []
+    for _ in range(2):
+        ctx = water_ctx(d, 1, ffi.NB | ffi.BONDED)
+        ctx.md_run(15)
+        res.append(ctx.get_positions())
+        ctx.close()
+    assert np.array_equal(res[0], res[1])
