@@ -1,0 +1,527 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 nonbonded / GB-SA path of PD.
+
+Headline workload (default, ``--workload c4``): batched REMD of 64 GB/SA
+peptides of uneven size (30-478 residues, ~210k atoms in total, built by PD),
+Langevin at 2 fs over a geometric 300-500 K ladder, exchange attempts every
+500 steps, all replicas advanced together by the batched kernels replayed from
+captured CUDA graphs.  One "step" = one MD step of every replica.
+
+metric: atom-steps/s (sum over systems of atoms x steps / s), reported beside
+the plain single-system GPU path on the same systems (one context per system,
+no batching, no graphs), the force error against the FP64 oracle, and the
+oracle's CPU throughput on the host cores.
+
+Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c1|c2|c3|c4] [--impl reference]
+Under torchrun each rank runs its own replica set (replicas only: the path has
+no exchange between GPUs); rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+KB = 1.38065E-23
+METRIC = "atom-steps/s batched vs plain GPU at force rel err <=1e-5 vs FP64; % HBM roofline"
+
+# flops per pair of the pair kernels (FP32, FMA = 2 flops), frozen planning figures
+FLOPS = {"gb_born": 40, "gb_pair": 120, "gb_chain": 60, "nb": 77}
+# bytes per atom-step of the integrator: read p, v, f (24 B each) + mass (8 B), write p, v
+INTEGRATOR_BYTES = 80 + 48
+
+WORKLOADS = {
+    "c1": dict(image="c1_water", desc="667 TIP3P waters (2,001 atoms), 27.5 A box, LJ+Coulomb 12/10 A energy switch, "
+               "2 A skin, velocity Verlet 1 fs", what=("NB", "BONDED"), integrator=0, dt=1e-15, padding=2.0),
+    "c2": dict(image="c2_solvated", desc="120-residue peptide in TIP3P (22,489 atoms), 62 A box, LJ+Coulomb 12/10 A, "
+               "2 A skin, Langevin 2 fs 300 K", what=("NB", "BONDED"), integrator=1, dt=2e-15, padding=2.0),
+    "c3": dict(image="c3_gb256", desc="256-residue peptide (4,235 atoms), GB/SA all pairs, Langevin 2 fs 300 K",
+               what=("GB", "SA", "BONDED"), integrator=1, dt=2e-15, padding=2.0),
+    "c4": dict(image="c4_remd64", desc="batched REMD of 64 GB/SA peptides (30-478 residues), all pairs, Langevin 2 fs, "
+               "geometric 300-500 K, exchange every 500 steps", what=("GB", "SA", "BONDED"), integrator=1, dt=2e-15,
+               padding=2.0),
+}
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (replicas only; barrier and a max over ranks of the time)
+# ---------------------------------------------------------------------------
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def dist_init(world, backend):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group(backend=backend)
+    return dist
+
+
+def reduce_max_sum(dist, t, units):
+    """(max over ranks of the time, sum over ranks of the units processed)."""
+    if dist is None:
+        return t, units
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    a = torch.tensor([t], dtype=torch.float64, device=dev)
+    b = torch.tensor([units], dtype=torch.float64, device=dev)
+    dist.all_reduce(a, op=dist.ReduceOp.MAX)
+    dist.all_reduce(b, op=dist.ReduceOp.SUM)
+    return float(a.item()), float(b.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workload construction
+# ---------------------------------------------------------------------------
+def flags(names):
+    from pd_gb300 import ffi
+    w = 0
+    for n in names:
+        w |= getattr(ffi, n)
+    return w
+
+
+def configure(ctx, wl, image):
+    """Component parameters of each workload (PD attribute names)."""
+    s14v, s14e = image.scaling14
+    if "NB" in wl["what"]:
+        ctx.set_nb(Cutoff=12.0, InnerCutoff=10.0, VdwCutoff=12.0, VdwInnerCutoff=10.0, Vdw14Scaling=s14v,
+                   Elec14Scaling=s14e, Dielectric=1.0, EnergySwitch=1, ForceSwitch=0, DoVdw=1, DoElec=1)
+    if "GB" in wl["what"]:
+        P = image.gb_P
+        ctx.set_gb(Cutoff=999.0, InnerCutoff=998.0, VdwCutoff=999.0, VdwInnerCutoff=998.0, Vdw14Scaling=s14v,
+                   Elec14Scaling=s14e, DielectricSolute=1.0, DielectricSolvent=80.0, GbsaStillCutoff=999.0,
+                   ExpApproxThreshold=-4.0, BornRadiusOffset=0.0, P4=P[3], P5=P[4])
+    ctx.set_list(wl["padding"])
+
+
+def temperatures(image, key):
+    if key == "c4":
+        n = image.nsystems
+        return 300.0 * (500.0 / 300.0) ** (np.arange(n) / max(n - 1, 1))
+    return np.full(image.nsystems, 300.0)
+
+
+def make_context(image, wl, key, seed, use_graph=True, device=0, update_nlist=10):
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.md import maxwell_boltzmann
+    ctx = DeviceContext(image, device)
+    configure(ctx, wl, image)
+    ctx.set_positions(image.pos)
+    temps = temperatures(image, key)
+    ctx.md_setup(temps, integrator=wl["integrator"], timestep=wl["dt"], fric=1e13, update_nlist=update_nlist,
+                 update_sasa=5, what=flags(wl["what"]), seed=seed, use_graph=use_graph)
+    ctx.set_velocities(maxwell_boltzmann(image.mass, temps, seed, image.natoms))
+    return ctx, temps
+
+
+# ---------------------------------------------------------------------------
+# parity against the FP64 oracle on one system of the workload
+# ---------------------------------------------------------------------------
+def parity_check(image, wl, key):
+    from oracle import pdoracle as O
+    from pd_gb300 import ffi
+    from pd_gb300.engine import DeviceContext
+    k = 0
+    if image.nsystems > 1:   # the median-size system of the batch
+        k = int(np.argsort(image.natoms)[image.nsystems // 2])
+    sub = image.subset(k)
+    ctx = DeviceContext(sub)
+    configure(ctx, wl, sub)
+    ctx.set_positions(sub.pos)
+    f = np.zeros((sub.natom, 3))
+    e = ctx.compute(flags(wl["what"]), f)[0]
+    ctx.close()
+    s = O.OracleSystem(sub.pos, sub.charge, sub.radius, sub.epsilon, sub.excl, tuple(sub.box[0]))
+    ref_f = np.zeros((sub.natom, 3))
+    ref_e = 0.0
+    threads = os.cpu_count() or 1
+    s14v, s14e = sub.scaling14
+    if "NB" in wl["what"]:
+        p = O.nb_params(Cutoff=12, InnerCutoff=10, Vdw14Scaling=s14v, Elec14Scaling=s14e, EnergySwitch=1,
+                        ListCutoff=12 + wl["padding"])
+        ee, ff = O.nonbonded(s, p, threads)
+        ref_f += ff
+        ref_e += ee[0]
+    if "GB" in wl["what"]:
+        P = sub.gb_P
+        gp = O.gb_params(Cutoff=999, InnerCutoff=998, VdwCutoff=999, VdwInnerCutoff=998, Vdw14Scaling=s14v,
+                         Elec14Scaling=s14e, GbsaStillCutoff=999, P1=P[0], P2=P[1], P3=P[2], P4=P[3], P5=P[4],
+                         ListCutoff=999 + wl["padding"])
+        ee, ff, _ = O.gb_forces(s, gp, sub.gb_radius, sub.gb_vj, sub.gb_terms123, threads)
+        ref_f += ff
+        ref_e += ee[0]
+    if "SA" in wl["what"]:
+        ee, ff, _ = O.lcpo_forces(s, 999 + wl["padding"], sub.lcpo_radius, sub.lcpo_p, sub.lcpo_sigma, sub.lcpo_use,
+                                  threads)
+        ref_f += ff
+        ref_e += ee[0]
+    if "BONDED" in wl["what"]:
+        ee, ff = O.bonded(sub.pos, *sub.bonds, *sub.angles, *sub.torsions, *sub.impropers)
+        ref_f += ff
+        ref_e += ee.sum()
+    frms = float(np.sqrt(((f - ref_f) ** 2).sum(1).mean() / (ref_f ** 2).sum(1).mean()))
+    return {"system_atoms": int(sub.natom), "force_rel_rms": frms, "energy_rel_err": abs(e["epot"] - ref_e) / abs(ref_e)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle's FP64 restatement of PD's path on the host cores
+# ---------------------------------------------------------------------------
+def cpu_baseline(image, wl, key, budget_s=20.0):
+    from oracle import pdoracle as O
+    threads = os.cpu_count() or 1
+    k = 0
+    if image.nsystems > 1:
+        k = int(np.argsort(image.natoms)[image.nsystems // 2])
+    sub = image.subset(k)
+    s14v, s14e = sub.scaling14
+    pos = sub.pos.copy()
+    rng = np.random.default_rng(1)
+    vel = np.zeros_like(pos)
+    t0 = time.perf_counter()
+    steps = 0
+    nlist = None
+    while True:
+        s = O.OracleSystem(pos, sub.charge, sub.radius, sub.epsilon, sub.excl, tuple(sub.box[0]))
+        f = np.zeros_like(pos)
+        if "NB" in wl["what"]:
+            # PD keeps the list for UpdateNList = 10 steps (protocolbase.cpp:135-144)
+            if steps % 10 == 0:
+                nlist = O.StoredList(s, 12 + wl["padding"], threads)
+            _, ff = O.nonbonded_list(s, nlist, O.nb_params(Cutoff=12, InnerCutoff=10, Vdw14Scaling=s14v,
+                                                           Elec14Scaling=s14e, ListCutoff=12 + wl["padding"]),
+                                     threads)
+            f += ff
+        if "GB" in wl["what"]:
+            P = sub.gb_P
+            gp = O.gb_params(Cutoff=999, InnerCutoff=998, VdwCutoff=999, VdwInnerCutoff=998, Vdw14Scaling=s14v,
+                             Elec14Scaling=s14e, GbsaStillCutoff=999, P1=P[0], P2=P[1], P3=P[2], P4=P[3], P5=P[4],
+                             ListCutoff=999 + wl["padding"])
+            _, ff, _ = O.gb_forces(s, gp, sub.gb_radius, sub.gb_vj, sub.gb_terms123, threads)
+            f += ff
+        if "SA" in wl["what"] and steps % 5 == 0:
+            _, ff, _ = O.lcpo_forces(s, 999 + wl["padding"], sub.lcpo_radius, sub.lcpo_p, sub.lcpo_sigma,
+                                     sub.lcpo_use, threads)
+            f += ff
+        if "BONDED" in wl["what"]:
+            _, ff = O.bonded(pos, *sub.bonds, *sub.angles, *sub.torsions, *sub.impropers)
+            f += ff
+        if wl["integrator"] == 1:
+            pos, vel, _ = O.langevin_step(pos, vel, f, sub.mass, wl["dt"], 1e13, 300.0,
+                                          rng.standard_normal((sub.natom, 6)), first_step=(steps == 0))
+        else:
+            pos, vel, _ = O.vv_step(pos, vel, f, sub.mass, wl["dt"])
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 10000:
+            break
+    return {"value": sub.natom * steps / el, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+            "sample": "%d MD steps (forces + FP64 integrator; PD's O(N^2) list rebuilt every 10 steps for "
+                      "cutoff systems, all pairs for GB) of system %d (%d atoms) of the workload, %.1f s, "
+                      "OpenMP over %d host threads" % (
+                          steps, k, sub.natom, el, threads)}
+
+
+# ---------------------------------------------------------------------------
+# the reference arm: PD's FP64 CPU path (oracle restatement) on the host cores
+# ---------------------------------------------------------------------------
+def run_reference(args, key, wl, image):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import pdoracle as O  # noqa: F401  (builds the C restatement if needed)
+    per_step = max(3.0, 120.0 / max(args.steps + args.warmup, 1))
+    res = [cpu_baseline(image, wl, key, budget_s=per_step) for _ in range(args.warmup + args.steps)]
+    vals = [r["value"] for r in res[args.warmup:]]
+    v = statistics.median(vals)
+    out = {"metric": METRIC, "value": v, "unit": "atom-steps/s", "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (systems built by PD, see DESIGN.md)",
+           "config": {"workload": key, "description": wl["desc"]},
+           "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": res[-1]["cores"], "kind": "port",
+                            "sample": res[-1]["sample"]},
+           "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def fp32_peak_tflops(torch):
+    """Measured FP32 FMA ceiling: cuBLAS SGEMM with TF32 off, best of 5."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+    b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ b
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def pairs_per_step(image, wl):
+    """Unordered atom pairs each pair kernel visits per step (all pairs for GB)."""
+    n = image.natoms.astype(np.float64)
+    return float((n * (n - 1) / 2).sum())
+
+
+def run_ours(args, key, wl, image):
+    import torch
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = dist_init(world, "nccl")
+    from pd_gb300 import ffi
+    seed = 1000 + rank
+    ctx, temps = make_context(image, wl, key, seed, device=local)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    tuned = None
+    if not args.no_autotune:
+        tuned = ctx.autotune(trial_steps=10)
+    natom = image.natom
+    exch_every = 500 if key == "c4" else 0
+    # warm-up (captures the step graphs)
+    ctx.md_run(args.warmup)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    step0 = args.warmup
+    launches0 = ctx.kernel_launches()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    ev = []
+    exchanges = 0
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)   # L2 flushed between steps (256 MB write > 126 MB L2)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s = step0 + k
+            due = exch_every and (s + 1) % exch_every == 0
+            ctx.md_enqueue(1, energy_on_last=bool(due))
+            if due:
+                ffi.check(ctx.lib.pdgpu_remd_exchange(ctx.h, (s // exch_every) % 2, None, None), "exchange")
+                exchanges += 1
+            e1.record(stream)
+            ev.append((e0, e1))
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    clocks = sampler.stop()
+    t_dev = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    launches = ctx.kernel_launches() - launches0
+    if dist is not None:
+        dist.barrier()
+    t_max, units = reduce_max_sum(dist, t_dev, float(natom) * args.steps)
+    value = units / t_max
+
+    # kernel roofline (dominant kernel measured on the live state, L2 flushed before each launch)
+    dom = "gb_pair" if "GB" in wl["what"] else "nb"
+    ms_dom = ctx.time_kernel(dom, reps=10)
+    ms_int = ctx.time_kernel("integrate", reps=10)
+    result = {}
+    if rank == 0:
+        peak = fp32_peak_tflops(torch)
+        pairs = pairs_per_step(image, wl) if "GB" in wl["what"] else None
+        if pairs is None:   # cutoff system: pairs inside the cutoff, from the list statistics
+            st = ctx.list_stats()
+            pairs = st["tiles"] * 1024.0 * (4.0 / 3.0 * math.pi * 12.0 ** 3) / (4.0 / 3.0 * math.pi * 14.0 ** 3) / 2
+        achieved = FLOPS[dom] * pairs / (ms_dom / 1e3) / 1e12
+        peaks = {}
+        pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(pk):
+            peaks = json.load(open(pk))
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        int_gbs = INTEGRATOR_BYTES * natom / (ms_int / 1e3) / 1e9
+        result["roofline"] = {"bound": "fp32", "kernel": "k_gb_pair" if dom == "gb_pair" else "k_nb_tiles",
+                              "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                              "traffic": None, "peak_source": "measured cuBLAS SGEMM (TF32 off) on this GPU",
+                              "flops_per_pair": FLOPS[dom], "pairs_per_launch": pairs, "ms_per_launch": ms_dom}
+        result["hbm_roofline"] = {"bound": "hbm", "kernel": "k_langevin" if wl["integrator"] else "k_vv",
+                                  "achieved": int_gbs, "peak": hbm, "unit": "GB/s", "frac": int_gbs / hbm,
+                                  "traffic": None, "bytes_per_atom": INTEGRATOR_BYTES, "ms_per_launch": ms_int,
+                                  "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    ctx.close()
+
+    # plain single-system path on the same systems (rank 0, N=1 semantics per rank)
+    plain = None
+    if rank == 0 and image.nsystems > 1 and not args.no_plain:
+        plain = run_plain(args, key, wl, image, torch)
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if rank == 0 and not args.no_e2e:
+        e2e = run_e2e(args, key, wl, image, torch)
+
+    if rank != 0:
+        return
+    out = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math / int64 fixed-point sums / f64 state",
+           "data": "synthetic systems built by PD (NewProtein + seeded compaction, TIP3P lattice), see DESIGN.md",
+           "config": {"workload": key, "description": wl["desc"], "atoms": int(natom),
+                      "systems": int(image.nsystems), "l2": "flushed before every timed step (256 MB write)",
+                      "graphs": True, "exchanges_in_timed_region": exchanges, "autotune": tuned,
+                      "parallelism": "replicas only (%d GPU%s)" % (world, "s" if world > 1 else "")},
+           "gpu_launches": int(launches), "clocks": clocks}
+    out.update(result)
+    if plain:
+        out["plain"] = plain
+        out["batched_over_plain"] = value / plain["value"] if plain["value"] else None
+    out["e2e"] = e2e or {"value": None, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    if not args.no_parity:
+        out["parity"] = parity_check(image, wl, key)
+    if not args.no_cpu and world == 1:
+        out["cpu_baseline"] = cpu_baseline(image, wl, key, budget_s=args.cpu_seconds)
+    print(json.dumps(out))
+
+
+def run_plain(args, key, wl, image, torch):
+    """Each system in its own context, launched one after the other, no graphs."""
+    ctxs = []
+    for k in range(image.nsystems):
+        sub = image.subset(k)
+        c, _ = make_context(sub, wl, key, 2000 + k, use_graph=False)
+        ctxs.append(c)
+    steps = max(3, min(args.steps, 20))
+    for c in ctxs:
+        c.md_run(2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for c in ctxs:
+            c.md_enqueue(1)
+    for c in ctxs:
+        c.synchronize()
+    el = time.perf_counter() - t0
+    for c in ctxs:
+        c.close()
+    return {"value": image.natom * steps / el, "unit": "atom-steps/s", "steps": steps,
+            "how": "one context per system (%d), launched in turn, no CUDA graphs, wall clock" % image.nsystems}
+
+
+def run_e2e(args, key, wl, image, torch):
+    """Per step through the C ABI with pinned host buffers: positions H2D, one MD step,
+    energies and positions D2H (the user-visible loop of a PD host protocol)."""
+    ctx, _ = make_context(image, wl, key, 3000, use_graph=True)
+    n = image.natom
+    pos_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    pos_h[:] = image.pos
+    steps = max(3, min(args.steps, 50))
+    ctx.md_run(3)
+    pos_h[:] = ctx.get_positions()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ctx.set_positions(pos_h)
+        ctx.md_run(1, energy_on_last=True)
+        ctx.energies()
+        pos_h[:] = ctx.get_positions()
+    el = time.perf_counter() - t0
+    ctx.close()
+    return {"value": n * steps / el, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * n,
+            "d2h_bytes_per_step": 24 * n + 96 * image.nsystems, "steps": steps}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--workload", default="c4", choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    from pd_gb300.workspace import load_workload
+    wl = WORKLOADS[args.workload]
+    image = load_workload(wl["image"])
+    if args.impl == "reference":
+        run_reference(args, args.workload, wl, image)
+    else:
+        from pd_gb300 import build as _b
+        _b.build()
+        run_ours(args, args.workload, wl, image)
+
+
+if __name__ == "__main__":
+    main()

@@ -197,6 +197,12 @@ int pdgpu_list_stats(pdgpu_ctx *ctx, long long *ntiles, long long *nmasked, long
 /* Number of kernels this context has launched so far (graph replays count
  * every kernel node they run). */
 long long pdgpu_kernel_launches(pdgpu_ctx *ctx);
+/* Timing probe: runs one kernel of the path `reps` times on the current state
+ * (0 LJ/Coulomb tiles, 1 GB Born sums, 2 GB fused pair, 3 GB chain rule,
+ * 4 LCPO, 5 integrator (advances the dynamics), 6 list build, 7 position pack,
+ * 8 bonded), each launch bracketed by CUDA events on the context stream, with
+ * an optional 256 MB L2 flush before each; returns the mean duration in ms. */
+int pdgpu_time_kernel(pdgpu_ctx *ctx, int kernel, int reps, int flush_l2, double *avg_ms);
 /* Stream the context launches on (cudaStream_t as void*), for event timing. */
 void *pdgpu_stream(pdgpu_ctx *ctx);
 

@@ -307,6 +307,119 @@ int pdo_nonbonded(const pdo_system *s, const pdo_nb_params *p, int nthreads, pdo
     return 0;
 }
 
+/* stored list, neighbourlist.cpp:336-439 */
+int pdo_list_build(const pdo_system *s, double list_cutoff, int nthreads, pdo_list *out) {
+    int n = s->natom;
+    double lim = SQR(list_cutoff);
+    int32_t *cnt = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    int nt = nthreads_eff(nthreads);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 32) num_threads(nt)
+#endif
+    for (int i = 0; i < n; i++) {
+        int c = 0;
+        for (int j = 0; j < i; j++) {
+            double d[3] = {s->pos[3 * j] - s->pos[3 * i], s->pos[3 * j + 1] - s->pos[3 * i + 1],
+                           s->pos[3 * j + 2] - s->pos[3 * i + 2]};
+            min_image(s->box, d);
+            if (d[0] * d[0] + d[1] * d[1] + d[2] * d[2] <= lim) c++;
+        }
+        cnt[i] = c;
+    }
+    out->natom = n;
+    out->start = (int64_t *)malloc(sizeof(int64_t) * ((size_t)n + 1));
+    out->start[0] = 0;
+    for (int i = 0; i < n; i++) out->start[i + 1] = out->start[i] + cnt[i];
+    out->j = (int32_t *)malloc(sizeof(int32_t) * (size_t)(out->start[n] + 1));
+    out->shift = (double *)malloc(sizeof(double) * 3 * (size_t)(out->start[n] + 1));
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 32) num_threads(nt)
+#endif
+    for (int i = 0; i < n; i++) {
+        int64_t k = out->start[i];
+        for (int j = 0; j < i; j++) {
+            double d[3] = {s->pos[3 * j] - s->pos[3 * i], s->pos[3 * j + 1] - s->pos[3 * i + 1],
+                           s->pos[3 * j + 2] - s->pos[3 * i + 2]};
+            double d0[3] = {d[0], d[1], d[2]};
+            min_image(s->box, d);
+            if (d[0] * d[0] + d[1] * d[1] + d[2] * d[2] > lim) continue;
+            out->j[k] = j;
+            for (int c = 0; c < 3; c++) out->shift[3 * k + c] = d[c] - d0[c];
+            k++;
+        }
+    }
+    free(cnt);
+    return 0;
+}
+
+void pdo_list_free(pdo_list *l) {
+    free(l->start);
+    free(l->j);
+    free(l->shift);
+    l->start = NULL;
+    l->j = NULL;
+    l->shift = NULL;
+}
+
+int pdo_nonbonded_list(const pdo_system *s, const pdo_list *l, const pdo_nb_params *p, int nthreads,
+                       pdo_energies *e, double *force) {
+    int n = s->natom;
+    nb_consts c;
+    nb_setup(p, &c);
+    bo_table bt;
+    bo_build(s, &bt);
+    double tabV[8] = {0, 0, 0, p->Vdw14Scaling, 1, 1, 1, 1};
+    double tabE[8] = {0, 0, 0, p->Elec14Scaling, 1, 1, 1, 1};
+    int nt = nthreads_eff(nthreads);
+    double *fbuf = (double *)calloc((size_t)nt * 3 * n, sizeof(double));
+    double *ebuf = (double *)calloc((size_t)nt * 3, sizeof(double));
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 32) num_threads(nt)
+#endif
+    for (int i = 0; i < n; i++) {
+#ifdef _OPENMP
+        int tid = omp_get_thread_num();
+#else
+        int tid = 0;
+#endif
+        double *f = fbuf + (size_t)tid * 3 * n;
+        double *eb = ebuf + 3 * tid;
+        double fi[3] = {0, 0, 0};
+        for (int64_t k = l->start[i]; k < l->start[i + 1]; k++) {
+            int j = l->j[k];
+            double d[3];
+            for (int q = 0; q < 3; q++) d[q] = s->pos[3 * j + q] - s->pos[3 * i + q] + l->shift[3 * k + q];
+            double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            int bo = bo_lookup(&bt, i, j);
+            double ev, ee, fm, dist;
+            if (!nb_pair(p, &c, r2, s->radius[i], s->radius[j], s->epsilon[i], s->epsilon[j], s->charge[i],
+                         s->charge[j], tabV[bo], tabE[bo], &ev, &ee, &fm, &dist))
+                continue;
+            eb[0] += ev;
+            eb[1] += ee;
+            eb[2] += dist * fm * PDO_ANGSTROM;
+            double sc = fm / dist;
+            for (int q = 0; q < 3; q++) {
+                fi[q] += d[q] * sc;
+                f[3 * j + q] -= d[q] * sc;
+            }
+        }
+        for (int q = 0; q < 3; q++) f[3 * i + q] += fi[q];
+    }
+    memset(e, 0, sizeof(*e));
+    for (int t = 0; t < nt; t++) {
+        e->vdw += ebuf[3 * t];
+        e->elec += ebuf[3 * t + 1];
+        e->virial += ebuf[3 * t + 2];
+        for (int k = 0; k < 3 * n; k++) force[k] += fbuf[(size_t)t * 3 * n + k];
+    }
+    e->epot = e->vdw + e->elec;
+    free(fbuf);
+    free(ebuf);
+    bo_free(&bt);
+    return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Generalised Born (Still)                                                 */
 /* ------------------------------------------------------------------------ */

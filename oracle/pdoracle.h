@@ -74,6 +74,21 @@ int pdo_list_checksums(const pdo_system *s, double list_cutoff, int32_t *count, 
 /* --- LJ + Coulomb (PD src/mmlib/forcefields/nonbonded.cpp:559-910) --- */
 int pdo_nonbonded(const pdo_system *s, const pdo_nb_params *p, int nthreads, pdo_energies *e, double *force);
 
+/* Stored half list as PD keeps it between rebuilds (neighbourlist.cpp:336-439):
+ * for each i the j < i within ListCutoff at minimum image, with the image shift
+ * fixed at build time.  pdo_list_build allocates; pdo_list_free releases. */
+typedef struct {
+    int natom;
+    int64_t *start;    /* natom+1 */
+    int32_t *j;
+    double *shift;     /* 3 per entry: image shift added to pj - pi */
+} pdo_list;
+int pdo_list_build(const pdo_system *s, double list_cutoff, int nthreads, pdo_list *out);
+void pdo_list_free(pdo_list *l);
+/* LJ + Coulomb over a stored list (the per-step work of PD's MD loop) */
+int pdo_nonbonded_list(const pdo_system *s, const pdo_list *l, const pdo_nb_params *p, int nthreads,
+                       pdo_energies *e, double *force);
+
 /* scalar pair law (PD src/mmlib/forcefields/nonbonded.cpp:400-534) */
 void pdo_pair_law(const pdo_nb_params *p, double r, double radiusij, double epsilon, double qi, double qj,
                   double *vdw_pot, double *vdw_force, double *elec_pot, double *elec_force);

@@ -37,6 +37,11 @@ class GBParams(ctypes.Structure):
         "BornRadiusOffset", "P1", "P2", "P3", "P4", "P5", "ListCutoff")]
 
 
+class NList(ctypes.Structure):
+    _fields_ = [("natom", ctypes.c_int), ("start", ctypes.c_void_p), ("j", ctypes.c_void_p),
+                ("shift", ctypes.c_void_p)]
+
+
 class Energies(ctypes.Structure):
     _fields_ = [(k, ctypes.c_double) for k in ("epot", "vdw", "elec", "pol", "pol_self", "pol_cross", "surf",
                                                 "virial")]
@@ -87,6 +92,10 @@ def lib():
         L.pdo_langevin_coeffs.argtypes = [ctypes.c_double, ctypes.c_double, _dp]
         L.pdo_bonded.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip, _dp, ctypes.c_int, _ip, _dp, ctypes.c_int,
                                  _ip, _dp, ctypes.c_int, _ip, _dp, _dp, _dp]
+        L.pdo_list_build.argtypes = [ctypes.POINTER(System), ctypes.c_double, ctypes.c_int, ctypes.POINTER(NList)]
+        L.pdo_list_free.argtypes = [ctypes.POINTER(NList)]
+        L.pdo_nonbonded_list.argtypes = [ctypes.POINTER(System), ctypes.POINTER(NList), ctypes.POINTER(NBParams),
+                                         ctypes.c_int, ctypes.POINTER(Energies), _dp]
         L.pdo_econv_joule.restype = ctypes.c_double
         L.pdo_halfeconv.restype = ctypes.c_double
         _lib = L
@@ -159,6 +168,28 @@ def nonbonded(sys_, params, nthreads=1):
     e = Energies()
     f = np.zeros((sys_.natom, 3))
     lib().pdo_nonbonded(ctypes.byref(sys_.rec), ctypes.byref(params), nthreads, ctypes.byref(e), _pd(f))
+    return e.as_array(), f
+
+
+class StoredList:
+    """A PD-style half list kept between rebuilds (freed with the object)."""
+
+    def __init__(self, sys_, list_cutoff, nthreads=1):
+        self.rec = NList()
+        lib().pdo_list_build(ctypes.byref(sys_.rec), list_cutoff, nthreads, ctypes.byref(self.rec))
+
+    def __del__(self):
+        try:
+            lib().pdo_list_free(ctypes.byref(self.rec))
+        except Exception:
+            pass
+
+
+def nonbonded_list(sys_, nlist, params, nthreads=1):
+    e = Energies()
+    f = np.zeros((sys_.natom, 3))
+    lib().pdo_nonbonded_list(ctypes.byref(sys_.rec), ctypes.byref(nlist.rec), ctypes.byref(params), nthreads,
+                             ctypes.byref(e), _pd(f))
     return e.as_array(), f
 
 

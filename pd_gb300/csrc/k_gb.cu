@@ -379,6 +379,17 @@ int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 
+// one GB pass on its own (timing probe): 1 Born sums, 2 fused pair (forces), 3 chain rule
+int launch_gb_stage(Context& c, const GBConst& k, int stage) {
+  DevView v = c.view();
+  int g = tile_grid(c);
+  c.kernel_launches += 1;
+  if (stage == 1) k_gb_born<<<g, 256, 0, c.stream>>>(v, k, c.d_gpol.p);
+  else if (stage == 2) k_gb_pair<false><<<g, 256, 0, c.stream>>>(v, k, c.d_born_f.p, c.d_deda.p);
+  else k_gb_chain<<<g, 256, 0, c.stream>>>(v, k, c.d_chain_f.p);
+  return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
+}
+
 // ---------------------------------------------------------------------------
 // LCPO
 // ---------------------------------------------------------------------------

@@ -61,7 +61,9 @@ int read_status(Context& c) {
   return PDGPU_OK;
 }
 
-NBConst make_nb_const(const pdgpu_nb_params& p) {
+}  // namespace
+
+NBConst pdgpu::make_nb_const(const pdgpu_nb_params& p) {
   NBConst k{};
   double C = p.Cutoff, I = p.InnerCutoff;
   k.cut2 = (float)(C * C);
@@ -99,7 +101,7 @@ NBConst make_nb_const(const pdgpu_nb_params& p) {
   return k;
 }
 
-GBConst make_gb_const(const pdgpu_gb_params& p, double listR) {
+GBConst pdgpu::make_gb_const(const pdgpu_gb_params& p, double listR) {
   GBConst k{};
   double C = p.Cutoff, I = p.InnerCutoff;
   k.cut2 = (float)(C * C);
@@ -137,7 +139,7 @@ GBConst make_gb_const(const pdgpu_gb_params& p, double listR) {
   return k;
 }
 
-}  // namespace
+
 
 extern "C" {
 

@@ -146,6 +146,9 @@ int launch_pack(Context& c, float check_disp);
 int launch_nb(Context& c, const NBConst& k, bool need_virial);
 int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset, double premul, bool energy);
 int launch_lcpo(Context& c, long long* facc_out, long long* esurf_out, int esurf_stride);
+int launch_gb_stage(Context& c, const GBConst& k, int stage);
+NBConst make_nb_const(const pdgpu_nb_params& p);
+GBConst make_gb_const(const pdgpu_gb_params& p, double listR);
 int launch_bonded(Context& c, bool energy);
 int launch_finalize_forces(Context& c, double* out, size_t stride_doubles, bool add, double scale);
 // host-side orchestration shared by the evaluation and dynamics entry points

@@ -252,6 +252,48 @@ int pdgpu_synchronize(pdgpu_ctx* h) {
 
 long long pdgpu_kernel_launches(pdgpu_ctx* h) { return h ? h->c.kernel_launches : -1; }
 
+int pdgpu_time_kernel(pdgpu_ctx* h, int kernel, int reps, int flush_l2, double* avg_ms) {
+  if (!h || reps < 1 || !avg_ms) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.list_built) return PDGPU_ERR_STATE;
+  if (kernel == 5 && (!c.md || !c.md->ready)) return PDGPU_ERR_STATE;
+  if ((kernel >= 1 && kernel <= 3) && !c.gb_set) return PDGPU_ERR_STATE;
+  if (kernel == 0 && !c.nb_set) return PDGPU_ERR_STATE;
+  if (kernel == 4 && !c.has_sa) return PDGPU_ERR_STATE;
+  CK(cudaSetDevice(c.device));
+  DBuf<char> scratch;
+  const size_t flush_bytes = (size_t)256 << 20;  // larger than the 126 MB L2
+  if (flush_l2 && scratch.alloc(flush_bytes) != cudaSuccess) return PDGPU_ERR_CUDA;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  float total = 0.f;
+  int st = PDGPU_OK;
+  for (int r = 0; r < reps && st == PDGPU_OK; r++) {
+    if (flush_l2) CK(cudaMemsetAsync(scratch.p, r & 0xff, flush_bytes, c.stream));
+    CK(cudaEventRecord(e0, c.stream));
+    switch (kernel) {
+      case 0: st = launch_nb(c, make_nb_const(c.nb), false); break;
+      case 1: case 2: case 3: st = launch_gb_stage(c, make_gb_const(c.gb, c.list_radius_built), kernel); break;
+      case 4: st = launch_lcpo(c, c.d_facc.p, nullptr, 0); break;
+      case 5: st = launch_integrate(c, *c.md, false, false); break;
+      case 6: st = launch_list_build(c, c.list_radius_built); break;
+      case 7: st = launch_pack(c, 0.f); break;
+      case 8: st = launch_bonded(c, false); break;
+      default: st = PDGPU_ERR_ARG;
+    }
+    CK(cudaEventRecord(e1, c.stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    total += ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *avg_ms = total / reps;
+  return st;
+}
+
 int pdgpu_get_kinetic(pdgpu_ctx* h, double* ekin) {
   if (!h || !ekin) return PDGPU_ERR_ARG;
   Context& c = h->c;

@@ -177,6 +177,15 @@ class DeviceContext:
     def synchronize(self):
         ffi.check(self.lib.pdgpu_synchronize(self.h), "pdgpu_synchronize")
 
+    KERNELS = {"nb": 0, "gb_born": 1, "gb_pair": 2, "gb_chain": 3, "lcpo": 4, "integrate": 5, "list": 6, "pack": 7,
+               "bonded": 8}
+
+    def time_kernel(self, name, reps=10, flush_l2=True):
+        ms = ctypes.c_double()
+        ffi.check(self.lib.pdgpu_time_kernel(self.h, self.KERNELS[name], int(reps), int(bool(flush_l2)),
+                                             ctypes.byref(ms)), "pdgpu_time_kernel")
+        return ms.value
+
     def kernel_launches(self):
         return int(self.lib.pdgpu_kernel_launches(self.h))
 

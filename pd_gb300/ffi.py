@@ -102,6 +102,7 @@ SIGNATURES = {
     "pdgpu_md_enqueue": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "pdgpu_synchronize": ([ctypes.c_void_p], ctypes.c_int),
     "pdgpu_kernel_launches": ([ctypes.c_void_p], ctypes.c_longlong),
+    "pdgpu_time_kernel": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp], ctypes.c_int),
 }
 
 _lib = None

@@ -42,7 +42,8 @@ def test_velocity_verlet_steps_match_oracle(goldens):
         f = oracle_forces(d, p)
         p, v, ek = O.vv_step(p, v, f, d["mass"], 1e-15)
     gp, gv = ctx.get_positions(), ctx.get_velocities()
-    assert np.max(np.abs(gp - p)) < 1e-8
+    # FP32 forces (rel. RMS <= 1e-5) propagate into the displacement at that level
+    assert rel_rms(gp - d["pos"], p - d["pos"]) < 1e-5
     assert rel_rms(gv, v) < 1e-5
 
 
@@ -61,7 +62,7 @@ def test_langevin_zero_temperature_matches_oracle(goldens):
         f = oracle_forces(d, p)
         p, v, _ = O.langevin_step(p, v, f, d["mass"], 1e-15, 1e13, 0.0, noise, first_step=(step == 0))
     gp, gv = ctx.get_positions(), ctx.get_velocities()
-    assert np.max(np.abs(gp - p)) < 1e-8
+    assert rel_rms(gp - d["pos"], p - d["pos"]) < 1e-5
     assert rel_rms(gv, v) < 1e-5
 
 

@@ -86,3 +86,15 @@ def test_langevin_coefficients_branches():
     a = O.langevin_coeffs(1e13, 0.0499e-14)
     b = O.langevin_coeffs(1e13, 0.0501e-14)
     assert np.allclose(a[:3], b[:3], rtol=1e-2)
+
+
+def test_stored_list_matches_direct_scan(goldens):
+    """PD keeps the list between rebuilds (neighbourlist.cpp:336-439); evaluating a
+    freshly built stored list equals the direct minimum-image scan."""
+    d = goldens["water_c1"]
+    s = oracle_system(d)
+    p = nb_params(d)
+    e1, f1 = O.nonbonded(s, p)
+    L = O.StoredList(s, list_cutoff(d), 2)
+    e2, f2 = O.nonbonded_list(s, L, p, 2)
+    assert np.allclose(e1, e2, rtol=1e-11) and rel_rms(f2, f1) < 1e-12
