@@ -169,15 +169,27 @@ def temperatures(image, key):
     return np.full(image.nsystems, 300.0)
 
 
-def make_context(image, wl, key, seed, use_graph=True, device=0, update_nlist=10):
+RELAX = dict(steps=300, dt=0.2e-15, fric=5e13, update_nlist=1)
+
+
+def make_context(image, wl, key, seed, use_graph=True, device=0, update_nlist=10, relax=True):
+    """Context at the workload's settings.  The PD-built starting structures are
+    not equilibrated (lattice waters, compacted chains), so an untimed relaxation
+    (Langevin, 0.2 fs, strong friction, list rebuilt every step) runs first;
+    production then starts from fresh Maxwell-Boltzmann velocities."""
     from pd_gb300.engine import DeviceContext
     from pd_gb300.md import maxwell_boltzmann
     ctx = DeviceContext(image, device)
     configure(ctx, wl, image)
     ctx.set_positions(image.pos)
     temps = temperatures(image, key)
+    what = flags(wl["what"])
+    if relax:
+        ctx.md_setup(temps, integrator=1, timestep=RELAX["dt"], fric=RELAX["fric"], update_nlist=RELAX["update_nlist"],
+                     update_sasa=5, what=what, seed=seed + 7, use_graph=True)
+        ctx.md_run(RELAX["steps"])
     ctx.md_setup(temps, integrator=wl["integrator"], timestep=wl["dt"], fric=1e13, update_nlist=update_nlist,
-                 update_sasa=5, what=flags(wl["what"]), seed=seed, use_graph=use_graph)
+                 update_sasa=5, what=what, seed=seed, use_graph=use_graph)
     ctx.set_velocities(maxwell_boltzmann(image.mass, temps, seed, image.natoms))
     return ctx, temps
 
@@ -435,6 +447,9 @@ def run_ours(args, key, wl, image):
            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math / int64 fixed-point sums / f64 state",
            "data": "synthetic systems built by PD (NewProtein + seeded compaction, TIP3P lattice), see DESIGN.md",
            "config": {"workload": key, "description": wl["desc"], "atoms": int(natom),
+                      "preparation": "untimed relaxation: %d Langevin steps at %.1f fs, friction %.0e/s, then "
+                                     "Maxwell-Boltzmann velocities" % (RELAX["steps"], RELAX["dt"] * 1e15,
+                                                                       RELAX["fric"]),
                       "systems": int(image.nsystems), "l2": "flushed before every timed step (256 MB write)",
                       "graphs": True, "exchanges_in_timed_region": exchanges, "autotune": tuned,
                       "parallelism": "replicas only (%d GPU%s)" % (world, "s" if world > 1 else "")},

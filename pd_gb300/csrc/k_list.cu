@@ -336,7 +336,7 @@ __global__ void k_masks(DevView v) {
 }
 
 // per-evaluation pack: FP64 positions -> float offsets from the block centre
-__global__ void k_pack(DevView v, const double* charge, float check2, int store_ref) {
+__global__ void k_pack(DevView v, const double* charge, float check2, int store_ref, long long ncand) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= v.nslots) return;
   int a = v.sorted_atom[s];
@@ -357,7 +357,8 @@ __global__ void k_pack(DevView v, const double* charge, float check2, int store_
     o = make_float4((float)r[0], (float)r[1], (float)r[2], (float)charge[a]);
     if (store_ref) {
       v.rel0[s] = o;
-    } else if (check2 > 0.f) {
+    } else if (check2 > 0.f && (long long)*v.ntiles < ncand) {
+      // (when every block pair of every system is a tile no pair can leave the list)
       float4 q = v.rel0[s];
       float dx = o.x - q.x, dy = o.y - q.y, dz = o.z - q.z;
       if (dx * dx + dy * dy + dz * dz > check2) atomicOr(v.status, (unsigned)ST_STALE_LIST);
@@ -400,7 +401,7 @@ int launch_list_build(Context& c, float list_radius) {
   k_tiles<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, list_radius, (float)c.lp.Padding);
   // masks: launched over the worst case; warps beyond *ntiles return at once
   k_masks<<<nblk(c.ncand * 32, 256), 256, 0, st>>>(v);
-  k_pack<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_charge.p, 0.f, 1);
+  k_pack<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_charge.p, 0.f, 1, c.ncand);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 
@@ -408,7 +409,7 @@ int launch_pack(Context& c, float check_disp) {
   c.kernel_launches += 1;
   DevView v = c.view();
   float c2 = check_disp > 0 ? check_disp * check_disp : 0.f;
-  k_pack<<<nblk(c.nslots, 256), 256, 0, c.stream>>>(v, c.d_charge.p, c2, 0);
+  k_pack<<<nblk(c.nslots, 256), 256, 0, c.stream>>>(v, c.d_charge.p, c2, 0, c.ncand);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

@@ -341,7 +341,7 @@ int pdgpu_md_autotune(pdgpu_ctx* h, int trial_steps, int* update_nlist, int* cta
   CK(cudaMemcpyAsync(sa0.data(), md.d_facc_sa.p, sa0.size() * 8, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
 
-  const int cadences[] = {5, 10, 20, 40, 80};
+  const int cadences[] = {1, 2, 3, 5, 10, 20, 40, 80};
   const int shapes[] = {4, 8, 16};
   double best = 1e300;
   int best_n = p0.UpdateNList, best_s = c.tile_ctas_per_sm;
@@ -361,6 +361,8 @@ int pdgpu_md_autotune(pdgpu_ctx* h, int trial_steps, int* update_nlist, int* cta
       int st = md_run_impl(c, md, trial_steps, false);
       auto t1 = std::chrono::steady_clock::now();
       if (st != PDGPU_OK) continue;  // stale list (or worse): cadence too long
+      // the cadence must also survive a longer stretch (4 rebuild windows)
+      if (md_run_impl(c, md, 4 * n, false) != PDGPU_OK) continue;
       double dt = std::chrono::duration<double>(t1 - t0).count();
       if (dt < best) {
         best = dt;

@@ -119,12 +119,20 @@ class SystemImage:
         box = d["box"].reshape(-1, 3)
         if len(box) != nsys:
             box = np.repeat(box[:1], nsys, axis=0)
-        excl = np.stack([d["excl_i"], d["excl_i"] + d["excl_dj"], d["excl_bo"].astype(np.int32)], axis=1)
+        ei = d["excl_i"] if "excl_i" in d else np.cumsum(d["excl_first_delta"].astype(np.int64)).astype(np.int32)
+        excl = np.stack([ei, ei + d["excl_dj"], d["excl_bo"].astype(np.int32)], axis=1)
         has_gb = bool(np.any(col("gb_vj") != 0))
         has_sa = bool(np.any(col("lcpo_use") != 0))
 
         def bonded(k):
-            return d[k + "_idx"], d[k + "_partable"][d[k + "_parclass"].astype(np.int64)]
+            par = d[k + "_partable"][d[k + "_parclass"].astype(np.int64)]
+            if k + "_idx" in d:
+                return d[k + "_idx"], par
+            first = np.cumsum(d[k + "_first_delta"].astype(np.int64))
+            cols = [first] + [first + d[k + "_rel"][:, c] for c in range(d[k + "_rel"].shape[1])]
+            if k + "_terms" in d:
+                cols.append(d[k + "_terms"].astype(np.int64))
+            return np.stack(cols, axis=1).astype(np.int32), par
 
         return cls(natoms, box, col("charge"), col("radius"), col("epsilon"), col("mass"), excl,
                    gb_radius=col("gb_radius") if has_gb else None, gb_vj=col("gb_vj") if has_gb else None,

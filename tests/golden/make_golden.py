@@ -144,13 +144,32 @@ def compact_image(d):
     return img
 
 
+def encode_indices(img):
+    """Delta-encode the index arrays of an image: first atom of each row as the
+    difference from the previous row, the other atoms relative to the first
+    (all small integers, so the npz compresses them to almost nothing)."""
+    out = dict(img)
+    for k in ("bond", "angle", "torsion", "improper"):
+        idx = img.pop(k + "_idx") if k + "_idx" in img else out.pop(k + "_idx")
+        out.pop(k + "_idx", None)
+        natom_cols = {"bond": 2, "angle": 3, "torsion": 4, "improper": 4}[k]
+        first = idx[:, 0].astype(np.int64)
+        out[k + "_first_delta"] = np.diff(first, prepend=0).astype(np.int32)
+        out[k + "_rel"] = (idx[:, 1:natom_cols] - idx[:, :1]).astype(np.int16)
+        if idx.shape[1] > natom_cols:
+            out[k + "_terms"] = idx[:, natom_cols].astype(np.int8)
+    ei = out.pop("excl_i")
+    out["excl_first_delta"] = np.diff(ei.astype(np.int64), prepend=0).astype(np.int32)
+    return out
+
+
 def make_workloads(which):
     os.makedirs(WORKLOADS, exist_ok=True)
     for name, (kind, opts) in WORKLOAD_SPECS.items():
         if which and name not in which:
             continue
         d = run_driver(kind, opts)
-        img = compact_image(d)
+        img = encode_indices(compact_image(d))
         path = os.path.join(WORKLOADS, name + ".npz")
         np.savez_compressed(path, **img)
         print("%-14s natoms=%6d  %7.1f kB" % (name, len(d["pos"]), os.path.getsize(path) / 1024))
@@ -219,7 +238,7 @@ def make_c4():
     img["gb_P"] = parts[0]["gb_P"]
     img["cfg_padding"] = parts[0]["cfg_padding"]
     path = os.path.join(WORKLOADS, "c4_remd64.npz")
-    np.savez_compressed(path, **img)
+    np.savez_compressed(path, **encode_indices(img))
     print("%-14s natoms=%6d  %7.1f kB" % ("c4_remd64", len(img["pos"]), os.path.getsize(path) / 1024))
 
 

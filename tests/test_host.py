@@ -1,0 +1,73 @@
+"""Host-side logic: workload images, batching, the PD-interface mirror (no GPU)."""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+
+@pytest.mark.parametrize("name,natom,nsys", [("c1_water", 2001, 1), ("c2_solvated", 22489, 1),
+                                             ("c3_gb256", 4235, 1), ("c4_remd64", 209991, 64)])
+def test_workload_images_load(name, natom, nsys):
+    from pd_gb300.workspace import load_workload
+    im = load_workload(name)
+    assert im.natom == natom and im.nsystems == nsys
+    assert np.all(np.isfinite(im.pos)) and np.all(im.mass > 0)
+    sys_of = np.repeat(np.arange(nsys), im.natoms)
+    # bonded pairs and terms never cross systems and name valid atoms
+    assert np.all(sys_of[im.excl[:, 0]] == sys_of[im.excl[:, 1]])
+    for idx, par in (im.bonds, im.angles, im.torsions, im.impropers):
+        ncol = {2: 2, 3: 3, 5: 4}[idx.shape[1]]
+        assert idx.shape[0] == par.shape[0]
+        if len(idx):
+            assert idx[:, :ncol].min() >= 0 and idx[:, :ncol].max() < natom
+            assert np.all(sys_of[idx[:, 0]][:, None] == sys_of[idx[:, :ncol]])
+    if nsys == 64:
+        assert 400 < im.natoms.min() and im.natoms.max() < 9000
+        assert im.has_gb and im.has_sa and not im.periodic
+
+
+def test_concat_and_subset_roundtrip():
+    from pd_gb300.workspace import SystemImage
+    a = SystemImage._from_fixture(golden("peptide30"))
+    b = SystemImage._from_fixture(golden("peptide120"))
+    cat = SystemImage.concat([a, b, a])
+    assert cat.nsystems == 3 and cat.natom == 2 * a.natom + b.natom
+    for k, ref in enumerate([a, b, a]):
+        sub = cat.subset(k)
+        assert np.array_equal(sub.pos, ref.pos) and np.array_equal(sub.excl, ref.excl)
+        for t in ("bonds", "angles", "torsions", "impropers"):
+            assert np.array_equal(getattr(sub, t)[0], getattr(ref, t)[0])
+            assert np.array_equal(getattr(sub, t)[1], getattr(ref, t)[1])
+
+
+def test_forcefield_defaults_mirror_pd():
+    """Constructor defaults of the components equal PD's (nonbonded.cpp:985-1021, gbff.cpp:33-55, lcpo.h)."""
+    import pd_gb300 as pdg
+    ws = pdg.WorkSpace(pdg.SystemImage._from_fixture(golden("peptide30")))
+    nb = pdg.FF_NonBonded_GPU(ws)
+    assert (nb.Cutoff, nb.InnerCutoff, nb.VdwCutoff, nb.VdwInnerCutoff) == (15, 12, 15, 12)
+    assert nb.ForceSwitch and not nb.EnergySwitch and nb.AutoScaling14
+    gb = pdg.FF_GeneralizedBorn_Still_GPU(ws)
+    assert gb.EnergySwitch and not gb.ForceSwitch and gb.FastMode
+    assert (gb.DielectricSolvent, gb.DielectricSolute, gb.GbsaStillCutoff, gb.ExpApproxThreshold) == (80, 1, 10, -4)
+    sa = pdg.FF_SASA_LCPO_GPU(ws)
+    assert sa.UpdateSasa == 5 and sa.GlobalASP == 0
+    nb.setup()
+    assert (nb.Vdw14Scaling, nb.Elec14Scaling) == (0.5, 0.83333)
+    assert ws.Padding == 0.5
+
+
+def test_maxwell_boltzmann_hits_target_temperature():
+    from pd_gb300.md import KB, maxwell_boltzmann
+    m = np.full(3000, 2e-26)
+    v = maxwell_boltzmann(m, [300.0, 450.0], 1, [1000, 2000])
+    for sl, T in ((slice(0, 1000), 300.0), (slice(1000, 3000), 450.0)):
+        ke = 0.5 * (m[sl, None] * v[sl] ** 2).sum()
+        assert abs(2 * ke / (3 * (sl.stop - sl.start) * KB) - T) < 1e-9 * T
+
+
+def test_geometric_ladder():
+    from pd_gb300.md import REX_Local
+    t = REX_Local.geometric_ladder(300.0, 500.0, 64)
+    assert t[0] == 300.0 and abs(t[-1] - 500.0) < 1e-9
+    assert np.allclose(t[1:] / t[:-1], (500 / 300.) ** (1 / 63))
