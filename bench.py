@@ -184,7 +184,7 @@ def make_context(image, wl, key, seed, use_graph=True, device=0, update_nlist=10
     ctx.set_positions(image.pos)
     temps = temperatures(image, key)
     what = flags(wl["what"])
-    if relax:
+    if relax and RELAX["steps"] > 0:
         ctx.md_setup(temps, integrator=1, timestep=RELAX["dt"], fric=RELAX["fric"], update_nlist=RELAX["update_nlist"],
                      update_sasa=5, what=what, seed=seed + 7, use_graph=True)
         ctx.md_run(RELAX["steps"])
@@ -430,15 +430,16 @@ def run_ours(args, key, wl, image):
                                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
     ctx.close()
 
+    nl = tuned["UpdateNList"] if tuned else 10
     # plain single-system path on the same systems (rank 0, N=1 semantics per rank)
     plain = None
     if rank == 0 and image.nsystems > 1 and not args.no_plain:
-        plain = run_plain(args, key, wl, image, torch)
+        plain = run_plain(args, key, wl, image, torch, nl)
 
     # end to end through the C ABI with host buffers
     e2e = None
     if rank == 0 and not args.no_e2e:
-        e2e = run_e2e(args, key, wl, image, torch)
+        e2e = run_e2e(args, key, wl, image, torch, nl)
 
     if rank != 0:
         return
@@ -466,50 +467,49 @@ def run_ours(args, key, wl, image):
     print(json.dumps(out))
 
 
-def run_plain(args, key, wl, image, torch):
-    """Each system in its own context, launched one after the other, no graphs."""
+def run_plain(args, key, wl, image, torch, update_nlist):
+    """The single-system path on the same systems, as PD's REX_Local runs its
+    replicas: one system at a time, each advanced a chunk of steps through its
+    own context (graphs on), waiting for it before moving to the next."""
     ctxs = []
     for k in range(image.nsystems):
         sub = image.subset(k)
-        c, _ = make_context(sub, wl, key, 2000 + k, use_graph=False)
+        c, _ = make_context(sub, wl, key, 2000 + k, update_nlist=update_nlist)
         ctxs.append(c)
-    steps = max(3, min(args.steps, 20))
+    chunk = max(5, min(args.steps, 20))
     for c in ctxs:
-        c.md_run(2)
+        c.md_run(chunk)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(steps):
-        for c in ctxs:
-            c.md_enqueue(1)
     for c in ctxs:
-        c.synchronize()
+        c.md_run(chunk)
     el = time.perf_counter() - t0
     for c in ctxs:
         c.close()
-    return {"value": image.natom * steps / el, "unit": "atom-steps/s", "steps": steps,
-            "how": "one context per system (%d), launched in turn, no CUDA graphs, wall clock" % image.nsystems}
+    return {"value": image.natom * chunk / el, "unit": "atom-steps/s", "steps": chunk,
+            "how": "one context per system (%d), each run %d steps in turn (PD REX_Local order), wall clock"
+                   % (image.nsystems, chunk)}
 
 
-def run_e2e(args, key, wl, image, torch):
-    """Per step through the C ABI with pinned host buffers: positions H2D, one MD step,
-    energies and positions D2H (the user-visible loop of a PD host protocol)."""
-    ctx, _ = make_context(image, wl, key, 3000, use_graph=True)
+def run_e2e(args, key, wl, image, torch, update_nlist):
+    """Per step through the C ABI with pinned host buffers: positions H2D, one MD
+    step of every system, positions and kinetic energies D2H."""
+    ctx, _ = make_context(image, wl, key, 3000, use_graph=True, update_nlist=update_nlist)
     n = image.natom
     pos_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
-    pos_h[:] = image.pos
     steps = max(3, min(args.steps, 50))
     ctx.md_run(3)
     pos_h[:] = ctx.get_positions()
     t0 = time.perf_counter()
     for _ in range(steps):
         ctx.set_positions(pos_h)
-        ctx.md_run(1, energy_on_last=True)
-        ctx.energies()
+        ctx.md_run(1)
+        ctx.kinetic()
         pos_h[:] = ctx.get_positions()
     el = time.perf_counter() - t0
     ctx.close()
     return {"value": n * steps / el, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * n,
-            "d2h_bytes_per_step": 24 * n + 96 * image.nsystems, "steps": steps}
+            "d2h_bytes_per_step": 24 * n + 8 * image.nsystems, "steps": steps}
 
 
 def main():
@@ -525,7 +525,10 @@ def main():
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--relax-steps", type=int, default=RELAX["steps"],
+                    help="untimed relaxation steps before timing (0 for short profiling runs)")
     args = ap.parse_args()
+    RELAX["steps"] = args.relax_steps
     args.warmup = max(args.warmup, 3)
     from pd_gb300.workspace import load_workload
     wl = WORKLOADS[args.workload]
