@@ -12,7 +12,10 @@ the plain single-system GPU path on the same systems (one context per system,
 no batching, no graphs), the force error against the FP64 oracle, and the
 oracle's CPU throughput on the host cores.
 
-Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c1|c2|c3|c4] [--impl reference]
+Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c1|c2|c3|c4|c5] [--impl reference]
+(c5 is the parameter-fitting task through the adjoint kernels: its own JSON
+line, frame-atom gradient evaluations per second, with a finite-difference
+check against the FP64 oracle.)
 Under torchrun each rank runs its own replica set (replicas only: the path has
 no exchange between GPUs); rank 0 prints one JSON line.
 """
@@ -148,6 +151,15 @@ def flags(names):
     return w
 
 
+def gb_settings(image):
+    """FF_GeneralizedBorn_Still attributes of the GB workloads: all pairs, eps 1 / 80."""
+    s14v, s14e = image.scaling14
+    P = image.gb_P
+    return dict(Cutoff=999.0, InnerCutoff=998.0, VdwCutoff=999.0, VdwInnerCutoff=998.0, Vdw14Scaling=s14v,
+                Elec14Scaling=s14e, DielectricSolute=1.0, DielectricSolvent=80.0, GbsaStillCutoff=999.0,
+                ExpApproxThreshold=-4.0, BornRadiusOffset=0.0, P4=P[3], P5=P[4])
+
+
 def configure(ctx, wl, image):
     """Component parameters of each workload (PD attribute names)."""
     s14v, s14e = image.scaling14
@@ -155,10 +167,7 @@ def configure(ctx, wl, image):
         ctx.set_nb(Cutoff=12.0, InnerCutoff=10.0, VdwCutoff=12.0, VdwInnerCutoff=10.0, Vdw14Scaling=s14v,
                    Elec14Scaling=s14e, Dielectric=1.0, EnergySwitch=1, ForceSwitch=0, DoVdw=1, DoElec=1)
     if "GB" in wl["what"]:
-        P = image.gb_P
-        ctx.set_gb(Cutoff=999.0, InnerCutoff=998.0, VdwCutoff=999.0, VdwInnerCutoff=998.0, Vdw14Scaling=s14v,
-                   Elec14Scaling=s14e, DielectricSolute=1.0, DielectricSolvent=80.0, GbsaStillCutoff=999.0,
-                   ExpApproxThreshold=-4.0, BornRadiusOffset=0.0, P4=P[3], P5=P[4])
+        ctx.set_gb(**gb_settings(image))
     ctx.set_list(wl["padding"])
 
 
@@ -512,12 +521,139 @@ def run_e2e(args, key, wl, image, torch, update_nlist):
             "d2h_bytes_per_step": 24 * n + 8 * image.nsystems, "steps": steps}
 
 
+# ---------------------------------------------------------------------------
+# C5: parameter fitting through the adjoint (not the headline metric)
+# ---------------------------------------------------------------------------
+def oracle_frame_loss(image, frames, tables, theta, target):
+    """The C5 loss of a few frames from the FP64 oracle (for the finite-difference check)."""
+    from oracle import pdoracle as O
+    from pd_gb300.adjoint import KCAL_TO_J
+    q, r, e, R, V, T = [a.detach().cpu().numpy() for a in tables.atom_arrays(
+        theta["radius"], theta["sqrt_well"], theta["charge"], theta["gb_radius"])]
+    s14v, s14e = image.scaling14
+    P = image.gb_P
+    gp = O.gb_params(Cutoff=999, InnerCutoff=998, VdwCutoff=999, VdwInnerCutoff=998, Vdw14Scaling=s14v,
+                     Elec14Scaling=s14e, GbsaStillCutoff=999, P1=P[0], P2=P[1], P3=P[2], P4=P[3], P5=P[4],
+                     ListCutoff=1001)
+    threads = os.cpu_count() or 1
+    tot = 0.0
+    for f, pos in enumerate(frames):
+        s = O.OracleSystem(pos, q, r, e, image.excl, tuple(image.box[0]))
+        E, _, _ = O.gb_forces(s, gp, R, V, T, threads)
+        tot += ((E[1] + E[2] + E[3] - float(target[f])) / KCAL_TO_J) ** 2
+    return tot / len(frames)
+
+
+def run_adjoint(args):
+    """C5: 256 frames taken every 100 Langevin steps of C3; loss = mean over frames
+    of (E(theta') - E(theta))^2 for the GB + LJ + Coulomb energy; Adam steps on
+    per-type LJ radius / sqrt(well depth), per-type GB radius and per-atom
+    charges through the adjoint kernels.  One timed step = energy + parameter
+    gradient of every frame (one device call), the torch chain rule through the
+    GB fixed terms and the per-type tables, and the Adam update."""
+    import torch
+    from pd_gb300 import ffi
+    from pd_gb300.adjoint import FrameSet, ParamTables, frame_loss, perturb
+    from pd_gb300.workspace import load_workload
+    wl = WORKLOADS["c3"]
+    image = load_workload(wl["image"])
+    nframes, every = args.frames, 100
+    ctx, _ = make_context(image, wl, "c3", 5, update_nlist=10)
+    frames = []
+    for _ in range(nframes):
+        ctx.md_run(every)
+        frames.append(ctx.get_positions())
+    ctx.close()
+    T = ParamTables(image, device="cuda")
+    fs = FrameSet(image, frames, ffi.GB, gb_settings(image), padding=wl["padding"])
+    with torch.no_grad():
+        target = fs.energies(*T.atom_arrays(T.radius, T.sqrt_well, T.charge, T.gb_radius))
+    theta0 = perturb(T, seed=5)
+    logp = ("radius", "sqrt_well", "gb_radius")
+    x0 = {k: v.detach() for k, v in theta0.items()}
+    svar = {k: torch.zeros_like(x0[k], requires_grad=True) for k in logp}
+    dq = torch.zeros_like(x0["charge"], requires_grad=True)
+    opt = torch.optim.Adam(list(svar.values()) + [dq], lr=1e-2)
+
+    def theta():
+        th = {k: x0[k] * torch.exp(svar[k]) for k in logp}
+        th["charge"] = x0["charge"] + 0.1 * (dq - dq.mean())
+        return th
+
+    def step():
+        opt.zero_grad()
+        loss = frame_loss(fs, T, theta(), target)
+        loss.backward()
+        opt.step()
+        return float(loss.detach())
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    hist = [step() for _ in range(args.warmup)]
+    launches0 = fs.ctx.kernel_launches()
+    sampler = ClockSampler(0)
+    sampler.start()
+    t_steps = []
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hist.append(step())
+        torch.cuda.synchronize()
+        t_steps.append(time.perf_counter() - t0)
+    clocks = sampler.stop()
+    launches = fs.ctx.kernel_launches() - launches0
+    el = sum(t_steps)
+    # finite-difference check of d loss / d theta on 32 parameters, loss over the first frames
+    nfd = min(8, nframes)
+    fs8 = FrameSet(image, frames[:nfd], ffi.GB, gb_settings(image), padding=wl["padding"])
+    th = {k: v.detach().clone().requires_grad_(True) for k, v in theta0.items()}
+    loss8 = frame_loss(fs8, T, th, target[:nfd])
+    loss8.backward()
+    rng = np.random.default_rng(32)
+    worst, within = 0.0, 0
+    checks = []
+    for name in ("radius", "sqrt_well", "gb_radius", "charge"):
+        g = th[name].grad.detach().cpu().numpy()
+        x = th[name].detach()
+        cand = np.flatnonzero(x.cpu().numpy() != 0)
+        for a in rng.choice(cand, 8, replace=False):
+            h = 1e-4 * (1.0 if name == "charge" else abs(float(x[a])))
+            tp = {k: v.detach().clone() for k, v in th.items()}
+            tm = {k: v.detach().clone() for k, v in th.items()}
+            tp[name][a] += h
+            tm[name][a] -= h
+            fd = (oracle_frame_loss(image, frames[:nfd], T, tp, target) -
+                  oracle_frame_loss(image, frames[:nfd], T, tm, target)) / (2 * h)
+            err = abs(g[a] - fd) / max(abs(fd), 1e-300)
+            ok = abs(g[a] - fd) <= 1e-4 * abs(fd) + 1e-6 * float(np.max(np.abs(g)))
+            within += int(ok)
+            worst = max(worst, err)
+            checks.append((name, int(a), float(g[a]), float(fd)))
+    n_atoms = image.natom
+    out = {"metric": "C5 adjoint: frame-atom energy+gradient evaluations/s inside Adam steps",
+           "value": nframes * n_atoms * args.steps / el, "unit": "frame-atoms/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math / f64 energies and sums",
+           "data": "synthetic: frames of the C3 peptide (%d atoms) every %d Langevin steps" % (n_atoms, every),
+           "config": {"workload": "c5", "frames": nframes, "atoms_per_frame": n_atoms,
+                      "parameters": {k: int(v.numel()) for k, v in theta0.items()},
+                      "l2": "flushed before every timed step (256 MB write)",
+                      "timing": "wall clock per Adam step with device synchronisation on both sides"},
+           "loss": {"first": hist[0], "last": hist[-1], "steps": len(hist)},
+           "fd_check": {"parameters": len(checks), "within_tolerance": within, "worst_rel_err": worst,
+                        "frames": nfd, "h": "1e-4 (relative; absolute e for charges)",
+                        "tolerance": "|g-fd| <= 1e-4|fd| + 1e-6 max|g|", "samples": checks[:4]},
+           "gpu_launches": int(launches), "clocks": clocks}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
-    ap.add_argument("--workload", default="c4", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c4", choices=sorted(WORKLOADS) + ["c5"])
+    ap.add_argument("--frames", type=int, default=256, help="c5: frames of the C3 trajectory")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -531,6 +667,15 @@ def main():
     RELAX["steps"] = args.relax_steps
     args.warmup = max(args.warmup, 3)
     from pd_gb300.workspace import load_workload
+    if args.workload == "c5":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "PD has no parameter gradient; its derivative is "
+                              "a finite difference of calcEnergies (c5 is checked against that in fd_check)"}))
+            return
+        from pd_gb300 import build as _b
+        _b.build()
+        run_adjoint(args)
+        return
     wl = WORKLOADS[args.workload]
     image = load_workload(wl["image"])
     if args.impl == "reference":

@@ -112,10 +112,16 @@ const char *pdgpu_error_string(int status);
 int pdgpu_set_nb_params(pdgpu_ctx *ctx, const pdgpu_nb_params *p);
 int pdgpu_set_gb_params(pdgpu_ctx *ctx, const pdgpu_gb_params *p);
 int pdgpu_set_list_params(pdgpu_ctx *ctx, const pdgpu_list_params *p);
-/* Per-atom charges / LJ radius / sqrt(eps) / GB Vj, terms123 (all optional, NULL keeps) —
- * the parameter update after FF re-setup. */
+/* Per-atom charges / LJ radius / epsilon (PD's sqrt(J) storage) / GB radius,
+ * Vj, terms123 (all optional, NULL keeps) — the parameter update after FF
+ * re-setup.  The list is kept; the per-slot copies are refreshed. */
 int pdgpu_update_params(pdgpu_ctx *ctx, const double *charge, const double *radius, const double *epsilon,
-                        const double *gb_vj, const double *gb_terms123);
+                        const double *gb_radius, const double *gb_vj, const double *gb_terms123);
+/* Same with device arrays (no host synchronisation); the per-slot copies are
+ * refreshed on the context stream without rebuilding the list. */
+int pdgpu_update_params_device(pdgpu_ctx *ctx, const double *d_charge, const double *d_radius,
+                               const double *d_epsilon, const double *d_gb_radius, const double *d_gb_vj,
+                               const double *d_gb_terms123);
 
 /* ---- state ---------------------------------------------------------------- */
 /* Upload positions (Angstrom).  stride_bytes is the distance between atoms;
@@ -148,6 +154,29 @@ int pdgpu_get_energies(pdgpu_ctx *ctx, pdgpu_energies *out);
  * the last evaluation that computed them. */
 int pdgpu_get_born_radii(pdgpu_ctx *ctx, double *born);
 int pdgpu_get_sasa(pdgpu_ctx *ctx, double *sasa);
+
+/* ---- parameter gradients (adjoint) ----------------------------------------
+ * PD has no counterpart: its parameter derivatives are finite differences of
+ * Forcefield::calcEnergies with setup() re-run after each edit
+ * (src/mmlib/forcefields/nonbonded.cpp:1078-1084).  One call evaluates the
+ * energies (FP64 per pair) and dE/dp for every per-atom parameter array of
+ * pdgpu_system_desc, in original atom order, J per unit of the parameter as
+ * it is given there (charge e, radius A, epsilon sqrt(J), gb_radius A, gb_vj
+ * A^3, gb_terms123 its own unit); E is the system's own energy, so atoms of
+ * different systems get the gradient of their own system's energy.  `what`
+ * names exactly one of PDGPU_NB / PDGPU_GB (SA / BONDED may be added; they
+ * contribute energies only).  The GB gradient is the exact derivative of the
+ * energy through the Born radii, including the fixed terms' inputs gb_vj and
+ * gb_terms123 (their own dependence on gb_radius is the caller's chain rule).
+ * Null pointers are skipped. */
+typedef struct {
+    double *charge, *radius, *epsilon;          /* LJ + Coulomb (and GB charge terms) */
+    double *gb_radius, *gb_vj, *gb_terms123;    /* GB only (zero for PDGPU_NB) */
+} pdgpu_param_grads;
+int pdgpu_param_grad(pdgpu_ctx *ctx, unsigned what, pdgpu_energies *out, const pdgpu_param_grads *g);
+/* Device-array form: queued on the context stream; energies stay on the device
+ * until pdgpu_get_energies(), status via pdgpu_synchronize(). */
+int pdgpu_param_grad_device(pdgpu_ctx *ctx, unsigned what, const pdgpu_param_grads *d_g);
 
 /* ---- dynamics: MolecularDynamics / REX_Local --------------------------------- */
 /* Integrator settings (PD src/mmlib/protocols/md.h, defaults md.cpp:60-86). */
@@ -186,10 +215,17 @@ int pdgpu_get_kinetic(pdgpu_ctx *ctx, double *ekin);
  * NULL) reports rung pair r; temps (may be NULL) returns each system's new
  * target temperature. */
 int pdgpu_remd_exchange(pdgpu_ctx *ctx, int parity, int *accepted, double *temps);
-/* Project autotuner: times short trial runs (state restored afterwards) over
- * list-rebuild cadences and tile-kernel launch shapes and keeps the fastest
- * setting whose list never goes stale.  Outputs may be NULL. */
-int pdgpu_md_autotune(pdgpu_ctx *ctx, int trial_steps, int *update_nlist, int *ctas_per_sm);
+/* Project autotuner (state restored afterwards): first the launch shape of the
+ * tile kernels (CTAs per SM x consecutive tiles per warp work item), timed on
+ * force evaluations of the current state; then the list-rebuild cadence,
+ * timed on short trial runs, keeping the fastest whose list never goes stale.
+ * Outputs may be NULL. */
+int pdgpu_md_autotune(pdgpu_ctx *ctx, int trial_steps, int *update_nlist, int *ctas_per_sm, int *tile_chunk);
+/* Launch shape of the pair-tile kernels (what the autotuner sets): resident
+ * CTAs per SM of their grid (1..64) and tiles per warp work item (1..64).
+ * Results do not depend on it (per-tile sums enter fixed point). */
+int pdgpu_set_launch_shape(pdgpu_ctx *ctx, int ctas_per_sm, int tile_chunk);
+int pdgpu_get_launch_shape(pdgpu_ctx *ctx, int *ctas_per_sm, int *tile_chunk);
 
 /* ---- diagnostics ---------------------------------------------------------- */
 /* Tile / pair counts of the current list: ntiles, nmasked tiles, slots. */

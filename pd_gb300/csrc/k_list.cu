@@ -241,10 +241,9 @@ __global__ void k_slot_params(DevView v, const double* radius, const double* sqe
   if (lc_par) lc_par[s] = l;
 }
 
-// candidate block pairs -> tiles
-__global__ void k_tiles(DevView v, long long ncand, float R, float margin) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncand) return;
+// candidate block pairs -> include flags, in candidate order (row-major: bi, then bj >= bi)
+__device__ __forceinline__ bool candidate_pair(const DevView& v, long long t, int& gi, int& gj, int& flags, float R,
+                                               float margin) {
   // system by binary search over cand_start
   int lo = 0, hi = v.nsys - 1;
   while (lo < hi) {
@@ -263,7 +262,8 @@ __global__ void k_tiles(DevView v, long long ncand, float R, float margin) {
   while (bi > 0 && bi * nb - bi * (bi - 1) / 2 > l) bi--;
   while (bi + 1 < nb && (bi + 1) * nb - (bi + 1) * bi / 2 <= l) bi++;
   long long bj = bi + (l - (bi * nb - bi * (bi - 1) / 2));
-  int gi = S.block_start + (int)bi, gj = S.block_start + (int)bj;
+  gi = S.block_start + (int)bi;
+  gj = S.block_start + (int)bj;
   float4 hi4 = v.half[gi], hj4 = v.half[gj];
   float hs[3] = {hi4.x + hj4.x, hi4.y + hj4.y, hi4.z + hj4.z};
   double dist2 = 0;
@@ -278,14 +278,33 @@ __global__ void k_tiles(DevView v, long long ncand, float R, float margin) {
     double g = fabs(d) - hs[c];
     if (g > 0) dist2 += g * g;
   }
-  if (dist2 > (double)R * R) return;
-  int idx = atomicAdd(v.ntiles, 1);
+  flags = (need_mi ? 1 : 0) | (gi == gj ? 2 : 0);
+  return dist2 <= (double)R * R;
+}
+
+__global__ void k_tile_flags(DevView v, long long ncand, float R, float margin, int* flag) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncand) return;
+  int gi, gj, fl;
+  flag[t] = candidate_pair(v, t, gi, gj, fl, R, margin) ? 1 : 0;
+}
+
+// write the included pairs at their scanned positions: the tile list is in
+// row-major order, so every run of tiles with one i-block is contiguous and
+// its order is the same on every build
+__global__ void k_tile_write(DevView v, long long ncand, float R, float margin, const int* flag, const int* pos) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncand) return;
+  if (t == ncand - 1) *v.ntiles = pos[t] + flag[t];
+  if (!flag[t]) return;
+  int gi, gj, fl;
+  candidate_pair(v, t, gi, gj, fl, R, margin);
   Tile T;
   T.bi = gi;
   T.bj = gj;
   T.mask = -1;
-  T.flags = (need_mi ? 1 : 0) | (gi == gj ? 2 : 0);
-  v.tiles[idx] = T;
+  T.flags = fl;
+  v.tiles[pos[t]] = T;
 }
 
 // bond order of an atom pair as PD's list stores it; 7 when not bonded
@@ -357,8 +376,9 @@ __global__ void k_pack(DevView v, const double* charge, float check2, int store_
     o = make_float4((float)r[0], (float)r[1], (float)r[2], (float)charge[a]);
     if (store_ref) {
       v.rel0[s] = o;
-    } else if (check2 > 0.f && (long long)*v.ntiles < ncand) {
-      // (when every block pair of every system is a tile no pair can leave the list)
+    } else if (check2 > 0.f && (S.periodic || (long long)*v.ntiles < ncand)) {
+      // (in open space, when every block pair of every system is a tile, no pair
+      // can leave the list; in a periodic box the tile images still depend on it)
       float4 q = v.rel0[s];
       float dx = o.x - q.x, dy = o.y - q.y, dz = o.z - q.z;
       if (dx * dx + dy * dy + dz * dz > check2) atomicOr(v.status, (unsigned)ST_STALE_LIST);
@@ -370,7 +390,7 @@ __global__ void k_pack(DevView v, const double* charge, float check2, int store_
 static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 int launch_list_build(Context& c, float list_radius) {
-  c.kernel_launches += 14;
+  c.kernel_launches += 18;
   DevView v = c.view();
   cudaStream_t st = c.stream;
   int ncells = c.nsys * kCellsPerSystem;
@@ -398,10 +418,30 @@ int launch_list_build(Context& c, float list_radius) {
                                                       c.has_sa ? c.d_lcpoUse.p : nullptr,
                                                       c.has_sa ? c.d_lc_par.p : nullptr);
   cudaMemsetAsync(c.d_counters.p, 0, sizeof(int) * 2, st);
-  k_tiles<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, list_radius, (float)c.lp.Padding);
+  k_tile_flags<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, list_radius, (float)c.lp.Padding, c.d_tile_flag.p);
+  {
+    int nb2 = nblk(c.ncand, 1024);
+    k_scan_block<<<nb2, 1024, 0, st>>>(c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
+    k_scan_sums<<<1, 1024, 0, st>>>(c.d_scan_tmp2.p, nb2);
+    k_scan_add<<<nb2, 1024, 0, st>>>(c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
+  }
+  k_tile_write<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, list_radius, (float)c.lp.Padding, c.d_tile_flag.p,
+                                                    c.d_tile_pos.p);
   // masks: launched over the worst case; warps beyond *ntiles return at once
   k_masks<<<nblk(c.ncand * 32, 256), 256, 0, st>>>(v);
   k_pack<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_charge.p, 0.f, 1, c.ncand);
+  return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
+}
+
+int launch_slot_params(Context& c) {
+  c.kernel_launches += 1;
+  DevView v = c.view();
+  k_slot_params<<<nblk(c.nslots, 256), 256, 0, c.stream>>>(v, c.d_radius.p, c.d_sqeps.p,
+                                                            c.has_gb ? c.d_gbR.p : nullptr,
+                                                            c.has_gb ? c.d_gbVj.p : nullptr,
+                                                            c.has_sa ? c.d_lcpoR.p : nullptr,
+                                                            c.has_sa ? c.d_lcpoUse.p : nullptr,
+                                                            c.has_sa ? c.d_lc_par.p : nullptr);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

@@ -30,13 +30,16 @@ __device__ __forceinline__ uint4 philox4x32(uint4 ctr, uint2 key) {
   return ctr;
 }
 __device__ __forceinline__ double u01(unsigned x) { return ((double)x + 0.5) * (1.0 / 4294967296.0); }
+// 24-bit uniform in (0, 1) for the noise: FP32 is ample for a Gaussian draw and
+// keeps the transcendental work off the FP64 pipe
+__device__ __forceinline__ float u01f(unsigned x) { return ((float)(x >> 8) + 0.5f) * (1.0f / 16777216.0f); }
 // two unit normals from two uniforms (Box-Muller)
 __device__ __forceinline__ void box_muller(unsigned a, unsigned b, double& n1, double& n2) {
-  double r = sqrt(-2.0 * log(u01(a)));
-  double s, c;
-  sincospi(2.0 * u01(b), &s, &c);
-  n1 = r * c;
-  n2 = r * s;
+  float r = sqrtf(-2.0f * logf(u01f(a)));
+  float s, c;
+  sincospif(2.0f * u01f(b), &s, &c);
+  n1 = (double)(r * c);
+  n2 = (double)(r * s);
 }
 
 __device__ __forceinline__ void atom_force(const MDView& m, int a, double f[3]) {

@@ -368,6 +368,9 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
   if (e == cudaSuccess) e = c.d_half.alloc(c.nblocks);
   if (e == cudaSuccess) e = c.d_tiles.alloc(c.ncand);
   if (e == cudaSuccess) e = c.d_counters.alloc(2);
+  if (e == cudaSuccess) e = c.d_tile_flag.alloc(c.ncand);
+  if (e == cudaSuccess) e = c.d_tile_pos.alloc(c.ncand);
+  if (e == cudaSuccess) e = c.d_scan_tmp2.alloc((c.ncand + 1023) / 1024 + 1);
   if (e == cudaSuccess) e = c.d_masks.alloc((size_t)c.ncand * 32);
   if (e == cudaSuccess) e = c.d_xq.alloc(c.nslots);
   if (e == cudaSuccess) e = c.d_par.alloc(c.nslots);
@@ -442,10 +445,13 @@ int pdgpu_set_list_params(pdgpu_ctx* h, const pdgpu_list_params* p) {
   return PDGPU_OK;
 }
 
+static int enqueue_compute(Context& c, unsigned what, bool energy);
+
 int pdgpu_update_params(pdgpu_ctx* h, const double* charge, const double* radius, const double* epsilon,
-                        const double* gb_vj, const double* gb_terms123) {
+                        const double* gb_radius, const double* gb_vj, const double* gb_terms123) {
   if (!h) return PDGPU_ERR_ARG;
   Context& c = h->c;
+  if ((gb_radius || gb_vj || gb_terms123) && !c.has_gb) return PDGPU_ERR_STATE;
   CK(cudaSetDevice(c.device));
   const size_t N = c.natom;
   if (charge) CK(cudaMemcpyAsync(c.d_charge.p, charge, N * 8, cudaMemcpyHostToDevice, c.stream));
@@ -457,12 +463,89 @@ int pdgpu_update_params(pdgpu_ctx* h, const double* charge, const double* radius
     CK(cudaMemcpyAsync(c.d_sqeps.p, sq.data(), N * 8, cudaMemcpyHostToDevice, c.stream));
     CK(cudaStreamSynchronize(c.stream));
   }
-  if ((gb_vj || gb_terms123) && !c.has_gb) return PDGPU_ERR_STATE;
+  if (gb_radius) CK(cudaMemcpyAsync(c.d_gbR.p, gb_radius, N * 8, cudaMemcpyHostToDevice, c.stream));
   if (gb_vj) CK(cudaMemcpyAsync(c.d_gbVj.p, gb_vj, N * 8, cudaMemcpyHostToDevice, c.stream));
   if (gb_terms123) CK(cudaMemcpyAsync(c.d_gbT.p, gb_terms123, N * 8, cudaMemcpyHostToDevice, c.stream));
+  // the list itself does not depend on the parameters: refresh the per-slot copies
+  if (c.list_built) {
+    int st = launch_slot_params(c);
+    if (st != PDGPU_OK) return st;
+  }
   CK(cudaStreamSynchronize(c.stream));
-  // slot parameters are refreshed at the next list build
-  c.list_built = false;
+  return PDGPU_OK;
+}
+
+}  // extern "C"
+
+static __global__ void k_scale_copy(double* dst, const double* src, size_t n, double f) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i] * f;
+}
+
+extern "C" {
+
+int pdgpu_update_params_device(pdgpu_ctx* h, const double* d_charge, const double* d_radius,
+                               const double* d_epsilon, const double* d_gb_radius, const double* d_gb_vj,
+                               const double* d_gb_terms123) {
+  if (!h) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if ((d_gb_radius || d_gb_vj || d_gb_terms123) && !c.has_gb) return PDGPU_ERR_STATE;
+  CK(cudaSetDevice(c.device));
+  const size_t N = c.natom;
+  const cudaMemcpyKind dd = cudaMemcpyDeviceToDevice;
+  if (d_charge) CK(cudaMemcpyAsync(c.d_charge.p, d_charge, N * 8, dd, c.stream));
+  if (d_radius) CK(cudaMemcpyAsync(c.d_radius.p, d_radius, N * 8, dd, c.stream));
+  if (d_epsilon && N) {
+    c.kernel_launches += 1;
+    k_scale_copy<<<(unsigned)((N + 255) / 256), 256, 0, c.stream>>>(c.d_sqeps.p, d_epsilon, N,
+                                                                     std::sqrt(kNa / kKcal2J));
+    CK(cudaGetLastError());
+  }
+  if (d_gb_radius) CK(cudaMemcpyAsync(c.d_gbR.p, d_gb_radius, N * 8, dd, c.stream));
+  if (d_gb_vj) CK(cudaMemcpyAsync(c.d_gbVj.p, d_gb_vj, N * 8, dd, c.stream));
+  if (d_gb_terms123) CK(cudaMemcpyAsync(c.d_gbT.p, d_gb_terms123, N * 8, dd, c.stream));
+  if (c.list_built) return launch_slot_params(c);
+  return PDGPU_OK;
+}
+
+static int param_grad_check(unsigned what) {
+  const unsigned pair = what & (PDGPU_NB | PDGPU_GB);
+  if (pair != PDGPU_NB && pair != PDGPU_GB) return PDGPU_ERR_ARG;
+  if (what & ~(PDGPU_NB | PDGPU_GB | PDGPU_SA | PDGPU_BONDED | PDGPU_ENERGY)) return PDGPU_ERR_ARG;
+  return PDGPU_OK;
+}
+
+int pdgpu_param_grad_device(pdgpu_ctx* h, unsigned what, const pdgpu_param_grads* g) {
+  if (!h || !g) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  int st = param_grad_check(what);
+  if (st != PDGPU_OK) return st;
+  CK(cudaSetDevice(c.device));
+  st = enqueue_compute(c, what & ~PDGPU_ENERGY, true);
+  if (st != PDGPU_OK) return st;
+  return launch_adjoint(c, what, g->charge, g->radius, g->epsilon, g->gb_radius, g->gb_vj, g->gb_terms123);
+}
+
+int pdgpu_param_grad(pdgpu_ctx* h, unsigned what, pdgpu_energies* out, const pdgpu_param_grads* g) {
+  if (!h || !g) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  int st = param_grad_check(what);
+  if (st != PDGPU_OK) return st;
+  CK(cudaSetDevice(c.device));
+  const size_t N = c.natom;
+  if (c.d_adj_out.n < 6 * N && c.d_adj_out.alloc(6 * N) != cudaSuccess) return PDGPU_ERR_CUDA;
+  double* host[6] = {g->charge, g->radius, g->epsilon, g->gb_radius, g->gb_vj, g->gb_terms123};
+  double* dev[6];
+  for (int k = 0; k < 6; k++) dev[k] = host[k] ? c.d_adj_out.p + k * N : nullptr;
+  st = enqueue_compute(c, what & ~PDGPU_ENERGY, true);
+  if (st != PDGPU_OK) return st;
+  st = launch_adjoint(c, what, dev[0], dev[1], dev[2], dev[3], dev[4], dev[5]);
+  if (st != PDGPU_OK) return st;
+  for (int k = 0; k < 6; k++)
+    if (host[k]) CK(cudaMemcpyAsync(host[k], dev[k], N * 8, cudaMemcpyDeviceToHost, c.stream));
+  st = read_status(c);
+  if (st != PDGPU_OK) return st;
+  if (out) return pdgpu_get_energies(h, out);
   return PDGPU_OK;
 }
 

@@ -123,6 +123,24 @@ __device__ __forceinline__ long long fix_force(float x) { return __float2ll_rn(x
 __device__ __forceinline__ long long fix_energy(float x) { return __float2ll_rn(x * 16777216.0f); }
 __device__ __forceinline__ long long fix_energy_d(double x) { return __double2ll_rn(x * 16777216.0); }
 __device__ __forceinline__ long long fix_sum(float x) { return __float2ll_rn(x * 4294967296.0f); }
+// float -> 64-bit fixed point with 32 fractional bits using integer operations
+// only (|x| < 2^31; larger magnitudes saturate near 2^62 so the overflow check
+// trips).  Rounds half away from zero.  The hardware float->int64 conversion
+// runs on the FP64 pipe, which is narrow on this GPU.
+__device__ __forceinline__ long long fx32(float x) {
+  const unsigned b = __float_as_uint(x);
+  const int e = (int)((b >> 23) & 0xffu);
+  const unsigned long long m = (unsigned long long)((b & 0x7fffffu) | 0x800000u);
+  const int sh = e - 118;  // x * 2^32 = m * 2^(e - 150 + 32)
+  unsigned long long r;
+  if (e == 0) r = 0ull;
+  else if (sh >= 39) r = 1ull << 62;
+  else if (sh >= 0) r = m << sh;
+  else if (sh > -25) r = (m + (1ull << (-sh - 1))) >> (-sh);
+  else r = 0ull;
+  return (b >> 31) ? -(long long)r : (long long)r;
+}
+
 __device__ __forceinline__ void atomic_add_ll(long long* p, long long v) {
   atomicAdd(reinterpret_cast<unsigned long long*>(p), static_cast<unsigned long long>(v));
 }
@@ -141,12 +159,20 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // host-side launchers (defined in the .cu files)
 // ---------------------------------------------------------------------------
 struct Context;
+int tile_grid(Context& c);        // grid of the chunked tile kernels (c.tile_chunk tiles per warp item)
+int tile_grid_plain(Context& c);  // grid of the tile kernels that take one tile per warp item
 int launch_list_build(Context& c, float list_radius);
 int launch_pack(Context& c, float check_disp);
 int launch_nb(Context& c, const NBConst& k, bool need_virial);
 int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset, double premul, bool energy);
 int launch_lcpo(Context& c, long long* facc_out, long long* esurf_out, int esurf_stride);
 int launch_gb_stage(Context& c, const GBConst& k, int stage);
+// parameter gradients after an energy evaluation of NB or GB (device outputs,
+// original atom order, J per parameter unit; null pointers are skipped)
+int launch_adjoint(Context& c, unsigned what, double* d_q, double* d_r, double* d_e, double* d_R, double* d_V,
+                   double* d_T);
+// static per-slot parameters refreshed from the per-atom arrays (after a parameter update)
+int launch_slot_params(Context& c);
 NBConst make_nb_const(const pdgpu_nb_params& p);
 GBConst make_gb_const(const pdgpu_gb_params& p, double listR);
 int launch_bonded(Context& c, bool energy);

@@ -43,6 +43,7 @@ struct Context {
   bool nb_set = false, gb_set = false;
   float list_radius_built = 0.f;
   int tile_ctas_per_sm = 8;    // launch shape of the tile kernels (autotuned)
+  int tile_chunk = 1;          // consecutive tiles per warp work item of the NB / GB kernels (autotuned)
   long long kernel_launches = 0;  // kernels this context has put on its stream (graph replays included)
 
   // static per-atom data (original order)
@@ -71,7 +72,8 @@ struct Context {
   DBuf<int> d_slot_of;         // [natom] sorted slot of each atom
   DBuf<double> d_center;       // [nblocks*3]
   DBuf<float4> d_half;         // [nblocks]
-  DBuf<Tile> d_tiles;          // [ncand]
+  DBuf<Tile> d_tiles;          // [ncand] row-major tile list
+  DBuf<int> d_tile_flag, d_tile_pos, d_scan_tmp2;  // tile-list compaction
   DBuf<int> d_counters;        // [0] ntiles, [1] nmasks
   DBuf<uint2> d_masks;         // [ncand*32] worst case
   DBuf<float4> d_xq, d_par, d_rel0;  // [nslots]
@@ -86,6 +88,10 @@ struct Context {
   DBuf<float> d_born_f;             // [nslots]
   DBuf<float> d_chain_f;            // [nslots] a^2/166 * dE/da * P4
   DBuf<double> d_born_d;            // [natom] original order
+  // parameter gradients (allocated on first use)
+  DBuf<long long> d_adj;            // [5*nslots] dE/dq, dE/dRmin, dE/dsqrt(eps), dE/dR_gb, dE/dVj
+  DBuf<float> d_adj_w;              // [nslots] dE/dGpol
+  DBuf<double> d_adj_out;           // [6*natom] staging for the host-array entry point
   // LCPO
   DBuf<int> d_lc_ncand;             // [nslots]
   DBuf<int> d_lc_cand;              // [nslots*kLcpoCand]

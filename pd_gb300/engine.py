@@ -92,10 +92,31 @@ class DeviceContext:
         p = ffi.ListParams(float(padding), int(check_skin))
         ffi.check(self.lib.pdgpu_set_list_params(self.h, ctypes.byref(p)), "pdgpu_set_list_params")
 
-    def update_params(self, charge=None, radius=None, epsilon=None, gb_vj=None, gb_terms123=None):
+    def update_params(self, charge=None, radius=None, epsilon=None, gb_radius=None, gb_vj=None, gb_terms123=None):
         arrs = [None if a is None else np.ascontiguousarray(a, np.float64) for a in
-                (charge, radius, epsilon, gb_vj, gb_terms123)]
+                (charge, radius, epsilon, gb_radius, gb_vj, gb_terms123)]
         ffi.check(self.lib.pdgpu_update_params(self.h, *[_pd(a) for a in arrs]), "pdgpu_update_params")
+
+    def update_params_device(self, charge=0, radius=0, epsilon=0, gb_radius=0, gb_vj=0, gb_terms123=0):
+        """Device pointers (int addresses, 0 = keep) of per-atom FP64 parameter arrays."""
+        ptrs = [ctypes.c_void_p(p or None) for p in (charge, radius, epsilon, gb_radius, gb_vj, gb_terms123)]
+        ffi.check(self.lib.pdgpu_update_params_device(self.h, *ptrs), "pdgpu_update_params_device")
+
+    def param_grad(self, what):
+        """Energies of every system and dE/dp per atom (J per parameter unit) for the
+        per-atom parameter arrays: dict charge, radius, epsilon, gb_radius, gb_vj, gb_terms123."""
+        names = ("charge", "radius", "epsilon", "gb_radius", "gb_vj", "gb_terms123")
+        out = {n: np.zeros(self.natom) for n in names}
+        g = ffi.ParamGrads(*[out[n].ctypes.data for n in names])
+        E = (ffi.Energies * self.nsystems)()
+        ffi.check(self.lib.pdgpu_param_grad(self.h, what, E, ctypes.byref(g)), "pdgpu_param_grad")
+        return [e.as_dict() for e in E], out
+
+    def param_grad_device(self, what, ptrs):
+        """Queue dE/dp into device arrays: ptrs maps the pdgpu_param_grads field names to addresses."""
+        names = ("charge", "radius", "epsilon", "gb_radius", "gb_vj", "gb_terms123")
+        g = ffi.ParamGrads(*[ptrs.get(n) or None for n in names])
+        ffi.check(self.lib.pdgpu_param_grad_device(self.h, what, ctypes.byref(g)), "pdgpu_param_grad_device")
 
     # -- state / evaluation ------------------------------------------------
     def set_positions(self, pos, stride=24):
@@ -201,7 +222,16 @@ class DeviceContext:
         return acc[:self.nsystems - 1], temps
 
     def autotune(self, trial_steps=20):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ffi.check(self.lib.pdgpu_md_autotune(self.h, int(trial_steps), ctypes.byref(a), ctypes.byref(b),
+                                             ctypes.byref(c)), "pdgpu_md_autotune")
+        return {"UpdateNList": a.value, "ctas_per_sm": b.value, "tile_chunk": c.value}
+
+    def set_launch_shape(self, ctas_per_sm, tile_chunk):
+        ffi.check(self.lib.pdgpu_set_launch_shape(self.h, int(ctas_per_sm), int(tile_chunk)),
+                  "pdgpu_set_launch_shape")
+
+    def launch_shape(self):
         a, b = ctypes.c_int(), ctypes.c_int()
-        ffi.check(self.lib.pdgpu_md_autotune(self.h, int(trial_steps), ctypes.byref(a), ctypes.byref(b)),
-                  "pdgpu_md_autotune")
-        return {"UpdateNList": a.value, "ctas_per_sm": b.value}
+        ffi.check(self.lib.pdgpu_get_launch_shape(self.h, ctypes.byref(a), ctypes.byref(b)), "pdgpu_get_launch_shape")
+        return a.value, b.value

@@ -70,6 +70,11 @@ class MDParams(ctypes.Structure):
                 ("seed", ctypes.c_ulonglong), ("use_graph", ctypes.c_int)]
 
 
+class ParamGrads(ctypes.Structure):
+    """pdgpu_param_grads: host (pdgpu_param_grad) or device (…_device) pointers, NULL = skip."""
+    _fields_ = [(n, ctypes.c_void_p) for n in ("charge", "radius", "epsilon", "gb_radius", "gb_vj", "gb_terms123")]
+
+
 # every symbol include/pdgpu.h declares, with its ctypes signature
 SIGNATURES = {
     "pdgpu_create": ([ctypes.c_int, ctypes.POINTER(SystemDesc), _ip], ctypes.c_void_p),
@@ -78,7 +83,11 @@ SIGNATURES = {
     "pdgpu_set_nb_params": ([ctypes.c_void_p, ctypes.POINTER(NBParams)], ctypes.c_int),
     "pdgpu_set_gb_params": ([ctypes.c_void_p, ctypes.POINTER(GBParams)], ctypes.c_int),
     "pdgpu_set_list_params": ([ctypes.c_void_p, ctypes.POINTER(ListParams)], ctypes.c_int),
-    "pdgpu_update_params": ([ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
+    "pdgpu_update_params": ([ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
+    "pdgpu_update_params_device": ([ctypes.c_void_p] + [ctypes.c_void_p] * 6, ctypes.c_int),
+    "pdgpu_param_grad": ([ctypes.c_void_p, ctypes.c_uint, ctypes.POINTER(Energies), ctypes.POINTER(ParamGrads)],
+                         ctypes.c_int),
+    "pdgpu_param_grad_device": ([ctypes.c_void_p, ctypes.c_uint, ctypes.POINTER(ParamGrads)], ctypes.c_int),
     "pdgpu_set_positions": ([ctypes.c_void_p, _dp, ctypes.c_size_t], ctypes.c_int),
     "pdgpu_set_positions_device": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "pdgpu_get_positions": ([ctypes.c_void_p, _dp, ctypes.c_size_t], ctypes.c_int),
@@ -98,7 +107,9 @@ SIGNATURES = {
     "pdgpu_md_run": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "pdgpu_get_kinetic": ([ctypes.c_void_p, _dp], ctypes.c_int),
     "pdgpu_remd_exchange": ([ctypes.c_void_p, ctypes.c_int, _ip, _dp], ctypes.c_int),
-    "pdgpu_md_autotune": ([ctypes.c_void_p, ctypes.c_int, _ip, _ip], ctypes.c_int),
+    "pdgpu_md_autotune": ([ctypes.c_void_p, ctypes.c_int, _ip, _ip, _ip], ctypes.c_int),
+    "pdgpu_set_launch_shape": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "pdgpu_get_launch_shape": ([ctypes.c_void_p, _ip, _ip], ctypes.c_int),
     "pdgpu_md_enqueue": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "pdgpu_synchronize": ([ctypes.c_void_p], ctypes.c_int),
     "pdgpu_kernel_launches": ([ctypes.c_void_p], ctypes.c_longlong),
