@@ -216,16 +216,16 @@ int pdgpu_get_kinetic(pdgpu_ctx *ctx, double *ekin);
  * target temperature. */
 int pdgpu_remd_exchange(pdgpu_ctx *ctx, int parity, int *accepted, double *temps);
 /* Project autotuner (state restored afterwards): first the launch shape of the
- * tile kernels (CTAs per SM x consecutive tiles per warp work item), timed on
- * force evaluations of the current state; then the list-rebuild cadence,
- * timed on short trial runs, keeping the fastest whose list never goes stale.
+ * tile kernels (CTAs per SM of their grid-stride grid), timed on force
+ * evaluations of the current state; then the list-rebuild cadence, timed on
+ * short trial runs, keeping the fastest whose list never goes stale.
  * Outputs may be NULL. */
-int pdgpu_md_autotune(pdgpu_ctx *ctx, int trial_steps, int *update_nlist, int *ctas_per_sm, int *tile_chunk);
-/* Launch shape of the pair-tile kernels (what the autotuner sets): resident
- * CTAs per SM of their grid (1..64) and tiles per warp work item (1..64).
- * Results do not depend on it (per-tile sums enter fixed point). */
-int pdgpu_set_launch_shape(pdgpu_ctx *ctx, int ctas_per_sm, int tile_chunk);
-int pdgpu_get_launch_shape(pdgpu_ctx *ctx, int *ctas_per_sm, int *tile_chunk);
+int pdgpu_md_autotune(pdgpu_ctx *ctx, int trial_steps, int *update_nlist, int *ctas_per_sm);
+/* Launch shape of the pair-tile kernels (what the autotuner sets): CTAs per SM
+ * of their grid (1..64).  Results do not depend on it (per-tile sums enter
+ * fixed point). */
+int pdgpu_set_launch_shape(pdgpu_ctx *ctx, int ctas_per_sm);
+int pdgpu_get_launch_shape(pdgpu_ctx *ctx, int *ctas_per_sm);
 
 /* ---- diagnostics ---------------------------------------------------------- */
 /* Tile / pair counts of the current list: ntiles, nmasked tiles, slots. */

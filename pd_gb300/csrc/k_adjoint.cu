@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(256) k_adj_gb_pair(DevView v, GBConst k, const
     tile_masks(v, T, lane, ex, m14);
     const unsigned dmask = (T.flags & 2) ? diag_exclusion(lane) : 0u;
     Acc3 I = {0.0, 0.0, 0.0}, J = {0.0, 0.0, 0.0};
-    if (ex | m14 | dmask) adj_gb_tile<true>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J);
+    if (tile_masked(T)) adj_gb_tile<true>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J);
     else adj_gb_tile<false>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J);
     acc_flush(v, gq, gr, ge, si, I);
     acc_flush(v, gq, gr, ge, T.bj * 32 + lane, J);
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(256) k_adj_born(DevView v, GBConst k, const fl
     tile_masks(v, T, lane, ex, m14);
     if (T.flags & 2) ex |= diag_exclusion(lane);
     Acc3 I = {0.0, 0.0, 0.0}, J = {0.0, 0.0, 0.0};
-    if (ex) adj_born_tile<true>(v, k, T, lane, si, xi, pi, wi, ex, w, I, J);
+    if (tile_masked(T)) adj_born_tile<true>(v, k, T, lane, si, xi, pi, wi, ex, w, I, J);
     else adj_born_tile<false>(v, k, T, lane, si, xi, pi, wi, ex, w, I, J);
     acc_flush(v, gR, gV, nullptr, si, I);
     acc_flush(v, gR, gV, nullptr, T.bj * 32 + lane, J);
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(256) k_adj_nb(DevView v, NBConst k, long long*
     }
     if (T.flags & 2) ex |= diag_exclusion(lane);
     Acc3 I = {0.0, 0.0, 0.0}, J = {0.0, 0.0, 0.0};
-    if (ex | m14) adj_nb_tile<ELEC, true>(v, k, T, S, lane, si, xi, pi, ex, m14, I, J);
+    if (tile_masked(T)) adj_nb_tile<ELEC, true>(v, k, T, S, lane, si, xi, pi, ex, m14, I, J);
     else adj_nb_tile<ELEC, false>(v, k, T, S, lane, si, xi, pi, ex, m14, I, J);
     acc_flush(v, gq, gr, ge, si, I);
     acc_flush(v, gq, gr, ge, T.bj * 32 + lane, J);
@@ -361,7 +361,7 @@ int launch_adjoint(Context& c, unsigned what, double* d_q, double* d_r, double* 
   cudaStream_t st = c.stream;
   const int ns = c.nslots;
   long long* g = c.d_adj.p;
-  const int grid = tile_grid_plain(c), nb = (ns + 255) / 256;
+  const int grid = tile_grid(c), nb = (ns + 255) / 256;
   const bool gb = (what & PDGPU_GB) != 0;
   const double ec = econv_kcal();
   const double halfeconv = 0.5 * ec;

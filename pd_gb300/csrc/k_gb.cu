@@ -6,12 +6,13 @@
 //   Born-radius chain     calcForcesIncludingVacuo loop2 :1768-1825
 // GB uses plain Euclidean distances, as PD does.
 //
-// Work decomposition: a warp takes a chunk of `chunk` consecutive tiles of the
-// row-major tile list.  The i-block's data and accumulators stay in registers
-// for the whole run of tiles sharing that i-block and are flushed (converted to
-// fixed point and added atomically) once per run; each j-block is rotated
-// through the warp by shuffles and flushed once per tile.  Tiles without bonded
-// pairs take a path without mask tests.
+// Work decomposition: one warp per 32x32 tile (grid-stride over the tile list);
+// lane l holds i atom l, the j block is rotated through the warp by shuffles,
+// and both sides' FP32 sums are converted to 64-bit fixed point and added
+// atomically once per tile (so a slot's total does not depend on the order in
+// which tiles run).  Tiles without bonded pairs take a path without mask tests.
+// Registers decide the occupancy of these kernels: the i side is re-read per
+// tile rather than kept across tiles.
 #include "pdgpu_tile.cuh"
 
 namespace pdgpu {
@@ -49,36 +50,22 @@ __device__ __forceinline__ void born_tile(const DevView& v, const GBConst& k, co
   }
 }
 
-__global__ void __launch_bounds__(256) k_gb_born(DevView v, GBConst k, long long* gpol, int chunk) {
+__global__ void __launch_bounds__(256) k_gb_born(DevView v, GBConst k, long long* gpol) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nt = *v.ntiles;
-  const int nchunks = (nt + chunk - 1) / chunk;
-  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nwarps) {
-    const int t1 = min(nt, (c + 1) * chunk);
-    int bi = -1, si = 0;
-    float4 xi = make_float4(0.f, 0.f, 0.f, 0.f), pi = xi;
-    long long gI = 0;
-    for (int t = c * chunk; t < t1; t++) {
-      const Tile T = v.tiles[t];
-      if (T.bi != bi) {
-        if (bi >= 0) atomic_add_ll(&gpol[si], gI);
-        bi = T.bi;
-        si = bi * 32 + lane;
-        xi = v.xq[si];
-        pi = v.par[si];
-        gI = 0;
-      }
-      unsigned ex, m14;
-      tile_masks(v, T, lane, ex, m14);
-      float gi = 0.f, gj = 0.f;
-      if (T.flags & 2) ex |= diag_exclusion(lane);
-      if (ex) born_tile<true>(v, k, T, lane, si, xi, pi, ex, gi, gj);
-      else born_tile<false>(v, k, T, lane, si, xi, pi, ex, gi, gj);
-      gI += fx32(gi);
-      atomic_add_ll(&gpol[T.bj * 32 + lane], fx32(gj));
-    }
-    if (bi >= 0) atomic_add_ll(&gpol[si], gI);
+  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
+    const Tile T = v.tiles[t];
+    const int si = T.bi * 32 + lane;
+    const float4 xi = v.xq[si], pi = v.par[si];
+    unsigned ex, m14;
+    tile_masks(v, T, lane, ex, m14);
+    if (T.flags & 2) ex |= diag_exclusion(lane);
+    float gi = 0.f, gj = 0.f;
+    if (tile_masked(T)) born_tile<true>(v, k, T, lane, si, xi, pi, ex, gi, gj);
+    else born_tile<false>(v, k, T, lane, si, xi, pi, ex, gi, gj);
+    atomic_add_ll(&gpol[si], fx32(gi));
+    atomic_add_ll(&gpol[T.bj * 32 + lane], fx32(gj));
   }
 }
 
@@ -304,50 +291,32 @@ __device__ __forceinline__ void flush_gb_energy(const DevView& v, int lane, int 
 }
 
 template <bool ENERGY>
-__global__ void __launch_bounds__(256) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda, int chunk) {
+__global__ void __launch_bounds__(256) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nt = *v.ntiles;
-  const int nchunks = (nt + chunk - 1) / chunk;
-  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nwarps) {
-    const int t1 = min(nt, (c + 1) * chunk);
-    int bi = -1, si = 0, atom_i = -1;
-    float4 xi = make_float4(0.f, 0.f, 0.f, 0.f), pi = xi;
-    float ai = 1.f;
-    FixAcc IF = {0, 0, 0, 0};
+  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
+    const Tile T = v.tiles[t];
+    const int si = T.bi * 32 + lane;
+    const float4 xi = v.xq[si], pi = v.par[si];
+    const float ai = born[si];
+    const int atom_i = ENERGY ? v.sorted_atom[si] : -1;
+    unsigned ex, m14;
+    tile_masks(v, T, lane, ex, m14);
+    const unsigned dmask = (T.flags & 2) ? diag_exclusion(lane) : 0u;
+    PairAcc I = {0.f, 0.f, 0.f, 0.f}, J = {0.f, 0.f, 0.f, 0.f};
     double evdw = 0.0, eel = 0.0, epol = 0.0;
-    EFix EF = {0, 0, 0};
-    for (int t = c * chunk; t < t1; t++) {
-      const Tile T = v.tiles[t];
-      if (T.bi != bi) {
-        if (bi >= 0) {
-          flush_fix(v, deda, si, IF);
-          if (ENERGY) flush_gb_energy(v, lane, bi, EF);
-        }
-        bi = T.bi;
-        si = bi * 32 + lane;
-        xi = v.xq[si];
-        pi = v.par[si];
-        ai = born[si];
-        atom_i = ENERGY ? v.sorted_atom[si] : -1;
-        IF = {0, 0, 0, 0};
-      }
-      unsigned ex, m14;
-      tile_masks(v, T, lane, ex, m14);
-      const unsigned dmask = (T.flags & 2) ? diag_exclusion(lane) : 0u;
-      PairAcc I = {0.f, 0.f, 0.f, 0.f}, J = {0.f, 0.f, 0.f, 0.f};
-      if (ex | m14 | dmask)
-        gb_pair_tile<true, ENERGY>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw, eel, epol);
-      else
-        gb_pair_tile<false, ENERGY>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw, eel,
-                                    epol);
-      fix_in(v, IF, I);
-      if (ENERGY) efix_in(EF, evdw, eel, epol);
-      flush_pair(v, deda, T.bj * 32 + lane, J);
-    }
-    if (bi >= 0) {
-      flush_fix(v, deda, si, IF);
-      if (ENERGY) flush_gb_energy(v, lane, bi, EF);
+    if (tile_masked(T))
+      gb_pair_tile<true, ENERGY>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw, eel, epol);
+    else
+      gb_pair_tile<false, ENERGY>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw, eel,
+                                  epol);
+    flush_pair(v, deda, si, I);
+    flush_pair(v, deda, T.bj * 32 + lane, J);
+    if (ENERGY) {
+      EFix EF = {0, 0, 0};
+      efix_in(EF, evdw, eel, epol);
+      flush_gb_energy(v, lane, T.bi, EF);
     }
   }
 }
@@ -416,50 +385,27 @@ __device__ __forceinline__ void flush_force(const DevView& v, int s, const PairA
   flush_fix(v, nullptr, s, F);
 }
 
-__global__ void __launch_bounds__(256) k_gb_chain(DevView v, GBConst k, const float* chain, int chunk) {
+__global__ void __launch_bounds__(256) k_gb_chain(DevView v, GBConst k, const float* chain) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nt = *v.ntiles;
-  const int nchunks = (nt + chunk - 1) / chunk;
-  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nwarps) {
-    const int t1 = min(nt, (c + 1) * chunk);
-    int bi = -1, si = 0;
-    float4 xi = make_float4(0.f, 0.f, 0.f, 0.f), pi = xi;
-    float ci = 0.f;
-    FixAcc IF = {0, 0, 0, 0};
-    for (int t = c * chunk; t < t1; t++) {
-      const Tile T = v.tiles[t];
-      if (T.bi != bi) {
-        if (bi >= 0) flush_fix(v, nullptr, si, IF);
-        bi = T.bi;
-        si = bi * 32 + lane;
-        xi = v.xq[si];
-        pi = v.par[si];
-        ci = chain[si];
-        IF = {0, 0, 0, 0};
-      }
-      unsigned ex, m14;
-      tile_masks(v, T, lane, ex, m14);
-      if (T.flags & 2) ex |= diag_exclusion(lane);
-      PairAcc I = {0.f, 0.f, 0.f, 0.f}, J = {0.f, 0.f, 0.f, 0.f};
-      if (ex) chain_tile<true>(v, k, T, lane, si, xi, pi, ci, ex, chain, I, J);
-      else chain_tile<false>(v, k, T, lane, si, xi, pi, ci, ex, chain, I, J);
-      fix_in(v, IF, I);
-      flush_force(v, T.bj * 32 + lane, J);
-    }
-    if (bi >= 0) flush_fix(v, nullptr, si, IF);
+  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
+    const Tile T = v.tiles[t];
+    const int si = T.bi * 32 + lane;
+    const float4 xi = v.xq[si], pi = v.par[si];
+    const float ci = chain[si];
+    unsigned ex, m14;
+    tile_masks(v, T, lane, ex, m14);
+    if (T.flags & 2) ex |= diag_exclusion(lane);
+    PairAcc I = {0.f, 0.f, 0.f, 0.f}, J = {0.f, 0.f, 0.f, 0.f};
+    if (tile_masked(T)) chain_tile<true>(v, k, T, lane, si, xi, pi, ci, ex, chain, I, J);
+    else chain_tile<false>(v, k, T, lane, si, xi, pi, ci, ex, chain, I, J);
+    flush_force(v, si, I);
+    flush_force(v, T.bj * 32 + lane, J);
   }
 }
 
 int tile_grid(Context& c) {
-  int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
-  long long want = (c.ncand / c.tile_chunk + 7) / 8 + 1;
-  long long g = (long long)sms * c.tile_ctas_per_sm;
-  return (int)(want < g ? want : g);
-}
-
-int tile_grid_plain(Context& c) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
   long long want = (c.ncand + 7) / 8;
@@ -475,12 +421,12 @@ int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset
   int nb = (c.nslots + 255) / 256;
   cudaMemsetAsync(c.d_gpol.p, 0, sizeof(long long) * c.nslots, st);
   cudaMemsetAsync(c.d_deda.p, 0, sizeof(long long) * c.nslots, st);
-  k_gb_born<<<g, 256, 0, st>>>(v, k, c.d_gpol.p, c.tile_chunk);
+  k_gb_born<<<g, 256, 0, st>>>(v, k, c.d_gpol.p);
   k_gb_radii<<<nb, 256, 0, st>>>(v, c.d_gbT.p, c.d_gpol.p, halfeconv, born_offset, c.d_born_f.p, c.d_born_d.p);
-  if (energy) k_gb_pair<true><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p, c.tile_chunk);
-  else k_gb_pair<false><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p, c.tile_chunk);
+  if (energy) k_gb_pair<true><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
+  else k_gb_pair<false><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
   k_gb_self<<<nb, 256, 0, st>>>(v, c.d_charge.p, k, premul, c.d_deda.p, c.d_born_d.p, c.d_chain_f.p);
-  k_gb_chain<<<g, 256, 0, st>>>(v, k, c.d_chain_f.p, c.tile_chunk);
+  k_gb_chain<<<g, 256, 0, st>>>(v, k, c.d_chain_f.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 
@@ -489,9 +435,9 @@ int launch_gb_stage(Context& c, const GBConst& k, int stage) {
   DevView v = c.view();
   int g = tile_grid(c);
   c.kernel_launches += 1;
-  if (stage == 1) k_gb_born<<<g, 256, 0, c.stream>>>(v, k, c.d_gpol.p, c.tile_chunk);
-  else if (stage == 2) k_gb_pair<false><<<g, 256, 0, c.stream>>>(v, k, c.d_born_f.p, c.d_deda.p, c.tile_chunk);
-  else k_gb_chain<<<g, 256, 0, c.stream>>>(v, k, c.d_chain_f.p, c.tile_chunk);
+  if (stage == 1) k_gb_born<<<g, 256, 0, c.stream>>>(v, k, c.d_gpol.p);
+  else if (stage == 2) k_gb_pair<false><<<g, 256, 0, c.stream>>>(v, k, c.d_born_f.p, c.d_deda.p);
+  else k_gb_chain<<<g, 256, 0, c.stream>>>(v, k, c.d_chain_f.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

@@ -195,7 +195,7 @@ __global__ void k_lcpo_main(DevView v, const float4* lc, const int* nl_n, const 
 int launch_lcpo(Context& c, long long* facc_out, long long* esurf_out, int esurf_stride) {
   DevView v = c.view();
   cudaStream_t st = c.stream;
-  int g = tile_grid_plain(c);
+  int g = tile_grid(c);
   c.kernel_launches += 3;
   cudaMemsetAsync(c.d_lc_ncand.p, 0, sizeof(int) * c.nslots, st);
   k_lcpo_cand<<<g, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_ncand.p, c.d_lc_cand.p);

@@ -139,55 +139,36 @@ __device__ __forceinline__ void nb_flush_energy(const DevView& v, int lane, int 
   F = {0, 0, 0};
 }
 
-// A warp walks a chunk of `chunk` consecutive tiles of the row-major list; the
-// i block stays in registers across each run of tiles that share it.
+// One warp per tile, grid-stride over the tile list.
 template <int ELEC, bool ENERGY>
-__global__ void __launch_bounds__(256) k_nb_tiles(DevView v, NBConst k, int chunk) {
+__global__ void __launch_bounds__(256) k_nb_tiles(DevView v, NBConst k) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nt = *v.ntiles;
-  const int nchunks = (nt + chunk - 1) / chunk;
-  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nwarps) {
-    const int t1 = min(nt, (c + 1) * chunk);
-    int bi = -1, si = 0, ai = 0;
-    float4 xi = make_float4(0.f, 0.f, 0.f, 0.f), pi = xi;
-    float qi = 0.f;
-    NBFix IF = {0, 0, 0};
-    double ev = 0.0, ee = 0.0, vir = 0.0;
-    NBEFix EF = {0, 0, 0};
-    for (int t = c * chunk; t < t1; t++) {
-      const Tile T = v.tiles[t];
-      if (T.bi != bi) {
-        if (bi >= 0) {
-          nb_flush_fix(v, si, IF);
-          if (ENERGY) nb_flush_energy(v, lane, bi, EF);
-        }
-        bi = T.bi;
-        si = bi * 32 + lane;
-        xi = v.xq[si];
-        pi = v.par[si];
-        qi = xi.w * k.econv_diel;
-        ai = ENERGY ? v.sorted_atom[si] : 0;
-        IF = {0, 0, 0};
-      }
-      const SystemInfo& S = v.sys[v.slot_sys[bi]];
-      unsigned ex = 0u, m14 = 0u;
-      if (T.mask >= 0) {
-        uint2 m = v.masks[T.mask * 32 + lane];
-        ex = m.x;
-        m14 = m.y;
-      }
-      if (T.flags & 2) ex |= ~((lane == 0) ? 0xffffffffu : ((1u << (32 - lane)) - 1u)) | 1u;
-      NBAcc I = {0.f, 0.f, 0.f}, J = {0.f, 0.f, 0.f};
-      if (ex | m14) nb_tile<ELEC, true, ENERGY>(v, k, T, S, lane, si, ai, xi, pi, qi, ex, m14, I, J, ev, ee, vir);
-      else nb_tile<ELEC, false, ENERGY>(v, k, T, S, lane, si, ai, xi, pi, qi, ex, m14, I, J, ev, ee, vir);
-      nb_fix_in(v, IF, I);
-      if (ENERGY) nb_efix_in(EF, ev, ee, vir);
-      nb_flush(v, T.bj * 32 + lane, J);
+  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
+    const Tile T = v.tiles[t];
+    const int si = T.bi * 32 + lane;
+    const float4 xi = v.xq[si], pi = v.par[si];
+    const float qi = xi.w * k.econv_diel;
+    const int ai = ENERGY ? v.sorted_atom[si] : 0;
+    const SystemInfo& S = v.sys[v.slot_sys[T.bi]];
+    unsigned ex = 0u, m14 = 0u;
+    if (T.mask >= 0) {
+      uint2 m = v.masks[T.mask * 32 + lane];
+      ex = m.x;
+      m14 = m.y;
     }
-    if (bi >= 0) {
-      nb_flush_fix(v, si, IF);
-      if (ENERGY) nb_flush_energy(v, lane, bi, EF);
+    if (T.flags & 2) ex |= diag_exclusion(lane);
+    NBAcc I = {0.f, 0.f, 0.f}, J = {0.f, 0.f, 0.f};
+    double ev = 0.0, ee = 0.0, vir = 0.0;
+    if (tile_masked(T)) nb_tile<ELEC, true, ENERGY>(v, k, T, S, lane, si, ai, xi, pi, qi, ex, m14, I, J, ev, ee, vir);
+    else nb_tile<ELEC, false, ENERGY>(v, k, T, S, lane, si, ai, xi, pi, qi, ex, m14, I, J, ev, ee, vir);
+    nb_flush(v, si, I);
+    nb_flush(v, T.bj * 32 + lane, J);
+    if (ENERGY) {
+      NBEFix EF = {0, 0, 0};
+      nb_efix_in(EF, ev, ee, vir);
+      nb_flush_energy(v, lane, T.bi, EF);
     }
   }
 }
@@ -196,10 +177,10 @@ template <bool E>
 static void launch_nb_mode(Context& c, const NBConst& k, int g) {
   DevView v = c.view();
   switch (k.elecmode) {
-    case 0: k_nb_tiles<0, E><<<g, 256, 0, c.stream>>>(v, k, c.tile_chunk); break;
-    case 1: k_nb_tiles<1, E><<<g, 256, 0, c.stream>>>(v, k, c.tile_chunk); break;
-    case 3: k_nb_tiles<3, E><<<g, 256, 0, c.stream>>>(v, k, c.tile_chunk); break;
-    default: k_nb_tiles<4, E><<<g, 256, 0, c.stream>>>(v, k, c.tile_chunk); break;
+    case 0: k_nb_tiles<0, E><<<g, 256, 0, c.stream>>>(v, k); break;
+    case 1: k_nb_tiles<1, E><<<g, 256, 0, c.stream>>>(v, k); break;
+    case 3: k_nb_tiles<3, E><<<g, 256, 0, c.stream>>>(v, k); break;
+    default: k_nb_tiles<4, E><<<g, 256, 0, c.stream>>>(v, k); break;
   }
 }
 

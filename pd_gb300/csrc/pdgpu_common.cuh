@@ -159,8 +159,7 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // host-side launchers (defined in the .cu files)
 // ---------------------------------------------------------------------------
 struct Context;
-int tile_grid(Context& c);        // grid of the chunked tile kernels (c.tile_chunk tiles per warp item)
-int tile_grid_plain(Context& c);  // grid of the tile kernels that take one tile per warp item
+int tile_grid(Context& c);   // grid of the tile kernels (grid-stride, one tile per warp item)
 int launch_list_build(Context& c, float list_radius);
 int launch_pack(Context& c, float check_disp);
 int launch_nb(Context& c, const NBConst& k, bool need_virial);

@@ -43,7 +43,6 @@ struct Context {
   bool nb_set = false, gb_set = false;
   float list_radius_built = 0.f;
   int tile_ctas_per_sm = 8;    // launch shape of the tile kernels (autotuned)
-  int tile_chunk = 1;          // consecutive tiles per warp work item of the NB / GB kernels (autotuned)
   long long kernel_launches = 0;  // kernels this context has put on its stream (graph replays included)
 
   // static per-atom data (original order)

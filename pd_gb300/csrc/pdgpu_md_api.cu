@@ -322,23 +322,21 @@ int pdgpu_remd_exchange(pdgpu_ctx* h, int parity, int* accepted, double* temps) 
   return PDGPU_OK;
 }
 
-int pdgpu_set_launch_shape(pdgpu_ctx* h, int ctas_per_sm, int tile_chunk) {
-  if (!h || ctas_per_sm < 1 || ctas_per_sm > 64 || tile_chunk < 1 || tile_chunk > 64) return PDGPU_ERR_ARG;
+int pdgpu_set_launch_shape(pdgpu_ctx* h, int ctas_per_sm) {
+  if (!h || ctas_per_sm < 1 || ctas_per_sm > 64) return PDGPU_ERR_ARG;
   Context& c = h->c;
   c.tile_ctas_per_sm = ctas_per_sm;
-  c.tile_chunk = tile_chunk;
   if (c.md) invalidate_graphs(*c.md);
   return PDGPU_OK;
 }
 
-int pdgpu_get_launch_shape(pdgpu_ctx* h, int* ctas_per_sm, int* tile_chunk) {
-  if (!h) return PDGPU_ERR_ARG;
-  if (ctas_per_sm) *ctas_per_sm = h->c.tile_ctas_per_sm;
-  if (tile_chunk) *tile_chunk = h->c.tile_chunk;
+int pdgpu_get_launch_shape(pdgpu_ctx* h, int* ctas_per_sm) {
+  if (!h || !ctas_per_sm) return PDGPU_ERR_ARG;
+  *ctas_per_sm = h->c.tile_ctas_per_sm;
   return PDGPU_OK;
 }
 
-int pdgpu_md_autotune(pdgpu_ctx* h, int trial_steps, int* update_nlist, int* ctas_per_sm, int* tile_chunk) {
+int pdgpu_md_autotune(pdgpu_ctx* h, int trial_steps, int* update_nlist, int* ctas_per_sm) {
   if (!h || trial_steps < 1) return PDGPU_ERR_ARG;
   Context& c = h->c;
   if (!c.md || !c.md->ready) return PDGPU_ERR_STATE;
@@ -357,12 +355,11 @@ int pdgpu_md_autotune(pdgpu_ctx* h, int trial_steps, int* update_nlist, int* cta
   CK(cudaMemcpyAsync(sa0.data(), md.d_facc_sa.p, sa0.size() * 8, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
 
-  // 1. launch shape of the tile kernels: force evaluations on the saved state
-  //    (the list does not change between them), timed with events
-  const int shapes[] = {4, 8, 16};
-  const int chunks[] = {1, 2, 4, 8};
+  // 1. launch shape of the tile kernels (grid = CTAs per SM x SMs): force
+  //    evaluations on the saved state (the list does not change), timed with events
+  const int shapes[] = {2, 4, 8, 16};
   const unsigned pair_what = md.p.what & (PDGPU_NB | PDGPU_GB);
-  int best_s = c.tile_ctas_per_sm, best_c = c.tile_chunk;
+  int best_s = c.tile_ctas_per_sm;
   if (pair_what) {
     c.list_built = false;
     if (rebuild_list_impl(c) != PDGPU_OK) return PDGPU_ERR_CUDA;
@@ -371,32 +368,27 @@ int pdgpu_md_autotune(pdgpu_ctx* h, int trial_steps, int* update_nlist, int* cta
     CK(cudaEventCreate(&e1));
     float best_ms = 1e30f;
     for (int shape : shapes) {
-      for (int ch : chunks) {
-        c.tile_ctas_per_sm = shape;
-        c.tile_chunk = ch;
-        float ms = 0.f;
-        bool ok = true;
-        for (int rep = 0; rep < 3 && ok; rep++) {  // first repetition warms up
-          CK(cudaEventRecord(e0, c.stream));
-          ok = enqueue_forces(c, pair_what, false, false, c.d_facc.p, nullptr, 0, false) == PDGPU_OK;
-          CK(cudaEventRecord(e1, c.stream));
-          CK(cudaEventSynchronize(e1));
-          float t = 0.f;
-          CK(cudaEventElapsedTime(&t, e0, e1));
-          if (rep) ms += t;
-        }
-        if (ok && ms < best_ms) {
-          best_ms = ms;
-          best_s = shape;
-          best_c = ch;
-        }
+      c.tile_ctas_per_sm = shape;
+      float ms = 0.f;
+      bool ok = true;
+      for (int rep = 0; rep < 3 && ok; rep++) {  // first repetition warms up
+        CK(cudaEventRecord(e0, c.stream));
+        ok = enqueue_forces(c, pair_what, false, false, c.d_facc.p, nullptr, 0, false) == PDGPU_OK;
+        CK(cudaEventRecord(e1, c.stream));
+        CK(cudaEventSynchronize(e1));
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, e0, e1));
+        if (rep) ms += t;
+      }
+      if (ok && ms < best_ms) {
+        best_ms = ms;
+        best_s = shape;
       }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
   }
   c.tile_ctas_per_sm = best_s;
-  c.tile_chunk = best_c;
 
   // 2. list cadence with that shape: short dynamics from the saved state
   const int cadences[] = {1, 2, 3, 5, 10, 20, 40, 80};
@@ -443,7 +435,6 @@ int pdgpu_md_autotune(pdgpu_ctx* h, int trial_steps, int* update_nlist, int* cta
   if (best >= 1e300) return PDGPU_ERR_STALE_LIST;
   if (update_nlist) *update_nlist = best_n;
   if (ctas_per_sm) *ctas_per_sm = best_s;
-  if (tile_chunk) *tile_chunk = best_c;
   return PDGPU_OK;
 }
 

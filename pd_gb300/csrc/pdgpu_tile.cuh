@@ -30,6 +30,11 @@ __device__ __forceinline__ float4 j_in_i_frame(const DevView& v, const Tile& T, 
   return xj;
 }
 
+// Whether a tile takes the masked body (bonded pairs or the diagonal).  The
+// choice must be the same for all 32 lanes: the tile bodies rotate the j block
+// with full-warp shuffles, which need every lane on the same path.
+__device__ __forceinline__ bool tile_masked(const Tile& T) { return T.mask >= 0 || (T.flags & 2); }
+
 __device__ __forceinline__ void tile_masks(const DevView& v, const Tile& T, int lane, unsigned& ex, unsigned& m14) {
   ex = 0u;
   m14 = 0u;

@@ -222,16 +222,15 @@ class DeviceContext:
         return acc[:self.nsystems - 1], temps
 
     def autotune(self, trial_steps=20):
-        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        ffi.check(self.lib.pdgpu_md_autotune(self.h, int(trial_steps), ctypes.byref(a), ctypes.byref(b),
-                                             ctypes.byref(c)), "pdgpu_md_autotune")
-        return {"UpdateNList": a.value, "ctas_per_sm": b.value, "tile_chunk": c.value}
+        a, b = ctypes.c_int(), ctypes.c_int()
+        ffi.check(self.lib.pdgpu_md_autotune(self.h, int(trial_steps), ctypes.byref(a), ctypes.byref(b)),
+                  "pdgpu_md_autotune")
+        return {"UpdateNList": a.value, "ctas_per_sm": b.value}
 
-    def set_launch_shape(self, ctas_per_sm, tile_chunk):
-        ffi.check(self.lib.pdgpu_set_launch_shape(self.h, int(ctas_per_sm), int(tile_chunk)),
-                  "pdgpu_set_launch_shape")
+    def set_launch_shape(self, ctas_per_sm):
+        ffi.check(self.lib.pdgpu_set_launch_shape(self.h, int(ctas_per_sm)), "pdgpu_set_launch_shape")
 
     def launch_shape(self):
-        a, b = ctypes.c_int(), ctypes.c_int()
-        ffi.check(self.lib.pdgpu_get_launch_shape(self.h, ctypes.byref(a), ctypes.byref(b)), "pdgpu_get_launch_shape")
-        return a.value, b.value
+        a = ctypes.c_int()
+        ffi.check(self.lib.pdgpu_get_launch_shape(self.h, ctypes.byref(a)), "pdgpu_get_launch_shape")
+        return a.value

@@ -107,9 +107,9 @@ SIGNATURES = {
     "pdgpu_md_run": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "pdgpu_get_kinetic": ([ctypes.c_void_p, _dp], ctypes.c_int),
     "pdgpu_remd_exchange": ([ctypes.c_void_p, ctypes.c_int, _ip, _dp], ctypes.c_int),
-    "pdgpu_md_autotune": ([ctypes.c_void_p, ctypes.c_int, _ip, _ip, _ip], ctypes.c_int),
-    "pdgpu_set_launch_shape": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
-    "pdgpu_get_launch_shape": ([ctypes.c_void_p, _ip, _ip], ctypes.c_int),
+    "pdgpu_md_autotune": ([ctypes.c_void_p, ctypes.c_int, _ip, _ip], ctypes.c_int),
+    "pdgpu_set_launch_shape": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "pdgpu_get_launch_shape": ([ctypes.c_void_p, _ip], ctypes.c_int),
     "pdgpu_md_enqueue": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "pdgpu_synchronize": ([ctypes.c_void_p], ctypes.c_int),
     "pdgpu_kernel_launches": ([ctypes.c_void_p], ctypes.c_longlong),
