@@ -132,6 +132,58 @@ class REX_Local:
     def geometric_ladder(tmin, tmax, n):
         return tmin * (tmax / tmin) ** (np.arange(n) / max(n - 1, 1))
 
+    # -- checkpoints in PD's MIME snapshot format (remd.cpp:319-331) -------------
+    def _rung_systems(self, ctx):
+        """System index at each temperature rung (rung r holds PD's replica r)."""
+        cur = getattr(self, "current_temps", None)
+        if cur is None:
+            return np.arange(len(self.temps))
+        return np.array([int(np.argmin(np.abs(cur - T))) for T in self.temps])
+
+    def writeCheckPointMIME(self, f):
+        """printCheckPointMIME into an open text file (or path): one section
+        ``remd<r>`` per replica r, the structure now at temperature rung r."""
+        from . import checkpoint
+        if isinstance(f, str):
+            with open(f, "w") as fh:
+                return self.writeCheckPointMIME(fh)
+        ctx = self.md.wspace.context()
+        pos, vel = ctx.get_positions(), ctx.get_velocities()
+        es = getattr(self.md.wspace, "per_system_energies", None)
+        off = self.md.wspace.image.offsets
+        for r, k in enumerate(self._rung_systems(ctx)):
+            sl = slice(int(off[k]), int(off[k + 1]))
+            epot = es[k]["epot"] if es else 0.0
+            checkpoint.write_snapshot(f, "remd%d" % r, pos[sl], vel[sl], None, epot)
+
+    def printCheckPointMIME(self):
+        import sys
+        self.writeCheckPointMIME(sys.stdout)
+
+    def readCheckPointMIME(self, filename):
+        """readCheckPointMIME: replica r's structure (positions, velocities) goes to
+        the system at rung r; every section must match that system's atom count."""
+        from . import checkpoint
+        with open(filename) as f:
+            secs = checkpoint.read_snapshots(f)
+        ctx = self.md.setup() if not self.md._setup_done else self.md.wspace.context()
+        pos, vel = ctx.get_positions(), ctx.get_velocities()
+        off = self.md.wspace.image.offsets
+        for r, k in enumerate(self._rung_systems(ctx)):
+            name = "remd%d" % r
+            if name not in secs:
+                raise KeyError("MIME snapshot '%s' not found in %s" % (name, filename))
+            snap = secs[name]
+            sl = slice(int(off[k]), int(off[k + 1]))
+            if len(snap["pos"]) != sl.stop - sl.start:
+                raise ValueError("%s holds %d atoms, replica %d has %d" % (name, len(snap["pos"]), r,
+                                                                         sl.stop - sl.start))
+            pos[sl] = snap["pos"]
+            vel[sl] = snap["vel"]
+        ctx.set_positions(pos)
+        ctx.set_velocities(vel)
+        self.md.sync(ctx, energies=False)
+
     def run(self, rounds=None):
         n = self.Steps if rounds is None else rounds
         ctx = self.md.setup() if not self.md._setup_done else self.md.wspace.context()

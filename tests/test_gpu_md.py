@@ -139,3 +139,42 @@ def test_md_is_deterministic(goldens):
         res.append(ctx.get_positions())
         ctx.close()
     assert np.array_equal(res[0], res[1])
+
+
+def test_rex_checkpoint_mime_round_trip(goldens, tmp_path):
+    """REX_Local writes PD's MIME checkpoint (one section per replica rung) and
+    reads it back into the systems at those rungs."""
+    from pd_gb300 import checkpoint
+    from pd_gb300.forcefield import FF_GeneralizedBorn_Still_GPU, Forcefield
+    from pd_gb300.md import MolecularDynamics, REX_Local
+    from pd_gb300.workspace import SystemImage, WorkSpace
+    d = goldens["peptide30"]
+    im = SystemImage.concat([SystemImage._from_fixture(d)] * 3)
+    ws = WorkSpace(im)
+    ws.Padding = 2.0
+    ff = Forcefield(ws)
+    gb = FF_GeneralizedBorn_Still_GPU(ws)
+    for k, v in gb_kwargs(d).items():
+        setattr(gb, k, v)
+    ff.add(gb)
+    md = MolecularDynamics(ff)
+    md.Timestep = 1e-15
+    rex = REX_Local(md, [300.0, 350.0, 400.0])
+    rex.ExchangeFreq = 20
+    rex.run(2)
+    path = str(tmp_path / "remd.mime")
+    rex.writeCheckPointMIME(path)
+    ctx = ws.context()
+    pos0, vel0 = ctx.get_positions(), ctx.get_velocities()
+    rungs = rex._rung_systems(ctx)
+    off = im.offsets
+    for r, k in enumerate(rungs):
+        s = checkpoint.read_snapshot(path, "remd%d" % r)
+        assert np.array_equal(s["pos"], pos0[off[k]:off[k + 1]])
+        assert np.array_equal(s["vel"], vel0[off[k]:off[k + 1]])
+    rex.run(1)                                   # move on, then restore
+    rex.readCheckPointMIME(path)
+    now = rex._rung_systems(ctx)                 # replica r goes to the system now at rung r
+    pos1 = ctx.get_positions()
+    for r in range(3):
+        assert np.array_equal(pos1[off[now[r]]:off[now[r] + 1]], pos0[off[rungs[r]]:off[rungs[r] + 1]])
