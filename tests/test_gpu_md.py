@@ -145,7 +145,7 @@ def test_rex_checkpoint_mime_round_trip(goldens, tmp_path):
     """REX_Local writes PD's MIME checkpoint (one section per replica rung) and
     reads it back into the systems at those rungs."""
     from pd_gb300 import checkpoint
-    from pd_gb300.forcefield import FF_GeneralizedBorn_Still_GPU, Forcefield
+    from pd_gb300.forcefield import FF_Bonded_GPU, FF_GeneralizedBorn_Still_GPU, Forcefield
     from pd_gb300.md import MolecularDynamics, REX_Local
     from pd_gb300.workspace import SystemImage, WorkSpace
     d = goldens["peptide30"]
@@ -153,12 +153,14 @@ def test_rex_checkpoint_mime_round_trip(goldens, tmp_path):
     ws = WorkSpace(im)
     ws.Padding = 2.0
     ff = Forcefield(ws)
+    ff.add(FF_Bonded_GPU(ws))
     gb = FF_GeneralizedBorn_Still_GPU(ws)
     for k, v in gb_kwargs(d).items():
         setattr(gb, k, v)
     ff.add(gb)
     md = MolecularDynamics(ff)
     md.Timestep = 1e-15
+    md.UpdateNList = 1          # the test is about the checkpoint, not the list cadence
     rex = REX_Local(md, [300.0, 350.0, 400.0])
     rex.ExchangeFreq = 20
     rex.run(2)
