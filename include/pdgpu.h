@@ -34,6 +34,7 @@ extern "C" {
 #define PDGPU_ERR_UNSUPPORTED (-7)    /* option not supported (e.g. GB in a periodic box)    */
 #define PDGPU_ERR_STALE_LIST (-8)     /* an atom moved more than Padding/2 since the rebuild */
 #define PDGPU_ERR_STATE (-9)          /* call sequence error (e.g. compute before positions) */
+#define PDGPU_ERR_CAPACITY (-10)      /* larger than a fixed-size entry point's static scratch */
 
 /* ---- what to compute ------------------------------------------------------ */
 #define PDGPU_NB 1u      /* FF_NonBonded: LJ + Coulomb with PD's switching     */
@@ -177,6 +178,18 @@ int pdgpu_param_grad(pdgpu_ctx *ctx, unsigned what, pdgpu_energies *out, const p
 /* Device-array form: queued on the context stream; energies stay on the device
  * until pdgpu_get_energies(), status via pdgpu_synchronize(). */
 int pdgpu_param_grad_device(pdgpu_ctx *ctx, unsigned what, const pdgpu_param_grads *d_g);
+/* Same result as pdgpu_param_grad_device, with no device allocation in the
+ * call.  It has no counterpart in PD.  It is for hosts that cannot let a call
+ * run cudaMalloc: the allocation synchronises the whole device (stalling the
+ * host's other streams), or the host's own pool already holds the free memory.
+ * The scratch is a static device array of the library, sized for 65,536
+ * sorted slots (about as many atoms; each system is padded to 32-atom
+ * blocks): a larger context gets PDGPU_ERR_CAPACITY and nothing is queued.
+ * The first call on a device looks up the array's address and may load the
+ * library's device code; make that call before any stream capture.  Each call
+ * clears its accumulators on the context stream.  All contexts on a device
+ * share the array, so calls whose GPU work overlaps race. */
+int pdgpu_param_grad_device_noalloc(pdgpu_ctx *ctx, unsigned what, const pdgpu_param_grads *d_g);
 
 /* ---- dynamics: MolecularDynamics / REX_Local --------------------------------- */
 /* Integrator settings (PD src/mmlib/protocols/md.h, defaults md.cpp:60-86). */

@@ -350,17 +350,13 @@ __global__ void k_adj_out(DevView v, const long long* g, int nslots, bool gb, co
 
 
 // Runs after an energy evaluation of the same component (its Born radii, Gpol
-// sums and dE/da are read from the context).
-int launch_adjoint(Context& c, unsigned what, double* d_q, double* d_r, double* d_e, double* d_R, double* d_V,
-                   double* d_T) {
-  if (c.d_adj.n < (size_t)G_NACC * c.nslots) {
-    if (c.d_adj.alloc((size_t)G_NACC * c.nslots) != cudaSuccess) return PDGPU_ERR_CUDA;
-    if (c.d_adj_w.alloc((size_t)c.nslots) != cudaSuccess) return PDGPU_ERR_CUDA;
-  }
+// sums and dE/da are read from the context).  g: G_NACC * nslots fixed-point
+// accumulators (cleared here), w: nslots floats (written in full here).
+static int launch_adjoint_into(Context& c, unsigned what, long long* g, float* w, double* d_q, double* d_r,
+                               double* d_e, double* d_R, double* d_V, double* d_T) {
   DevView v = c.view();
   cudaStream_t st = c.stream;
   const int ns = c.nslots;
-  long long* g = c.d_adj.p;
   const int grid = tile_grid(c), nb = (ns + 255) / 256;
   const bool gb = (what & PDGPU_GB) != 0;
   const double ec = econv_kcal();
@@ -372,8 +368,8 @@ int launch_adjoint(Context& c, unsigned what, double* d_q, double* d_r, double* 
     GBConst k = make_gb_const(c.gb, c.list_radius_built);
     c.kernel_launches += 3;
     k_adj_gb_pair<<<grid, 256, 0, st>>>(v, k, c.d_born_f.p, gq, gr, ge);
-    k_adj_w<<<nb, 256, 0, st>>>(v, c.d_gbT.p, c.d_gpol.p, c.d_deda.p, premul, halfeconv, c.d_adj_w.p);
-    k_adj_born<<<grid, 256, 0, st>>>(v, k, c.d_adj_w.p, g + G_GBR * (size_t)ns, g + G_VJ * (size_t)ns);
+    k_adj_w<<<nb, 256, 0, st>>>(v, c.d_gbT.p, c.d_gpol.p, c.d_deda.p, premul, halfeconv, w);
+    k_adj_born<<<grid, 256, 0, st>>>(v, k, w, g + G_GBR * (size_t)ns, g + G_VJ * (size_t)ns);
   } else {
     NBConst k = make_nb_const(c.nb);
     c.kernel_launches += 1;
@@ -389,6 +385,47 @@ int launch_adjoint(Context& c, unsigned what, double* d_q, double* d_r, double* 
   k_adj_out<<<nb, 256, 0, st>>>(v, g, ns, gb, c.d_gbT.p, c.d_gpol.p, c.d_deda.p, premul, halfeconv,
                                 std::sqrt(kNa / kKcal2J), o);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
+}
+
+int launch_adjoint(Context& c, unsigned what, double* d_q, double* d_r, double* d_e, double* d_R, double* d_V,
+                   double* d_T) {
+  if (c.d_adj.n < (size_t)G_NACC * c.nslots) {
+    if (c.d_adj.alloc((size_t)G_NACC * c.nslots) != cudaSuccess) return PDGPU_ERR_CUDA;
+    if (c.d_adj_w.alloc((size_t)c.nslots) != cudaSuccess) return PDGPU_ERR_CUDA;
+  }
+  return launch_adjoint_into(c, what, c.d_adj.p, c.d_adj_w.p, d_q, d_r, d_e, d_R, d_V, d_T);
+}
+
+// ---------------------------------------------------------------------------
+// Fixed scratch for the gradient call of hosts that must not allocate device
+// memory inside a call.  cudaMalloc and cudaFree synchronise the whole device,
+// so a host that keeps other streams busy (a fitting loop beside dynamics of
+// other replicas), or whose own pool allocator holds the free memory, cannot
+// let pdgpu_param_grad_device allocate its scratch on first use.  This array
+// sits in the library's static device data instead: kNoAllocMaxSlots sorted
+// slots, G_NACC int64 accumulators and one float each (2.75 MiB), held by every
+// GPU that loads the library until the process exits.  All contexts on a
+// device share it, so calls whose GPU work overlaps race.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_adj_scratch[(size_t)kNoAllocMaxSlots *
+                                                             (G_NACC * sizeof(long long) + sizeof(float))];
+static void* g_adj_scratch_addr[kNoAllocMaxDevices] = {};
+
+int launch_adjoint_static(Context& c, unsigned what, double* d_q, double* d_r, double* d_e, double* d_R, double* d_V,
+                          double* d_T) {
+  if (c.nslots > kNoAllocMaxSlots) return PDGPU_ERR_CAPACITY;
+  if (c.device < 0 || c.device >= kNoAllocMaxDevices) return PDGPU_ERR_ARG;
+  if (!g_adj_scratch_addr[c.device]) {
+    // once per device, with that device current: the array's device address
+    // (in host code its name only stands in for the symbol)
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_adj_scratch) != cudaSuccess || !p) return PDGPU_ERR_CUDA;
+    g_adj_scratch_addr[c.device] = p;
+  }
+  unsigned char* base = static_cast<unsigned char*>(g_adj_scratch_addr[c.device]);
+  long long* g = reinterpret_cast<long long*>(base);
+  float* w = reinterpret_cast<float*>(base + (size_t)kNoAllocMaxSlots * G_NACC * sizeof(long long));
+  return launch_adjoint_into(c, what, g, w, d_q, d_r, d_e, d_R, d_V, d_T);
 }
 
 }  // namespace pdgpu

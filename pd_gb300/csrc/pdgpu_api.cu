@@ -155,6 +155,7 @@ const char* pdgpu_error_string(int status) {
     case PDGPU_ERR_UNSUPPORTED: return "unsupported option";
     case PDGPU_ERR_STALE_LIST: return "an atom moved more than Padding/2 since the list was built";
     case PDGPU_ERR_STATE: return "call sequence error";
+    case PDGPU_ERR_CAPACITY: return "larger than the static scratch of the allocation-free entry point";
     default: return "unknown status";
   }
 }
@@ -524,6 +525,18 @@ int pdgpu_param_grad_device(pdgpu_ctx* h, unsigned what, const pdgpu_param_grads
   st = enqueue_compute(c, what & ~PDGPU_ENERGY, true);
   if (st != PDGPU_OK) return st;
   return launch_adjoint(c, what, g->charge, g->radius, g->epsilon, g->gb_radius, g->gb_vj, g->gb_terms123);
+}
+
+int pdgpu_param_grad_device_noalloc(pdgpu_ctx* h, unsigned what, const pdgpu_param_grads* g) {
+  if (!h || !g) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  int st = param_grad_check(what);
+  if (st != PDGPU_OK) return st;
+  if (c.nslots > kNoAllocMaxSlots) return PDGPU_ERR_CAPACITY;
+  CK(cudaSetDevice(c.device));
+  st = enqueue_compute(c, what & ~PDGPU_ENERGY, true);
+  if (st != PDGPU_OK) return st;
+  return launch_adjoint_static(c, what, g->charge, g->radius, g->epsilon, g->gb_radius, g->gb_vj, g->gb_terms123);
 }
 
 int pdgpu_param_grad(pdgpu_ctx* h, unsigned what, pdgpu_energies* out, const pdgpu_param_grads* g) {

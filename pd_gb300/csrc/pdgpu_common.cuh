@@ -170,6 +170,12 @@ int launch_gb_stage(Context& c, const GBConst& k, int stage);
 // original atom order, J per parameter unit; null pointers are skipped)
 int launch_adjoint(Context& c, unsigned what, double* d_q, double* d_r, double* d_e, double* d_R, double* d_V,
                    double* d_T);
+// the same into a static device array: no allocation during the call (at most
+// kNoAllocMaxSlots sorted slots; one scratch per device shared by all contexts)
+constexpr int kNoAllocMaxSlots = 65536;
+constexpr int kNoAllocMaxDevices = 64;
+int launch_adjoint_static(Context& c, unsigned what, double* d_q, double* d_r, double* d_e, double* d_R, double* d_V,
+                          double* d_T);
 // static per-slot parameters refreshed from the per-atom arrays (after a parameter update)
 int launch_slot_params(Context& c);
 NBConst make_nb_const(const pdgpu_nb_params& p);

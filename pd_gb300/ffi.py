@@ -16,7 +16,9 @@ ERRORS = {
     -1: "invalid argument", -2: "CUDA runtime error", -3: "LCPO overlap list overflow",
     -4: "fixed-point accumulator overflow", -5: "NaN energy or force", -6: "device wait timed out",
     -7: "unsupported option", -8: "stale neighbour list", -9: "call sequence error",
+    -10: "larger than the static scratch of the allocation-free entry point",
 }
+ERR_CAPACITY = -10
 NB, GB, SA, BONDED, ENERGY = 1, 2, 4, 8, 0x100
 
 
@@ -88,6 +90,7 @@ SIGNATURES = {
     "pdgpu_param_grad": ([ctypes.c_void_p, ctypes.c_uint, ctypes.POINTER(Energies), ctypes.POINTER(ParamGrads)],
                          ctypes.c_int),
     "pdgpu_param_grad_device": ([ctypes.c_void_p, ctypes.c_uint, ctypes.POINTER(ParamGrads)], ctypes.c_int),
+    "pdgpu_param_grad_device_noalloc": ([ctypes.c_void_p, ctypes.c_uint, ctypes.POINTER(ParamGrads)], ctypes.c_int),
     "pdgpu_set_positions": ([ctypes.c_void_p, _dp, ctypes.c_size_t], ctypes.c_int),
     "pdgpu_set_positions_device": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "pdgpu_get_positions": ([ctypes.c_void_p, _dp, ctypes.c_size_t], ctypes.c_int),
