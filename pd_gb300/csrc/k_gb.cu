@@ -20,7 +20,7 @@ namespace pdgpu {
 // ---------------------------------------------------------------------------
 // pass 1: Born-radius pair sums  Gpol_i += P4 Vj CCF / r^4  (bond order > 2)
 // ---------------------------------------------------------------------------
-template <bool MASKED>
+template <bool MASKED, bool FULL>
 __device__ __forceinline__ void born_tile(const DevView& v, const GBConst& k, const Tile& T, int lane, int si,
                                           const float4& xi, const float4& pi, unsigned ex, float& gi, float& gj) {
   float4 xj = j_in_i_frame(v, T, lane);
@@ -29,9 +29,12 @@ __device__ __forceinline__ void born_tile(const DevView& v, const GBConst& k, co
   for (int kk = 0; kk < 32; kk++) {
     const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
     const float r2 = dx * dx + dy * dy + dz * dz;
-    bool in = r2 <= k.still2;
-    if (fabsf(r2 - k.still2) <= 2e-6f * k.still2)
-      in = r2_slots_fp64(v, si, T.bj * 32 + ((lane + kk) & 31)) <= k.still2_d;
+    bool in = true;  // FULL: the whole tile lies inside the Still cutoff
+    if (!FULL) {
+      in = r2 <= k.still2;
+      if (fabsf(r2 - k.still2) <= 2e-6f * k.still2)
+        in = r2_slots_fp64(v, si, T.bj * 32 + ((lane + kk) & 31)) <= k.still2_d;
+    }
     if (MASKED) in = in && !((ex >> kk) & 1u);
     if (in) {
       const float rs = pi.z + pj.z;
@@ -62,8 +65,14 @@ __global__ void __launch_bounds__(256) k_gb_born(DevView v, GBConst k, long long
     tile_masks(v, T, lane, ex, m14);
     if (T.flags & 2) ex |= diag_exclusion(lane);
     float gi = 0.f, gj = 0.f;
-    if (tile_masked(T)) born_tile<true>(v, k, T, lane, si, xi, pi, ex, gi, gj);
-    else born_tile<false>(v, k, T, lane, si, xi, pi, ex, gi, gj);
+    const bool full = tile_full(T);
+    if (tile_masked(T)) {
+      if (full) born_tile<true, true>(v, k, T, lane, si, xi, pi, ex, gi, gj);
+      else born_tile<true, false>(v, k, T, lane, si, xi, pi, ex, gi, gj);
+    } else {
+      if (full) born_tile<false, true>(v, k, T, lane, si, xi, pi, ex, gi, gj);
+      else born_tile<false, false>(v, k, T, lane, si, xi, pi, ex, gi, gj);
+    }
     atomic_add_ll(&gpol[si], fx32(gi));
     atomic_add_ll(&gpol[T.bj * 32 + lane], fx32(gj));
   }
@@ -143,7 +152,7 @@ struct PairAcc {
   float fx, fy, fz, da;
 };
 
-template <bool MASKED, bool ENERGY>
+template <bool MASKED, bool ENERGY, bool FULL>
 __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k, const Tile& T, int lane, int si,
                                              int atom_i, const float4& xi, const float4& pi, float ai, unsigned ex,
                                              unsigned m14, unsigned dmask, const float* born, PairAcc& I, PairAcc& J,
@@ -167,7 +176,7 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
       if (atom_i >= 0 && atom_j >= 0)
         gb_pair_energy(k, v, atom_i, atom_j, r2_slots_fp64(v, si, sjk), excl, is14, evdw, eel, epol);
     }
-    if (r2 <= k.cut2 && pair) {
+    if ((FULL || r2 <= k.cut2) && pair) {
       const float invr = rsqrtf(r2);
       const float r = r2 * invr;
       const float qiqj = xi.w * xj.w;
@@ -179,7 +188,7 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
       float g = 0.f;  // scalar multiplying (xj - xi) in the force on i
       float elec = 0.f, delec = 0.f;
       const float s14 = is14 ? k.elec14 : 1.f;
-      const bool sw_on = r >= k.inner;
+      const bool sw_on = !FULL && r >= k.inner;  // FULL: inside the inner cutoff
       float S = 1.f, dS = 0.f;
       if (sw_on) {
         const float w = r - k.inner;
@@ -212,14 +221,14 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
       if (!excl) {
         if (sw_on) delec = S * delec + elec * dS;
         float dvdw = 0.f;
-        if (r < k.vdwcut) {
+        if (FULL || r < k.vdwcut) {
           const float t = (pi.x + pj.x) * invr;
           float B = t * t;
           B = B * B * B;
           const float A = B * B;
           const float eps = pi.y * pj.y * (is14 ? k.vdw14 : 1.f);
           dvdw = -12.f * eps * invr * (A - B);
-          if (r > k.vdwinner) {
+          if (!FULL && r > k.vdwinner) {
             const float Ev = eps * (A - 2.f * B);
             const float w = r - k.vdwinner;
             const float sw = 1.f - w * w * k.vdwinvw2;
@@ -291,7 +300,7 @@ __device__ __forceinline__ void flush_gb_energy(const DevView& v, int lane, int 
 }
 
 template <bool ENERGY>
-__global__ void __launch_bounds__(256) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
+__global__ void __launch_bounds__(256, ENERGY ? 1 : 4) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nt = *v.ntiles;
@@ -306,11 +315,22 @@ __global__ void __launch_bounds__(256) k_gb_pair(DevView v, GBConst k, const flo
     const unsigned dmask = (T.flags & 2) ? diag_exclusion(lane) : 0u;
     PairAcc I = {0.f, 0.f, 0.f, 0.f}, J = {0.f, 0.f, 0.f, 0.f};
     double evdw = 0.0, eel = 0.0, epol = 0.0;
-    if (tile_masked(T))
-      gb_pair_tile<true, ENERGY>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw, eel, epol);
-    else
-      gb_pair_tile<false, ENERGY>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw, eel,
-                                  epol);
+    const bool full = tile_full(T);
+    if (tile_masked(T)) {
+      if (full)
+        gb_pair_tile<true, ENERGY, true>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
+                                         eel, epol);
+      else
+        gb_pair_tile<true, ENERGY, false>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
+                                          eel, epol);
+    } else {
+      if (full)
+        gb_pair_tile<false, ENERGY, true>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
+                                          eel, epol);
+      else
+        gb_pair_tile<false, ENERGY, false>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
+                                           eel, epol);
+    }
     flush_pair(v, deda, si, I);
     flush_pair(v, deda, T.bj * 32 + lane, J);
     if (ENERGY) {
@@ -343,7 +363,7 @@ __global__ void k_gb_self(DevView v, const double* charge, GBConst k, double pre
 // ---------------------------------------------------------------------------
 // pass 3: dE/da chain rule through the Born radii, both directions of a pair
 // ---------------------------------------------------------------------------
-template <bool MASKED>
+template <bool MASKED, bool FULL>
 __device__ __forceinline__ void chain_tile(const DevView& v, const GBConst& k, const Tile& T, int lane, int si,
                                            const float4& xi, const float4& pi, float ci, unsigned ex,
                                            const float* chain, PairAcc& I, PairAcc& J) {
@@ -354,9 +374,12 @@ __device__ __forceinline__ void chain_tile(const DevView& v, const GBConst& k, c
   for (int kk = 0; kk < 32; kk++) {
     const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
     const float r2 = dx * dx + dy * dy + dz * dz;
-    bool in = r2 <= k.still2;
-    if (fabsf(r2 - k.still2) <= 2e-6f * k.still2)
-      in = r2_slots_fp64(v, si, T.bj * 32 + ((lane + kk) & 31)) <= k.still2_d;
+    bool in = true;  // FULL: the whole tile lies inside the Still cutoff
+    if (!FULL) {
+      in = r2 <= k.still2;
+      if (fabsf(r2 - k.still2) <= 2e-6f * k.still2)
+        in = r2_slots_fp64(v, si, T.bj * 32 + ((lane + kk) & 31)) <= k.still2_d;
+    }
     if (MASKED) in = in && !((ex >> kk) & 1u);
     if (in) {
       const float rs = pi.z + pj.z;
@@ -398,8 +421,14 @@ __global__ void __launch_bounds__(256) k_gb_chain(DevView v, GBConst k, const fl
     tile_masks(v, T, lane, ex, m14);
     if (T.flags & 2) ex |= diag_exclusion(lane);
     PairAcc I = {0.f, 0.f, 0.f, 0.f}, J = {0.f, 0.f, 0.f, 0.f};
-    if (tile_masked(T)) chain_tile<true>(v, k, T, lane, si, xi, pi, ci, ex, chain, I, J);
-    else chain_tile<false>(v, k, T, lane, si, xi, pi, ci, ex, chain, I, J);
+    const bool full = tile_full(T);
+    if (tile_masked(T)) {
+      if (full) chain_tile<true, true>(v, k, T, lane, si, xi, pi, ci, ex, chain, I, J);
+      else chain_tile<true, false>(v, k, T, lane, si, xi, pi, ci, ex, chain, I, J);
+    } else {
+      if (full) chain_tile<false, true>(v, k, T, lane, si, xi, pi, ci, ex, chain, I, J);
+      else chain_tile<false, false>(v, k, T, lane, si, xi, pi, ci, ex, chain, I, J);
+    }
     flush_force(v, si, I);
     flush_force(v, T.bj * 32 + lane, J);
   }

@@ -243,7 +243,7 @@ __global__ void k_slot_params(DevView v, const double* radius, const double* sqe
 
 // candidate block pairs -> include flags, in candidate order (row-major: bi, then bj >= bi)
 __device__ __forceinline__ bool candidate_pair(const DevView& v, long long t, int& gi, int& gj, int& flags, float R,
-                                               float margin) {
+                                               float margin, float full_R, float full_margin) {
   // system by binary search over cand_start
   int lo = 0, hi = v.nsys - 1;
   while (lo < hi) {
@@ -266,7 +266,7 @@ __device__ __forceinline__ bool candidate_pair(const DevView& v, long long t, in
   gj = S.block_start + (int)bj;
   float4 hi4 = v.half[gi], hj4 = v.half[gj];
   float hs[3] = {hi4.x + hj4.x, hi4.y + hj4.y, hi4.z + hj4.z};
-  double dist2 = 0;
+  double dist2 = 0, dmax2 = 0;
   bool need_mi = false;
 #pragma unroll
   for (int c = 0; c < 3; c++) {
@@ -277,8 +277,13 @@ __device__ __forceinline__ bool candidate_pair(const DevView& v, long long t, in
     }
     double g = fabs(d) - hs[c];
     if (g > 0) dist2 += g * g;
+    const double m = fabs(d) + hs[c];
+    dmax2 += m * m;
   }
-  flags = (need_mi ? 1 : 0) | (gi == gj ? 2 : 0);
+  // full: the farthest pair of the two boxes, grown by the displacement margin,
+  // stays inside every cutoff and switch radius
+  const bool full = full_R > 0.f && !need_mi && sqrt(dmax2) + (double)full_margin < (double)full_R;
+  flags = (need_mi ? 1 : 0) | (gi == gj ? 2 : 0) | (full ? 4 : 0);
   return dist2 <= (double)R * R;
 }
 
@@ -286,19 +291,20 @@ __global__ void k_tile_flags(DevView v, long long ncand, float R, float margin, 
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ncand) return;
   int gi, gj, fl;
-  flag[t] = candidate_pair(v, t, gi, gj, fl, R, margin) ? 1 : 0;
+  flag[t] = candidate_pair(v, t, gi, gj, fl, R, margin, 0.f, 0.f) ? 1 : 0;
 }
 
 // write the included pairs at their scanned positions: the tile list is in
 // row-major order, so every run of tiles with one i-block is contiguous and
 // its order is the same on every build
-__global__ void k_tile_write(DevView v, long long ncand, float R, float margin, const int* flag, const int* pos) {
+__global__ void k_tile_write(DevView v, long long ncand, float R, float margin, float full_R, float full_margin,
+                             const int* flag, const int* pos) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ncand) return;
   if (t == ncand - 1) *v.ntiles = pos[t] + flag[t];
   if (!flag[t]) return;
   int gi, gj, fl;
-  candidate_pair(v, t, gi, gj, fl, R, margin);
+  candidate_pair(v, t, gi, gj, fl, R, margin, full_R, full_margin);
   Tile T;
   T.bi = gi;
   T.bj = gj;
@@ -355,7 +361,9 @@ __global__ void k_masks(DevView v) {
 }
 
 // per-evaluation pack: FP64 positions -> float offsets from the block centre
-__global__ void k_pack(DevView v, const double* charge, float check2, int store_ref, long long ncand) {
+// check2: squared skin limit (0 = no skin check); full2: squared limit that keeps
+// tiles flagged full valid (0 = none flagged), checked where the skin check is not
+__global__ void k_pack(DevView v, const double* charge, float check2, float full2, int store_ref, long long ncand) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= v.nslots) return;
   int a = v.sorted_atom[s];
@@ -376,12 +384,16 @@ __global__ void k_pack(DevView v, const double* charge, float check2, int store_
     o = make_float4((float)r[0], (float)r[1], (float)r[2], (float)charge[a]);
     if (store_ref) {
       v.rel0[s] = o;
-    } else if (check2 > 0.f && (S.periodic || (long long)*v.ntiles < ncand)) {
+    } else {
       // (in open space, when every block pair of every system is a tile, no pair
       // can leave the list; in a periodic box the tile images still depend on it)
-      float4 q = v.rel0[s];
-      float dx = o.x - q.x, dy = o.y - q.y, dz = o.z - q.z;
-      if (dx * dx + dy * dy + dz * dz > check2) atomicOr(v.status, (unsigned)ST_STALE_LIST);
+      const bool skin = check2 > 0.f && (S.periodic || (long long)*v.ntiles < ncand);
+      const float lim = skin ? check2 : full2;
+      if (lim > 0.f) {
+        float4 q = v.rel0[s];
+        float dx = o.x - q.x, dy = o.y - q.y, dz = o.z - q.z;
+        if (dx * dx + dy * dy + dz * dz > lim) atomicOr(v.status, (unsigned)ST_STALE_LIST);
+      }
     }
   }
   v.xq[s] = o;
@@ -389,7 +401,7 @@ __global__ void k_pack(DevView v, const double* charge, float check2, int store_
 
 static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
-int launch_list_build(Context& c, float list_radius) {
+int launch_list_build(Context& c, float list_radius, float full_radius) {
   c.kernel_launches += 18;
   DevView v = c.view();
   cudaStream_t st = c.stream;
@@ -425,11 +437,11 @@ int launch_list_build(Context& c, float list_radius) {
     k_scan_sums<<<1, 1024, 0, st>>>(c.d_scan_tmp2.p, nb2);
     k_scan_add<<<nb2, 1024, 0, st>>>(c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
   }
-  k_tile_write<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, list_radius, (float)c.lp.Padding, c.d_tile_flag.p,
-                                                    c.d_tile_pos.p);
+  k_tile_write<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, list_radius, (float)c.lp.Padding, full_radius,
+                                                    c.full_margin(), c.d_tile_flag.p, c.d_tile_pos.p);
   // masks: launched over the worst case; warps beyond *ntiles return at once
   k_masks<<<nblk(c.ncand * 32, 256), 256, 0, st>>>(v);
-  k_pack<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_charge.p, 0.f, 1, c.ncand);
+  k_pack<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_charge.p, 0.f, 0.f, 1, c.ncand);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 
@@ -449,7 +461,12 @@ int launch_pack(Context& c, float check_disp) {
   c.kernel_launches += 1;
   DevView v = c.view();
   float c2 = check_disp > 0 ? check_disp * check_disp : 0.f;
-  k_pack<<<nblk(c.nslots, 256), 256, 0, c.stream>>>(v, c.d_charge.p, c2, 0, c.ncand);
+  float f2 = 0.f;
+  if (c.full_radius_built > 0.f) {
+    const float h = 0.5f * c.full_margin();
+    f2 = h * h;
+  }
+  k_pack<<<nblk(c.nslots, 256), 256, 0, c.stream>>>(v, c.d_charge.p, c2, f2, 0, c.ncand);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

@@ -49,6 +49,17 @@ double list_radius(const Context& c) {
   return r + c.lp.Padding;
 }
 
+// Distance below which no cutoff or switch of the set components acts (tiles
+// entirely inside it skip those tests); 0 when the skin check is off, since the
+// full-tile margin is only guaranteed by the per-step displacement check.
+double full_radius(const Context& c) {
+  if (!c.lp.check_skin || (!c.nb_set && !c.gb_set)) return 0.0;
+  double r = 1e300;
+  if (c.nb_set) r = std::min(r, std::min(c.nb.InnerCutoff, c.nb.VdwInnerCutoff));
+  if (c.gb_set) r = std::min(r, std::min(std::min(c.gb.InnerCutoff, c.gb.VdwInnerCutoff), c.gb.GbsaStillCutoff));
+  return r;
+}
+
 int read_status(Context& c) {
   unsigned st = 0;
   cudaError_t e = cudaMemcpyAsync(&st, c.d_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, c.stream);
@@ -597,9 +608,11 @@ int pdgpu::rebuild_list_impl(Context& c) {
   if (!c.nb_set && !c.gb_set && !c.has_sa) return PDGPU_ERR_STATE;
   CK(cudaSetDevice(c.device));
   float R = (float)list_radius(c);
-  int st = launch_list_build(c, R);
+  float F = (float)std::min(full_radius(c), (double)R);
+  int st = launch_list_build(c, R, F);
   if (st != PDGPU_OK) return st;
   c.list_radius_built = R;
+  c.full_radius_built = F;
   c.list_built = true;
   return PDGPU_OK;
 }

@@ -59,7 +59,8 @@ struct SystemInfo {
 struct Tile {
   int bi, bj;
   int mask;    // index into the exclusion-mask table or -1
-  int flags;   // bit0: per-pair minimum image needed, bit1: diagonal tile
+  int flags;   // bit0: per-pair minimum image needed, bit1: diagonal tile,
+               // bit2: every pair inside all cutoffs and switch radii (with margin)
 };
 
 // Pair-law constants for the LJ + Coulomb kernel (FF_NonBonded)
@@ -160,7 +161,9 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // ---------------------------------------------------------------------------
 struct Context;
 int tile_grid(Context& c);   // grid of the tile kernels (grid-stride, one tile per warp item)
-int launch_list_build(Context& c, float list_radius);
+// full_radius: distance below which every cutoff and switch of the set
+// components is inactive (0 = never mark tiles full)
+int launch_list_build(Context& c, float list_radius, float full_radius);
 int launch_pack(Context& c, float check_disp);
 int launch_nb(Context& c, const NBConst& k, bool need_virial);
 int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset, double premul, bool energy);

@@ -42,6 +42,10 @@ struct Context {
   pdgpu_list_params lp{};
   bool nb_set = false, gb_set = false;
   float list_radius_built = 0.f;
+  float full_radius_built = 0.f;   // tiles flagged full: max distance + full_margin() below this
+  // displacement margin of full tiles: every atom stays within half of it of its
+  // position at the build (checked every step by the position pack)
+  float full_margin() const { return (float)(lp.Padding > 10.0 ? lp.Padding : 10.0); }
   int tile_ctas_per_sm = 8;    // launch shape of the tile kernels (autotuned)
   long long kernel_launches = 0;  // kernels this context has put on its stream (graph replays included)
 

@@ -277,7 +277,7 @@ int pdgpu_time_kernel(pdgpu_ctx* h, int kernel, int reps, int flush_l2, double* 
       case 1: case 2: case 3: st = launch_gb_stage(c, make_gb_const(c.gb, c.list_radius_built), kernel); break;
       case 4: st = launch_lcpo(c, c.d_facc.p, nullptr, 0); break;
       case 5: st = launch_integrate(c, *c.md, false, false); break;
-      case 6: st = launch_list_build(c, c.list_radius_built); break;
+      case 6: st = launch_list_build(c, c.list_radius_built, c.full_radius_built); break;
       case 7: st = launch_pack(c, 0.f); break;
       case 8: st = launch_bonded(c, false); break;
       default: st = PDGPU_ERR_ARG;

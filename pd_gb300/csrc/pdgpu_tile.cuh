@@ -35,6 +35,10 @@ __device__ __forceinline__ float4 j_in_i_frame(const DevView& v, const Tile& T, 
 // with full-warp shuffles, which need every lane on the same path.
 __device__ __forceinline__ bool tile_masked(const Tile& T) { return T.mask >= 0 || (T.flags & 2); }
 
+// Whether every pair of the tile lies inside all cutoffs and switch radii of
+// the list's components, with the list's displacement margin (set at build).
+__device__ __forceinline__ bool tile_full(const Tile& T) { return (T.flags & 4) != 0; }
+
 __device__ __forceinline__ void tile_masks(const DevView& v, const Tile& T, int lane, unsigned& ex, unsigned& m14) {
   ex = 0u;
   m14 = 0u;
