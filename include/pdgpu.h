@@ -228,6 +228,25 @@ int pdgpu_get_kinetic(pdgpu_ctx *ctx, double *ekin);
  * NULL) reports rung pair r; temps (may be NULL) returns each system's new
  * target temperature. */
 int pdgpu_remd_exchange(pdgpu_ctx *ctx, int parity, int *accepted, double *temps);
+/* REX_Replica::ExchangeMode per rung (remd.h:49, applied at remd.cpp:186-200;
+ * the lower replica's mode governs a pair).  Swap trades temperatures (the
+ * default); Downward copies the upper structure onto the lower rung, Upward the
+ * lower onto the upper, with PD's velocity rescaling of both rungs.  The copy
+ * modes need systems of one molecule (equal atom counts, else
+ * PDGPU_ERR_UNSUPPORTED); after a copy the list is rebuilt at the next step. */
+#define PDGPU_REX_SWAP 0
+#define PDGPU_REX_DOWNWARD 1
+#define PDGPU_REX_UPWARD 2
+int pdgpu_remd_set_modes(pdgpu_ctx *ctx, const int *modes);
+/* Crash rescue of REX_Local::runcore (remd.cpp:118-147): pdgpu_md_checkpoint
+ * saves the positions (call it at the start of a round); after a round that
+ * ended in PDGPU_ERR_NAN, pdgpu_md_rescue puts every system holding a
+ * non-finite position or velocity back to its saved positions with fresh
+ * Maxwell-Boltzmann velocities at its target temperature (PD's 200 conjugate-
+ * gradient minimisation steps are not run).  rescued (nsystems ints, may be
+ * NULL) flags them, count gets their number. */
+int pdgpu_md_checkpoint(pdgpu_ctx *ctx);
+int pdgpu_md_rescue(pdgpu_ctx *ctx, unsigned long long seed, int *rescued, int *count);
 /* Project autotuner (state restored afterwards): first the launch shape of the
  * tile kernels (CTAs per SM of their grid-stride grid), timed on force
  * evaluations of the current state; then the list-rebuild cadence, timed on

@@ -129,11 +129,24 @@ __global__ void k_langevin(MDView m, LangevinCoeffs L, int first_step, int last_
 
 // REMD: one thread walks the temperature ladder (remd.cpp:178-215, 349-356).
 // temp_sys[r] = system holding temperature rung r; ladder[r] = temperature (K).
+// Exchange sweep over rung pairs (r, r+1) of one parity (remd.cpp:178-215).
+// mode[r] is the lower rung's REX_Replica::ExchangeMode (remd.h:49):
+//   0 Swap:     the two structures trade temperatures (here: the systems trade
+//               target temperatures; velocities scale by sqrt(T'/T));
+//   1 Downward: the lower rung takes a copy of the upper structure,
+//   2 Upward:   the upper rung takes a copy of the lower structure;
+// in both copy modes PD rescales the velocities of both rungs after the copy
+// (lower / factor, upper * factor, factor = sqrt(T_upper / T_lower)).  A copy
+// is recorded as copy_src[dst] = src with copy_scale[dst]; k_remd_copy applies it.
 __global__ void k_remd_exchange(const long long* eacc, int nsys, int parity, const double* ladder, int* temp_sys,
                                 double* temp, double* vscale, int* accepted, unsigned long long seed,
-                                unsigned long long round) {
+                                unsigned long long round, const int* mode, int* copy_src, double* copy_scale) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  for (int s = 0; s < nsys; s++) vscale[s] = 1.0;
+  for (int s = 0; s < nsys; s++) {
+    vscale[s] = 1.0;
+    copy_src[s] = -1;
+    copy_scale[s] = 1.0;
+  }
   for (int r = parity; r < nsys - 1; r += 2) {
     int lo = temp_sys[r], hi = temp_sys[r + 1];
     double Tlo = ladder[r], Thi = ladder[r + 1];
@@ -152,15 +165,93 @@ __global__ void k_remd_exchange(const long long* eacc, int nsys, int parity, con
     bool acc = (delta <= 0) || (exp(-delta) > u01(rr.x));
     accepted[r] = acc ? 1 : 0;
     if (acc) {
-      // the structure at Tlo moves to Thi and vice versa; velocities follow sqrt(T'/T)
-      temp_sys[r] = hi;
-      temp_sys[r + 1] = lo;
-      temp[hi] = Tlo;
-      temp[lo] = Thi;
-      vscale[lo] *= sqrt(Thi / Tlo);
-      vscale[hi] *= sqrt(Tlo / Thi);
+      const double factor = sqrt(Thi / Tlo);
+      const int m = mode ? mode[r] : 0;
+      if (m == 1) {            // Downward: lower <- copy of upper
+        copy_src[lo] = hi;
+        copy_scale[lo] = 1.0 / factor;
+        vscale[hi] *= factor;
+      } else if (m == 2) {     // Upward: upper <- copy of lower
+        copy_src[hi] = lo;
+        copy_scale[hi] = factor;
+        vscale[lo] *= 1.0 / factor;
+      } else {
+        // the structure at Tlo moves to Thi and vice versa; velocities follow sqrt(T'/T)
+        temp_sys[r] = hi;
+        temp_sys[r + 1] = lo;
+        temp[hi] = Tlo;
+        temp[lo] = Thi;
+        vscale[lo] *= factor;
+        vscale[hi] *= 1.0 / factor;
+      }
     }
   }
+}
+
+// structure copies of the copy modes: atom i of a destination system takes atom
+// i of its source (equal atom counts); sources are never destinations in a sweep
+__global__ void k_remd_copy(MDView m, const SystemInfo* sys, const int* copy_src, const double* copy_scale) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= m.natom) return;
+  const int s = m.atom_sys[a];
+  const int t = copy_src[s];
+  if (t < 0) return;
+  const int i = a - sys[s].atom_start;
+  if (i >= sys[t].natom) return;
+  const int b = sys[t].atom_start + i;
+  const double f = copy_scale[s];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    m.pos[3 * a + c] = m.pos[3 * b + c];
+    m.vel[3 * a + c] = m.vel[3 * b + c] * f;
+  }
+}
+
+// crash rescue: flag the systems holding a non-finite position or velocity
+__global__ void k_nonfinite(MDView m, int* bad) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= m.natom) return;
+  bool ok = true;
+#pragma unroll
+  for (int c = 0; c < 3; c++) ok = ok && isfinite(m.pos[3 * a + c]) && isfinite(m.vel[3 * a + c]);
+  if (!ok) atomicOr(&bad[m.atom_sys[a]], 1);
+}
+
+// crash rescue of the flagged systems: positions from the checkpoint, fresh
+// Gaussian velocities sqrt(kB T / m) (setInitialSpeeds, md.cpp:359-380; the
+// kinetic energy is then scaled per system by k_rescale_ke)
+__global__ void k_rescue(MDView m, const int* bad, const double* pos0, unsigned long long seed, long long* ke) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= m.natom) return;
+  const int s = m.atom_sys[a];
+  if (!bad[s]) return;
+  const uint2 key = make_uint2((unsigned)seed ^ 0x2545f491u, (unsigned)(seed >> 32));
+  const uint4 r = philox4x32(make_uint4((unsigned)a, 0u, 0u, 11u), key);
+  double n[4];
+  box_muller(r.x, r.y, n[0], n[1]);
+  box_muller(r.z, r.w, n[2], n[3]);
+  const double sd = sqrt(1.38065E-23 * m.temp[s] / m.mass[a]);
+  double e = 0.0;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    m.pos[3 * a + c] = pos0[3 * a + c];
+    const double v = n[c] * sd;
+    m.vel[3 * a + c] = v;
+    e += 0.5 * m.mass[a] * v * v;
+  }
+  atomic_add_ll(&ke[s], __double2ll_rn(e * 1e30));  // J, 1e-30 J resolution
+}
+
+__global__ void k_rescale_ke(MDView m, const int* bad, const SystemInfo* sys, const long long* ke) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= m.natom) return;
+  const int s = m.atom_sys[a];
+  if (!bad[s]) return;
+  const double have = (double)ke[s] * 1e-30;
+  const double want = 1.5 * sys[s].natom * 1.38065E-23 * m.temp[s];
+  const double f = have > 0 ? sqrt(want / have) : 0.0;
+#pragma unroll
+  for (int c = 0; c < 3; c++) m.vel[3 * a + c] *= f;
 }
 
 __global__ void k_scale_vel(MDView m, const double* vscale) {
@@ -195,11 +286,33 @@ int launch_integrate(Context& c, MDState& md, bool first, bool last) {
 }
 
 int launch_remd(Context& c, MDState& md, int parity, unsigned long long round) {
-  c.kernel_launches += 2;
+  c.kernel_launches += 3;
   MDView m = md_view(c, md);
+  const int nb = (c.natom + 255) / 256;
   k_remd_exchange<<<1, 32, 0, c.stream>>>(c.d_eacc.p, c.nsys, parity, md.d_ladder.p, md.d_temp_sys.p, md.d_temp.p,
-                                          md.d_vscale.p, md.d_accepted.p, md.p.seed, round);
-  k_scale_vel<<<(c.natom + 255) / 256, 256, 0, c.stream>>>(m, md.d_vscale.p);
+                                          md.d_vscale.p, md.d_accepted.p, md.p.seed, round, md.d_mode.p,
+                                          md.d_copy_src.p, md.d_copy_scale.p);
+  k_remd_copy<<<nb, 256, 0, c.stream>>>(m, c.d_sys.p, md.d_copy_src.p, md.d_copy_scale.p);
+  k_scale_vel<<<nb, 256, 0, c.stream>>>(m, md.d_vscale.p);
+  return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
+}
+
+int launch_rescue(Context& c, MDState& md, unsigned long long seed, int* bad_host) {
+  MDView m = md_view(c, md);
+  const int nb = (c.natom + 255) / 256;
+  c.kernel_launches += 1;
+  if (cudaMemsetAsync(md.d_bad.p, 0, sizeof(int) * c.nsys, c.stream) != cudaSuccess) return PDGPU_ERR_CUDA;
+  k_nonfinite<<<nb, 256, 0, c.stream>>>(m, md.d_bad.p);
+  if (cudaMemcpyAsync(bad_host, md.d_bad.p, sizeof(int) * c.nsys, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess ||
+      cudaStreamSynchronize(c.stream) != cudaSuccess)
+    return PDGPU_ERR_CUDA;
+  bool any = false;
+  for (int s = 0; s < c.nsys; s++) any = any || bad_host[s];
+  if (!any) return PDGPU_OK;
+  c.kernel_launches += 2;
+  if (cudaMemsetAsync(md.d_ke.p, 0, sizeof(long long) * c.nsys, c.stream) != cudaSuccess) return PDGPU_ERR_CUDA;
+  k_rescue<<<nb, 256, 0, c.stream>>>(m, md.d_bad.p, md.d_ckpt_pos.p, seed, md.d_ke.p);
+  k_rescale_ke<<<nb, 256, 0, c.stream>>>(m, md.d_bad.p, c.d_sys.p, md.d_ke.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

@@ -28,6 +28,13 @@ struct MDState {
   DBuf<long long> d_ke;               // [nsys] kinetic energy, fixed point kcal/mol
   DBuf<long long> d_facc_sa;          // [nslots*3] cached LCPO forces
   DBuf<long long> d_surf_cache;       // [nsys] cached LCPO energy
+  DBuf<int> d_mode;                   // [nsys] exchange mode of each rung's lower replica (0 swap, 1 down, 2 up)
+  DBuf<int> d_copy_src;               // [nsys] structure source of each system in the last sweep (-1 none)
+  DBuf<double> d_copy_scale;          // [nsys] velocity factor of copied structures
+  DBuf<double> d_ckpt_pos;            // [natom*3] positions at the last checkpoint (crash rescue)
+  DBuf<int> d_bad;                    // [nsys] systems flagged non-finite
+  bool copy_modes = false;            // some rung copies structures (list and LCPO cache refreshed after)
+  bool force_sasa = false;            // recompute LCPO at the next step
   std::map<int, cudaGraphExec_t> graphs;
   std::map<int, long long> graph_kernels;  // kernel nodes of each captured flavour
 };
@@ -67,5 +74,8 @@ inline MDView md_view(Context& c, MDState& md) {
 int launch_integrate(Context& c, MDState& md, bool first, bool last);
 int launch_remd(Context& c, MDState& md, int parity, unsigned long long round);
 int launch_zero_ll(Context& c, long long* p, size_t n);
+// crash rescue: flags non-finite systems into bad_host (nsys ints, synchronous)
+// and restores them from the checkpoint with fresh velocities
+int launch_rescue(Context& c, MDState& md, unsigned long long seed, int* bad_host);
 
 }  // namespace pdgpu

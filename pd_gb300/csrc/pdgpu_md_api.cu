@@ -6,6 +6,7 @@
 // between, as FF_SASA_LCPO::calcForces does, lcpo.cpp:193-206), then the
 // integrator.  The step sequence of each distinct flavour (rebuild / LCPO /
 // energy) is captured once into a CUDA graph and replayed.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <vector>
@@ -143,7 +144,8 @@ int md_enqueue_impl(Context& c, MDState& md, int nsteps, bool energy_on_last) {
     const unsigned long long s = md.step;
     int flags = 0;
     if (s % (unsigned long long)md.p.UpdateNList == 0 || !c.list_built) flags |= 1;
-    if ((md.p.what & PDGPU_SA) && s % (unsigned long long)md.p.UpdateSasa == 0) flags |= 2;
+    if ((md.p.what & PDGPU_SA) && (s % (unsigned long long)md.p.UpdateSasa == 0 || md.force_sasa)) flags |= 2;
+    md.force_sasa = false;
     if (energy_on_last && k == nsteps - 1) flags |= 4;
     bool first = !md.trajectory_started;
     int st = run_step(c, md, flags, first);
@@ -188,8 +190,11 @@ int pdgpu_md_setup(pdgpu_ctx* h, const pdgpu_md_params* p, const double* temps) 
       md.d_ladder.alloc(c.nsys) != cudaSuccess || md.d_temp_sys.alloc(c.nsys) != cudaSuccess ||
       md.d_vscale.alloc(c.nsys) != cudaSuccess || md.d_accepted.alloc(c.nsys) != cudaSuccess ||
       md.d_ke.alloc(c.nsys) != cudaSuccess || md.d_facc_sa.alloc(3 * (size_t)c.nslots) != cudaSuccess ||
-      md.d_surf_cache.alloc(c.nsys) != cudaSuccess || md.d_step.alloc(1) != cudaSuccess)
+      md.d_surf_cache.alloc(c.nsys) != cudaSuccess || md.d_step.alloc(1) != cudaSuccess ||
+      md.d_mode.alloc(c.nsys) != cudaSuccess || md.d_copy_src.alloc(c.nsys) != cudaSuccess ||
+      md.d_copy_scale.alloc(c.nsys) != cudaSuccess || md.d_bad.alloc(c.nsys) != cudaSuccess)
     return PDGPU_ERR_CUDA;
+  CK(cudaMemsetAsync(md.d_mode.p, 0, sizeof(int) * c.nsys, c.stream));
   std::vector<int> order(c.nsys);
   for (int s = 0; s < c.nsys; s++) order[s] = s;
   CK(cudaMemsetAsync(md.d_vel.p, 0, sizeof(double) * 3 * N, c.stream));
@@ -315,10 +320,73 @@ int pdgpu_remd_exchange(pdgpu_ctx* h, int parity, int* accepted, double* temps) 
   CK(cudaMemsetAsync(md.d_accepted.p, 0, sizeof(int) * c.nsys, c.stream));
   int st = launch_remd(c, md, parity, md.exchange_round++);
   if (st != PDGPU_OK) return st;
-  if (accepted && c.nsys > 1)
-    CK(cudaMemcpyAsync(accepted, md.d_accepted.p, sizeof(int) * (c.nsys - 1), cudaMemcpyDeviceToHost, c.stream));
+  std::vector<int> acc(c.nsys, 0);
+  CK(cudaMemcpyAsync(acc.data(), md.d_accepted.p, sizeof(int) * c.nsys, cudaMemcpyDeviceToHost, c.stream));
   if (temps) CK(cudaMemcpyAsync(temps, md.d_temp.p, sizeof(double) * c.nsys, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
+  if (accepted && c.nsys > 1) std::copy(acc.begin(), acc.begin() + (c.nsys - 1), accepted);
+  if (md.copy_modes) {
+    // a copied structure jumped: new list (and skin reference) and LCPO at the next step
+    bool any = false;
+    for (int r = 0; r + 1 < c.nsys; r++) any = any || acc[r];
+    if (any) {
+      c.list_built = false;
+      md.force_sasa = true;
+    }
+  }
+  return PDGPU_OK;
+}
+
+int pdgpu_remd_set_modes(pdgpu_ctx* h, const int* modes) {
+  if (!h || !modes) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.md) return PDGPU_ERR_STATE;
+  bool copy = false;
+  for (int r = 0; r < c.nsys; r++) {
+    if (modes[r] < PDGPU_REX_SWAP || modes[r] > PDGPU_REX_UPWARD) return PDGPU_ERR_ARG;
+    copy = copy || modes[r] != PDGPU_REX_SWAP;
+  }
+  if (copy)
+    for (int s = 1; s < c.nsys; s++)
+      if (c.sys[s].natom != c.sys[0].natom) return PDGPU_ERR_UNSUPPORTED;
+  CK(cudaSetDevice(c.device));
+  CK(cudaMemcpyAsync(c.md->d_mode.p, modes, sizeof(int) * c.nsys, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  c.md->copy_modes = copy;
+  return PDGPU_OK;
+}
+
+int pdgpu_md_checkpoint(pdgpu_ctx* h) {
+  if (!h) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.md) return PDGPU_ERR_STATE;
+  MDState& md = *c.md;
+  CK(cudaSetDevice(c.device));
+  if (md.d_ckpt_pos.n < 3 * (size_t)c.natom && md.d_ckpt_pos.alloc(3 * (size_t)c.natom) != cudaSuccess)
+    return PDGPU_ERR_CUDA;
+  CK(cudaMemcpyAsync(md.d_ckpt_pos.p, c.d_pos.p, 24 * (size_t)c.natom, cudaMemcpyDeviceToDevice, c.stream));
+  return PDGPU_OK;
+}
+
+int pdgpu_md_rescue(pdgpu_ctx* h, unsigned long long seed, int* rescued, int* count) {
+  if (!h) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.md || !c.md->d_ckpt_pos.p) return PDGPU_ERR_STATE;
+  MDState& md = *c.md;
+  CK(cudaSetDevice(c.device));
+  std::vector<int> bad(c.nsys, 0);
+  int st = launch_rescue(c, md, seed, bad.data());
+  if (st != PDGPU_OK) return st;
+  int n = 0;
+  for (int s = 0; s < c.nsys; s++) n += bad[s] ? 1 : 0;
+  if (rescued) std::copy(bad.begin(), bad.end(), rescued);
+  if (count) *count = n;
+  if (n) {
+    c.list_built = false;
+    md.force_sasa = true;
+    CK(cudaMemsetAsync(c.d_status.p, 0, sizeof(unsigned), c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+  }
   return PDGPU_OK;
 }
 

@@ -221,6 +221,23 @@ class DeviceContext:
         ffi.check(self.lib.pdgpu_remd_exchange(self.h, int(parity), _pi(acc), _pd(temps)), "pdgpu_remd_exchange")
         return acc[:self.nsystems - 1], temps
 
+    def remd_set_modes(self, modes):
+        """Exchange mode of each rung's lower replica: 0 Swap, 1 Downward, 2 Upward."""
+        m = np.ascontiguousarray(np.broadcast_to(np.asarray(modes, np.int32), (self.nsystems,)))
+        ffi.check(self.lib.pdgpu_remd_set_modes(self.h, _pi(m)), "pdgpu_remd_set_modes")
+
+    def md_checkpoint(self):
+        ffi.check(self.lib.pdgpu_md_checkpoint(self.h), "pdgpu_md_checkpoint")
+
+    def md_rescue(self, seed):
+        """Systems with non-finite state back to the checkpoint with fresh velocities;
+        returns the per-system flags of the rescued ones."""
+        flags = np.zeros(self.nsystems, np.int32)
+        n = ctypes.c_int()
+        ffi.check(self.lib.pdgpu_md_rescue(self.h, ctypes.c_ulonglong(seed), _pi(flags), ctypes.byref(n)),
+                  "pdgpu_md_rescue")
+        return flags.astype(bool)
+
     def autotune(self, trial_steps=20):
         a, b = ctypes.c_int(), ctypes.c_int()
         ffi.check(self.lib.pdgpu_md_autotune(self.h, int(trial_steps), ctypes.byref(a), ctypes.byref(b)),

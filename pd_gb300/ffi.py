@@ -111,6 +111,9 @@ SIGNATURES = {
     "pdgpu_get_kinetic": ([ctypes.c_void_p, _dp], ctypes.c_int),
     "pdgpu_remd_exchange": ([ctypes.c_void_p, ctypes.c_int, _ip, _dp], ctypes.c_int),
     "pdgpu_md_autotune": ([ctypes.c_void_p, ctypes.c_int, _ip, _ip], ctypes.c_int),
+    "pdgpu_remd_set_modes": ([ctypes.c_void_p, _ip], ctypes.c_int),
+    "pdgpu_md_checkpoint": ([ctypes.c_void_p], ctypes.c_int),
+    "pdgpu_md_rescue": ([ctypes.c_void_p, ctypes.c_ulonglong, _ip, _ip], ctypes.c_int),
     "pdgpu_set_launch_shape": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "pdgpu_get_launch_shape": ([ctypes.c_void_p, _ip], ctypes.c_int),
     "pdgpu_md_enqueue": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),

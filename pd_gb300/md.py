@@ -120,12 +120,17 @@ class REX_Local:
     runs on the device (remd.cpp:178-215).
     """
 
-    def __init__(self, md, temps):
+    Swap, Downward, Upward = 0, 1, 2     # REX_Replica::ExchangeModeType (remd.h:49)
+
+    def __init__(self, md, temps, exchange_mode=0):
         self.md = md
         self.temps = np.asarray(temps, np.float64)
         self.ExchangeFreq = 500
         self.Steps = 0            # number of exchange rounds
         self.accepted = None
+        self.rescues = 0          # replicas rescued after an unstable round (remd.cpp:118-147)
+        # per replica (rung), as addReplica(..., exmode) sets it; the lower replica's mode governs a pair
+        self.ExchangeMode = np.broadcast_to(np.asarray(exchange_mode, np.int32), self.temps.shape).copy()
         self.md.setTargetTemp(self.temps)
 
     @staticmethod
@@ -188,8 +193,22 @@ class REX_Local:
         n = self.Steps if rounds is None else rounds
         ctx = self.md.setup() if not self.md._setup_done else self.md.wspace.context()
         acc = np.zeros(max(len(self.temps) - 1, 1))
+        ctx.remd_set_modes(self.ExchangeMode)
         for r in range(n):
-            ctx.md_run(self.ExchangeFreq, energy_on_last=True)
+            ctx.md_checkpoint()
+            try:
+                ctx.md_run(self.ExchangeFreq, energy_on_last=True)
+            except ffi.PDGPUError as e:
+                # an unstable replica: back to its structure at the start of the
+                # round with new velocities (PD: remd.run_core_failure), then the
+                # energies for the exchange criterion
+                if e.status != -5:
+                    raise
+                bad = ctx.md_rescue(self.md.Seed * 7919 + r)
+                if not bad.any():
+                    raise
+                self.rescues += int(bad.sum())
+                ctx.md_run(1, energy_on_last=True)
             a, current = ctx.remd_exchange(r % 2)
             acc[:len(a)] += a
             self.current_temps = current

@@ -180,3 +180,93 @@ def test_rex_checkpoint_mime_round_trip(goldens, tmp_path):
     pos1 = ctx.get_positions()
     for r in range(3):
         assert np.array_equal(pos1[off[now[r]]:off[now[r] + 1]], pos0[off[rungs[r]]:off[rungs[r] + 1]])
+
+
+def _four_copies(d, ladder, what_extra=0, update_nlist=10):
+    from pd_gb300 import ffi
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.workspace import SystemImage
+    n = len(ladder)
+    im = SystemImage.concat([SystemImage._from_fixture(d)] * n)
+    ctx = DeviceContext(im)
+    ctx.set_list(2.0)
+    ctx.set_gb(**gb_kwargs(d))
+    rng = np.random.default_rng(5)
+    ctx.set_positions(np.concatenate([d["pos"] + 0.01 * rng.standard_normal(d["pos"].shape) for _ in range(n)]))
+    ctx.md_setup(np.asarray(ladder, float), integrator=1, timestep=1e-15, update_nlist=update_nlist,
+                 what=ffi.GB | ffi.BONDED | what_extra, seed=3)
+    return im, ctx
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_remd_copy_modes_move_structures(goldens, mode):
+    """Downward (1) / Upward (2) exchange (remd.cpp:186-200): equal temperatures
+    always accept; the destination rung gets the other structure and PD's
+    velocity rescaling (factor 1 at equal T), temperatures stay with the systems."""
+    d = goldens["peptide30"]
+    im, ctx = _four_copies(d, [300.0, 300.0, 400.0, 400.0])
+    ctx.remd_set_modes(mode)
+    ctx.md_run(3, energy_on_last=True)
+    p0, v0 = ctx.get_positions(), ctx.get_velocities()
+    acc, temps = ctx.remd_exchange(0)          # rung pairs (0,1) and (2,3)
+    assert acc[0] == 1 and acc[2] == 1
+    assert np.allclose(temps, [300, 300, 400, 400])
+    p1, v1 = ctx.get_positions(), ctx.get_velocities()
+    n = im.natoms[0]
+    sl = lambda k: slice(k * n, (k + 1) * n)
+    for lo, hi in ((0, 1), (2, 3)):
+        dst, src = (lo, hi) if mode == 1 else (hi, lo)
+        assert np.array_equal(p1[sl(dst)], p0[sl(src)]) and np.array_equal(p1[sl(src)], p0[sl(src)])
+        assert np.allclose(v1[sl(dst)], v0[sl(src)], rtol=1e-15, atol=0)
+    ctx.md_run(3)                              # the list is rebuilt after the copies: no stale-list error
+    acc, temps = ctx.remd_exchange(1)          # rungs (1,2): 300 K <-> 400 K
+    if acc[1]:
+        p2 = ctx.get_positions()
+        dst, src = (1, 2) if mode == 1 else (2, 1)
+        assert np.array_equal(p2[sl(dst)], p2[sl(src)])
+
+
+def test_remd_copy_modes_need_one_molecule(goldens):
+    from pd_gb300 import ffi
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.workspace import SystemImage
+    names = ["peptide30", "peptide120"]
+    im = SystemImage.concat([SystemImage._from_fixture(goldens[k]) for k in names])
+    ctx = DeviceContext(im)
+    ctx.set_list(2.0)
+    ctx.set_gb(**gb_kwargs(goldens["peptide30"]))
+    ctx.set_positions(np.concatenate([goldens[k]["pos"] for k in names]))
+    ctx.md_setup([300.0, 350.0], integrator=1, timestep=1e-15, what=ffi.GB, seed=1)
+    with pytest.raises(ffi.PDGPUError) as ei:
+        ctx.remd_set_modes(1)
+    assert ei.value.status == -7
+    ctx.remd_set_modes(0)                       # swapping temperatures works for any batch
+
+
+def test_crash_rescue_restores_unstable_system(goldens):
+    """A system whose state turns non-finite (planted from the host: one atom's
+    position NaN) is put back to the checkpoint with fresh velocities at its
+    target temperature; the other systems keep their state (remd.cpp:118-147)."""
+    from pd_gb300 import ffi
+    d = goldens["peptide30"]
+    im, ctx = _four_copies(d, [300.0, 350.0])
+    ctx.md_run(5)
+    ctx.md_checkpoint()
+    p0 = ctx.get_positions()
+    bad = p0.copy()
+    n = im.natoms[0]
+    bad[n + 3, 1] = np.nan                      # system 1
+    ctx.set_positions(bad)
+    with pytest.raises(ffi.PDGPUError) as ei:
+        ctx.md_run(4)
+    assert ei.value.status == -5
+    p_ok, v_ok = ctx.get_positions()[:n], ctx.get_velocities()[:n]
+    flags = ctx.md_rescue(17)
+    assert list(flags) == [False, True]
+    p1, v1 = ctx.get_positions(), ctx.get_velocities()
+    assert np.array_equal(p1[n:], p0[n:])
+    assert np.array_equal(p1[:n], p_ok) and np.array_equal(v1[:n], v_ok)
+    ke = 0.5 * (im.mass[n:, None] * v1[n:] ** 2).sum()
+    assert np.isclose(ke, 1.5 * n * 1.38065e-23 * 350.0, rtol=1e-9)
+    ctx.md_run(10)                              # runs on from the rescued state
+    assert np.all(np.isfinite(ctx.get_positions()))
