@@ -240,7 +240,8 @@ int pdgpu_remd_exchange(pdgpu_ctx *ctx, int parity, int *accepted, double *temps
 int pdgpu_remd_set_modes(pdgpu_ctx *ctx, const int *modes);
 /* Crash rescue of REX_Local::runcore (remd.cpp:118-147): pdgpu_md_checkpoint
  * saves the positions (call it at the start of a round); after a round that
- * ended in PDGPU_ERR_NAN, pdgpu_md_rescue puts every system holding a
+ * failed (a non-finite atom ends it with PDGPU_ERR_NAN, _FIXED_OVERFLOW or
+ * _STALE_LIST, whichever its kernels meet first), pdgpu_md_rescue puts every system holding a
  * non-finite position or velocity back to its saved positions with fresh
  * Maxwell-Boltzmann velocities at its target temperature (PD's 200 conjugate-
  * gradient minimisation steps are not run).  rescued (nsystems ints, may be

@@ -52,26 +52,44 @@ __device__ __forceinline__ void atom_force(const MDView& m, int a, double f[3]) 
   }
 }
 
-__device__ __forceinline__ void add_ke(const MDView& m, int a, const double v[3]) {
-  double ke = 0.5 * m.mass[a] * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-  // J -> kcal/mol fixed point, per system
-  atomic_add_ll(&m.ke[m.atom_sys[a]], fix_energy_d(ke / kKcalMolToJ));
+// kinetic energy into the per-system fixed-point sum (J -> kcal/mol).  Atoms
+// are in system order, so a warp almost always holds one system: it adds one
+// warp sum instead of 32 atomics on the same address.  Every lane of the warp
+// calls this (valid = false for lanes past the last atom).
+__device__ __forceinline__ void add_ke(const MDView& m, int a, bool valid, const double v[3]) {
+  long long q = 0;
+  int s = -1;
+  if (valid) {
+    const double ke = 0.5 * m.mass[a] * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    q = fix_energy_d(ke * (1.0 / kKcalMolToJ));
+    s = m.atom_sys[a];
+  }
+  const int s0 = __shfl_sync(0xffffffffu, s, 0);
+  if (__all_sync(0xffffffffu, s == s0)) {
+    q = warp_sum_ll(q);
+    if ((threadIdx.x & 31) == 0) atomic_add_ll(&m.ke[s0], q);
+  } else if (valid) {
+    atomic_add_ll(&m.ke[s], q);
+  }
 }
 
 // PD velocity Verlet as written: half kick, (KE), half kick, drift t*(v+dv), kick
 __global__ void k_vv(MDView m, double dt) {
-  int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= m.natom) return;
-  double f[3];
-  atom_force(m, a, f);
-  double tm = 0.5 * dt / m.mass[a];
-  double v[3], p[3];
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = a < m.natom;
+  double f[3] = {0.0, 0.0, 0.0}, v[3] = {0.0, 0.0, 0.0}, p[3];
+  double tm = 0.0;
+  if (valid) {
+    atom_force(m, a, f);
+    tm = 0.5 * dt / m.mass[a];
 #pragma unroll
-  for (int c = 0; c < 3; c++) {
-    v[c] = m.vel[3 * a + c] + f[c] * tm;
-    p[c] = m.pos[3 * a + c];
+    for (int c = 0; c < 3; c++) {
+      v[c] = m.vel[3 * a + c] + f[c] * tm;
+      p[c] = m.pos[3 * a + c];
+    }
   }
-  add_ke(m, a, v);
+  add_ke(m, a, valid, v);
+  if (!valid) return;
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     double dv = f[c] * tm;
@@ -84,26 +102,32 @@ __global__ void k_vv(MDView m, double dt) {
 }
 
 // PD Langevin step (gamma*dt > 1e-5 branch) with per-system target temperature
+// Per-launch constants are folded on the host (LangevinCoeffs: kick = (1 -
+// c0/c1)/gt, drift_f = c0 c2 / c1, sv = sqrt(varv), sr = sqrt(varr)/gamma):
+// one division and one square root per atom remain on the narrow FP64 pipe.
 __global__ void k_langevin(MDView m, LangevinCoeffs L, int first_step, int last_step) {
-  int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= m.natom) return;
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = a < m.natom;
   const unsigned long long step = *m.stepc;
-  double f[3];
-  atom_force(m, a, f);
-  const double mass = m.mass[a];
-  const double tm = L.dt / mass;
-  double v[3];
+  double f[3] = {0.0, 0.0, 0.0}, v[3] = {0.0, 0.0, 0.0};
+  double inv_mass = 0.0, tm = 0.0;
+  if (valid) {
+    atom_force(m, a, f);
+    inv_mass = 1.0 / m.mass[a];
+    tm = L.dt * inv_mass;
 #pragma unroll
-  for (int c = 0; c < 3; c++) {
-    v[c] = m.vel[3 * a + c];
-    if (!first_step) v[c] += (1.0 - L.c0 / L.c1) * f[c] * tm / L.gt;
+    for (int c = 0; c < 3; c++) {
+      v[c] = m.vel[3 * a + c];
+      if (!first_step) v[c] += L.kick * f[c] * tm;
+    }
   }
-  add_ke(m, a, v);
+  add_ke(m, a, valid, v);
+  if (!valid) return;
   if (!last_step) {
     const double T = m.temp[m.atom_sys[a]];
-    const double kTdivm = 1.38065E-23 * T / mass;
-    const double sigmav = sqrt(kTdivm * L.varv);
-    const double sigmar = sqrt(kTdivm * L.varr) / L.gamma;
+    const double s = sqrt(1.38065E-23 * T * inv_mass);
+    const double sigmav = s * L.sv;
+    const double sigmar = s * L.sr;
     // six normals, in PD's draw order n1x n2y | n2x n1z | n1y n2z (md.cpp:1017-1019)
     uint2 key = make_uint2((unsigned)m.seed, (unsigned)(m.seed >> 32));
     uint4 r0 = philox4x32(make_uint4((unsigned)step, (unsigned)(step >> 32), (unsigned)a, 0u), key);
@@ -118,7 +142,7 @@ __global__ void k_langevin(MDView m, LangevinCoeffs L, int first_step, int last_
       double dvr = sigmav * (L.crv * n1[c] + L.sq1mcrv2 * n2[c]);
       double drr = sigmar * n1[c];
       double dr = L.dt * (L.c1 * v[c] + L.c2 * f[c] * tm) + drr;
-      double dv = (L.c0 * L.c2) * f[c] * tm / L.c1 + dvr;
+      double dv = L.drift_f * f[c] * tm + dvr;
       m.pos[3 * a + c] += dr * (1.0 / kAngstrom);
       v[c] = v[c] * L.c0 + dv;
     }

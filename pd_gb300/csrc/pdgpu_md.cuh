@@ -9,6 +9,7 @@ namespace pdgpu {
 // Langevin coefficients (md.cpp:941-1003), FP64
 struct LangevinCoeffs {
   double dt, gamma, gt, c0, c1, c2, varv, varr, crv, sq1mcrv2;
+  double kick, drift_f, sv, sr;   // (1 - c0/c1)/gt, c0 c2 / c1, sqrt(varv), sqrt(varr)/gamma
 };
 
 struct MDState {

@@ -125,6 +125,10 @@ LangevinCoeffs coeffs(double gamma, double t) {
                               1429487.0 * g6 / 13212057600.0);
   }
   L.sq1mcrv2 = std::sqrt(1.0 - L.crv * L.crv);
+  L.kick = (1.0 - L.c0 / L.c1) / L.gt;
+  L.drift_f = L.c0 * L.c2 / L.c1;
+  L.sv = std::sqrt(L.varv);
+  L.sr = std::sqrt(L.varr) / L.gamma;
   return L;
 }
 

@@ -201,8 +201,9 @@ class REX_Local:
             except ffi.PDGPUError as e:
                 # an unstable replica: back to its structure at the start of the
                 # round with new velocities (PD: remd.run_core_failure), then the
-                # energies for the exchange criterion
-                if e.status != -5:
+                # energies for the exchange criterion.  A non-finite atom shows
+                # as NaN, fixed-point overflow or a stale list.
+                if e.status not in (-5, -4, -8):
                     raise
                 bad = ctx.md_rescue(self.md.Seed * 7919 + r)
                 if not bad.any():

@@ -259,7 +259,9 @@ def test_crash_rescue_restores_unstable_system(goldens):
     ctx.set_positions(bad)
     with pytest.raises(ffi.PDGPUError) as ei:
         ctx.md_run(4)
-    assert ei.value.status == -5
+    # a non-finite atom drops out of every cutoff test, so the round ends on the
+    # list check (or on NaN / overflow if its forces were formed)
+    assert ei.value.status in (-5, -4, -8)
     p_ok, v_ok = ctx.get_positions()[:n], ctx.get_velocities()[:n]
     flags = ctx.md_rescue(17)
     assert list(flags) == [False, True]
