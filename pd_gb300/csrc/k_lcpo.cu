@@ -43,12 +43,24 @@ __global__ void __launch_bounds__(256) k_lcpo_cand(DevView v, const float4* lc, 
 // per atom (one warp): order candidates by original atom index, keep the first
 // 80 (PD's insertion order, lcpo.cpp:705-744) and store s_ij
 __global__ void k_lcpo_sort(DevView v, const float4* lc, const int* ncand, const int* cand, int* nl_n, int* nl_idx,
-                            float* nl_s) {
+                            float* nl_s, float4* lpos) {
   __shared__ int sh_key[8][kLcpoCand];
   __shared__ int sh_slot[8][kLcpoCand];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (s >= v.nslots) return;
+  if (lane == 0) {
+    // the triple loop's positions (w: LCPO radius): from the system's first block centre, rounded
+    // once to FP32 (the same rounding the block-centre offsets get elsewhere)
+    const int a = v.sorted_atom[s];
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a >= 0) {
+      const int ref = v.sys[v.slot_sys[s >> 5]].block_start;
+      p = make_float4((float)(v.pos[3 * a] - v.center[3 * ref]), (float)(v.pos[3 * a + 1] - v.center[3 * ref + 1]),
+                      (float)(v.pos[3 * a + 2] - v.center[3 * ref + 2]), lc[s].x);
+    }
+    lpos[s] = p;
+  }
   int n = ncand[s];
   if (n > kLcpoCand) {
     if (lane == 0) atomicOr(v.status, (unsigned)ST_LCPO_OVERFLOW);
@@ -84,22 +96,17 @@ __global__ void k_lcpo_sort(DevView v, const float4* lc, const int* ncand, const
   if (lane == 0) nl_n[s] = keep;
 }
 
-// relative position of slot b seen from slot a (block-centre offsets in FP64)
-__device__ __forceinline__ float3 rel_vec(const DevView& v, int a, int b) {
-  float4 xa = v.xq[a], xb = v.xq[b];
-  int ba = a >> 5, bb = b >> 5;
-  float3 d;
-  d.x = xb.x - xa.x + (float)(v.center[3 * bb] - v.center[3 * ba]);
-  d.y = xb.y - xa.y + (float)(v.center[3 * bb + 1] - v.center[3 * ba + 1]);
-  d.z = xb.z - xa.z + (float)(v.center[3 * bb + 2] - v.center[3 * ba + 2]);
-  return d;
+// relative position of slot b seen from slot a
+__device__ __forceinline__ float3 rel_vec(const float4* lpos, const float4& xa, int b) {
+  const float4 xb = lpos[b];
+  return make_float3(xb.x - xa.x, xb.y - xa.y, xb.z - xa.z);
 }
 
 // per atom i (one warp, lanes over i's overlap partners j): SASA_i and the
 // derivative terms collected on atom i (lcpo.cpp:781-949)
-__global__ void k_lcpo_main(DevView v, const float4* lc, const int* nl_n, const int* nl_idx, const float* nl_s,
-                            const double* P, const double* sigma, double* sasa_out, long long* facc_out,
-                            long long* esurf_out, int esurf_stride) {
+__global__ void k_lcpo_main(DevView v, const float4* lc, const float4* lpos, const int* nl_n, const int* nl_idx,
+                            const float* nl_s, const double* P, const double* sigma, double* sasa_out,
+                            long long* facc_out, long long* esurf_out, int esurf_stride) {
   const int lane = threadIdx.x & 31;
   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (s >= v.nslots) return;
@@ -111,6 +118,7 @@ __global__ void k_lcpo_main(DevView v, const float4* lc, const int* nl_n, const 
     return;
   }
   const float ri = li.x;
+  const float4 xi = lpos[s];
   const float PI = 3.14159265358979f;
   const int n = nl_n[s];
   double Si2 = 0, Si3 = 0, Si4 = 0;
@@ -119,7 +127,7 @@ __global__ void k_lcpo_main(DevView v, const float4* lc, const int* nl_n, const 
     const int sj = nl_idx[(size_t)s * kLcpoMax + jj];
     const int ja = v.sorted_atom[sj];
     const float Si2_t = nl_s[(size_t)s * kLcpoMax + jj];
-    float3 dij = rel_vec(v, s, sj);  // j - i
+    float3 dij = rel_vec(lpos, xi, sj);  // j - i
     float d = sqrtf(dij.x * dij.x + dij.y * dij.y + dij.z * dij.z);
     float rj = lc[sj].x;
     float invd = 1.f / d;
@@ -137,8 +145,9 @@ __global__ void k_lcpo_main(DevView v, const float4* lc, const int* nl_n, const 
     for (int kk = 0; kk < nk; kk++) {
       const int sk = nl_idx[(size_t)sj * kLcpoMax + kk];
       if (sk == s) continue;
-      const float rk = lc[sk].x;
-      float3 dik = rel_vec(v, s, sk);
+      const float4 xk = lpos[sk];
+      const float rk = xk.w;
+      const float3 dik = make_float3(xk.x - xi.x, xk.y - xi.y, xk.z - xi.z);
       float dik2 = dik.x * dik.x + dik.y * dik.y + dik.z * dik.z;
       if ((ri + rk) * (ri + rk) < dik2) continue;
       float invdik = rsqrtf(dik2);
@@ -201,9 +210,9 @@ int launch_lcpo(Context& c, long long* facc_out, long long* esurf_out, int esurf
   k_lcpo_cand<<<g, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_ncand.p, c.d_lc_cand.p);
   int nw = (int)(((long long)c.nslots * 32 + 255) / 256);
   k_lcpo_sort<<<nw, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_ncand.p, c.d_lc_cand.p, c.d_lc_n.p, c.d_lc_idx.p,
-                                   c.d_lc_s.p);
-  k_lcpo_main<<<nw, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_n.p, c.d_lc_idx.p, c.d_lc_s.p, c.d_lcpoP.p,
-                                   c.d_lcpoSig.p, c.d_sasa.p, facc_out, esurf_out, esurf_stride);
+                                   c.d_lc_s.p, c.d_lc_pos.p);
+  k_lcpo_main<<<nw, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_pos.p, c.d_lc_n.p, c.d_lc_idx.p, c.d_lc_s.p,
+                                   c.d_lcpoP.p, c.d_lcpoSig.p, c.d_sasa.p, facc_out, esurf_out, esurf_stride);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

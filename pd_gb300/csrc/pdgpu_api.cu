@@ -405,6 +405,7 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
     if (e == cudaSuccess) e = c.d_lc_s.alloc((size_t)c.nslots * kLcpoMax);
     if (e == cudaSuccess) e = c.d_sasa.alloc(N);
     if (e == cudaSuccess) e = c.d_lc_par.alloc(c.nslots);
+    if (e == cudaSuccess) e = c.d_lc_pos.alloc(c.nslots);
   }
   if (e == cudaSuccess) e = cudaMemset(c.d_status.p, 0, sizeof(unsigned));
   if (e != cudaSuccess) return bad(PDGPU_ERR_CUDA);

@@ -103,6 +103,7 @@ struct Context {
   DBuf<float> d_lc_s;               // [nslots*kLcpoMax] overlap s_ij
   DBuf<double> d_sasa;              // [natom]
   DBuf<float4> d_lc_par;            // [nslots] (radius, use, -, -)
+  DBuf<float4> d_lc_pos;            // [nslots] position from its system's first block centre (FP32)
 
   // bonded
   int nbond = 0, nangle = 0, ntors = 0, nimpr = 0;
