@@ -612,11 +612,15 @@ def run_adjoint(args):
     rng = np.random.default_rng(32)
     worst, within = 0.0, 0
     checks = []
+    left = 32
     for name in ("radius", "sqrt_well", "gb_radius", "charge"):
         g = th[name].grad.detach().cpu().numpy()
         x = th[name].detach()
         cand = np.flatnonzero(x.cpu().numpy() != 0)
-        for a in rng.choice(cand, 8, replace=False):
+        # 8 per-type parameters of each kind (fewer if the kind has fewer types), charges fill up to 32
+        take = min(left if name == "charge" else 8, len(cand))
+        left -= take
+        for a in rng.choice(cand, take, replace=False):
             h = 1e-4 * (1.0 if name == "charge" else abs(float(x[a])))
             tp = {k: v.detach().clone() for k, v in th.items()}
             tm = {k: v.detach().clone() for k, v in th.items()}
