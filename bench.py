@@ -318,7 +318,8 @@ def run_reference(args, key, wl, image):
     if rank != 0:
         return
     from oracle import pdoracle as O  # noqa: F401  (builds the C restatement if needed)
-    per_step = max(3.0, 120.0 / max(args.steps + args.warmup, 1))
+    # the whole arm (warm-up included) stays near two minutes of host time
+    per_step = max(0.25, 120.0 / max(args.steps + args.warmup, 1))
     res = [cpu_baseline(image, wl, key, budget_s=per_step) for _ in range(args.warmup + args.steps)]
     vals = [r["value"] for r in res[args.warmup:]]
     v = statistics.median(vals)
