@@ -160,8 +160,6 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
   float4 xj = j_in_i_frame(v, T, lane);
   float4 pj = v.par[T.bj * 32 + lane];
   float aj = born[T.bj * 32 + lane];
-  // per-lane factors of q_i: the pair terms below multiply them by q_j
-  const float pq_i = k.premul * xi.w, cin_i = k.econv_in * xi.w, cout_i = k.econv_out * xi.w;
 #pragma unroll 2
   for (int kk = 0; kk < 32; kk++) {
     const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
@@ -179,67 +177,65 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
         gb_pair_energy(k, v, atom_i, atom_j, r2_slots_fp64(v, si, sjk), excl, is14, evdw, eel, epol);
     }
     if ((FULL || r2 <= k.cut2) && pair) {
-      // g multiplies (xj - xi) in the force on i; every term below is already
-      // divided by r (2 dE/dr / r for the GB cross term, counted for i>j and j>i)
       const float invr = rsqrtf(r2);
-      const float ir2 = invr * invr;
+      const float r = r2 * invr;
+      const float qiqj = xi.w * xj.w;
       const float aiaj = ai * aj;
       const float u = -0.25f * __fdividef(r2, aiaj);
       bool gbon = u > k.thresh;
       if (fabsf(u - k.thresh) <= 2e-6f * fabsf(k.thresh))
         gbon = gb_on_fp64(v, si, T.bj * 32 + ((lane + kk) & 31), k.thresh_d);
-      float g = 0.f;
-      float elec = 0.f;
+      float g = 0.f;  // scalar multiplying (xj - xi) in the force on i
+      float elec = 0.f, delec = 0.f;
       const float s14 = is14 ? k.elec14 : 1.f;
-      float r = 0.f, S = 1.f, dS = 0.f;
-      bool sw_on = false;
-      if (!FULL) {  // FULL: inside the inner cutoff, no switch
-        r = r2 * invr;
-        sw_on = r >= k.inner;
-        if (sw_on) {
-          const float w = r - k.inner;
-          const float sw = 1.f - w * w * k.invw2;
-          dS = -4.f * k.invw2 * w * sw;
-          S = sw * sw;
-        }
+      const bool sw_on = !FULL && r >= k.inner;  // FULL: inside the inner cutoff
+      float S = 1.f, dS = 0.f;
+      if (sw_on) {
+        const float w = r - k.inner;
+        const float sw = 1.f - w * w * k.invw2;
+        dS = -4.f * k.invw2 * w * sw;
+        S = sw * sw;
       }
       if (gbon) {
         const float tg = __expf(u);
-        const float fgb = rsqrtf(fmaf(tg, aiaj, r2));
-        const float ep = pq_i * xj.w * fgb;
-        const float epl = ep * fgb * fgb;
-        float gg = -2.f * epl * (1.f - 0.25f * tg);
-        float dalpha = -epl * tg * (1.f - u);
+        const float fgb = rsqrtf(r2 + tg * aiaj);
+        const float l = fgb * fgb;
+        const float ep = k.premul * qiqj * fgb;
+        float dedr = -ep * (r - 0.25f * r * tg) * l;
+        float dalpha = -ep * tg * (1.f - u) * l;
+        if (!excl) {
+          elec = k.econv_in * s14 * qiqj * invr;
+          delec = -elec * invr;
+        }
         if (sw_on) {
-          gg = S * gg + 2.f * dS * ep * invr;
+          dedr = S * dedr + dS * ep;
           dalpha *= S;
         }
-        g += gg;
+        g += 2.f * dedr * invr;
         I.da += dalpha * aj;
         J.da += dalpha * ai;
-        if (!excl) elec = cin_i * s14 * xj.w * invr;
       } else if (!excl) {
-        elec = cout_i * s14 * xj.w * invr;
+        elec = k.econv_out * s14 * qiqj * invr;
+        delec = -elec * invr;
       }
       if (!excl) {
-        float gel = -elec * ir2;
-        if (sw_on) gel = S * gel + elec * dS * invr;
-        float glj = 0.f;
+        if (sw_on) delec = S * delec + elec * dS;
+        float dvdw = 0.f;
         if (FULL || r < k.vdwcut) {
-          const float R = pi.x + pj.x;
-          const float t2 = R * R * ir2;
-          const float B = t2 * t2 * t2;
+          const float t = (pi.x + pj.x) * invr;
+          float B = t * t;
+          B = B * B * B;
           const float A = B * B;
           const float eps = pi.y * pj.y * (is14 ? k.vdw14 : 1.f);
-          glj = -12.f * eps * ir2 * (A - B);
+          dvdw = -12.f * eps * invr * (A - B);
           if (!FULL && r > k.vdwinner) {
             const float Ev = eps * (A - 2.f * B);
             const float w = r - k.vdwinner;
             const float sw = 1.f - w * w * k.vdwinvw2;
-            glj = sw * sw * glj + Ev * (-4.f * k.vdwinvw2 * w * sw) * invr;
+            dvdw = sw * sw * dvdw + Ev * (-4.f * k.vdwinvw2 * w * sw);
           }
         }
-        g += glj + gel;
+        g += (dvdw + delec) * invr;
       }
       I.fx += g * dx; I.fy += g * dy; I.fz += g * dz;
       J.fx -= g * dx; J.fy -= g * dy; J.fz -= g * dz;
