@@ -18,6 +18,46 @@ struct NBAcc {
   float fx, fy, fz;
 };
 
+// Force part of the pair law in FP32 (same law as nb_pair): dE/dr divided by r.
+template <int ELEC>
+__device__ __forceinline__ float nb_force_f(const NBConst& k, float r2, float rsum, float eps, float qq) {
+  const float invr = rsqrtf(r2), ir2 = invr * invr;
+  const float r = r2 * invr;
+  float g = 0.f;
+  if (k.dovdw && r < k.vdwcut_f) {
+    const float t2 = rsum * rsum * ir2;
+    const float B = t2 * t2 * t2, A = B * B;
+    float gv = -12.f * eps * ir2 * (A - B);
+    if (r > k.vdwinner_f) {
+      const float u = r - k.vdwinner_f;
+      const float sw = 1.f - u * u * k.vdwinvw2_f;
+      gv = sw * sw * gv + eps * (A - 2.f * B) * (-4.f * k.vdwinvw2_f * u * sw) * invr;
+    }
+    g += gv;
+  }
+  if (ELEC == 1) {
+    g -= qq * invr * ir2;
+  } else if (ELEC == 3) {
+    const float Ee = qq * invr;
+    float ge = -Ee * ir2;
+    if (r > k.inner_f) {
+      const float u = r - k.inner_f;
+      const float sw = 1.f - u * u * k.invw2_f;
+      ge = sw * sw * ge + Ee * (-4.f * k.invw2_f * u * sw) * invr;
+    }
+    g += ge;
+  } else if (ELEC == 4) {
+    // Steinbach & Brooks force switch, nonbonded.cpp:798-819
+    if (r > k.inner_f) {
+      const float c2mr2 = k.cut2 - r2;
+      g -= qq * k.sA_f * ir2 * c2mr2 * c2mr2 * (k.fsw_k + 2.f * r2) * invr;
+    } else {
+      g -= qq * ir2 * invr;
+    }
+  }
+  return g;
+}
+
 template <int ELEC, bool MASKED, bool ENERGY>
 __device__ __forceinline__ void nb_tile(const DevView& v, const NBConst& k, const Tile& T, const SystemInfo& S,
                                         int lane, int si, int ai, const float4& xi, const float4& pi, float qi,
@@ -62,9 +102,8 @@ __device__ __forceinline__ void nb_tile(const DevView& v, const NBConst& k, cons
       const bool is14 = MASKED && ((m14 >> kk) & 1u);
       const float eps = pi.y * pj.y * (is14 ? k.vdw14 : 1.f);
       const float qq = qi * xj.w * (is14 ? k.elec14 : 1.f);
-      float fs, rd, evf = 0.f, eef = 0.f;
       if (r2d > 0.0 && !ENERGY) r2 = (float)r2d;
-      nb_pair<float, ELEC>(k, r2, pi.x + pj.x, eps, qq, evf, eef, fs, rd);
+      const float fs = nb_force_f<ELEC>(k, r2, pi.x + pj.x, eps, qq);
       if (ENERGY) {
         // energy of this pair in FP64 from FP64 positions and parameters
         const int aj = v.sorted_atom[T.bj * 32 + ((lane + kk) & 31)];

@@ -104,6 +104,14 @@ NBConst pdgpu::make_nb_const(const pdgpu_nb_params& p) {
   k.eshift = I < C ? 1.0 / I + (innerV - k.fsw_cutV) : 0.0;
   k.cut2_d = C2;
   k.inner2_d = I2;
+  k.vdwcut_f = (float)p.VdwCutoff;
+  k.vdwinner_f = (float)p.VdwInnerCutoff;
+  k.vdwinvw2_f = (float)k.vdwinvw2_d;
+  k.inner_f = (float)I;
+  k.invw2_f = (float)k.invw2_d;
+  k.inner2_f = (float)I2;
+  k.sA_f = (float)k.sA;
+  k.fsw_k = (float)(C2 - 3.0 * I2);
   k.elecmode = 1;
   if (p.EnergySwitch) k.elecmode = 3;
   if (p.ForceSwitch) k.elecmode = 4;

@@ -69,6 +69,8 @@ struct NBConst {
   float cut2, vdwcut2, vdw14, elec14, econv_diel;
   double cut2_dd, vdwcut_d, vdwinner_d, inner_d, vdwinvw2_d, invw2_d, econv_diel_d, vdw14_d, elec14_d;
   double sA, sB, sC, sD, sE, fsw_cutV, eshift, cut2_d, inner2_d;
+  // FP32 copies for the force pair law
+  float vdwcut_f, vdwinner_f, vdwinvw2_f, inner_f, invw2_f, inner2_f, sA_f, fsw_k;  // fsw_k = cut2 - 3 inner2
   int elecmode;            // 0 none, 1 plain, 3 energy switch, 4 force switch
   int dovdw;
 };
