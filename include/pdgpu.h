@@ -247,6 +247,17 @@ int pdgpu_remd_set_modes(pdgpu_ctx *ctx, const int *modes);
  * gradient minimisation steps are not run).  rescued (nsystems ints, may be
  * NULL) flags them, count gets their number. */
 int pdgpu_md_checkpoint(pdgpu_ctx *ctx);
+/* Trajectory frames without stalling the step stream (PD writes a frame every
+ * UpdateTra steps, md.cpp:277, through OutTra, fileio/tra.h:78-87): every
+ * `every` steps the positions of all systems (original order, Angstrom, natom*3
+ * doubles) are copied asynchronously on the context stream into slot
+ * frame % nslots of host_ring, which the caller owns (page-locked memory keeps
+ * the copy asynchronous; the ring must outlive the run).  Frames are complete
+ * once pdgpu_synchronize / pdgpu_md_run returns; a slot is overwritten after
+ * nslots further frames.  every = 0 switches it off.  pdgpu_md_trajectory_frames
+ * counts the frames queued since the last pdgpu_md_set_trajectory. */
+int pdgpu_md_set_trajectory(pdgpu_ctx *ctx, int every, double *host_ring, int nslots);
+long long pdgpu_md_trajectory_frames(pdgpu_ctx *ctx);
 int pdgpu_md_rescue(pdgpu_ctx *ctx, unsigned long long seed, int *rescued, int *count);
 /* Project autotuner (state restored afterwards): first the launch shape of the
  * tile kernels (CTAs per SM of their grid-stride grid), timed on force

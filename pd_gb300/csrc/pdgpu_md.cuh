@@ -35,6 +35,11 @@ struct MDState {
   DBuf<double> d_ckpt_pos;            // [natom*3] positions at the last checkpoint (crash rescue)
   DBuf<int> d_bad;                    // [nsys] systems flagged non-finite
   bool copy_modes = false;            // some rung copies structures (list and LCPO cache refreshed after)
+  // trajectory frames copied to a caller's host ring without a synchronisation
+  int traj_every = 0;
+  double* traj_ring = nullptr;
+  int traj_slots = 0;
+  long long traj_frames = 0;
   bool force_sasa = false;            // recompute LCPO at the next step
   std::map<int, cudaGraphExec_t> graphs;
   std::map<int, long long> graph_kernels;  // kernel nodes of each captured flavour

@@ -156,6 +156,12 @@ int md_enqueue_impl(Context& c, MDState& md, int nsteps, bool energy_on_last) {
     if (st != PDGPU_OK) return st;
     md.trajectory_started = true;
     md.step++;
+    if (md.traj_every > 0 && md.step % (unsigned long long)md.traj_every == 0) {
+      // a frame of every system's positions, queued behind the step on the context stream
+      double* dst = md.traj_ring + (size_t)(md.traj_frames % md.traj_slots) * 3 * (size_t)c.natom;
+      CK(cudaMemcpyAsync(dst, c.d_pos.p, 24 * (size_t)c.natom, cudaMemcpyDeviceToHost, c.stream));
+      md.traj_frames++;
+    }
   }
   return PDGPU_OK;
 }
@@ -358,6 +364,22 @@ int pdgpu_remd_set_modes(pdgpu_ctx* h, const int* modes) {
   CK(cudaStreamSynchronize(c.stream));
   c.md->copy_modes = copy;
   return PDGPU_OK;
+}
+
+int pdgpu_md_set_trajectory(pdgpu_ctx* h, int every, double* host_ring, int nslots) {
+  if (!h || every < 0 || (every > 0 && (!host_ring || nslots < 1))) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.md) return PDGPU_ERR_STATE;
+  c.md->traj_every = every;
+  c.md->traj_ring = every > 0 ? host_ring : nullptr;
+  c.md->traj_slots = every > 0 ? nslots : 0;
+  c.md->traj_frames = 0;
+  return PDGPU_OK;
+}
+
+long long pdgpu_md_trajectory_frames(pdgpu_ctx* h) {
+  if (!h || !h->c.md) return -1;
+  return h->c.md->traj_frames;
 }
 
 int pdgpu_md_checkpoint(pdgpu_ctx* h) {

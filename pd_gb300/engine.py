@@ -226,6 +226,26 @@ class DeviceContext:
         m = np.ascontiguousarray(np.broadcast_to(np.asarray(modes, np.int32), (self.nsystems,)))
         ffi.check(self.lib.pdgpu_remd_set_modes(self.h, _pi(m)), "pdgpu_remd_set_modes")
 
+    def md_set_trajectory(self, every, nslots=16):
+        """Frames every `every` steps into a page-locked ring of nslots frames (returned,
+        shape (nslots, natom, 3)); every = 0 switches it off."""
+        if every <= 0:
+            ffi.check(self.lib.pdgpu_md_set_trajectory(self.h, 0, None, 0), "pdgpu_md_set_trajectory")
+            self._traj_ring = None
+            return None
+        try:
+            import torch
+            ring = torch.zeros((nslots, self.natom, 3), dtype=torch.float64, pin_memory=True).numpy()
+        except Exception:       # no CUDA torch: pageable memory (the copy then waits for the step)
+            ring = np.zeros((nslots, self.natom, 3))
+        self._traj_ring = ring   # kept alive with the context
+        ffi.check(self.lib.pdgpu_md_set_trajectory(self.h, int(every), _pd(ring), int(nslots)),
+                  "pdgpu_md_set_trajectory")
+        return ring
+
+    def md_trajectory_frames(self):
+        return int(self.lib.pdgpu_md_trajectory_frames(self.h))
+
     def md_checkpoint(self):
         ffi.check(self.lib.pdgpu_md_checkpoint(self.h), "pdgpu_md_checkpoint")
 

@@ -113,6 +113,8 @@ SIGNATURES = {
     "pdgpu_md_autotune": ([ctypes.c_void_p, ctypes.c_int, _ip, _ip], ctypes.c_int),
     "pdgpu_remd_set_modes": ([ctypes.c_void_p, _ip], ctypes.c_int),
     "pdgpu_md_checkpoint": ([ctypes.c_void_p], ctypes.c_int),
+    "pdgpu_md_set_trajectory": ([ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int], ctypes.c_int),
+    "pdgpu_md_trajectory_frames": ([ctypes.c_void_p], ctypes.c_longlong),
     "pdgpu_md_rescue": ([ctypes.c_void_p, ctypes.c_ulonglong, _ip, _ip], ctypes.c_int),
     "pdgpu_set_launch_shape": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "pdgpu_get_launch_shape": ([ctypes.c_void_p, _ip], ctypes.c_int),

@@ -49,6 +49,8 @@ class MolecularDynamics:
         self.UpdateNList = 10
         self.Seed = 1
         self.UseGraph = True
+        self.UpdateTra = 0          # frame every UpdateTra steps (md.cpp:277); 0 = none
+        self.trajectory = None      # a writer with append(frames), e.g. trajectory.PDBTrajectory
         self._temp = np.array([300.0])
         self._setup_done = False
         self.Step = 0
@@ -83,7 +85,15 @@ class MolecularDynamics:
         """Run Steps (or `steps`) steps; positions, velocities and energies come back to the WorkSpace."""
         n = self.Steps if steps is None else steps
         ctx = self.setup() if not self._setup_done else self.wspace.context()
+        ring = None
+        if self.UpdateTra > 0 and self.trajectory is not None:
+            # every frame of this run fits the ring: no slot is reused before it is written out
+            ring = ctx.md_set_trajectory(self.UpdateTra, nslots=max(1, n // self.UpdateTra))
         ctx.md_run(n, energy_on_last=energies)
+        if ring is not None:
+            k = ctx.md_trajectory_frames()
+            self.trajectory.append(ring[:k])
+            ctx.md_set_trajectory(0)
         self.Step += n
         self.sync(ctx, energies)
         return n

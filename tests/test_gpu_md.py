@@ -272,3 +272,25 @@ def test_crash_rescue_restores_unstable_system(goldens):
     assert np.isclose(ke, 1.5 * n * 1.38065e-23 * 350.0, rtol=1e-9)
     ctx.md_run(10)                              # runs on from the rescued state
     assert np.all(np.isfinite(ctx.get_positions()))
+
+
+def test_trajectory_frames_without_host_sync(goldens, tmp_path):
+    """Frames copied every UpdateTra steps into the host ring equal the positions a
+    step-by-step run reaches, and the PDB writer stores them as models."""
+    from pd_gb300.trajectory import PDBTrajectory, read_pdb_models
+    d = goldens["peptide30"]
+    im, ctx = _four_copies(d, [300.0, 320.0])
+    ring = ctx.md_set_trajectory(5, nslots=4)
+    ctx.md_run(20)
+    assert ctx.md_trajectory_frames() == 4
+    assert np.array_equal(ring[3], ctx.get_positions())
+    assert not np.array_equal(ring[0], ring[3])
+    # the same trajectory run step by step from the same start reproduces frame 2 (step 15)
+    im2, ctx2 = _four_copies(d, [300.0, 320.0])
+    ctx2.md_run(15)
+    assert np.array_equal(ring[2], ctx2.get_positions())
+    path = str(tmp_path / "tra.pdb")
+    w = PDBTrajectory(path, im)
+    w.append(ring)
+    back = read_pdb_models(path)
+    assert back.shape == (4, im.natom, 3) and np.allclose(back, ring, atol=6e-4)
