@@ -156,6 +156,20 @@ int pdgpu_get_energies(pdgpu_ctx *ctx, pdgpu_energies *out);
 int pdgpu_get_born_radii(pdgpu_ctx *ctx, double *born);
 int pdgpu_get_sasa(pdgpu_ctx *ctx, double *sasa);
 
+/* ---- Monte Carlo energies (FF_NonBonded::calcEnergies, nonbonded.cpp:1154-1182)
+ * pdgpu_nb_energy_full evaluates the FF_NonBonded energies (vdw, elec, epot;
+ * other fields zero) of every system and keeps them with the current positions
+ * as the reference.  pdgpu_nb_energy_update (UsePartialRecalc,
+ * nonbonded.cpp:76-386) then returns the energies after the atoms whose
+ * positions differ from the reference moved: the reference minus every pair
+ * touching a moved atom at its reference position plus the same pairs now
+ * (FP64 pair energies, all pairs of the system inside Cutoff), and makes the
+ * current positions the reference.  nmoved (may be NULL) counts the moved
+ * atoms.  Call pdgpu_nb_energy_full again after a list-changing event, as PD
+ * does after a full list update. */
+int pdgpu_nb_energy_full(pdgpu_ctx *ctx, pdgpu_energies *out);
+int pdgpu_nb_energy_update(pdgpu_ctx *ctx, pdgpu_energies *out, int *nmoved);
+
 /* ---- parameter gradients (adjoint) ----------------------------------------
  * PD has no counterpart: its parameter derivatives are finite differences of
  * Forcefield::calcEnergies with setup() re-run after each edit

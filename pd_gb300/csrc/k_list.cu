@@ -8,7 +8,7 @@
 // exclusion / 1-4 bit mask.
 #include <cstdio>
 
-#include "pdgpu_context.cuh"
+#include "pdgpu_tile.cuh"
 
 namespace pdgpu {
 
@@ -311,23 +311,6 @@ __global__ void k_tile_write(DevView v, long long ncand, float R, float margin, 
   T.mask = -1;
   T.flags = fl;
   v.tiles[pos[t]] = T;
-}
-
-// bond order of an atom pair as PD's list stores it; 7 when not bonded
-__device__ __forceinline__ int pair_bondorder(const DevView& v, int a, int b) {
-  int lo = a < b ? a : b, hi = a < b ? b : a;
-  int d = hi - lo;
-  if (d == 0) return 0;
-  if (d <= kBandWidth) {
-    unsigned long long bit = 1ull << (d - 1);
-    if (v.band_excl[lo] & bit) return 2;  // 1-1/1-2/1-3: all treated alike (excluded)
-    if (v.band_14[lo] & bit) return 3;
-    return 7;
-  }
-  int best = 7;
-  for (int k = v.far_start[lo]; k < v.far_start[lo + 1]; k++)
-    if (v.far_idx[k] == hi && v.far_bo[k] < best) best = v.far_bo[k];
-  return best;
 }
 
 // exclusion masks in rotation order (bit k <-> j slot (lane+k)&31); one warp per tile

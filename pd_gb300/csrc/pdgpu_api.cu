@@ -536,6 +536,63 @@ static int param_grad_check(unsigned what) {
   return PDGPU_OK;
 }
 
+static int mc_alloc(Context& c) {
+  if (c.d_mc_ref.p) return PDGPU_OK;
+  const size_t N = c.natom;
+  if (c.d_mc_ref.alloc(3 * N) != cudaSuccess || c.d_mc_eref.alloc(2 * (size_t)c.nsys) != cudaSuccess ||
+      c.d_mc_moved.alloc(N) != cudaSuccess || c.d_mc_list.alloc(N) != cudaSuccess ||
+      c.d_mc_count.alloc(1) != cudaSuccess)
+    return PDGPU_ERR_CUDA;
+  return PDGPU_OK;
+}
+
+static void mc_energies(Context& c, const std::vector<long long>& e, pdgpu_energies* out) {
+  for (int s = 0; s < c.nsys; s++) {
+    pdgpu_energies o{};
+    o.vdw = (double)e[2 * s] / kEnergyScale * kKcalMolToJ;
+    o.elec = (double)e[2 * s + 1] / kEnergyScale * kKcalMolToJ;
+    o.epot = o.vdw + o.elec;
+    out[s] = o;
+  }
+}
+
+int pdgpu_nb_energy_full(pdgpu_ctx* h, pdgpu_energies* out) {
+  if (!h || !out) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.nb_set) return PDGPU_ERR_STATE;
+  CK(cudaSetDevice(c.device));
+  int st = mc_alloc(c);
+  if (st != PDGPU_OK) return st;
+  st = enqueue_compute(c, PDGPU_NB, true);
+  if (st != PDGPU_OK) return st;
+  st = launch_mc_reference(c);
+  if (st != PDGPU_OK) return st;
+  std::vector<long long> e(2 * (size_t)c.nsys);
+  CK(cudaMemcpyAsync(e.data(), c.d_mc_eref.p, sizeof(long long) * e.size(), cudaMemcpyDeviceToHost, c.stream));
+  st = read_status(c);
+  if (st != PDGPU_OK) return st;
+  c.mc_ready = true;
+  mc_energies(c, e, out);
+  return PDGPU_OK;
+}
+
+int pdgpu_nb_energy_update(pdgpu_ctx* h, pdgpu_energies* out, int* nmoved) {
+  if (!h || !out) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.nb_set || !c.mc_ready) return PDGPU_ERR_STATE;
+  CK(cudaSetDevice(c.device));
+  int st = launch_mc_update(c);
+  if (st != PDGPU_OK) return st;
+  std::vector<long long> e(2 * (size_t)c.nsys);
+  int n = 0;
+  CK(cudaMemcpyAsync(e.data(), c.d_mc_eref.p, sizeof(long long) * e.size(), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(&n, c.d_mc_count.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  if (nmoved) *nmoved = n;
+  mc_energies(c, e, out);
+  return PDGPU_OK;
+}
+
 int pdgpu_param_grad_device(pdgpu_ctx* h, unsigned what, const pdgpu_param_grads* g) {
   if (!h || !g) return PDGPU_ERR_ARG;
   Context& c = h->c;

@@ -181,6 +181,10 @@ constexpr int kNoAllocMaxSlots = 65536;
 constexpr int kNoAllocMaxDevices = 64;
 int launch_adjoint_static(Context& c, unsigned what, double* d_q, double* d_r, double* d_e, double* d_R, double* d_V,
                           double* d_T);
+// Monte Carlo partial NB energies: take the reference from the last energy
+// evaluation / update it by the pairs of the moved atoms
+int launch_mc_reference(Context& c);
+int launch_mc_update(Context& c);
 // static per-slot parameters refreshed from the per-atom arrays (after a parameter update)
 int launch_slot_params(Context& c);
 NBConst make_nb_const(const pdgpu_nb_params& p);

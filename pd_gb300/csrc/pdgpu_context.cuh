@@ -91,6 +91,12 @@ struct Context {
   DBuf<float> d_born_f;             // [nslots]
   DBuf<float> d_chain_f;            // [nslots] a^2/166 * dE/da * P4
   DBuf<double> d_born_d;            // [natom] original order
+  // Monte Carlo partial energy updates (allocated on first use)
+  DBuf<double> d_mc_ref;            // [natom*3] positions of the reference evaluation
+  DBuf<long long> d_mc_eref;        // [nsys*2] reference vdw, elec (fixed point, energy scale)
+  DBuf<unsigned char> d_mc_moved;   // [natom]
+  DBuf<int> d_mc_list, d_mc_count;  // [natom], [1]
+  bool mc_ready = false;
   // parameter gradients (allocated on first use)
   DBuf<long long> d_adj;            // [5*nslots] dE/dq, dE/dRmin, dE/dsqrt(eps), dE/dR_gb, dE/dVj
   DBuf<float> d_adj_w;              // [nslots] dE/dGpol

@@ -49,6 +49,23 @@ __device__ __forceinline__ void tile_masks(const DevView& v, const Tile& T, int 
   }
 }
 
+// bond order of an atom pair as PD's list stores it; 7 when not bonded
+__device__ __forceinline__ int pair_bondorder(const DevView& v, int a, int b) {
+  int lo = a < b ? a : b, hi = a < b ? b : a;
+  int d = hi - lo;
+  if (d == 0) return 0;
+  if (d <= kBandWidth) {
+    unsigned long long bit = 1ull << (d - 1);
+    if (v.band_excl[lo] & bit) return 2;  // 1-1/1-2/1-3: all treated alike (excluded)
+    if (v.band_14[lo] & bit) return 3;
+    return 7;
+  }
+  int best = 7;
+  for (int k = v.far_start[lo]; k < v.far_start[lo + 1]; k++)
+    if (v.far_idx[k] == hi && v.far_bo[k] < best) best = v.far_bo[k];
+  return best;
+}
+
 // Pair law in arithmetic type T (float for forces, double for energies).
 template <typename T, int ELEC>
 __device__ __forceinline__ void nb_pair(const NBConst& k, T r2, T rsum, T eps, T qq, T& ev, T& ee, T& dEdr_over_r,

@@ -102,6 +102,19 @@ class DeviceContext:
         ptrs = [ctypes.c_void_p(p or None) for p in (charge, radius, epsilon, gb_radius, gb_vj, gb_terms123)]
         ffi.check(self.lib.pdgpu_update_params_device(self.h, *ptrs), "pdgpu_update_params_device")
 
+    def nb_energy_full(self):
+        """FF_NonBonded energies of every system; they and the positions become the reference."""
+        E = (ffi.Energies * self.nsystems)()
+        ffi.check(self.lib.pdgpu_nb_energy_full(self.h, E), "pdgpu_nb_energy_full")
+        return [e.as_dict() for e in E]
+
+    def nb_energy_update(self):
+        """Energies after the atoms that moved since the reference (partial recalculation)."""
+        E = (ffi.Energies * self.nsystems)()
+        n = ctypes.c_int()
+        ffi.check(self.lib.pdgpu_nb_energy_update(self.h, E, ctypes.byref(n)), "pdgpu_nb_energy_update")
+        return [e.as_dict() for e in E], n.value
+
     def param_grad(self, what):
         """Energies of every system and dE/dp per atom (J per parameter unit) for the
         per-atom parameter arrays: dict charge, radius, epsilon, gb_radius, gb_vj, gb_terms123."""

@@ -87,6 +87,8 @@ SIGNATURES = {
     "pdgpu_set_list_params": ([ctypes.c_void_p, ctypes.POINTER(ListParams)], ctypes.c_int),
     "pdgpu_update_params": ([ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
     "pdgpu_update_params_device": ([ctypes.c_void_p] + [ctypes.c_void_p] * 6, ctypes.c_int),
+    "pdgpu_nb_energy_full": ([ctypes.c_void_p, ctypes.POINTER(Energies)], ctypes.c_int),
+    "pdgpu_nb_energy_update": ([ctypes.c_void_p, ctypes.POINTER(Energies), _ip], ctypes.c_int),
     "pdgpu_param_grad": ([ctypes.c_void_p, ctypes.c_uint, ctypes.POINTER(Energies), ctypes.POINTER(ParamGrads)],
                          ctypes.c_int),
     "pdgpu_param_grad_device": ([ctypes.c_void_p, ctypes.c_uint, ctypes.POINTER(ParamGrads)], ctypes.c_int),

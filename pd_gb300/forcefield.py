@@ -92,6 +92,7 @@ class FF_NonBonded_GPU(ForcefieldBase):
         self.DDDielectric = False
         self.ForceSwitch = True
         self.EnergySwitch = False
+        self.UsePartialRecalc = False   # calcEnergies after small moves (nonbonded.cpp:1154-1182)
         self.epot_vdw = 0.0
         self.epot_elec = 0.0
 
@@ -318,6 +319,25 @@ class Forcefield:
             ws.ene.epot = float("nan")
 
     def calcEnergies(self):
+        """Forcefield::calcEnergies.  When FF_NonBonded with UsePartialRecalc is the
+        only active component (PD's Monte Carlo set-up), energies after a move come
+        from the pairs of the moved atoms only (pdgpu_nb_energy_update); the first
+        call, and the first after a parameter or cutoff change, is a full one."""
+        act = [c for c in self.components if c.Active]
+        if len(act) == 1 and isinstance(act[0], FF_NonBonded_GPU) and act[0].UsePartialRecalc:
+            ws = self.wspace
+            ctx = self._prepare()
+            ctx.set_positions(ws.cur.p)
+            key = ws._ctx_params
+            if getattr(self, "_mc_key", None) != key:
+                energies = ctx.nb_energy_full()
+                self._mc_key = key
+            else:
+                energies, _ = ctx.nb_energy_update()
+            ws.zeroForces()
+            ws.per_system_energies = energies
+            act[0].distribute({k: sum(e[k] for e in energies) for k in energies[0]})
+            return
         self.calcForces()
 
     def printEnergySummary(self):
