@@ -1,5 +1,10 @@
 """Monte Carlo energies: FF_NonBonded partial recalculation after small moves
-(nonbonded.cpp:76-386, 1154-1182) against full evaluations and the oracle."""
+(nonbonded.cpp:76-386, 1154-1182) against full evaluations and the oracle.
+
+Update vs full evaluation: 1e-7 relative (both are FP64 pair sums entered into
+2^-24 kcal/mol fixed point, the full one per tile, so they differ by that
+rounding; water's electrostatics cancel about 5000-fold).  Against the oracle:
+the 1e-6 energy bar of the parity tests."""
 import numpy as np
 import pytest
 
@@ -33,7 +38,7 @@ def test_partial_update_matches_full_evaluation(goldens, name, tag):
         assert n == len(moved)
         full = ctx.compute(ffi.NB)[0]
         for k in ("vdw", "elec"):
-            assert rel_err(e1[0][k], full[k]) <= 1e-9, (k, e1[0][k], full[k])
+            assert rel_err(e1[0][k], full[k]) <= 1e-7, (k, e1[0][k], full[k])
         ref, _ = O.nonbonded(O.OracleSystem(pos, d["charge"], d["radius"], d["epsilon"], d["excl"], tuple(d["box"])),
                              nb_params(d, tag))
         assert rel_err(e1[0]["epot"], ref[0]) <= 1e-6
@@ -61,4 +66,4 @@ def test_forcefield_calc_energies_uses_partial_recalc(goldens):
     e1 = ws.ene.epot
     nb.UsePartialRecalc = False
     ff.calcEnergies()                    # full evaluation of the same positions
-    assert e1 != e0 and rel_err(e1, ws.ene.epot) <= 1e-9
+    assert e1 != e0 and rel_err(e1, ws.ene.epot) <= 1e-7
