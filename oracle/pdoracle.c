@@ -495,7 +495,11 @@ int pdo_gb_born_radii(const pdo_system *s, const pdo_gb_params *p, const double 
     return 0;
 }
 
-/* gbff.cpp:1466-1835 (FastMode); radii from calcBornRadii_PairwiseApprox first (gbff.cpp:185-197) */
+/* gbff.cpp:1466-1835 (FastMode); radii from calcBornRadii_PairwiseApprox first (gbff.cpp:185-197).
+ * FastMode = 0: calcBornForces (gbff.cpp:1189-1437), the GB part alone: every pair
+ * within Cutoff (bonded ones too), the GB term above ExpApproxThreshold and
+ * premul q_i q_j / r below it; PD's calcBornEnergy (gbff.cpp:537-596) is that
+ * energy with no threshold (ExpApproxThreshold = -inf). */
 int pdo_gb_forces(const pdo_system *s, const pdo_gb_params *p, const double *gbR, const double *vj,
                   const double *terms123, int nthreads, pdo_energies *e, double *force, double *born_out) {
     int n = s->natom;
@@ -548,6 +552,42 @@ int pdo_gb_forces(const pdo_system *s, const pdo_gb_params *p, const double *gbR
             double uGB = -srij * 0.25 / aiaj;
             double s14 = typej == 3 ? p->Elec14Scaling : 1.0;
             double elec_pot = 0, elec_f = 0;
+            if (!p->FastMode) {
+                double epol, dedr;
+                if (uGB > p->ExpApproxThreshold) {
+                    double tGB = exp(uGB);
+                    double lGB = srij + tGB * aiaj;
+                    epol = premul * qiqj / sqrt(lGB);
+                    dedr = -epol * (dist - 0.25 * dist * tGB) / lGB;
+                    double dedalpha = -epol * tGB * (1.0 + 0.25 * srij / aiaj) / lGB;
+                    if (dist >= p->InnerCutoff) {
+                        double S = 1.0 - SQR(invSwidth * (dist - p->InnerCutoff));
+                        double dSdd = -4.0 * SQR(invSwidth) * (dist - p->InnerCutoff) * S;
+                        S = S * S;
+                        dedr = S * dedr + dSdd * epol;
+                        dedalpha *= S;
+                        epol *= S;
+                    }
+                    dedai += dedalpha * aj;
+                    A[j] += dedalpha * ai;
+                } else {
+                    epol = premul * qiqj * invd;
+                    dedr = -epol * invd;
+                    if (dist >= p->InnerCutoff) {
+                        double S = 1.0 - SQR(invSwidth * (dist - p->InnerCutoff));
+                        double dSdd = -4.0 * SQR(invSwidth) * (dist - p->InnerCutoff) * S;
+                        S = S * S;
+                        dedr = S * dedr + dSdd * epol;
+                        epol *= S;
+                    }
+                }
+                dedr *= 2 * invd;
+                D[3 * i] += dedr * dx; D[3 * i + 1] += dedr * dy; D[3 * i + 2] += dedr * dz;
+                D[3 * j] -= dedr * dx; D[3 * j + 1] -= dedr * dy; D[3 * j + 2] -= dedr * dz;
+                E[2] += 2 * epol;
+                E[3] += 2 * epol;
+                continue;
+            }
             if (uGB > p->ExpApproxThreshold) {
                 double tGB = exp(uGB);
                 double mGB = tGB * aiaj;

@@ -60,6 +60,8 @@ typedef struct {
     double GbsaStillCutoff, ExpApproxThreshold, DielectricOffset, BornRadiusOffset;
     double P1, P2, P3, P4, P5;
     double ListCutoff;
+    int FastMode;   /* 1: calcForcesIncludingVacuo (GB + LJ + Coulomb); 0: calcBornForces (GB only,
+                       gbff.cpp:1189-1437; the vacuum part is FF_NonBonded's, pdo_nonbonded) */
 } pdo_gb_params;
 
 typedef struct {

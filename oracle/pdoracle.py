@@ -34,7 +34,7 @@ class GBParams(ctypes.Structure):
     _fields_ = [(k, ctypes.c_double) for k in (
         "Cutoff", "InnerCutoff", "VdwCutoff", "VdwInnerCutoff", "Vdw14Scaling", "Elec14Scaling",
         "DielectricSolute", "DielectricSolvent", "GbsaStillCutoff", "ExpApproxThreshold", "DielectricOffset",
-        "BornRadiusOffset", "P1", "P2", "P3", "P4", "P5", "ListCutoff")]
+        "BornRadiusOffset", "P1", "P2", "P3", "P4", "P5", "ListCutoff")] + [("FastMode", ctypes.c_int)]
 
 
 class NList(ctypes.Structure):
@@ -153,7 +153,7 @@ def gb_params(**kw):
     d = dict(Cutoff=12.0, InnerCutoff=9.0, VdwCutoff=None, VdwInnerCutoff=None, Vdw14Scaling=0.5,
              Elec14Scaling=0.83333, DielectricSolute=1.0, DielectricSolvent=80.0, GbsaStillCutoff=10.0,
              ExpApproxThreshold=-4.0, DielectricOffset=-0.09, BornRadiusOffset=0.0, P1=0.073, P2=0.921,
-             P3=6.211, P4=15.236, P5=1.254, ListCutoff=None)
+             P3=6.211, P4=15.236, P5=1.254, ListCutoff=None, FastMode=1)
     d.update(kw)
     if d["VdwCutoff"] is None:
         d["VdwCutoff"] = d["Cutoff"]

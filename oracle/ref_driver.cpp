@@ -653,6 +653,27 @@ int main(int argc, char **argv) {
             born[i] = gb.GB_atom_param[i].bornradius;
         }
         put_f64("gb_radius", R); put_f64("gb_vj", vj); put_f64("gb_terms123", t123); put_f64("gb_born", born);
+        // FastMode = false: FF_NonBonded::calcForces + calcBornForces (gbff.cpp:185-197, 1189-1437)
+        gb.FastMode = false;
+        {
+            Forcefield ff2(ws);
+            ff2.add(gb);
+            evaluate(ff2, ws);
+            export_result(ws, "gbslow");
+        }
+        // calcEnergies (gbff.cpp:178-183): Born radii, FF_NonBonded::calcEnergies, calcBornEnergy
+        {
+            Forcefield ff3(ws);
+            ff3.add(gb);
+            ff3.ensuresetup(ws);
+            ws.nlist().calcNewList();
+            ff3.calcEnergies();
+            const Hamiltonian &e = ws.ene;
+            double ene[8] = {e.epot, e.epot_vdw, e.epot_elec, e.epot_pol, e.epot_pol_self, e.epot_pol_cross,
+                             e.epot_surf, e.InternalVirial};
+            put_f64("gbene_ene", std::vector<double>(ene, ene + 8));
+        }
+        gb.FastMode = true;
     }
     if (want_sasa) {
         sasa.GlobalASP = optd("asp", 0.005);

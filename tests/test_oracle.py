@@ -98,3 +98,24 @@ def test_stored_list_matches_direct_scan(goldens):
     L = O.StoredList(s, list_cutoff(d), 2)
     e2, f2 = O.nonbonded_list(s, L, p, 2)
     assert np.allclose(e1, e2, rtol=1e-11) and rel_rms(f2, f1) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["peptide30", "peptide30_ap", "peptide120"])
+def test_gb_slow_mode_and_calc_energies_match_pd(goldens, name):
+    """FastMode = false (FF_NonBonded::calcForces + calcBornForces, gbff.cpp:185-197,
+    1189-1437) and calcEnergies (calcBornEnergy, no ExpApproxThreshold,
+    gbff.cpp:178-183, 537-596) against PD's own outputs."""
+    d = goldens[name]
+    s = oracle_system(d)
+    p = gb_params(d)
+    p.FastMode = 0
+    e, f, _ = O.gb_forces(s, p, d["gb_radius"], d["gb_vj"], d["gb_terms123"])
+    en, fn = O.nonbonded(s, nb_params(d, "gb"))     # the GB object's own FF_NonBonded settings
+    ref = d["gbslow_ene"]
+    assert abs(e[0] + en[0] - ref[0]) <= 1e-12 * abs(ref[0])
+    assert abs(en[1] - ref[1]) <= 1e-12 * abs(ref[1]) and abs(en[2] - ref[2]) <= 1e-12 * abs(ref[2])
+    rf = d["gbslow_f"]
+    assert np.sqrt(((f + fn - rf) ** 2).sum(1).mean() / (rf ** 2).sum(1).mean()) <= 1e-12
+    p.ExpApproxThreshold = -1e300
+    e2, _, _ = O.gb_forces(s, p, d["gb_radius"], d["gb_vj"], d["gb_terms123"])
+    assert abs(e2[0] + en[0] - d["gbene_ene"][0]) <= 1e-12 * abs(d["gbene_ene"][0])
