@@ -42,6 +42,11 @@ extern "C" {
 #define PDGPU_SA 4u      /* FF_SASA_LCPO                                        */
 #define PDGPU_BONDED 8u  /* FF_Bonded: bonds, angles, torsions, impropers       */
 #define PDGPU_ENERGY 0x100u /* pdgpu_compute_device: also form the energies (in FP64) */
+/* with PDGPU_GB: the energies as FF_GeneralizedBorn_Still::calcEnergies forms them
+ * (gbff.cpp:178-183: Born radii, FF_NonBonded::calcEnergies with the GB object's
+ * own settings, calcBornEnergy without ExpApproxThreshold, gbff.cpp:537-596);
+ * forces, if asked for, are those of that energy */
+#define PDGPU_PD_ENERGIES 0x200u
 
 /* Per-system energies in J per molecule; the fields mirror PD's Hamiltonian
  * (src/mmlib/workspace/hamiltonian.h:43-66). */
@@ -113,6 +118,16 @@ const char *pdgpu_error_string(int status);
 int pdgpu_set_nb_params(pdgpu_ctx *ctx, const pdgpu_nb_params *p);
 int pdgpu_set_gb_params(pdgpu_ctx *ctx, const pdgpu_gb_params *p);
 int pdgpu_set_list_params(pdgpu_ctx *ctx, const pdgpu_list_params *p);
+/* FF_GeneralizedBorn_Still::FastMode (gbff.cpp:37, 185-197).  1 (PD's default):
+ * calcForcesIncludingVacuo, GB fused with LJ + Coulomb.  0: FF_NonBonded::
+ * calcForces with the GB object's own settings (`vacuum`) plus calcBornForces
+ * (gbff.cpp:1189-1437: the GB term of every pair within Cutoff, bonded pairs
+ * too, premul q q / r below ExpApproxThreshold).  vacuum may be NULL: the GB
+ * cutoffs and 1-4 scalings with Dielectric 1 and the energy switch, PD's
+ * defaults for the GB object; it also serves PDGPU_PD_ENERGIES.  Parameter
+ * gradients need FastMode on.  Set it before pdgpu_md_setup (PDGPU_ERR_STATE
+ * after it: captured step graphs hold the launch sequence). */
+int pdgpu_set_gb_mode(pdgpu_ctx *ctx, int fast_mode, const pdgpu_nb_params *vacuum);
 /* Per-atom charges / LJ radius / epsilon (PD's sqrt(J) storage) / GB radius,
  * Vj, terms123 (all optional, NULL keeps) — the parameter update after FF
  * re-setup.  The list is kept; the per-slot copies are refreshed. */

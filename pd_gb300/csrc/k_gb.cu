@@ -110,6 +110,10 @@ __device__ __noinline__ void gb_pair_energy(const GBConst& k, const DevView& v, 
     S = sw * sw;
   }
   double elec = 0.0;
+  if (!k.fast) {  // calcBornForces / calcBornEnergy: the GB part only, every pair
+    epol += 2.0 * S * k.premul_d * qiqj * (u > k.thresh_d ? 1.0 / sqrt(r2 + exp(u) * aiaj) : invr);
+    return;
+  }
   if (u > k.thresh_d) {
     double t = exp(u);
     double ep = k.premul_d * qiqj / sqrt(r2 + t * aiaj);
@@ -152,7 +156,7 @@ struct PairAcc {
   float fx, fy, fz, da;
 };
 
-template <bool MASKED, bool ENERGY, bool FULL>
+template <bool MASKED, bool ENERGY, bool FULL, bool FAST = true>
 __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k, const Tile& T, int lane, int si,
                                              int atom_i, const float4& xi, const float4& pi, float ai, unsigned ex,
                                              unsigned m14, unsigned dmask, const float* born, PairAcc& I, PairAcc& J,
@@ -203,7 +207,7 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
         const float ep = k.premul * qiqj * fgb;
         float dedr = -ep * (r - 0.25f * r * tg) * l;
         float dalpha = -ep * tg * (1.f - u) * l;
-        if (!excl) {
+        if (FAST && !excl) {
           elec = k.econv_in * s14 * qiqj * invr;
           delec = -elec * invr;
         }
@@ -214,11 +218,17 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
         g += 2.f * dedr * invr;
         I.da += dalpha * aj;
         J.da += dalpha * ai;
-      } else if (!excl) {
+      } else if (FAST && !excl) {
         elec = k.econv_out * s14 * qiqj * invr;
         delec = -elec * invr;
+      } else if (!FAST) {
+        // calcBornForces below the threshold (gbff.cpp:1308-1325): premul q_i q_j / r
+        const float ep = k.premul * qiqj * invr;
+        float dedr = -ep * invr;
+        if (sw_on) dedr = S * dedr + dS * ep;
+        g += 2.f * dedr * invr;
       }
-      if (!excl) {
+      if (FAST && !excl) {
         if (sw_on) delec = S * delec + elec * dS;
         float dvdw = 0.f;
         if (FULL || r < k.vdwcut) {
@@ -341,6 +351,39 @@ __global__ void __launch_bounds__(256, ENERGY ? 1 : 4) k_gb_pair(DevView v, GBCo
   }
 }
 
+// FastMode off (calcBornForces, gbff.cpp:1189-1340): the GB term of every pair
+// within Cutoff, premul q_i q_j / r below the threshold; LJ and Coulomb come from
+// the NB kernel with the GB object's own FF_NonBonded settings.  One masked body
+// serves every tile: this mode exists for parity with PD, not for speed.
+template <bool ENERGY>
+__global__ void __launch_bounds__(256) k_gb_pair_born_only(DevView v, GBConst k, const float* born,
+                                                           long long* deda) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int nt = *v.ntiles;
+  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
+    const Tile T = v.tiles[t];
+    const int si = T.bi * 32 + lane;
+    const float4 xi = v.xq[si], pi = v.par[si];
+    const float ai = born[si];
+    const int atom_i = ENERGY ? v.sorted_atom[si] : -1;
+    unsigned ex, m14;
+    tile_masks(v, T, lane, ex, m14);
+    const unsigned dmask = (T.flags & 2) ? diag_exclusion(lane) : 0u;
+    PairAcc I = {0.f, 0.f, 0.f, 0.f}, J = {0.f, 0.f, 0.f, 0.f};
+    double evdw = 0.0, eel = 0.0, epol = 0.0;
+    gb_pair_tile<true, ENERGY, false, false>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J,
+                                             evdw, eel, epol);
+    flush_pair(v, deda, si, I);
+    flush_pair(v, deda, T.bj * 32 + lane, J);
+    if (ENERGY) {
+      EFix EF = {0, 0, 0};
+      efix_in(EF, evdw, eel, epol);
+      flush_gb_energy(v, lane, T.bi, EF);
+    }
+  }
+}
+
 // self term, total dE/da and the chain-rule prefactor a^2/166 * dE/da * P4
 __global__ void k_gb_self(DevView v, const double* charge, GBConst k, double premul, const long long* deda,
                           const double* born_d, float* chain) {
@@ -452,8 +495,14 @@ int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset
   cudaMemsetAsync(c.d_deda.p, 0, sizeof(long long) * c.nslots, st);
   k_gb_born<<<g, 256, 0, st>>>(v, k, c.d_gpol.p);
   k_gb_radii<<<nb, 256, 0, st>>>(v, c.d_gbT.p, c.d_gpol.p, halfeconv, born_offset, c.d_born_f.p, c.d_born_d.p);
-  if (energy) k_gb_pair<true><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
-  else k_gb_pair<false><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
+  if (!k.fast) {
+    if (energy) k_gb_pair_born_only<true><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
+    else k_gb_pair_born_only<false><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
+  } else if (energy) {
+    k_gb_pair<true><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
+  } else {
+    k_gb_pair<false><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
+  }
   k_gb_self<<<nb, 256, 0, st>>>(v, c.d_charge.p, k, premul, c.d_deda.p, c.d_born_d.p, c.d_chain_f.p);
   k_gb_chain<<<g, 256, 0, st>>>(v, k, c.d_chain_f.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;

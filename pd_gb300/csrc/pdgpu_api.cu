@@ -41,6 +41,25 @@ cudaError_t upload(DBuf<T>& b, const T* h, size_t n) {
   return cudaMemcpy(b.p, h, n * sizeof(T), cudaMemcpyHostToDevice);
 }
 
+// The GB object's FF_NonBonded settings: as set, else PD's defaults for the GB
+// object (its cutoffs and 1-4 scalings, Dielectric 1, energy switch).
+pdgpu_nb_params gb_vacuum_params(const Context& c) {
+  if (c.gb_vac_set) return c.gb_vac;
+  pdgpu_nb_params p{};
+  p.Cutoff = c.gb.Cutoff;
+  p.InnerCutoff = c.gb.InnerCutoff;
+  p.VdwCutoff = c.gb.VdwCutoff;
+  p.VdwInnerCutoff = c.gb.VdwInnerCutoff;
+  p.Vdw14Scaling = c.gb.Vdw14Scaling;
+  p.Elec14Scaling = c.gb.Elec14Scaling;
+  p.Dielectric = 1.0;
+  p.EnergySwitch = 1;
+  p.ForceSwitch = 0;
+  p.DoVdw = 1;
+  p.DoElec = 1;
+  return p;
+}
+
 double list_radius(const Context& c) {
   double r = 0;
   if (c.nb_set) r = std::max(r, std::max(c.nb.Cutoff, c.nb.VdwCutoff));
@@ -155,6 +174,7 @@ GBConst pdgpu::make_gb_const(const pdgpu_gb_params& p, double listR) {
   k.vdw14_d = p.Vdw14Scaling;
   k.elec14_d = p.Elec14Scaling;
   k.thresh_d = p.ExpApproxThreshold;
+  k.fast = 1;
   return k;
 }
 
@@ -459,6 +479,18 @@ int pdgpu_set_gb_params(pdgpu_ctx* h, const pdgpu_gb_params* p) {
   return PDGPU_OK;
 }
 
+int pdgpu_set_gb_mode(pdgpu_ctx* h, int fast_mode, const pdgpu_nb_params* vacuum) {
+  if (!h || (fast_mode != 0 && fast_mode != 1)) return PDGPU_ERR_ARG;
+  if (vacuum && (vacuum->Cutoff <= 0 || vacuum->InnerCutoff > vacuum->Cutoff || vacuum->Dielectric == 0))
+    return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (c.md) return PDGPU_ERR_STATE;  // captured step graphs hold the launch sequence
+  c.gb_fast = fast_mode != 0;
+  c.gb_vac_set = vacuum != nullptr;
+  if (vacuum) c.gb_vac = *vacuum;
+  return PDGPU_OK;
+}
+
 int pdgpu_set_list_params(pdgpu_ctx* h, const pdgpu_list_params* p) {
   if (!h || !p || p->Padding < 0) return PDGPU_ERR_ARG;
   h->c.lp = *p;
@@ -529,7 +561,9 @@ int pdgpu_update_params_device(pdgpu_ctx* h, const double* d_charge, const doubl
   return PDGPU_OK;
 }
 
-static int param_grad_check(unsigned what) {
+static int param_grad_check(const Context& c, unsigned what) {
+  if (what & PDGPU_PD_ENERGIES) return PDGPU_ERR_ARG;
+  if ((what & PDGPU_GB) && !c.gb_fast) return PDGPU_ERR_UNSUPPORTED;  // gradients of FastMode's energy
   const unsigned pair = what & (PDGPU_NB | PDGPU_GB);
   if (pair != PDGPU_NB && pair != PDGPU_GB) return PDGPU_ERR_ARG;
   if (what & ~(PDGPU_NB | PDGPU_GB | PDGPU_SA | PDGPU_BONDED | PDGPU_ENERGY)) return PDGPU_ERR_ARG;
@@ -596,7 +630,7 @@ int pdgpu_nb_energy_update(pdgpu_ctx* h, pdgpu_energies* out, int* nmoved) {
 int pdgpu_param_grad_device(pdgpu_ctx* h, unsigned what, const pdgpu_param_grads* g) {
   if (!h || !g) return PDGPU_ERR_ARG;
   Context& c = h->c;
-  int st = param_grad_check(what);
+  int st = param_grad_check(c, what);
   if (st != PDGPU_OK) return st;
   CK(cudaSetDevice(c.device));
   st = enqueue_compute(c, what & ~PDGPU_ENERGY, true);
@@ -607,7 +641,7 @@ int pdgpu_param_grad_device(pdgpu_ctx* h, unsigned what, const pdgpu_param_grads
 int pdgpu_param_grad_device_noalloc(pdgpu_ctx* h, unsigned what, const pdgpu_param_grads* g) {
   if (!h || !g) return PDGPU_ERR_ARG;
   Context& c = h->c;
-  int st = param_grad_check(what);
+  int st = param_grad_check(c, what);
   if (st != PDGPU_OK) return st;
   if (c.nslots > kNoAllocMaxSlots) return PDGPU_ERR_CAPACITY;
   CK(cudaSetDevice(c.device));
@@ -619,7 +653,7 @@ int pdgpu_param_grad_device_noalloc(pdgpu_ctx* h, unsigned what, const pdgpu_par
 int pdgpu_param_grad(pdgpu_ctx* h, unsigned what, pdgpu_energies* out, const pdgpu_param_grads* g) {
   if (!h || !g) return PDGPU_ERR_ARG;
   Context& c = h->c;
-  int st = param_grad_check(what);
+  int st = param_grad_check(c, what);
   if (st != PDGPU_OK) return st;
   CK(cudaSetDevice(c.device));
   const size_t N = c.natom;
@@ -714,9 +748,21 @@ int pdgpu::enqueue_forces(Context& c, unsigned what, bool energy, bool rebuild, 
   if (what & PDGPU_NB) st = launch_nb(c, make_nb_const(c.nb), energy);
   if (st == PDGPU_OK && (what & PDGPU_GB)) {
     GBConst k = make_gb_const(c.gb, c.list_radius_built);
+    // FastMode off, or PD's calcEnergies (gbff.cpp:178-183: calcBornEnergy, no
+    // ExpApproxThreshold): the GB part alone plus the vacuum part from the GB
+    // object's own FF_NonBonded settings
+    const bool pd_energies = (what & PDGPU_PD_ENERGIES) != 0;
+    if (!c.gb_fast || pd_energies) {
+      k.fast = 0;
+      if (pd_energies) {
+        k.thresh = -1e30f;
+        k.thresh_d = -1e300;
+      }
+      st = launch_nb(c, make_nb_const(gb_vacuum_params(c)), energy);
+    }
     double ec = econv_kcal();
     double premul = -0.5 * ec * (1.0 / c.gb.DielectricSolute - 1.0 / c.gb.DielectricSolvent);
-    st = launch_gb(c, k, 0.5 * ec, c.gb.BornRadiusOffset, premul, energy);
+    if (st == PDGPU_OK) st = launch_gb(c, k, 0.5 * ec, c.gb.BornRadiusOffset, premul, energy);
   }
   if (st == PDGPU_OK && (what & PDGPU_SA) && run_lcpo) st = launch_lcpo(c, lcpo_f, lcpo_e, lcpo_e_stride);
   if (st == PDGPU_OK && (what & PDGPU_BONDED)) st = launch_bonded(c, energy);

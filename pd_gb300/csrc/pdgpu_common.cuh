@@ -85,6 +85,9 @@ struct GBConst {
   // FP64 copies for the energy arithmetic
   double cut2_d, inner_d, invw2_d, vdwcut_d, vdwinner_d, vdwinvw2_d, still2_d;
   double econv_in_d, econv_out_d, premul_d, vdw14_d, elec14_d, thresh_d;
+  // 1: FastMode (GB fused with LJ + Coulomb, εout Coulomb below the threshold);
+  // 0: calcBornForces (GB term alone for every pair, premul q q / r below it)
+  int fast;
 };
 
 // Device-side view of a context, passed by value to kernels.

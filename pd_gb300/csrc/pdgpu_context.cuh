@@ -41,6 +41,9 @@ struct Context {
   pdgpu_gb_params gb{};
   pdgpu_list_params lp{};
   bool nb_set = false, gb_set = false;
+  bool gb_fast = true;             // FF_GeneralizedBorn_Still::FastMode
+  pdgpu_nb_params gb_vac{};        // the GB object's own FF_NonBonded settings (FastMode off, calcEnergies)
+  bool gb_vac_set = false;
   float list_radius_built = 0.f;
   float full_radius_built = 0.f;   // tiles flagged full: max distance + full_margin() below this
   // displacement margin of full tiles: every atom stays within half of it of its

@@ -88,6 +88,12 @@ class DeviceContext:
         p = ffi.GBParams(**kw)
         ffi.check(self.lib.pdgpu_set_gb_params(self.h, ctypes.byref(p)), "pdgpu_set_gb_params")
 
+    def set_gb_mode(self, fast_mode, **vacuum):
+        """FastMode of the GB component; vacuum: the GB object's FF_NonBonded settings (PD names)."""
+        p = ffi.NBParams(**vacuum) if vacuum else None
+        ffi.check(self.lib.pdgpu_set_gb_mode(self.h, int(bool(fast_mode)), ctypes.byref(p) if p else None),
+                  "pdgpu_set_gb_mode")
+
     def set_list(self, padding, check_skin=True):
         p = ffi.ListParams(float(padding), int(check_skin))
         ffi.check(self.lib.pdgpu_set_list_params(self.h, ctypes.byref(p)), "pdgpu_set_list_params")

@@ -19,7 +19,7 @@ ERRORS = {
     -10: "larger than the static scratch of the allocation-free entry point",
 }
 ERR_CAPACITY = -10
-NB, GB, SA, BONDED, ENERGY = 1, 2, 4, 8, 0x100
+NB, GB, SA, BONDED, ENERGY, PD_ENERGIES = 1, 2, 4, 8, 0x100, 0x200
 
 
 class PDGPUError(RuntimeError):
@@ -85,6 +85,7 @@ SIGNATURES = {
     "pdgpu_set_nb_params": ([ctypes.c_void_p, ctypes.POINTER(NBParams)], ctypes.c_int),
     "pdgpu_set_gb_params": ([ctypes.c_void_p, ctypes.POINTER(GBParams)], ctypes.c_int),
     "pdgpu_set_list_params": ([ctypes.c_void_p, ctypes.POINTER(ListParams)], ctypes.c_int),
+    "pdgpu_set_gb_mode": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(NBParams)], ctypes.c_int),
     "pdgpu_update_params": ([ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
     "pdgpu_update_params_device": ([ctypes.c_void_p] + [ctypes.c_void_p] * 6, ctypes.c_int),
     "pdgpu_nb_energy_full": ([ctypes.c_void_p, ctypes.POINTER(Energies)], ctypes.c_int),

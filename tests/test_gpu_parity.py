@@ -180,3 +180,38 @@ def test_forcefield_mirror_matches_pd(goldens):
     assert rel_rms(ws.cur.f, d["gb_f"] + d["sasa_f"]) <= F_TOL
     assert rel_err(ws.ene.epot_pol, ref_energy(d, "gb", "pol")) <= E_TOL
     assert rel_err(ws.ene.epot_surf, ref_energy(d, "sasa", "surf")) <= E_TOL
+
+
+@pytest.mark.parametrize("name", ["peptide30", "peptide30_ap", "peptide120"])
+def test_gb_fastmode_off_matches_pd(goldens, name):
+    """FastMode = false: FF_NonBonded::calcForces with the GB object's own settings
+    plus calcBornForces (gbff.cpp:185-197, 1189-1437), against PD."""
+    from pd_gb300 import ffi
+    d = goldens[name]
+    ctx = make_ctx(d)
+    ctx.set_gb(**gb_kwargs(d))
+    ctx.set_gb_mode(0, **nb_kwargs(d, "gb"))
+    f = np.zeros((len(d["pos"]), 3))
+    e = ctx.compute(ffi.GB, f)[0]
+    ref = d["gbslow_ene"]
+    assert rel_err(e["epot"], ref[0]) <= E_TOL and rel_err(e["vdw"], ref[1]) <= E_TOL
+    assert rel_err(e["elec"], ref[2]) <= E_TOL
+    assert rel_err(e["pol"], ref[0] - ref[1] - ref[2]) <= E_TOL     # PD keeps it in the component
+    assert rel_rms(f, d["gbslow_f"]) <= F_TOL
+
+
+@pytest.mark.parametrize("name", ["peptide30", "peptide120"])
+def test_gb_pd_energies_match_calc_energies(goldens, name):
+    """PDGPU_PD_ENERGIES: FF_GeneralizedBorn_Still::calcEnergies (calcBornEnergy,
+    no ExpApproxThreshold, gbff.cpp:178-183, 537-596), with the GB object's
+    default FF_NonBonded settings."""
+    from pd_gb300 import ffi
+    d = goldens[name]
+    ctx = make_ctx(d)
+    ctx.set_gb(**gb_kwargs(d))
+    e = ctx.compute(ffi.GB | ffi.PD_ENERGIES)[0]
+    ref = d["gbene_ene"]
+    assert rel_err(e["epot"], ref[0]) <= E_TOL
+    assert rel_err(e["vdw"], ref[1]) <= E_TOL and rel_err(e["elec"], ref[2]) <= E_TOL
+    e_fast = ctx.compute(ffi.GB)[0]                  # the mode itself is unchanged
+    assert rel_err(e_fast["epot"], d["gb_ene"][0]) <= E_TOL
