@@ -484,6 +484,9 @@ int pdgpu_set_gb_mode(pdgpu_ctx* h, int fast_mode, const pdgpu_nb_params* vacuum
   if (vacuum && (vacuum->Cutoff <= 0 || vacuum->InnerCutoff > vacuum->Cutoff || vacuum->Dielectric == 0))
     return PDGPU_ERR_ARG;
   Context& c = h->c;
+  const bool same = c.gb_fast == (fast_mode != 0) && c.gb_vac_set == (vacuum != nullptr) &&
+                    (!vacuum || std::memcmp(&c.gb_vac, vacuum, sizeof(pdgpu_nb_params)) == 0);
+  if (same) return PDGPU_OK;
   if (c.md) return PDGPU_ERR_STATE;  // captured step graphs hold the launch sequence
   c.gb_fast = fast_mode != 0;
   c.gb_vac_set = vacuum != nullptr;

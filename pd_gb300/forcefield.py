@@ -131,7 +131,9 @@ class FF_NonBonded_GPU(ForcefieldBase):
 
 
 class FF_GeneralizedBorn_Still_GPU(FF_NonBonded_GPU):
-    """Still GB, FastMode path including vacuum LJ/Coulomb (gbff.cpp:1466-1835)."""
+    """Still GB (gbff.cpp): FastMode (default) fuses GB with the vacuum LJ/Coulomb
+    (calcForcesIncludingVacuo, :1466-1835); FastMode off runs FF_NonBonded's
+    calcForces with this object's own settings plus calcBornForces (:1189-1437)."""
 
     name = "Generalised Born Still (GPU)"
     flag = ffi.GB
@@ -153,8 +155,6 @@ class FF_GeneralizedBorn_Still_GPU(FF_NonBonded_GPU):
 
     def setup(self):
         super().setup()
-        if not self.FastMode:
-            raise ffi.PDGPUError(-7, "only FastMode (calcForcesIncludingVacuo) is implemented on the GPU")
         im = self.wspace.image
         if not im.has_gb:
             raise ffi.PDGPUError(-1, "the system image carries no GB radii / Vj / terms123")
@@ -169,6 +169,13 @@ class FF_GeneralizedBorn_Still_GPU(FF_NonBonded_GPU):
                    DielectricSolvent=float(self.DielectricSolvent), GbsaStillCutoff=float(self.GbsaStillCutoff),
                    ExpApproxThreshold=float(self.ExpApproxThreshold), BornRadiusOffset=float(self.BornRadiusOffset),
                    P4=float(self.P4), P5=float(self.P5))
+        # this object's FF_NonBonded settings: the vacuum part when FastMode is off and in calcEnergies
+        ctx.set_gb_mode(self.FastMode, Cutoff=float(self.Cutoff), InnerCutoff=float(self.InnerCutoff),
+                        VdwCutoff=float(self.VdwCutoff), VdwInnerCutoff=float(self.VdwInnerCutoff),
+                        Vdw14Scaling=float(self.Vdw14Scaling), Elec14Scaling=float(self.Elec14Scaling),
+                        Dielectric=float(self.Dielectric), EnergySwitch=int(bool(self.EnergySwitch)),
+                        ForceSwitch=int(bool(self.ForceSwitch)), DoVdw=int(bool(self.DoVdw)),
+                        DoElec=int(bool(self.DoElec)))
 
     def distribute(self, e):
         ene = self.wspace.ene
@@ -294,8 +301,10 @@ class Forcefield:
             ws._ctx_params = key
         return ctx
 
-    def calcForces(self, zero=True):
-        """Forcefield::calcForces: zero, evaluate every component, apply max_force, NaN check."""
+    def calcForces(self, zero=True, energies_only=False):
+        """Forcefield::calcForces: zero, evaluate every component, apply max_force, NaN check.
+        energies_only: Forcefield::calcEnergies (no forces; a GB component forms its
+        energies as FF_GeneralizedBorn_Still::calcEnergies does, gbff.cpp:178-183)."""
         ws = self.wspace
         if zero:
             ws.zeroForces()
@@ -305,7 +314,9 @@ class Forcefield:
             if c.Active:
                 what |= c.flag
         ctx.set_positions(ws.cur.p)
-        energies = ctx.compute(what, ws.cur.f)
+        if energies_only and (what & ffi.GB):
+            what |= ffi.PD_ENERGIES
+        energies = ctx.compute(what, None if energies_only else ws.cur.f)
         ws.per_system_energies = energies
         tot = {k: sum(e[k] for e in energies) for k in energies[0]}
         for c in self.components:
@@ -338,7 +349,7 @@ class Forcefield:
             ws.per_system_energies = energies
             act[0].distribute({k: sum(e[k] for e in energies) for k in energies[0]})
             return
-        self.calcForces()
+        self.calcForces(energies_only=True)
 
     def printEnergySummary(self):
         self.calcForces()

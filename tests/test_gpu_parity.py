@@ -215,3 +215,23 @@ def test_gb_pd_energies_match_calc_energies(goldens, name):
     assert rel_err(e["vdw"], ref[1]) <= E_TOL and rel_err(e["elec"], ref[2]) <= E_TOL
     e_fast = ctx.compute(ffi.GB)[0]                  # the mode itself is unchanged
     assert rel_err(e_fast["epot"], d["gb_ene"][0]) <= E_TOL
+
+
+def test_forcefield_mirror_gb_modes_match_pd(goldens):
+    """PD-style use of the GB component: FastMode off through calcForces, and
+    Forcefield.calcEnergies (FF_GeneralizedBorn_Still::calcEnergies)."""
+    import pd_gb300 as pdg
+    d = goldens["peptide30"]
+    ws = pdg.WorkSpace(pdg.SystemImage._from_fixture(d))
+    ws.Padding = 2.0
+    ff = pdg.Forcefield(ws)
+    gb = pdg.FF_GeneralizedBorn_Still_GPU(ws)
+    gb.Cutoff, gb.InnerCutoff = 12.0, 9.0
+    gb.VdwCutoff, gb.VdwInnerCutoff = 12.0, 9.0
+    ff.add(gb)
+    ff.calcEnergies()
+    assert rel_err(ws.ene.epot, float(d["gbene_ene"][0])) <= E_TOL
+    gb.FastMode = False
+    ff.calcForces()
+    assert rel_err(ws.ene.epot, float(d["gbslow_ene"][0])) <= E_TOL
+    assert rel_rms(ws.cur.f, d["gbslow_f"]) <= F_TOL
