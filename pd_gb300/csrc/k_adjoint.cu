@@ -233,19 +233,13 @@ __device__ __forceinline__ void adj_nb_tile(const DevView& v, const NBConst& k, 
                                             unsigned m14, Acc3& I, Acc3& J) {
   float4 xj = v.xq[T.bj * 32 + lane];
   float4 pj = v.par[T.bj * 32 + lane];
-  double dcx = v.center[3 * T.bj] - v.center[3 * T.bi];
-  double dcy = v.center[3 * T.bj + 1] - v.center[3 * T.bi + 1];
-  double dcz = v.center[3 * T.bj + 2] - v.center[3 * T.bi + 2];
   float Lx = 1.f, Ly = 1.f, Lz = 1.f;
   if (S.periodic) {
-    dcx -= S.box[0] * rint(dcx / S.box[0]);
-    dcy -= S.box[1] * rint(dcy / S.box[1]);
-    dcz -= S.box[2] * rint(dcz / S.box[2]);
     Lx = (float)S.box[0]; Ly = (float)S.box[1]; Lz = (float)S.box[2];
   }
-  xj.x += (float)dcx;
-  xj.y += (float)dcy;
-  xj.z += (float)dcz;
+  xj.x += T.ox;
+  xj.y += T.oy;
+  xj.z += T.oz;
   const bool mi = T.flags & 1;
   const float iLx = 1.f / Lx, iLy = 1.f / Ly, iLz = 1.f / Lz;
 #pragma unroll 2

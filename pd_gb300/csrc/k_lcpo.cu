@@ -17,9 +17,9 @@ __global__ void __launch_bounds__(256) k_lcpo_cand(DevView v, const float4* lc, 
   for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
     const Tile T = v.tiles[t];
     float4 xi = v.xq[T.bi * 32 + lane], xj = v.xq[T.bj * 32 + lane];
-    xj.x += (float)(v.center[3 * T.bj] - v.center[3 * T.bi]);
-    xj.y += (float)(v.center[3 * T.bj + 1] - v.center[3 * T.bi + 1]);
-    xj.z += (float)(v.center[3 * T.bj + 2] - v.center[3 * T.bi + 2]);
+    xj.x += T.ox;
+    xj.y += T.oy;
+    xj.z += T.oz;
     const unsigned dmask = (T.flags & 2) ? diag_exclusion(lane) : 0u;
     const int si = T.bi * 32 + lane;
     const float4 li = lc[si];

@@ -310,6 +310,19 @@ __global__ void k_tile_write(DevView v, long long ncand, float R, float margin, 
   T.bj = gj;
   T.mask = -1;
   T.flags = fl;
+  {
+    const SystemInfo& S = v.sys[v.slot_sys[gi]];
+    double o[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      o[c] = v.center[3 * gj + c] - v.center[3 * gi + c];
+      if (S.periodic) o[c] -= S.box[c] * rint(o[c] / S.box[c]);
+    }
+    T.ox = (float)o[0];
+    T.oy = (float)o[1];
+    T.oz = (float)o[2];
+    T.pad = 0.f;
+  }
   v.tiles[pos[t]] = T;
 }
 

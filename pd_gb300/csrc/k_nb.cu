@@ -65,20 +65,14 @@ __device__ __forceinline__ void nb_tile(const DevView& v, const NBConst& k, cons
                                         double& vir) {
   float4 xj = v.xq[T.bj * 32 + lane];
   float4 pj = v.par[T.bj * 32 + lane];
-  // j positions moved into i's frame: centre offset in FP64, once per tile
-  double dcx = v.center[3 * T.bj] - v.center[3 * T.bi];
-  double dcy = v.center[3 * T.bj + 1] - v.center[3 * T.bi + 1];
-  double dcz = v.center[3 * T.bj + 2] - v.center[3 * T.bi + 2];
+  // j positions moved into i's frame (the tile's centre offset, periodic image included)
   float Lx = 1.f, Ly = 1.f, Lz = 1.f;
   if (S.periodic) {
-    dcx -= S.box[0] * rint(dcx / S.box[0]);
-    dcy -= S.box[1] * rint(dcy / S.box[1]);
-    dcz -= S.box[2] * rint(dcz / S.box[2]);
     Lx = (float)S.box[0]; Ly = (float)S.box[1]; Lz = (float)S.box[2];
   }
-  xj.x += (float)dcx;
-  xj.y += (float)dcy;
-  xj.z += (float)dcz;
+  xj.x += T.ox;
+  xj.y += T.oy;
+  xj.z += T.oz;
   const bool mi = T.flags & 1;
   const float iLx = 1.f / Lx, iLy = 1.f / Ly, iLz = 1.f / Lz;
 #pragma unroll 4

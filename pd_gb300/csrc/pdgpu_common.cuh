@@ -56,11 +56,15 @@ struct SystemInfo {
   double box[3];
 };
 
-struct Tile {
+struct __align__(16) Tile {
   int bi, bj;
   int mask;    // index into the exclusion-mask table or -1
   int flags;   // bit0: per-pair minimum image needed, bit1: diagonal tile,
                // bit2: every pair inside all cutoffs and switch radii (with margin)
+  // centre of block bj seen from block bi (its periodic image in a box), formed
+  // in FP64 at the list build and rounded once: the pair kernels add it to the
+  // j positions without per-tile FP64 work
+  float ox, oy, oz, pad;
 };
 
 // Pair-law constants for the LJ + Coulomb kernel (FF_NonBonded)

@@ -24,9 +24,9 @@ static __device__ __noinline__ double r2_slots_fp64(const DevView& v, int sa, in
 // j block of a tile moved into the i block's frame (centre offset in FP64)
 __device__ __forceinline__ float4 j_in_i_frame(const DevView& v, const Tile& T, int lane) {
   float4 xj = v.xq[T.bj * 32 + lane];
-  xj.x += (float)(v.center[3 * T.bj] - v.center[3 * T.bi]);
-  xj.y += (float)(v.center[3 * T.bj + 1] - v.center[3 * T.bi + 1]);
-  xj.z += (float)(v.center[3 * T.bj + 2] - v.center[3 * T.bi + 2]);
+  xj.x += T.ox;
+  xj.y += T.oy;
+  xj.z += T.oz;
   return xj;
 }
 
