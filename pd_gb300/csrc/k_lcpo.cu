@@ -9,13 +9,68 @@ namespace pdgpu {
 // ---------------------------------------------------------------------------
 // LCPO
 // ---------------------------------------------------------------------------
-// candidate overlaps: heavy-atom pairs (use == 1) with r < r_i + r_j
-__global__ void __launch_bounds__(256) k_lcpo_cand(DevView v, const float4* lc, int* ncand, int* cand) {
+// per block (one warp, a lane per slot), once per recalculation:
+//  * lpos: the slot's position from its system's first block centre, rounded once
+//    to FP32 (the rounding the block-centre offsets get elsewhere), w = LCPO radius;
+//  * psig: (P2, P3, P4) x sigma of the slot's atom in FP32 (zero for padding);
+//  * box: the block's bounding box over its LCPO atoms in the block frame of xq,
+//    lo.w = their largest LCPO radius, or -1 when the block holds none
+__global__ void __launch_bounds__(256) k_lcpo_prep(DevView v, const float4* lc, const double* P, const double* sigma,
+                                                   float4* lpos, float4* psig, float4* box) {
+  const int lane = threadIdx.x & 31;
+  const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (b >= v.nblocks) return;  // whole warps
+  const int s = b * 32 + lane;
+  const int a = v.sorted_atom[s];
+  const float4 l = lc[s];
+  float4 p = make_float4(0.f, 0.f, 0.f, 0.f), q = p;
+  if (a >= 0) {
+    const int ref = v.sys[v.slot_sys[b]].block_start;
+    p = make_float4((float)(v.pos[3 * a] - v.center[3 * ref]), (float)(v.pos[3 * a + 1] - v.center[3 * ref + 1]),
+                    (float)(v.pos[3 * a + 2] - v.center[3 * ref + 2]), l.x);
+    q = make_float4((float)(P[4 * a + 1] * sigma[a]), (float)(P[4 * a + 2] * sigma[a]),
+                    (float)(P[4 * a + 3] * sigma[a]), 0.f);
+  }
+  lpos[s] = p;
+  psig[s] = q;
+  const bool use = a >= 0 && l.y > 0.f;
+  const float4 x = v.xq[s];
+  float lo0 = use ? x.x : INFINITY, lo1 = use ? x.y : INFINITY, lo2 = use ? x.z : INFINITY;
+  float hi0 = use ? x.x : -INFINITY, hi1 = use ? x.y : -INFINITY, hi2 = use ? x.z : -INFINITY;
+  float rmax = use ? l.x : -1.f;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo0 = fminf(lo0, __shfl_xor_sync(0xffffffffu, lo0, o));
+    lo1 = fminf(lo1, __shfl_xor_sync(0xffffffffu, lo1, o));
+    lo2 = fminf(lo2, __shfl_xor_sync(0xffffffffu, lo2, o));
+    hi0 = fmaxf(hi0, __shfl_xor_sync(0xffffffffu, hi0, o));
+    hi1 = fmaxf(hi1, __shfl_xor_sync(0xffffffffu, hi1, o));
+    hi2 = fmaxf(hi2, __shfl_xor_sync(0xffffffffu, hi2, o));
+    rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+  }
+  if (lane == 0) {
+    box[2 * b] = make_float4(lo0, lo1, lo2, rmax);
+    box[2 * b + 1] = make_float4(hi0, hi1, hi2, 0.f);
+  }
+}
+
+// candidate overlaps: heavy-atom pairs (use == 1) with r < r_i + r_j.  A tile
+// whose two block boxes lie farther apart than their largest radii can reach
+// holds none and is skipped (warp-uniform test; the margin covers rounding).
+__global__ void __launch_bounds__(256) k_lcpo_cand(DevView v, const float4* lc, const float4* box, int* ncand,
+                                                   int* cand) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nt = *v.ntiles;
   for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
     const Tile T = v.tiles[t];
+    const float4 bli = box[2 * T.bi], bhi = box[2 * T.bi + 1], blj = box[2 * T.bj], bhj = box[2 * T.bj + 1];
+    if (bli.w < 0.f || blj.w < 0.f) continue;
+    const float gx = fmaxf(0.f, fmaxf((blj.x + T.ox) - bhi.x, bli.x - (bhj.x + T.ox)));
+    const float gy = fmaxf(0.f, fmaxf((blj.y + T.oy) - bhi.y, bli.y - (bhj.y + T.oy)));
+    const float gz = fmaxf(0.f, fmaxf((blj.z + T.oz) - bhi.z, bli.z - (bhj.z + T.oz)));
+    const float reach = (bli.w + blj.w) * 1.001f + 1e-3f;
+    if (gx * gx + gy * gy + gz * gz > reach * reach) continue;
     float4 xi = v.xq[T.bi * 32 + lane], xj = v.xq[T.bj * 32 + lane];
     xj.x += T.ox;
     xj.y += T.oy;
@@ -41,26 +96,16 @@ __global__ void __launch_bounds__(256) k_lcpo_cand(DevView v, const float4* lc, 
 }
 
 // per atom (one warp): order candidates by original atom index, keep the first
-// 80 (PD's insertion order, lcpo.cpp:705-744) and store s_ij
-__global__ void k_lcpo_sort(DevView v, const float4* lc, const int* ncand, const int* cand, int* nl_n, int* nl_idx,
-                            float* nl_s, float4* lpos) {
+// 80 (PD's insertion order, lcpo.cpp:705-744) and store each kept partner as a
+// record: (slot, s_ij) and (its lpos, radius), so the triple loop reads a row of
+// records in sequence instead of chasing slot indices
+__global__ void k_lcpo_sort(DevView v, const float4* lc, const float4* lpos, const int* ncand, const int* cand,
+                            int* nl_n, int2* nl_e2, float4* nl_ent) {
   __shared__ int sh_key[8][kLcpoCand];
   __shared__ int sh_slot[8][kLcpoCand];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (s >= v.nslots) return;
-  if (lane == 0) {
-    // the triple loop's positions (w: LCPO radius): from the system's first block centre, rounded
-    // once to FP32 (the same rounding the block-centre offsets get elsewhere)
-    const int a = v.sorted_atom[s];
-    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (a >= 0) {
-      const int ref = v.sys[v.slot_sys[s >> 5]].block_start;
-      p = make_float4((float)(v.pos[3 * a] - v.center[3 * ref]), (float)(v.pos[3 * a + 1] - v.center[3 * ref + 1]),
-                      (float)(v.pos[3 * a + 2] - v.center[3 * ref + 2]), lc[s].x);
-    }
-    lpos[s] = p;
-  }
   int n = ncand[s];
   if (n > kLcpoCand) {
     if (lane == 0) atomicOr(v.status, (unsigned)ST_LCPO_OVERFLOW);
@@ -80,7 +125,6 @@ __global__ void k_lcpo_sort(DevView v, const float4* lc, const int* ncand, const
     for (int q = 0; q < n; q++) rank += sh_key[w][q] < key;
     if (rank < keep) {
       int sj = sh_slot[w][p];
-      nl_idx[(size_t)s * kLcpoMax + rank] = sj;
       // overlap of i's sphere by j: 2 pi ri (ri - d/2 - (ri^2 - rj^2)/(2d))  (lcpo.cpp:731-733)
       float4 xi = v.xq[s], xj = v.xq[sj];
       int bi = s >> 5, bj = sj >> 5;
@@ -90,23 +134,22 @@ __global__ void k_lcpo_sort(DevView v, const float4* lc, const int* ncand, const
       float d = sqrtf(dx * dx + dy * dy + dz * dz);
       float ri = lc[s].x, rj = lc[sj].x;
       float rr = 0.5f * (ri * ri - rj * rj) / d;
-      nl_s[(size_t)s * kLcpoMax + rank] = 6.283185307179586f * ri * (ri - 0.5f * d - rr);
+      const float sij = 6.283185307179586f * ri * (ri - 0.5f * d - rr);
+      nl_e2[(size_t)s * kLcpoMax + rank] = make_int2(sj, __float_as_int(sij));
+      nl_ent[(size_t)s * kLcpoMax + rank] = lpos[sj];
     }
   }
   if (lane == 0) nl_n[s] = keep;
 }
 
-// relative position of slot b seen from slot a
-__device__ __forceinline__ float3 rel_vec(const float4* lpos, const float4& xa, int b) {
-  const float4 xb = lpos[b];
-  return make_float3(xb.x - xa.x, xb.y - xa.y, xb.z - xa.z);
-}
-
 // per atom i (one warp, lanes over i's overlap partners j): SASA_i and the
-// derivative terms collected on atom i (lcpo.cpp:781-949)
-__global__ void k_lcpo_main(DevView v, const float4* lc, const float4* lpos, const int* nl_n, const int* nl_idx,
-                            const float* nl_s, const double* P, const double* sigma, double* sasa_out,
-                            long long* facc_out, long long* esurf_out, int esurf_stride) {
+// derivative terms collected on atom i (lcpo.cpp:781-949).  Each lane sums its
+// partners' terms in FP32 (already folded with the P x sigma weights, so a lane
+// carries SA and the force only); the lanes combine in FP64.
+__global__ void __launch_bounds__(256) k_lcpo_main(DevView v, const float4* lc, const float4* lpos, const float4* psig,
+                                                   const int* nl_n, const int2* nl_e2, const float4* nl_ent,
+                                                   const double* P, const double* sigma, double* sasa_out,
+                                                   long long* facc_out, long long* esurf_out, int esurf_stride) {
   const int lane = threadIdx.x & 31;
   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (s >= v.nslots) return;
@@ -119,17 +162,20 @@ __global__ void k_lcpo_main(DevView v, const float4* lc, const float4* lpos, con
   }
   const float ri = li.x;
   const float4 xi = lpos[s];
+  const float4 qi = psig[s];
+  const float pa2 = (float)P[4 * a + 1], pa3 = (float)P[4 * a + 2], pa4 = (float)P[4 * a + 3];
   const float PI = 3.14159265358979f;
   const int n = nl_n[s];
-  double Si2 = 0, Si3 = 0, Si4 = 0;
-  double der[3] = {0, 0, 0}, d2[3] = {0, 0, 0}, d4[3] = {0, 0, 0};
+  float sa = 0.f, fl[3] = {0.f, 0.f, 0.f};
   for (int jj = lane; jj < n; jj += 32) {
-    const int sj = nl_idx[(size_t)s * kLcpoMax + jj];
-    const int ja = v.sorted_atom[sj];
-    const float Si2_t = nl_s[(size_t)s * kLcpoMax + jj];
-    float3 dij = rel_vec(lpos, xi, sj);  // j - i
+    const int2 ej = nl_e2[(size_t)s * kLcpoMax + jj];
+    const float4 xj = nl_ent[(size_t)s * kLcpoMax + jj];
+    const int sj = ej.x;
+    const float Si2_t = __int_as_float(ej.y);
+    const float4 qj = psig[sj];
+    const float3 dij = make_float3(xj.x - xi.x, xj.y - xi.y, xj.z - xi.z);  // j - i
     float d = sqrtf(dij.x * dij.x + dij.y * dij.y + dij.z * dij.z);
-    float rj = lc[sj].x;
+    float rj = xj.w;
     float invd = 1.f / d;
     float rr = 0.5f * (ri * ri - rj * rj) * invd;
     float sji = 6.283185307179586f * rj * (rj - 0.5f * d + rr);
@@ -142,10 +188,12 @@ __global__ void k_lcpo_main(DevView v, const float4* lc, const float4* lpos, con
     float n3[3] = {0, 0, 0}, n3b[3] = {0, 0, 0}, n4b[3] = {0, 0, 0};
     float Si3_t = 0.f, Si3ik_t = 0.f;
     const int nk = nl_n[sj];
+    const int2* rowe = nl_e2 + (size_t)sj * kLcpoMax;
+    const float4* rowx = nl_ent + (size_t)sj * kLcpoMax;
     for (int kk = 0; kk < nk; kk++) {
-      const int sk = nl_idx[(size_t)sj * kLcpoMax + kk];
-      if (sk == s) continue;
-      const float4 xk = lpos[sk];
+      const int2 ek = rowe[kk];
+      if (ek.x == s) continue;
+      const float4 xk = rowx[kk];
       const float rk = xk.w;
       const float3 dik = make_float3(xk.x - xi.x, xk.y - xi.y, xk.z - xi.z);
       float dik2 = dik.x * dik.x + dik.y * dik.y + dik.z * dik.z;
@@ -155,7 +203,7 @@ __global__ void k_lcpo_main(DevView v, const float4* lc, const float4* lpos, con
       float rrk = (ri * ri - rk * rk) * invdik * invdik;
       float dA = PI * ri * (rrk - 1.f);
       float u0 = dik.x * invdik, u1 = dik.y * invdik, u2 = dik.z * invdik;
-      float sjk = nl_s[(size_t)sj * kLcpoMax + kk];
+      float sjk = __int_as_float(ek.y);
       n3[0] += dA * u0; n3[1] += dA * u1; n3[2] += dA * u2;
       dA = PI * rk * (-rrk - 1.f);
       Si3ik_t += PI * ri * (2.f * ri - dk - dk * rrk);
@@ -163,32 +211,24 @@ __global__ void k_lcpo_main(DevView v, const float4* lc, const float4* lpos, con
       n4b[0] += sjk * dA * u0; n4b[1] += sjk * dA * u1; n4b[2] += sjk * dA * u2;
       Si3_t += sjk;
     }
-    const double p2 = P[4 * ja + 1] * sigma[ja], p3 = P[4 * ja + 2] * sigma[ja], p4 = P[4 * ja + 3] * sigma[ja];
+    // j's weights (P2, P3, P4) sigma_j on the n2, n3, n4 terms; i's P2 sigma_i and
+    // P4 sigma_i on the a2 terms (lcpo.cpp:900-949)
+    const float wa = qi.x + Si3_t * qi.z;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-      double n4 = (double)sji * n3[c] + n4b[c] + (double)n2[c] * Si3ik_t;
-      double n3t = (double)n3[c] + n3b[c];
-      der[c] += n2[c] * p2 + n3t * p3 + n4 * p4;
-      d2[c] += a2t[c];
-      d4[c] += (double)Si3_t * a2t[c];
+      const float n4 = sji * n3[c] + n4b[c] + n2[c] * Si3ik_t;
+      const float n3t = n3[c] + n3b[c];
+      fl[c] += n2[c] * qj.x + n3t * qj.y + n4 * qj.z + a2t[c] * wa;
     }
-    Si4 += (double)Si3_t * Si2_t;
-    Si3 += Si3_t;
-    Si2 += Si2_t;
+    sa += pa2 * Si2_t + pa3 * Si3_t + pa4 * (Si3_t * Si2_t);
   }
-  Si2 = warp_sum_d(Si2);
-  Si3 = warp_sum_d(Si3);
-  Si4 = warp_sum_d(Si4);
-  for (int c = 0; c < 3; c++) {
-    der[c] = warp_sum_d(der[c]);
-    d2[c] = warp_sum_d(d2[c]);
-    d4[c] = warp_sum_d(d4[c]);
-  }
+  double SAp = warp_sum_d((double)sa);
+  double f[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) f[c] = warp_sum_d((double)fl[c]);
   if (lane == 0) {
     const double Si = 4.0 * 3.14159265358979323846 * (double)ri * ri;
-    double SA = P[4 * a] * Si + P[4 * a + 1] * Si2 + P[4 * a + 2] * Si3 + P[4 * a + 3] * Si4;
-    double f[3];
-    for (int c = 0; c < 3; c++) f[c] = der[c] + d2[c] * (P[4 * a + 1] * sigma[a]) + d4[c] * (P[4 * a + 3] * sigma[a]);
+    double SA = P[4 * a] * Si + SAp;
     if (SA < 0) {
       SA = 0;
       f[0] = f[1] = f[2] = 0;
@@ -205,14 +245,17 @@ int launch_lcpo(Context& c, long long* facc_out, long long* esurf_out, int esurf
   DevView v = c.view();
   cudaStream_t st = c.stream;
   int g = tile_grid(c);
-  c.kernel_launches += 3;
+  c.kernel_launches += 4;
   cudaMemsetAsync(c.d_lc_ncand.p, 0, sizeof(int) * c.nslots, st);
-  k_lcpo_cand<<<g, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_ncand.p, c.d_lc_cand.p);
+  k_lcpo_prep<<<(int)(((long long)c.nblocks * 32 + 255) / 256), 256, 0, st>>>(
+      v, c.d_lc_par.p, c.d_lcpoP.p, c.d_lcpoSig.p, c.d_lc_pos.p, c.d_lc_psig.p, c.d_lc_box.p);
+  k_lcpo_cand<<<g, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_box.p, c.d_lc_ncand.p, c.d_lc_cand.p);
   int nw = (int)(((long long)c.nslots * 32 + 255) / 256);
-  k_lcpo_sort<<<nw, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_ncand.p, c.d_lc_cand.p, c.d_lc_n.p, c.d_lc_idx.p,
-                                   c.d_lc_s.p, c.d_lc_pos.p);
-  k_lcpo_main<<<nw, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_pos.p, c.d_lc_n.p, c.d_lc_idx.p, c.d_lc_s.p,
-                                   c.d_lcpoP.p, c.d_lcpoSig.p, c.d_sasa.p, facc_out, esurf_out, esurf_stride);
+  k_lcpo_sort<<<nw, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_pos.p, c.d_lc_ncand.p, c.d_lc_cand.p, c.d_lc_n.p,
+                                   c.d_lc_e2.p, c.d_lc_ent.p);
+  k_lcpo_main<<<nw, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_pos.p, c.d_lc_psig.p, c.d_lc_n.p, c.d_lc_e2.p,
+                                   c.d_lc_ent.p, c.d_lcpoP.p, c.d_lcpoSig.p, c.d_sasa.p, facc_out, esurf_out,
+                                   esurf_stride);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

@@ -429,8 +429,10 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
     if (e == cudaSuccess) e = c.d_lc_ncand.alloc(c.nslots);
     if (e == cudaSuccess) e = c.d_lc_cand.alloc((size_t)c.nslots * kLcpoCand);
     if (e == cudaSuccess) e = c.d_lc_n.alloc(c.nslots);
-    if (e == cudaSuccess) e = c.d_lc_idx.alloc((size_t)c.nslots * kLcpoMax);
-    if (e == cudaSuccess) e = c.d_lc_s.alloc((size_t)c.nslots * kLcpoMax);
+    if (e == cudaSuccess) e = c.d_lc_e2.alloc((size_t)c.nslots * kLcpoMax);
+    if (e == cudaSuccess) e = c.d_lc_ent.alloc((size_t)c.nslots * kLcpoMax);
+    if (e == cudaSuccess) e = c.d_lc_psig.alloc(c.nslots);
+    if (e == cudaSuccess) e = c.d_lc_box.alloc((size_t)c.nblocks * 2);
     if (e == cudaSuccess) e = c.d_sasa.alloc(N);
     if (e == cudaSuccess) e = c.d_lc_par.alloc(c.nslots);
     if (e == cudaSuccess) e = c.d_lc_pos.alloc(c.nslots);

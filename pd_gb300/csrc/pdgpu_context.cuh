@@ -108,11 +108,13 @@ struct Context {
   DBuf<int> d_lc_ncand;             // [nslots]
   DBuf<int> d_lc_cand;              // [nslots*kLcpoCand]
   DBuf<int> d_lc_n;                 // [nslots]
-  DBuf<int> d_lc_idx;               // [nslots*kLcpoMax] slot indices, ascending original index
-  DBuf<float> d_lc_s;               // [nslots*kLcpoMax] overlap s_ij
+  DBuf<int2> d_lc_e2;               // [nslots*kLcpoMax] (partner slot, s_ij bits), ascending original index
+  DBuf<float4> d_lc_ent;            // [nslots*kLcpoMax] partner position (lc_pos frame) and LCPO radius
+  DBuf<float4> d_lc_psig;           // [nslots] (P2, P3, P4) x sigma of the slot's atom, FP32
+  DBuf<float4> d_lc_box;            // [nblocks*2] block box over its LCPO atoms (lo + max radius, hi)
   DBuf<double> d_sasa;              // [natom]
   DBuf<float4> d_lc_par;            // [nslots] (radius, use, -, -)
-  DBuf<float4> d_lc_pos;            // [nslots] position from its system's first block centre (FP32)
+  DBuf<float4> d_lc_pos;            // [nslots] position from its system's first block centre (FP32), radius
 
   // bonded
   int nbond = 0, nangle = 0, ntors = 0, nimpr = 0;
