@@ -94,52 +94,6 @@ __global__ void k_gb_radii(DevView v, const double* terms123, const long long* g
   born_d[a] = r;
 }
 
-// Energies of one loop-1 pair (gbff.cpp:1546-1746) in FP64.
-__device__ __noinline__ void gb_pair_energy(const GBConst& k, const DevView& v, int a, int b, double r2, bool excl,
-                                            bool is14, double& evdw, double& eel, double& epol) {
-  if (r2 > k.cut2_d) return;
-  double r = sqrt(r2), invr = 1.0 / r;
-  double qiqj = v.charge[a] * v.charge[b];
-  double aiaj = v.born[a] * v.born[b];
-  double u = -0.25 * r2 / aiaj;
-  double s14 = is14 ? k.elec14_d : 1.0;
-  double S = 1.0;
-  if (r >= k.inner_d) {
-    double w = r - k.inner_d;
-    double sw = 1.0 - w * w * k.invw2_d;
-    S = sw * sw;
-  }
-  double elec = 0.0;
-  if (!k.fast) {  // calcBornForces / calcBornEnergy: the GB part only, every pair
-    epol += 2.0 * S * k.premul_d * qiqj * (u > k.thresh_d ? 1.0 / sqrt(r2 + exp(u) * aiaj) : invr);
-    return;
-  }
-  if (u > k.thresh_d) {
-    double t = exp(u);
-    double ep = k.premul_d * qiqj / sqrt(r2 + t * aiaj);
-    if (!excl) elec = k.econv_in_d * s14 * qiqj * invr;
-    epol += 2.0 * ep * S;
-  } else if (!excl) {
-    elec = k.econv_out_d * s14 * qiqj * invr;
-  }
-  if (excl) return;
-  eel += elec * S;
-  if (r < k.vdwcut_d) {
-    double t = (v.radius[a] + v.radius[b]) * invr;
-    double B = t * t;
-    B = B * B * B;
-    double A = B * B;
-    double eps = v.sqeps[a] * v.sqeps[b] * (is14 ? k.vdw14_d : 1.0);
-    double Ev = eps * (A - 2.0 * B);
-    if (r > k.vdwinner_d) {
-      double w = r - k.vdwinner_d;
-      double sw = 1.0 - w * w * k.vdwinvw2_d;
-      Ev *= sw * sw;
-    }
-    evdw += Ev;
-  }
-}
-
 // the exp-approximation switch is discontinuous: pairs within FP32 rounding of
 // the threshold are decided in FP64
 __device__ __noinline__ bool gb_on_fp64(const DevView& v, int si, int sj, double thresh) {
@@ -150,7 +104,8 @@ __device__ __noinline__ bool gb_on_fp64(const DevView& v, int si, int sj, double
 
 // ---------------------------------------------------------------------------
 // pass 2: GB cross term fused with vacuum LJ + Coulomb, i > j pairs within Cutoff
-// (forces, dE/da in FP32; with ENERGY the pair energies are formed in FP64)
+// (forces, dE/da and, with ENERGY, the pair energies in FP32; energies are summed
+// in FP32 over 8 rotation steps, then in FP64, then per tile in fixed point)
 // ---------------------------------------------------------------------------
 struct PairAcc {
   float fx, fy, fz, da;
@@ -158,12 +113,13 @@ struct PairAcc {
 
 template <bool MASKED, bool ENERGY, bool FULL, bool FAST = true>
 __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k, const Tile& T, int lane, int si,
-                                             int atom_i, const float4& xi, const float4& pi, float ai, unsigned ex,
+                                             const float4& xi, const float4& pi, float ai, unsigned ex,
                                              unsigned m14, unsigned dmask, const float* born, PairAcc& I, PairAcc& J,
                                              double& evdw, double& eel, double& epol) {
   float4 xj = j_in_i_frame(v, T, lane);
   float4 pj = v.par[T.bj * 32 + lane];
   float aj = born[T.bj * 32 + lane];
+  float cv = 0.f, ce = 0.f, cp = 0.f;  // (ENERGY) vdW, Coulomb, GB cross over the current 8 steps
 #pragma unroll 2
   for (int kk = 0; kk < 32; kk++) {
     const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
@@ -173,12 +129,6 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
       pair = !((dmask >> kk) & 1u);
       excl = (ex >> kk) & 1u;  // bond order <= 2: GB term only
       is14 = (m14 >> kk) & 1u;
-    }
-    if (ENERGY && pair) {
-      const int sjk = T.bj * 32 + ((lane + kk) & 31);
-      const int atom_j = v.sorted_atom[sjk];
-      if (atom_i >= 0 && atom_j >= 0)
-        gb_pair_energy(k, v, atom_i, atom_j, r2_slots_fp64(v, si, sjk), excl, is14, evdw, eel, epol);
     }
     if ((FULL || r2 <= k.cut2) && pair) {
       const float invr = rsqrtf(r2);
@@ -207,6 +157,7 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
         const float ep = k.premul * qiqj * fgb;
         float dedr = -ep * (r - 0.25f * r * tg) * l;
         float dalpha = -ep * tg * (1.f - u) * l;
+        if (ENERGY) cp += 2.f * ep * S;
         if (FAST && !excl) {
           elec = k.econv_in * s14 * qiqj * invr;
           delec = -elec * invr;
@@ -225,10 +176,12 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
         // calcBornForces below the threshold (gbff.cpp:1308-1325): premul q_i q_j / r
         const float ep = k.premul * qiqj * invr;
         float dedr = -ep * invr;
+        if (ENERGY) cp += 2.f * ep * S;
         if (sw_on) dedr = S * dedr + dS * ep;
         g += 2.f * dedr * invr;
       }
       if (FAST && !excl) {
+        if (ENERGY) ce += elec * S;
         if (sw_on) delec = S * delec + elec * dS;
         float dvdw = 0.f;
         if (FULL || r < k.vdwcut) {
@@ -238,17 +191,26 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
           const float A = B * B;
           const float eps = pi.y * pj.y * (is14 ? k.vdw14 : 1.f);
           dvdw = -12.f * eps * invr * (A - B);
+          float Ev = ENERGY ? eps * (A - 2.f * B) : 0.f;
           if (!FULL && r > k.vdwinner) {
-            const float Ev = eps * (A - 2.f * B);
+            if (!ENERGY) Ev = eps * (A - 2.f * B);
             const float w = r - k.vdwinner;
             const float sw = 1.f - w * w * k.vdwinvw2;
             dvdw = sw * sw * dvdw + Ev * (-4.f * k.vdwinvw2 * w * sw);
+            if (ENERGY) Ev *= sw * sw;
           }
+          if (ENERGY) cv += Ev;
         }
         g += (dvdw + delec) * invr;
       }
       I.fx += g * dx; I.fy += g * dy; I.fz += g * dz;
       J.fx -= g * dx; J.fy -= g * dy; J.fz -= g * dz;
+    }
+    if (ENERGY && (kk & 7) == 7) {
+      evdw += (double)cv;
+      eel += (double)ce;
+      epol += (double)cp;
+      cv = ce = cp = 0.f;
     }
     ROT(xj.x); ROT(xj.y); ROT(xj.z); ROT(xj.w); ROT(pj.x); ROT(pj.y); ROT(aj);
     ROT(J.fx); ROT(J.fy); ROT(J.fz); ROT(J.da);
@@ -310,7 +272,7 @@ __device__ __forceinline__ void flush_gb_energy(const DevView& v, int lane, int 
 }
 
 template <bool ENERGY>
-__global__ void __launch_bounds__(256, ENERGY ? 1 : 4) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
+__global__ void __launch_bounds__(256, ENERGY ? 2 : 4) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nt = *v.ntiles;
@@ -319,7 +281,6 @@ __global__ void __launch_bounds__(256, ENERGY ? 1 : 4) k_gb_pair(DevView v, GBCo
     const int si = T.bi * 32 + lane;
     const float4 xi = v.xq[si], pi = v.par[si];
     const float ai = born[si];
-    const int atom_i = ENERGY ? v.sorted_atom[si] : -1;
     unsigned ex, m14;
     tile_masks(v, T, lane, ex, m14);
     const unsigned dmask = (T.flags & 2) ? diag_exclusion(lane) : 0u;
@@ -328,17 +289,17 @@ __global__ void __launch_bounds__(256, ENERGY ? 1 : 4) k_gb_pair(DevView v, GBCo
     const bool full = tile_full(T);
     if (tile_masked(T)) {
       if (full)
-        gb_pair_tile<true, ENERGY, true>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
+        gb_pair_tile<true, ENERGY, true>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
                                          eel, epol);
       else
-        gb_pair_tile<true, ENERGY, false>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
+        gb_pair_tile<true, ENERGY, false>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
                                           eel, epol);
     } else {
       if (full)
-        gb_pair_tile<false, ENERGY, true>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
+        gb_pair_tile<false, ENERGY, true>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
                                           eel, epol);
       else
-        gb_pair_tile<false, ENERGY, false>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
+        gb_pair_tile<false, ENERGY, false>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
                                            eel, epol);
     }
     flush_pair(v, deda, si, I);
@@ -366,13 +327,12 @@ __global__ void __launch_bounds__(256) k_gb_pair_born_only(DevView v, GBConst k,
     const int si = T.bi * 32 + lane;
     const float4 xi = v.xq[si], pi = v.par[si];
     const float ai = born[si];
-    const int atom_i = ENERGY ? v.sorted_atom[si] : -1;
     unsigned ex, m14;
     tile_masks(v, T, lane, ex, m14);
     const unsigned dmask = (T.flags & 2) ? diag_exclusion(lane) : 0u;
     PairAcc I = {0.f, 0.f, 0.f, 0.f}, J = {0.f, 0.f, 0.f, 0.f};
     double evdw = 0.0, eel = 0.0, epol = 0.0;
-    gb_pair_tile<true, ENERGY, false, false>(v, k, T, lane, si, atom_i, xi, pi, ai, ex, m14, dmask, born, I, J,
+    gb_pair_tile<true, ENERGY, false, false>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J,
                                              evdw, eel, epol);
     flush_pair(v, deda, si, I);
     flush_pair(v, deda, T.bj * 32 + lane, J);
