@@ -20,6 +20,28 @@ namespace pdgpu {
 // ---------------------------------------------------------------------------
 // pass 1: Born-radius pair sums  Gpol_i += P4 Vj CCF / r^4  (bond order > 2)
 // ---------------------------------------------------------------------------
+// inside GbsaStillCutoff (FULL: the whole tile is); pairs within FP32 rounding of
+// the cutoff are decided in FP64
+template <bool FULL>
+__device__ __forceinline__ bool still_in(const DevView& v, const GBConst& k, float r2, int sa, int sb) {
+  if (FULL) return true;
+  bool in = r2 <= k.still2;
+  if (fabsf(r2 - k.still2) <= 2e-6f * k.still2) in = r2_slots_fp64(v, sa, sb) <= k.still2_d;
+  return in;
+}
+
+// P4 CCF / r^4 of one pair (rs = R_i + R_j, raw type radii)
+__device__ __forceinline__ float born_w(const GBConst& k, float r2, float rs) {
+  const float rdivR = __fdividef(r2, rs * rs);
+  float ccf = 1.f;
+  if (rdivR <= k.invP5) {
+    const float h = 0.5f - 0.5f * cospif(rdivR * k.P5);
+    ccf = h * h;
+  }
+  const float ir2 = __fdividef(1.f, r2);
+  return k.P4 * ccf * ir2 * ir2;
+}
+
 template <bool MASKED, bool FULL>
 __device__ __forceinline__ void born_tile(const DevView& v, const GBConst& k, const Tile& T, int lane, int si,
                                           const float4& xi, const float4& pi, unsigned ex, float& gi, float& gj) {
@@ -29,23 +51,10 @@ __device__ __forceinline__ void born_tile(const DevView& v, const GBConst& k, co
   for (int kk = 0; kk < 32; kk++) {
     const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
     const float r2 = dx * dx + dy * dy + dz * dz;
-    bool in = true;  // FULL: the whole tile lies inside the Still cutoff
-    if (!FULL) {
-      in = r2 <= k.still2;
-      if (fabsf(r2 - k.still2) <= 2e-6f * k.still2)
-        in = r2_slots_fp64(v, si, T.bj * 32 + ((lane + kk) & 31)) <= k.still2_d;
-    }
+    bool in = still_in<FULL>(v, k, r2, si, T.bj * 32 + ((lane + kk) & 31));
     if (MASKED) in = in && !((ex >> kk) & 1u);
     if (in) {
-      const float rs = pi.z + pj.z;
-      const float rdivR = __fdividef(r2, rs * rs);
-      float ccf = 1.f;
-      if (rdivR <= k.invP5) {
-        const float h = 0.5f - 0.5f * cospif(rdivR * k.P5);
-        ccf = h * h;
-      }
-      const float ir2 = __fdividef(1.f, r2);
-      const float w = k.P4 * ccf * ir2 * ir2;
+      const float w = born_w(k, r2, pi.z + pj.z);
       gi += w * pj.w;
       gj += w * pi.w;
     }
@@ -53,12 +62,67 @@ __device__ __forceinline__ void born_tile(const DevView& v, const GBConst& k, co
   }
 }
 
+// Tile pairs: two unmasked, off-diagonal tiles (bi, bj) and (bi, bj + 1) of one
+// row at once.  The shared bi block rotates through the warp and each lane keeps
+// one atom of each j block (moved into bi's frame), so one rotation of the bi
+// atom (its data and its running sums) serves two pairs instead of one.
+template <bool FULL>
+__device__ __forceinline__ void born_tile2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B, int lane,
+                                           long long* gpol) {
+  const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
+  const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
+  const float4 pa = v.par[sa], pb = v.par[sb];
+  float4 xr = v.xq[r0 + lane], pr = v.par[r0 + lane];
+  float ga = 0.f, gb = 0.f, gr = 0.f;
+#pragma unroll 4
+  for (int kk = 0; kk < 32; kk++) {
+    const int sr = r0 + ((lane + kk) & 31);
+    {
+      const float dx = xr.x - xa.x, dy = xr.y - xa.y, dz = xr.z - xa.z;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (still_in<FULL>(v, k, r2, sa, sr)) {
+        const float w = born_w(k, r2, pa.z + pr.z);
+        ga += w * pr.w;
+        gr += w * pa.w;
+      }
+    }
+    {
+      const float dx = xr.x - xb.x, dy = xr.y - xb.y, dz = xr.z - xb.z;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (still_in<FULL>(v, k, r2, sb, sr)) {
+        const float w = born_w(k, r2, pb.z + pr.z);
+        gb += w * pr.w;
+        gr += w * pb.w;
+      }
+    }
+    ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(pr.z); ROT(pr.w); ROT(gr);
+  }
+  atomic_add_ll(&gpol[sa], fx32(ga));
+  atomic_add_ll(&gpol[sb], fx32(gb));
+  atomic_add_ll(&gpol[r0 + lane], fx32(gr));
+}
+
+// the warp's next work item: a tile (t) or a tile pair (t, t + 1)
+__device__ __forceinline__ int item_tile(const DevView& v, int it, bool& two) {
+  const unsigned code = v.items[it];
+  two = (code >> 31) != 0u;
+  return (int)(code & 0x7fffffffu);
+}
+
 __global__ void __launch_bounds__(256) k_gb_born(DevView v, GBConst k, long long* gpol) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const int nt = *v.ntiles;
-  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
+  const int ni = *v.nitems;
+  for (int it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < ni; it += nwarps) {
+    bool two;
+    const int t = item_tile(v, it, two);
     const Tile T = v.tiles[t];
+    if (two) {
+      const Tile U = v.tiles[t + 1];
+      if (tile_full(T)) born_tile2<true>(v, k, T, U, lane, gpol);
+      else born_tile2<false>(v, k, T, U, lane, gpol);
+      continue;
+    }
     const int si = T.bi * 32 + lane;
     const float4 xi = v.xq[si], pi = v.par[si];
     unsigned ex, m14;
@@ -111,6 +175,92 @@ struct PairAcc {
   float fx, fy, fz, da;
 };
 
+// One pair of the fused law: i = (xi.w, pix, piy, ai), j = (qj, pjx, pjy, aj),
+// (dx, dy, dz) = x_j - x_i.  Adds the force on i along d to I and its opposite to
+// J, dE/da to both, and (ENERGY) the pair energies to cv, ce, cp.  si, sj: slots
+// for the FP64 threshold tie-break.
+template <bool ENERGY, bool FULL, bool FAST>
+__device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, float dx, float dy, float dz,
+                                            float r2, float qi, float qj, float pix, float piy, float pjx,
+                                            float pjy, float ai, float aj, bool excl, bool is14, int si, int sj,
+                                            PairAcc& I, PairAcc& J, float& cv, float& ce, float& cp) {
+    const float invr = rsqrtf(r2);
+    const float r = r2 * invr;
+    const float qiqj = qi * qj;
+    const float aiaj = ai * aj;
+    const float u = -0.25f * __fdividef(r2, aiaj);
+    bool gbon = u > k.thresh;
+    if (fabsf(u - k.thresh) <= 2e-6f * fabsf(k.thresh))
+      gbon = gb_on_fp64(v, si, sj, k.thresh_d);
+    float g = 0.f;  // scalar multiplying (xj - xi) in the force on i
+    float elec = 0.f, delec = 0.f;
+    const float s14 = is14 ? k.elec14 : 1.f;
+    const bool sw_on = !FULL && r >= k.inner;  // FULL: inside the inner cutoff
+    float S = 1.f, dS = 0.f;
+    if (sw_on) {
+      const float w = r - k.inner;
+      const float sw = 1.f - w * w * k.invw2;
+      dS = -4.f * k.invw2 * w * sw;
+      S = sw * sw;
+    }
+    if (gbon) {
+      const float tg = __expf(u);
+      const float fgb = rsqrtf(r2 + tg * aiaj);
+      const float l = fgb * fgb;
+      const float ep = k.premul * qiqj * fgb;
+      float dedr = -ep * (r - 0.25f * r * tg) * l;
+      float dalpha = -ep * tg * (1.f - u) * l;
+      if (ENERGY) cp += 2.f * ep * S;
+      if (FAST && !excl) {
+        elec = k.econv_in * s14 * qiqj * invr;
+        delec = -elec * invr;
+      }
+      if (sw_on) {
+        dedr = S * dedr + dS * ep;
+        dalpha *= S;
+      }
+      g += 2.f * dedr * invr;
+      I.da += dalpha * aj;
+      J.da += dalpha * ai;
+    } else if (FAST && !excl) {
+      elec = k.econv_out * s14 * qiqj * invr;
+      delec = -elec * invr;
+    } else if (!FAST) {
+      // calcBornForces below the threshold (gbff.cpp:1308-1325): premul q_i q_j / r
+      const float ep = k.premul * qiqj * invr;
+      float dedr = -ep * invr;
+      if (ENERGY) cp += 2.f * ep * S;
+      if (sw_on) dedr = S * dedr + dS * ep;
+      g += 2.f * dedr * invr;
+    }
+    if (FAST && !excl) {
+      if (ENERGY) ce += elec * S;
+      if (sw_on) delec = S * delec + elec * dS;
+      float dvdw = 0.f;
+      if (FULL || r < k.vdwcut) {
+        const float t = (pix + pjx) * invr;
+        float B = t * t;
+        B = B * B * B;
+        const float A = B * B;
+        const float eps = piy * pjy * (is14 ? k.vdw14 : 1.f);
+        dvdw = -12.f * eps * invr * (A - B);
+        float Ev = ENERGY ? eps * (A - 2.f * B) : 0.f;
+        if (!FULL && r > k.vdwinner) {
+          if (!ENERGY) Ev = eps * (A - 2.f * B);
+          const float w = r - k.vdwinner;
+          const float sw = 1.f - w * w * k.vdwinvw2;
+          dvdw = sw * sw * dvdw + Ev * (-4.f * k.vdwinvw2 * w * sw);
+          if (ENERGY) Ev *= sw * sw;
+        }
+        if (ENERGY) cv += Ev;
+      }
+      g += (dvdw + delec) * invr;
+    }
+    I.fx += g * dx; I.fy += g * dy; I.fz += g * dz;
+    J.fx -= g * dx; J.fy -= g * dy; J.fz -= g * dz;
+  
+}
+
 template <bool MASKED, bool ENERGY, bool FULL, bool FAST = true>
 __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k, const Tile& T, int lane, int si,
                                              const float4& xi, const float4& pi, float ai, unsigned ex,
@@ -130,82 +280,9 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
       excl = (ex >> kk) & 1u;  // bond order <= 2: GB term only
       is14 = (m14 >> kk) & 1u;
     }
-    if ((FULL || r2 <= k.cut2) && pair) {
-      const float invr = rsqrtf(r2);
-      const float r = r2 * invr;
-      const float qiqj = xi.w * xj.w;
-      const float aiaj = ai * aj;
-      const float u = -0.25f * __fdividef(r2, aiaj);
-      bool gbon = u > k.thresh;
-      if (fabsf(u - k.thresh) <= 2e-6f * fabsf(k.thresh))
-        gbon = gb_on_fp64(v, si, T.bj * 32 + ((lane + kk) & 31), k.thresh_d);
-      float g = 0.f;  // scalar multiplying (xj - xi) in the force on i
-      float elec = 0.f, delec = 0.f;
-      const float s14 = is14 ? k.elec14 : 1.f;
-      const bool sw_on = !FULL && r >= k.inner;  // FULL: inside the inner cutoff
-      float S = 1.f, dS = 0.f;
-      if (sw_on) {
-        const float w = r - k.inner;
-        const float sw = 1.f - w * w * k.invw2;
-        dS = -4.f * k.invw2 * w * sw;
-        S = sw * sw;
-      }
-      if (gbon) {
-        const float tg = __expf(u);
-        const float fgb = rsqrtf(r2 + tg * aiaj);
-        const float l = fgb * fgb;
-        const float ep = k.premul * qiqj * fgb;
-        float dedr = -ep * (r - 0.25f * r * tg) * l;
-        float dalpha = -ep * tg * (1.f - u) * l;
-        if (ENERGY) cp += 2.f * ep * S;
-        if (FAST && !excl) {
-          elec = k.econv_in * s14 * qiqj * invr;
-          delec = -elec * invr;
-        }
-        if (sw_on) {
-          dedr = S * dedr + dS * ep;
-          dalpha *= S;
-        }
-        g += 2.f * dedr * invr;
-        I.da += dalpha * aj;
-        J.da += dalpha * ai;
-      } else if (FAST && !excl) {
-        elec = k.econv_out * s14 * qiqj * invr;
-        delec = -elec * invr;
-      } else if (!FAST) {
-        // calcBornForces below the threshold (gbff.cpp:1308-1325): premul q_i q_j / r
-        const float ep = k.premul * qiqj * invr;
-        float dedr = -ep * invr;
-        if (ENERGY) cp += 2.f * ep * S;
-        if (sw_on) dedr = S * dedr + dS * ep;
-        g += 2.f * dedr * invr;
-      }
-      if (FAST && !excl) {
-        if (ENERGY) ce += elec * S;
-        if (sw_on) delec = S * delec + elec * dS;
-        float dvdw = 0.f;
-        if (FULL || r < k.vdwcut) {
-          const float t = (pi.x + pj.x) * invr;
-          float B = t * t;
-          B = B * B * B;
-          const float A = B * B;
-          const float eps = pi.y * pj.y * (is14 ? k.vdw14 : 1.f);
-          dvdw = -12.f * eps * invr * (A - B);
-          float Ev = ENERGY ? eps * (A - 2.f * B) : 0.f;
-          if (!FULL && r > k.vdwinner) {
-            if (!ENERGY) Ev = eps * (A - 2.f * B);
-            const float w = r - k.vdwinner;
-            const float sw = 1.f - w * w * k.vdwinvw2;
-            dvdw = sw * sw * dvdw + Ev * (-4.f * k.vdwinvw2 * w * sw);
-            if (ENERGY) Ev *= sw * sw;
-          }
-          if (ENERGY) cv += Ev;
-        }
-        g += (dvdw + delec) * invr;
-      }
-      I.fx += g * dx; I.fy += g * dy; I.fz += g * dz;
-      J.fx -= g * dx; J.fy -= g * dy; J.fz -= g * dz;
-    }
+    if ((FULL || r2 <= k.cut2) && pair)
+      gb_pair_one<ENERGY, FULL, FAST>(v, k, dx, dy, dz, r2, xi.w, xj.w, pi.x, pi.y, pj.x, pj.y, ai, aj, excl, is14,
+                                      si, T.bj * 32 + ((lane + kk) & 31), I, J, cv, ce, cp);
     if (ENERGY && (kk & 7) == 7) {
       evdw += (double)cv;
       eel += (double)ce;
@@ -271,13 +348,70 @@ __device__ __forceinline__ void flush_gb_energy(const DevView& v, int lane, int 
   F = {0, 0, 0};
 }
 
+template <bool ENERGY, bool FULL>
+__device__ __forceinline__ void gb_pair_tile2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B,
+                                              int lane, const float* born, long long* deda, double& evdw,
+                                              double& eel, double& epol) {
+  const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
+  const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
+  const float4 pa = v.par[sa], pb = v.par[sb];
+  const float aa = born[sa], ab = born[sb];
+  float4 xr = v.xq[r0 + lane], pr = v.par[r0 + lane];
+  float ar = born[r0 + lane];
+  PairAcc IA = {0.f, 0.f, 0.f, 0.f}, IB = {0.f, 0.f, 0.f, 0.f}, R = {0.f, 0.f, 0.f, 0.f};
+  float cv = 0.f, ce = 0.f, cp = 0.f;
+#pragma unroll 2
+  for (int kk = 0; kk < 32; kk++) {
+    const int sr = r0 + ((lane + kk) & 31);
+    {
+      const float dx = xr.x - xa.x, dy = xr.y - xa.y, dz = xr.z - xa.z;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (FULL || r2 <= k.cut2)
+        gb_pair_one<ENERGY, FULL, true>(v, k, dx, dy, dz, r2, xa.w, xr.w, pa.x, pa.y, pr.x, pr.y, aa, ar, false,
+                                        false, sa, sr, IA, R, cv, ce, cp);
+    }
+    {
+      const float dx = xr.x - xb.x, dy = xr.y - xb.y, dz = xr.z - xb.z;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (FULL || r2 <= k.cut2)
+        gb_pair_one<ENERGY, FULL, true>(v, k, dx, dy, dz, r2, xb.w, xr.w, pb.x, pb.y, pr.x, pr.y, ab, ar, false,
+                                        false, sb, sr, IB, R, cv, ce, cp);
+    }
+    if (ENERGY && (kk & 7) == 7) {
+      evdw += (double)cv;
+      eel += (double)ce;
+      epol += (double)cp;
+      cv = ce = cp = 0.f;
+    }
+    ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(xr.w); ROT(pr.x); ROT(pr.y); ROT(ar);
+    ROT(R.fx); ROT(R.fy); ROT(R.fz); ROT(R.da);
+  }
+  flush_pair(v, deda, sa, IA);
+  flush_pair(v, deda, sb, IB);
+  flush_pair(v, deda, r0 + lane, R);
+}
+
 template <bool ENERGY>
-__global__ void __launch_bounds__(256, ENERGY ? 2 : 4) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
+__global__ void __launch_bounds__(256, ENERGY ? 2 : 3) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const int nt = *v.ntiles;
-  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
+  const int ni = *v.nitems;
+  for (int it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < ni; it += nwarps) {
+    bool two;
+    const int t = item_tile(v, it, two);
     const Tile T = v.tiles[t];
+    if (two) {
+      const Tile U = v.tiles[t + 1];
+      double evdw = 0.0, eel = 0.0, epol = 0.0;
+      if (tile_full(T)) gb_pair_tile2<ENERGY, true>(v, k, T, U, lane, born, deda, evdw, eel, epol);
+      else gb_pair_tile2<ENERGY, false>(v, k, T, U, lane, born, deda, evdw, eel, epol);
+      if (ENERGY) {
+        EFix EF = {0, 0, 0};
+        efix_in(EF, evdw, eel, epol);
+        flush_gb_energy(v, lane, T.bi, EF);
+      }
+      continue;
+    }
     const int si = T.bi * 32 + lane;
     const float4 xi = v.xq[si], pi = v.par[si];
     const float ai = born[si];
@@ -366,6 +500,22 @@ __global__ void k_gb_self(DevView v, const double* charge, GBConst k, double pre
 // ---------------------------------------------------------------------------
 // pass 3: dE/da chain rule through the Born radii, both directions of a pair
 // ---------------------------------------------------------------------------
+// (c_i V_j + c_j V_i) (4 CCF - dCCF) / r^6 of one pair: the chain-rule force per unit d
+__device__ __forceinline__ float chain_w(const GBConst& k, float r2, float rs, float cv) {
+  const float rdivR = __fdividef(r2, rs * rs);
+  float ccf = 1.f, dccf = 0.f;
+  if (rdivR <= k.invP5) {
+    float sn, cs;
+    const float x = rdivR * k.P5;
+    sincospif(x, &sn, &cs);
+    const float h = 0.5f - 0.5f * cs;
+    ccf = h * h;
+    dccf = 2.f * h * sn * (x * 3.14159265358979f);
+  }
+  const float ir2 = __fdividef(1.f, r2);
+  return cv * (4.f * ccf - dccf) * ir2 * ir2 * ir2;
+}
+
 template <bool MASKED, bool FULL>
 __device__ __forceinline__ void chain_tile(const DevView& v, const GBConst& k, const Tile& T, int lane, int si,
                                            const float4& xi, const float4& pi, float ci, unsigned ex,
@@ -377,27 +527,10 @@ __device__ __forceinline__ void chain_tile(const DevView& v, const GBConst& k, c
   for (int kk = 0; kk < 32; kk++) {
     const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
     const float r2 = dx * dx + dy * dy + dz * dz;
-    bool in = true;  // FULL: the whole tile lies inside the Still cutoff
-    if (!FULL) {
-      in = r2 <= k.still2;
-      if (fabsf(r2 - k.still2) <= 2e-6f * k.still2)
-        in = r2_slots_fp64(v, si, T.bj * 32 + ((lane + kk) & 31)) <= k.still2_d;
-    }
+    bool in = still_in<FULL>(v, k, r2, si, T.bj * 32 + ((lane + kk) & 31));
     if (MASKED) in = in && !((ex >> kk) & 1u);
     if (in) {
-      const float rs = pi.z + pj.z;
-      const float rdivR = __fdividef(r2, rs * rs);
-      float ccf = 1.f, dccf = 0.f;
-      if (rdivR <= k.invP5) {
-        float sn, cs;
-        const float x = rdivR * k.P5;
-        sincospif(x, &sn, &cs);
-        const float h = 0.5f - 0.5f * cs;
-        ccf = h * h;
-        dccf = 2.f * h * sn * (x * 3.14159265358979f);
-      }
-      const float ir2 = __fdividef(1.f, r2);
-      const float w = (ci * pj.w + cj * pi.w) * (4.f * ccf - dccf) * ir2 * ir2 * ir2;
+      const float w = chain_w(k, r2, pi.z + pj.z, ci * pj.w + cj * pi.w);
       I.fx -= w * dx; I.fy -= w * dy; I.fz -= w * dz;
       J.fx += w * dx; J.fy += w * dy; J.fz += w * dz;
     }
@@ -411,12 +544,58 @@ __device__ __forceinline__ void flush_force(const DevView& v, int s, const PairA
   flush_fix(v, nullptr, s, F);
 }
 
+template <bool FULL>
+__device__ __forceinline__ void chain_tile2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B, int lane,
+                                            const float* chain) {
+  const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
+  const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
+  const float4 pa = v.par[sa], pb = v.par[sb];
+  const float ca = chain[sa], cb = chain[sb];
+  float4 xr = v.xq[r0 + lane], pr = v.par[r0 + lane];
+  float cr = chain[r0 + lane];
+  PairAcc FA = {0.f, 0.f, 0.f, 0.f}, FB = {0.f, 0.f, 0.f, 0.f}, FR = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+  for (int kk = 0; kk < 32; kk++) {
+    const int sr = r0 + ((lane + kk) & 31);
+    {
+      const float dx = xr.x - xa.x, dy = xr.y - xa.y, dz = xr.z - xa.z;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (still_in<FULL>(v, k, r2, sa, sr)) {
+        const float w = chain_w(k, r2, pa.z + pr.z, ca * pr.w + cr * pa.w);
+        FA.fx -= w * dx; FA.fy -= w * dy; FA.fz -= w * dz;
+        FR.fx += w * dx; FR.fy += w * dy; FR.fz += w * dz;
+      }
+    }
+    {
+      const float dx = xr.x - xb.x, dy = xr.y - xb.y, dz = xr.z - xb.z;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (still_in<FULL>(v, k, r2, sb, sr)) {
+        const float w = chain_w(k, r2, pb.z + pr.z, cb * pr.w + cr * pb.w);
+        FB.fx -= w * dx; FB.fy -= w * dy; FB.fz -= w * dz;
+        FR.fx += w * dx; FR.fy += w * dy; FR.fz += w * dz;
+      }
+    }
+    ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(pr.z); ROT(pr.w); ROT(cr); ROT(FR.fx); ROT(FR.fy); ROT(FR.fz);
+  }
+  flush_force(v, sa, FA);
+  flush_force(v, sb, FB);
+  flush_force(v, r0 + lane, FR);
+}
+
 __global__ void __launch_bounds__(256) k_gb_chain(DevView v, GBConst k, const float* chain) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const int nt = *v.ntiles;
-  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
+  const int ni = *v.nitems;
+  for (int it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < ni; it += nwarps) {
+    bool two;
+    const int t = item_tile(v, it, two);
     const Tile T = v.tiles[t];
+    if (two) {
+      const Tile U = v.tiles[t + 1];
+      if (tile_full(T)) chain_tile2<true>(v, k, T, U, lane, chain);
+      else chain_tile2<false>(v, k, T, U, lane, chain);
+      continue;
+    }
     const int si = T.bi * 32 + lane;
     const float4 xi = v.xq[si], pi = v.par[si];
     const float ci = chain[si];

@@ -395,6 +395,32 @@ __global__ void k_pack(DevView v, const double* charge, float check2, float full
   v.xq[s] = o;
 }
 
+// GB work items: tiles t and t + 1 go together when they share the row, sit in
+// adjacent columns with bj - bi odd for the first (a fixed pairing that does not
+// depend on the other systems of a batch), are both unmasked and off-diagonal,
+// need no per-pair image and agree on the all-inside flag
+__device__ __forceinline__ bool tile_pairable(const DevView& v, int t, int nt) {
+  if (t < 0 || t + 1 >= nt) return false;
+  const Tile A = v.tiles[t], B = v.tiles[t + 1];
+  return A.bi == B.bi && B.bj == A.bj + 1 && ((A.bj - A.bi) & 1) && !tile_masked(A) && !tile_masked(B) &&
+         tile_full(A) == tile_full(B) && !((A.flags | B.flags) & 1);
+}
+
+__global__ void k_item_flags(DevView v, long long ncand, int* flag) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncand) return;
+  const int nt = *v.ntiles;
+  flag[t] = (t < nt && !tile_pairable(v, (int)t - 1, nt)) ? 1 : 0;
+}
+
+__global__ void k_item_write(DevView v, long long ncand, const int* flag, const int* pos) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncand) return;
+  if (t == ncand - 1) *v.nitems = pos[t] + flag[t];
+  if (!flag[t]) return;
+  v.items[pos[t]] = (unsigned)t | (tile_pairable(v, (int)t, *v.ntiles) ? 0x80000000u : 0u);
+}
+
 static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 int launch_list_build(Context& c, float list_radius, float full_radius) {
@@ -425,7 +451,7 @@ int launch_list_build(Context& c, float list_radius, float full_radius) {
                                                       c.has_sa ? c.d_lcpoR.p : nullptr,
                                                       c.has_sa ? c.d_lcpoUse.p : nullptr,
                                                       c.has_sa ? c.d_lc_par.p : nullptr);
-  cudaMemsetAsync(c.d_counters.p, 0, sizeof(int) * 2, st);
+  cudaMemsetAsync(c.d_counters.p, 0, sizeof(int) * 3, st);
   k_tile_flags<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, list_radius, (float)c.lp.Padding, c.d_tile_flag.p);
   {
     int nb2 = nblk(c.ncand, 1024);
@@ -437,6 +463,15 @@ int launch_list_build(Context& c, float list_radius, float full_radius) {
                                                     c.full_margin(), c.d_tile_flag.p, c.d_tile_pos.p);
   // masks: launched over the worst case; warps beyond *ntiles return at once
   k_masks<<<nblk(c.ncand * 32, 256), 256, 0, st>>>(v);
+  if (c.has_gb) {
+    c.kernel_launches += 5;
+    int nb2 = nblk(c.ncand, 1024);
+    k_item_flags<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, c.d_tile_flag.p);
+    k_scan_block<<<nb2, 1024, 0, st>>>(c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
+    k_scan_sums<<<1, 1024, 0, st>>>(c.d_scan_tmp2.p, nb2);
+    k_scan_add<<<nb2, 1024, 0, st>>>(c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
+    k_item_write<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, c.d_tile_flag.p, c.d_tile_pos.p);
+  }
   k_pack<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_charge.p, 0.f, 0.f, 1, c.ncand);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }

@@ -407,7 +407,8 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
   if (e == cudaSuccess) e = c.d_center.alloc(3 * (size_t)c.nblocks);
   if (e == cudaSuccess) e = c.d_half.alloc(c.nblocks);
   if (e == cudaSuccess) e = c.d_tiles.alloc(c.ncand);
-  if (e == cudaSuccess) e = c.d_counters.alloc(2);
+  if (e == cudaSuccess) e = c.d_counters.alloc(3);
+  if (e == cudaSuccess && c.has_gb) e = c.d_items.alloc(c.ncand);
   if (e == cudaSuccess) e = c.d_tile_flag.alloc(c.ncand);
   if (e == cudaSuccess) e = c.d_tile_pos.alloc(c.ncand);
   if (e == cudaSuccess) e = c.d_scan_tmp2.alloc((c.ncand + 1023) / 1024 + 1);

@@ -119,6 +119,10 @@ struct DevView {
   const int* far_bo;
   Tile* tiles;
   int* ntiles;
+  // GB work items over the tile list: tile index, bit 31 set when the item is the
+  // tile pair (t, t + 1) (same row, adjacent columns, both unmasked off-diagonal)
+  unsigned* items;
+  int* nitems;
   uint2* masks;              // [nmask*32] per lane: (excluded bits, 1-4 bits) in rotation order
   int* nmasks;
   long long* facc;           // [nslots*3]

@@ -80,7 +80,8 @@ struct Context {
   DBuf<float4> d_half;         // [nblocks]
   DBuf<Tile> d_tiles;          // [ncand] row-major tile list
   DBuf<int> d_tile_flag, d_tile_pos, d_scan_tmp2;  // tile-list compaction
-  DBuf<int> d_counters;        // [0] ntiles, [1] nmasks
+  DBuf<int> d_counters;        // [0] ntiles, [1] nmasks, [2] nitems
+  DBuf<unsigned> d_items;      // [ncand] GB work items (with GB only)
   DBuf<uint2> d_masks;         // [ncand*32] worst case
   DBuf<float4> d_xq, d_par, d_rel0;  // [nslots]
 
@@ -156,6 +157,8 @@ struct Context {
     v.far_bo = d_far_bo.p;
     v.tiles = d_tiles.p;
     v.ntiles = d_counters.p;
+    v.items = d_items.p;
+    v.nitems = d_counters.p + 2;
     v.masks = d_masks.p;
     v.nmasks = d_counters.p + 1;
     v.facc = d_facc.p;
