@@ -65,40 +65,52 @@ __device__ __forceinline__ void born_tile(const DevView& v, const GBConst& k, co
 // Tile pairs: two unmasked, off-diagonal tiles (bi, bj) and (bi, bj + 1) of one
 // row at once.  The shared bi block rotates through the warp and each lane keeps
 // one atom of each j block (moved into bi's frame), so one rotation of the bi
-// atom (its data and its running sums) serves two pairs instead of one.
+// atom (its data and its running sums) serves two pairs instead of one.  The two
+// pairs' arithmetic runs on packed FP32x2 instructions (.x: the atom of bj,
+// .y: the atom of bj + 1), which halves the instructions issued for it.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+
 template <bool FULL>
 __device__ __forceinline__ void born_tile2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B, int lane,
                                            long long* gpol) {
   const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
   const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
   const float4 pa = v.par[sa], pb = v.par[sb];
+  const float2 nx = make_float2(-xa.x, -xb.x), ny = make_float2(-xa.y, -xb.y), nz = make_float2(-xa.z, -xb.z);
+  const float2 RS = make_float2(pa.z, pb.z), P4 = f2(k.P4);
   float4 xr = v.xq[r0 + lane], pr = v.par[r0 + lane];
-  float ga = 0.f, gb = 0.f, gr = 0.f;
+  float2 G = f2(0.f);
+  float gr = 0.f;
 #pragma unroll 4
   for (int kk = 0; kk < 32; kk++) {
     const int sr = r0 + ((lane + kk) & 31);
-    {
-      const float dx = xr.x - xa.x, dy = xr.y - xa.y, dz = xr.z - xa.z;
-      const float r2 = dx * dx + dy * dy + dz * dz;
-      if (still_in<FULL>(v, k, r2, sa, sr)) {
-        const float w = born_w(k, r2, pa.z + pr.z);
-        ga += w * pr.w;
-        gr += w * pa.w;
-      }
+    const float2 dx = __fadd2_rn(f2(xr.x), nx), dy = __fadd2_rn(f2(xr.y), ny), dz = __fadd2_rn(f2(xr.z), nz);
+    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    const float2 rs = __fadd2_rn(RS, f2(pr.z));
+    const float2 rs2 = __fmul2_rn(rs, rs);
+    const float qa = __fdividef(r2.x, rs2.x), qb = __fdividef(r2.y, rs2.y);
+    float2 ccf = f2(1.f);
+    if (qa <= k.invP5) {
+      const float h = 0.5f - 0.5f * cospif(qa * k.P5);
+      ccf.x = h * h;
     }
-    {
-      const float dx = xr.x - xb.x, dy = xr.y - xb.y, dz = xr.z - xb.z;
-      const float r2 = dx * dx + dy * dy + dz * dz;
-      if (still_in<FULL>(v, k, r2, sb, sr)) {
-        const float w = born_w(k, r2, pb.z + pr.z);
-        gb += w * pr.w;
-        gr += w * pb.w;
-      }
+    if (qb <= k.invP5) {
+      const float h = 0.5f - 0.5f * cospif(qb * k.P5);
+      ccf.y = h * h;
     }
+    const float2 ir2 = make_float2(__fdividef(1.f, r2.x), __fdividef(1.f, r2.y));
+    float2 w = __fmul2_rn(__fmul2_rn(P4, ccf), __fmul2_rn(ir2, ir2));
+    if (!FULL) {
+      if (!still_in<false>(v, k, r2.x, sa, sr)) w.x = 0.f;
+      if (!still_in<false>(v, k, r2.y, sb, sr)) w.y = 0.f;
+    }
+    G = __ffma2_rn(w, f2(pr.w), G);
+    gr = fmaf(w.x, pa.w, gr);
+    gr = fmaf(w.y, pb.w, gr);
     ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(pr.z); ROT(pr.w); ROT(gr);
   }
-  atomic_add_ll(&gpol[sa], fx32(ga));
-  atomic_add_ll(&gpol[sb], fx32(gb));
+  atomic_add_ll(&gpol[sa], fx32(G.x));
+  atomic_add_ll(&gpol[sb], fx32(G.y));
   atomic_add_ll(&gpol[r0 + lane], fx32(gr));
 }
 
@@ -391,6 +403,93 @@ __device__ __forceinline__ void gb_pair_tile2(const DevView& v, const GBConst& k
   flush_pair(v, deda, r0 + lane, R);
 }
 
+// gb_pair_tile2 for a tile pair whose pairs all lie inside every cutoff and switch
+// radius (no switching, LJ everywhere; unmasked: no exclusions, no 1-4 scaling),
+// the all-pairs case, on packed FP32x2 arithmetic, used for the energy variant.
+// The GB part runs when either pair of the lane is above the exp threshold and is
+// kept per pair by a select.
+template <bool ENERGY>
+__device__ __forceinline__ void gb_pair_full2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B,
+                                              int lane, const float* born, long long* deda, double& evdw,
+                                              double& eel, double& epol) {
+  const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
+  const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
+  const float4 pa = v.par[sa], pb = v.par[sb];
+  const float2 nx = make_float2(-xa.x, -xb.x), ny = make_float2(-xa.y, -xb.y), nz = make_float2(-xa.z, -xb.z);
+  const float2 QS = make_float2(xa.w, xb.w), SG = make_float2(pa.x, pb.x), EP = make_float2(pa.y, pb.y);
+  const float2 AS = make_float2(born[sa], born[sb]);
+  const float tol = 2e-6f * fabsf(k.thresh);
+  float4 xr = v.xq[r0 + lane], pr = v.par[r0 + lane];
+  float ar = born[r0 + lane];
+  float2 FX = f2(0.f), FY = f2(0.f), FZ = f2(0.f), DA = f2(0.f);  // the two j atoms' sums
+  PairAcc R = {0.f, 0.f, 0.f, 0.f};                                 // the rotating atom's sums
+  float2 CV = f2(0.f), CE = f2(0.f), CP = f2(0.f);                  // (ENERGY) over 8 steps
+#pragma unroll 2
+  for (int kk = 0; kk < 32; kk++) {
+    const float2 dx = __fadd2_rn(f2(xr.x), nx), dy = __fadd2_rn(f2(xr.y), ny), dz = __fadd2_rn(f2(xr.z), nz);
+    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    const float2 invr = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+    const float2 qq = __fmul2_rn(QS, f2(xr.w));
+    const float2 aa = __fmul2_rn(AS, f2(ar));
+    const float2 u = __fmul2_rn(f2(-0.25f), make_float2(__fdividef(r2.x, aa.x), __fdividef(r2.y, aa.y)));
+    bool gx = u.x > k.thresh, gy = u.y > k.thresh;
+    const float2 du = __fadd2_rn(u, f2(-k.thresh));
+    if (fabsf(du.x) <= tol) gx = gb_on_fp64(v, sa, r0 + ((lane + kk) & 31), k.thresh_d);
+    if (fabsf(du.y) <= tol) gy = gb_on_fp64(v, sb, r0 + ((lane + kk) & 31), k.thresh_d);
+    // Coulomb with eps_in above the threshold, eps_out below; en = -E_elec
+    const float2 en = __fmul2_rn(__fmul2_rn(make_float2(gx ? -k.econv_in : -k.econv_out,
+                                                        gy ? -k.econv_in : -k.econv_out), qq), invr);
+    float2 g = f2(0.f), dal = f2(0.f);
+    if (gx || gy) {
+      const float2 r = __fmul2_rn(r2, invr);
+      const float2 tg = make_float2(__expf(u.x), __expf(u.y));
+      const float2 t = __ffma2_rn(tg, aa, r2);
+      const float2 fgb = make_float2(rsqrtf(t.x), rsqrtf(t.y));
+      const float2 l = __fmul2_rn(fgb, fgb);
+      const float2 nep = __fmul2_rn(__fmul2_rn(f2(-k.premul), qq), fgb);  // -E_GB pair factor
+      const float2 dedr = __fmul2_rn(__fmul2_rn(nep, __fmul2_rn(r, __ffma2_rn(f2(-0.25f), tg, f2(1.f)))), l);
+      const float2 da = __fmul2_rn(__fmul2_rn(__fmul2_rn(nep, tg), __ffma2_rn(u, f2(-1.f), f2(1.f))), l);
+      const float2 gg = __fmul2_rn(__fmul2_rn(f2(2.f), dedr), invr);
+      g = make_float2(gx ? gg.x : 0.f, gy ? gg.y : 0.f);
+      dal = make_float2(gx ? da.x : 0.f, gy ? da.y : 0.f);
+      if (ENERGY) CP = __ffma2_rn(f2(-2.f), make_float2(gx ? nep.x : 0.f, gy ? nep.y : 0.f), CP);
+    }
+    // LJ
+    const float2 tt = __fmul2_rn(__fadd2_rn(SG, f2(pr.x)), invr);
+    const float2 b2 = __fmul2_rn(tt, tt);
+    const float2 b6 = __fmul2_rn(__fmul2_rn(b2, b2), b2);
+    const float2 a12 = __fmul2_rn(b6, b6);
+    const float2 eps = __fmul2_rn(EP, f2(pr.y));
+    const float2 dv = __fmul2_rn(__fmul2_rn(__fmul2_rn(f2(-12.f), eps), invr), __ffma2_rn(b6, f2(-1.f), a12));
+    if (ENERGY) {
+      CV = __ffma2_rn(eps, __ffma2_rn(b6, f2(-2.f), a12), CV);
+      CE = __ffma2_rn(en, f2(-1.f), CE);
+    }
+    // g: dE/dr / r;  dE_elec/dr = -E_elec / r = en / r
+    g = __ffma2_rn(__ffma2_rn(en, invr, dv), invr, g);
+    FX = __ffma2_rn(g, dx, FX);
+    FY = __ffma2_rn(g, dy, FY);
+    FZ = __ffma2_rn(g, dz, FZ);
+    R.fx = fmaf(-g.x, dx.x, R.fx); R.fx = fmaf(-g.y, dx.y, R.fx);
+    R.fy = fmaf(-g.x, dy.x, R.fy); R.fy = fmaf(-g.y, dy.y, R.fy);
+    R.fz = fmaf(-g.x, dz.x, R.fz); R.fz = fmaf(-g.y, dz.y, R.fz);
+    DA = __ffma2_rn(dal, f2(ar), DA);
+    R.da = fmaf(dal.x, AS.x, R.da);
+    R.da = fmaf(dal.y, AS.y, R.da);
+    if (ENERGY && (kk & 7) == 7) {
+      evdw += (double)CV.x + (double)CV.y;
+      eel += (double)CE.x + (double)CE.y;
+      epol += (double)CP.x + (double)CP.y;
+      CV = CE = CP = f2(0.f);
+    }
+    ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(xr.w); ROT(pr.x); ROT(pr.y); ROT(ar);
+    ROT(R.fx); ROT(R.fy); ROT(R.fz); ROT(R.da);
+  }
+  flush_pair(v, deda, sa, PairAcc{FX.x, FY.x, FZ.x, DA.x});
+  flush_pair(v, deda, sb, PairAcc{FX.y, FY.y, FZ.y, DA.y});
+  flush_pair(v, deda, r0 + lane, R);
+}
+
 template <bool ENERGY>
 __global__ void __launch_bounds__(256, ENERGY ? 2 : 3) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
   const int lane = threadIdx.x & 31;
@@ -403,8 +502,13 @@ __global__ void __launch_bounds__(256, ENERGY ? 2 : 3) k_gb_pair(DevView v, GBCo
     if (two) {
       const Tile U = v.tiles[t + 1];
       double evdw = 0.0, eel = 0.0, epol = 0.0;
-      if (tile_full(T)) gb_pair_tile2<ENERGY, true>(v, k, T, U, lane, born, deda, evdw, eel, epol);
-      else gb_pair_tile2<ENERGY, false>(v, k, T, U, lane, born, deda, evdw, eel, epol);
+      // (the packed body issues fewer instructions only where the energies ride along)
+      if (tile_full(T)) {
+        if (ENERGY) gb_pair_full2<true>(v, k, T, U, lane, born, deda, evdw, eel, epol);
+        else gb_pair_tile2<false, true>(v, k, T, U, lane, born, deda, evdw, eel, epol);
+      } else {
+        gb_pair_tile2<ENERGY, false>(v, k, T, U, lane, born, deda, evdw, eel, epol);
+      }
       if (ENERGY) {
         EFix EF = {0, 0, 0};
         efix_in(EF, evdw, eel, epol);
@@ -550,35 +654,54 @@ __device__ __forceinline__ void chain_tile2(const DevView& v, const GBConst& k, 
   const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
   const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
   const float4 pa = v.par[sa], pb = v.par[sb];
-  const float ca = chain[sa], cb = chain[sb];
+  const float2 nx = make_float2(-xa.x, -xb.x), ny = make_float2(-xa.y, -xb.y), nz = make_float2(-xa.z, -xb.z);
+  const float2 RS = make_float2(pa.z, pb.z), VS = make_float2(pa.w, pb.w);
+  const float2 CS = make_float2(chain[sa], chain[sb]);
   float4 xr = v.xq[r0 + lane], pr = v.par[r0 + lane];
   float cr = chain[r0 + lane];
-  PairAcc FA = {0.f, 0.f, 0.f, 0.f}, FB = {0.f, 0.f, 0.f, 0.f}, FR = {0.f, 0.f, 0.f, 0.f};
+  float2 FX = f2(0.f), FY = f2(0.f), FZ = f2(0.f);  // the two j atoms' sums
+  PairAcc FR = {0.f, 0.f, 0.f, 0.f};               // the rotating atom's sums
 #pragma unroll 4
   for (int kk = 0; kk < 32; kk++) {
     const int sr = r0 + ((lane + kk) & 31);
-    {
-      const float dx = xr.x - xa.x, dy = xr.y - xa.y, dz = xr.z - xa.z;
-      const float r2 = dx * dx + dy * dy + dz * dz;
-      if (still_in<FULL>(v, k, r2, sa, sr)) {
-        const float w = chain_w(k, r2, pa.z + pr.z, ca * pr.w + cr * pa.w);
-        FA.fx -= w * dx; FA.fy -= w * dy; FA.fz -= w * dz;
-        FR.fx += w * dx; FR.fy += w * dy; FR.fz += w * dz;
-      }
+    const float2 dx = __fadd2_rn(f2(xr.x), nx), dy = __fadd2_rn(f2(xr.y), ny), dz = __fadd2_rn(f2(xr.z), nz);
+    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    const float2 rs = __fadd2_rn(RS, f2(pr.z));
+    const float2 rs2 = __fmul2_rn(rs, rs);
+    const float qa = __fdividef(r2.x, rs2.x), qb = __fdividef(r2.y, rs2.y);
+    float2 fac = f2(4.f);  // 4 CCF - dCCF
+    if (qa <= k.invP5) {
+      float sn, cs;
+      const float x = qa * k.P5;
+      sincospif(x, &sn, &cs);
+      const float h = 0.5f - 0.5f * cs;
+      fac.x = 4.f * h * h - 2.f * h * sn * (x * 3.14159265358979f);
     }
-    {
-      const float dx = xr.x - xb.x, dy = xr.y - xb.y, dz = xr.z - xb.z;
-      const float r2 = dx * dx + dy * dy + dz * dz;
-      if (still_in<FULL>(v, k, r2, sb, sr)) {
-        const float w = chain_w(k, r2, pb.z + pr.z, cb * pr.w + cr * pb.w);
-        FB.fx -= w * dx; FB.fy -= w * dy; FB.fz -= w * dz;
-        FR.fx += w * dx; FR.fy += w * dy; FR.fz += w * dz;
-      }
+    if (qb <= k.invP5) {
+      float sn, cs;
+      const float x = qb * k.P5;
+      sincospif(x, &sn, &cs);
+      const float h = 0.5f - 0.5f * cs;
+      fac.y = 4.f * h * h - 2.f * h * sn * (x * 3.14159265358979f);
     }
+    const float2 ir2 = make_float2(__fdividef(1.f, r2.x), __fdividef(1.f, r2.y));
+    const float2 cvv = __ffma2_rn(CS, f2(pr.w), __fmul2_rn(f2(cr), VS));
+    float2 w = __fmul2_rn(__fmul2_rn(cvv, fac), __fmul2_rn(__fmul2_rn(ir2, ir2), ir2));
+    if (!FULL) {
+      if (!still_in<false>(v, k, r2.x, sa, sr)) w.x = 0.f;
+      if (!still_in<false>(v, k, r2.y, sb, sr)) w.y = 0.f;
+    }
+    const float2 nw = __fmul2_rn(w, f2(-1.f));
+    FX = __ffma2_rn(nw, dx, FX);
+    FY = __ffma2_rn(nw, dy, FY);
+    FZ = __ffma2_rn(nw, dz, FZ);
+    FR.fx = fmaf(w.x, dx.x, FR.fx); FR.fx = fmaf(w.y, dx.y, FR.fx);
+    FR.fy = fmaf(w.x, dy.x, FR.fy); FR.fy = fmaf(w.y, dy.y, FR.fy);
+    FR.fz = fmaf(w.x, dz.x, FR.fz); FR.fz = fmaf(w.y, dz.y, FR.fz);
     ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(pr.z); ROT(pr.w); ROT(cr); ROT(FR.fx); ROT(FR.fy); ROT(FR.fz);
   }
-  flush_force(v, sa, FA);
-  flush_force(v, sb, FB);
+  flush_force(v, sa, PairAcc{FX.x, FY.x, FZ.x, 0.f});
+  flush_force(v, sb, PairAcc{FX.y, FY.y, FZ.y, 0.f});
   flush_force(v, r0 + lane, FR);
 }
 
