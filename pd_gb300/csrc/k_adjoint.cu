@@ -14,12 +14,15 @@
 // which differs from it by the Born offset and by 166 vs halfeconv.
 //
 // Layout: the same tiles and slots as the force kernels.  Pair distances and
-// most pair terms are FP32; the Coulomb energy per unit charge product is formed
-// in FP64 (the force-switch form cancels badly in FP32) and every per-tile sum
-// is FP64, entered into 64-bit fixed point (2^32 per kcal/mol per parameter
-// unit), so the result does not depend on scheduling.  A charge gradient is a
-// potential: a sum of many terms of both signs, which FP32 sums do not resolve
-// to the 1e-4 a parameter fit checks against.
+// most pair terms are FP32; for FF_NonBonded the Coulomb energy per unit charge
+// product is formed in FP64 (the force-switch form cancels badly in FP32).  A
+// charge gradient is a potential: a sum of many terms of both signs, which plain
+// FP32 sums do not resolve to the 1e-4 a parameter fit checks against.  The GB
+// kernels therefore sum per tile in compensated FP32 (value plus running
+// rounding error, about 48 significant bits, on the FP32 pipe: GB300's FP64 rate
+// is a small fraction of its FP32 rate), the NB kernel in FP64.  Per-tile sums
+// enter 64-bit fixed point (2^32 per kcal/mol per parameter unit), so the result
+// does not depend on scheduling.
 #include "pdgpu_tile.cuh"
 
 namespace pdgpu {
@@ -31,6 +34,35 @@ struct Acc3 {
 };
 
 __device__ __forceinline__ long long fix_sum_d(double x) { return __double2ll_rn(x * kSumScale); }
+
+// Compensated FP32 sum: hi carries the running sum and lo the rounding errors
+// of its additions, each recovered exactly by Knuth's TwoSum (the _rn
+// intrinsics keep the compiler from contracting or reordering the steps).
+struct CSum {
+  float hi, lo;
+};
+
+__device__ __forceinline__ void csum_add(CSum& c, float x) {
+  const float s = __fadd_rn(c.hi, x);
+  const float bb = __fsub_rn(s, c.hi);
+  const float e = __fadd_rn(__fsub_rn(c.hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+  c.lo = __fadd_rn(c.lo, e);
+  c.hi = s;
+}
+
+__device__ __forceinline__ double csum_value(const CSum& c) { return (double)c.hi + (double)c.lo; }
+
+struct CAcc3 {
+  CSum a, b, c;
+};
+
+__device__ __forceinline__ Acc3 cacc_value(const CAcc3& x) {
+  return Acc3{csum_value(x.a), csum_value(x.b), csum_value(x.c)};
+}
+
+#define ROT_CSUM(x) \
+  ROT(x.hi);        \
+  ROT(x.lo)
 
 __device__ __forceinline__ void acc_flush(const DevView& v, long long* g0, long long* g1, long long* g2, int s,
                                           const Acc3& x) {
@@ -58,7 +90,7 @@ __device__ __forceinline__ float lj_dR(float R, float invr) {
 template <bool MASKED>
 __device__ __forceinline__ void adj_gb_tile(const DevView& v, const GBConst& k, const Tile& T, int lane, int si,
                                             const float4& xi, const float4& pi, float ai, unsigned ex, unsigned m14,
-                                            unsigned dmask, const float* born, Acc3& I, Acc3& J) {
+                                            unsigned dmask, const float* born, CAcc3& I, CAcc3& J) {
   float4 xj = j_in_i_frame(v, T, lane);
   float4 pj = v.par[T.bj * 32 + lane];
   float aj = born[T.bj * 32 + lane];
@@ -97,8 +129,8 @@ __device__ __forceinline__ void adj_gb_tile(const DevView& v, const GBConst& k, 
       } else if (!excl) {
         phi = k.econv_out * s14 * invr * S;
       }
-      I.a += (double)(phi * xj.w);
-      J.a += (double)(phi * xi.w);
+      csum_add(I.a, phi * xj.w);
+      csum_add(J.a, phi * xi.w);
       if (!excl && r < k.vdwcut) {
         const float R = pi.x + pj.x;
         const float t = R * invr;
@@ -112,14 +144,14 @@ __device__ __forceinline__ void adj_gb_tile(const DevView& v, const GBConst& k, 
         }
         const float e1 = (B * B - 2.f * B) * Sv;  // energy per unit sqrt(eps_i) sqrt(eps_j)
         const float dR = lj_dR(R, invr) * Sv * pi.y * pj.y;
-        I.b += (double)dR;
-        J.b += (double)dR;
-        I.c += (double)(e1 * pj.y);
-        J.c += (double)(e1 * pi.y);
+        csum_add(I.b, dR);
+        csum_add(J.b, dR);
+        csum_add(I.c, e1 * pj.y);
+        csum_add(J.c, e1 * pi.y);
       }
     }
     ROT(xj.x); ROT(xj.y); ROT(xj.z); ROT(xj.w); ROT(pj.x); ROT(pj.y); ROT(aj);
-    ROT(J.a); ROT(J.b); ROT(J.c);
+    ROT_CSUM(J.a); ROT_CSUM(J.b); ROT_CSUM(J.c);
   }
 }
 
@@ -136,11 +168,11 @@ __global__ void __launch_bounds__(256) k_adj_gb_pair(DevView v, GBConst k, const
     unsigned ex, m14;
     tile_masks(v, T, lane, ex, m14);
     const unsigned dmask = (T.flags & 2) ? diag_exclusion(lane) : 0u;
-    Acc3 I = {0.0, 0.0, 0.0}, J = {0.0, 0.0, 0.0};
+    CAcc3 I = {}, J = {};
     if (tile_masked(T)) adj_gb_tile<true>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J);
     else adj_gb_tile<false>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J);
-    acc_flush(v, gq, gr, ge, si, I);
-    acc_flush(v, gq, gr, ge, T.bj * 32 + lane, J);
+    acc_flush(v, gq, gr, ge, si, cacc_value(I));
+    acc_flush(v, gq, gr, ge, T.bj * 32 + lane, cacc_value(J));
   }
 }
 
@@ -151,7 +183,7 @@ __global__ void __launch_bounds__(256) k_adj_gb_pair(DevView v, GBConst k, const
 template <bool MASKED>
 __device__ __forceinline__ void adj_born_tile(const DevView& v, const GBConst& k, const Tile& T, int lane, int si,
                                               const float4& xi, const float4& pi, float wi, unsigned ex,
-                                              const float* w, Acc3& I, Acc3& J) {
+                                              const float* w, CAcc3& I, CAcc3& J) {
   float4 xj = j_in_i_frame(v, T, lane);
   float4 pj = v.par[T.bj * 32 + lane];
   float wj = w[T.bj * 32 + lane];
@@ -176,13 +208,13 @@ __device__ __forceinline__ void adj_born_tile(const DevView& v, const GBConst& k
       }
       const float ir2 = __fdividef(1.f, r2);
       const float h4 = k.P4 * ir2 * ir2;
-      I.b += (double)(wj * h4 * ccf);  // dE/dV_i from Gpol_j
-      J.b += (double)(wi * h4 * ccf);  // dE/dV_j from Gpol_i
+      csum_add(I.b, wj * h4 * ccf);  // dE/dV_i from Gpol_j
+      csum_add(J.b, wi * h4 * ccf);  // dE/dV_j from Gpol_i
       const float gR = (wi * pj.w + wj * pi.w) * h4 * dccf * (-2.f * __fdividef(x, rs));
-      I.a += (double)gR;
-      J.a += (double)gR;
+      csum_add(I.a, gR);
+      csum_add(J.a, gR);
     }
-    ROT(xj.x); ROT(xj.y); ROT(xj.z); ROT(pj.z); ROT(pj.w); ROT(wj); ROT(J.a); ROT(J.b);
+    ROT(xj.x); ROT(xj.y); ROT(xj.z); ROT(pj.z); ROT(pj.w); ROT(wj); ROT_CSUM(J.a); ROT_CSUM(J.b);
   }
 }
 
@@ -199,11 +231,11 @@ __global__ void __launch_bounds__(256) k_adj_born(DevView v, GBConst k, const fl
     unsigned ex, m14;
     tile_masks(v, T, lane, ex, m14);
     if (T.flags & 2) ex |= diag_exclusion(lane);
-    Acc3 I = {0.0, 0.0, 0.0}, J = {0.0, 0.0, 0.0};
+    CAcc3 I = {}, J = {};
     if (tile_masked(T)) adj_born_tile<true>(v, k, T, lane, si, xi, pi, wi, ex, w, I, J);
     else adj_born_tile<false>(v, k, T, lane, si, xi, pi, wi, ex, w, I, J);
-    acc_flush(v, gR, gV, nullptr, si, I);
-    acc_flush(v, gR, gV, nullptr, T.bj * 32 + lane, J);
+    acc_flush(v, gR, gV, nullptr, si, cacc_value(I));
+    acc_flush(v, gR, gV, nullptr, T.bj * 32 + lane, cacc_value(J));
   }
 }
 
