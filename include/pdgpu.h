@@ -205,7 +205,9 @@ typedef struct {
 } pdgpu_param_grads;
 int pdgpu_param_grad(pdgpu_ctx *ctx, unsigned what, pdgpu_energies *out, const pdgpu_param_grads *g);
 /* Device-array form: queued on the context stream; energies stay on the device
- * until pdgpu_get_energies(), status via pdgpu_synchronize(). */
+ * until pdgpu_get_energies(), status via pdgpu_synchronize().  The gradient
+ * calls evaluate energies only: forces read after one of them are not the
+ * system's forces until the next force evaluation. */
 int pdgpu_param_grad_device(pdgpu_ctx *ctx, unsigned what, const pdgpu_param_grads *d_g);
 /* Same result as pdgpu_param_grad_device, with no device allocation in the
  * call.  It has no counterpart in PD.  It is for hosts that cannot let a call

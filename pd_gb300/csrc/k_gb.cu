@@ -766,7 +766,8 @@ int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset
     k_gb_pair<false><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
   }
   k_gb_self<<<nb, 256, 0, st>>>(v, c.d_charge.p, k, premul, c.d_deda.p, c.d_born_d.p, c.d_chain_f.p);
-  k_gb_chain<<<g, 256, 0, st>>>(v, k, c.d_chain_f.p);
+  if (c.gb_no_chain) c.kernel_launches -= 1;
+  else k_gb_chain<<<g, 256, 0, st>>>(v, k, c.d_chain_f.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

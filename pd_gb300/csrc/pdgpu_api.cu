@@ -506,6 +506,15 @@ int pdgpu_set_list_params(pdgpu_ctx* h, const pdgpu_list_params* p) {
 
 static int enqueue_compute(Context& c, unsigned what, bool energy);
 
+// the energy pass a parameter gradient reads (Born radii, Gpol sums, dE/da and
+// energies); the GB chain-rule pass only forms forces and is left out
+static int enqueue_grad_energies(Context& c, unsigned what) {
+  c.gb_no_chain = true;
+  const int st = enqueue_compute(c, what & ~PDGPU_ENERGY, true);
+  c.gb_no_chain = false;
+  return st;
+}
+
 int pdgpu_update_params(pdgpu_ctx* h, const double* charge, const double* radius, const double* epsilon,
                         const double* gb_radius, const double* gb_vj, const double* gb_terms123) {
   if (!h) return PDGPU_ERR_ARG;
@@ -639,7 +648,7 @@ int pdgpu_param_grad_device(pdgpu_ctx* h, unsigned what, const pdgpu_param_grads
   int st = param_grad_check(c, what);
   if (st != PDGPU_OK) return st;
   CK(cudaSetDevice(c.device));
-  st = enqueue_compute(c, what & ~PDGPU_ENERGY, true);
+  st = enqueue_grad_energies(c, what);
   if (st != PDGPU_OK) return st;
   return launch_adjoint(c, what, g->charge, g->radius, g->epsilon, g->gb_radius, g->gb_vj, g->gb_terms123);
 }
@@ -651,7 +660,7 @@ int pdgpu_param_grad_device_noalloc(pdgpu_ctx* h, unsigned what, const pdgpu_par
   if (st != PDGPU_OK) return st;
   if (c.nslots > kNoAllocMaxSlots) return PDGPU_ERR_CAPACITY;
   CK(cudaSetDevice(c.device));
-  st = enqueue_compute(c, what & ~PDGPU_ENERGY, true);
+  st = enqueue_grad_energies(c, what);
   if (st != PDGPU_OK) return st;
   return launch_adjoint_static(c, what, g->charge, g->radius, g->epsilon, g->gb_radius, g->gb_vj, g->gb_terms123);
 }
@@ -667,7 +676,7 @@ int pdgpu_param_grad(pdgpu_ctx* h, unsigned what, pdgpu_energies* out, const pdg
   double* host[6] = {g->charge, g->radius, g->epsilon, g->gb_radius, g->gb_vj, g->gb_terms123};
   double* dev[6];
   for (int k = 0; k < 6; k++) dev[k] = host[k] ? c.d_adj_out.p + k * N : nullptr;
-  st = enqueue_compute(c, what & ~PDGPU_ENERGY, true);
+  st = enqueue_grad_energies(c, what);
   if (st != PDGPU_OK) return st;
   st = launch_adjoint(c, what, dev[0], dev[1], dev[2], dev[3], dev[4], dev[5]);
   if (st != PDGPU_OK) return st;

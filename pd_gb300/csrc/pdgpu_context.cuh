@@ -42,6 +42,7 @@ struct Context {
   pdgpu_list_params lp{};
   bool nb_set = false, gb_set = false;
   bool gb_fast = true;             // FF_GeneralizedBorn_Still::FastMode
+  bool gb_no_chain = false;        // energies only: skip the GB chain-rule (force) pass
   pdgpu_nb_params gb_vac{};        // the GB object's own FF_NonBonded settings (FastMode off, calcEnergies)
   bool gb_vac_set = false;
   float list_radius_built = 0.f;
