@@ -564,13 +564,13 @@ def run_e2e(args, key, wl, image, torch, update_nlist):
     pos_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
     steps = max(3, min(args.steps, 50))
     ctx.md_run(3)
-    pos_h[:] = ctx.get_positions()
+    ctx.get_positions(out=pos_h)
     t0 = time.perf_counter()
     for _ in range(steps):
         ctx.set_positions(pos_h)
         ctx.md_run(1)
         ctx.kinetic()
-        pos_h[:] = ctx.get_positions()
+        ctx.get_positions(out=pos_h)
     el = time.perf_counter() - t0
     ctx.close()
     return {"value": n * steps / el, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * n,

@@ -692,7 +692,7 @@ int pdgpu_set_positions(pdgpu_ctx* h, const double* xyz, size_t stride) {
   if (!h || !xyz || stride < 24 || stride % 8) return PDGPU_ERR_ARG;
   Context& c = h->c;
   CK(cudaSetDevice(c.device));
-  CK(cudaMemcpy2DAsync(c.d_pos.p, 24, xyz, stride, 24, c.natom, cudaMemcpyHostToDevice, c.stream));
+  CK(copy_xyz_rows(c.d_pos.p, 24, xyz, stride, c.natom, cudaMemcpyHostToDevice, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   c.positions_set = true;
   return PDGPU_OK;
@@ -711,7 +711,7 @@ int pdgpu_get_positions(pdgpu_ctx* h, double* xyz, size_t stride) {
   if (!h || !xyz || stride < 24 || stride % 8) return PDGPU_ERR_ARG;
   Context& c = h->c;
   CK(cudaSetDevice(c.device));
-  CK(cudaMemcpy2DAsync(xyz, stride, c.d_pos.p, 24, 24, c.natom, cudaMemcpyDeviceToHost, c.stream));
+  CK(copy_xyz_rows(xyz, stride, c.d_pos.p, 24, c.natom, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   return PDGPU_OK;
 }

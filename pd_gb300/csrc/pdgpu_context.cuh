@@ -169,6 +169,15 @@ struct Context {
   }
 };
 
+// n rows of 3 doubles between a packed device array and a host array with
+// `pitch` bytes per row: one contiguous copy when the host rows are packed as
+// well (a 2D copy of 24-byte rows moves row by row, far below copy bandwidth)
+inline cudaError_t copy_xyz_rows(void* dst, size_t dpitch, const void* src, size_t spitch, size_t n,
+                                 cudaMemcpyKind kind, cudaStream_t st) {
+  if (dpitch == 24 && spitch == 24) return cudaMemcpyAsync(dst, src, 24 * n, kind, st);
+  return cudaMemcpy2DAsync(dst, dpitch, src, spitch, 24, n, kind, st);
+}
+
 // unit conversions (PD PhysicsConst, src/mmlib/forcefields/forcefield.cpp:35-55)
 constexpr double kKcal2J = 4184.0;
 constexpr double kNa = 6.0221418E23;

@@ -225,7 +225,7 @@ int pdgpu_set_velocities(pdgpu_ctx* h, const double* v, size_t stride) {
   Context& c = h->c;
   if (!c.md) return PDGPU_ERR_STATE;
   CK(cudaSetDevice(c.device));
-  CK(cudaMemcpy2DAsync(c.md->d_vel.p, 24, v, stride, 24, c.natom, cudaMemcpyHostToDevice, c.stream));
+  CK(copy_xyz_rows(c.md->d_vel.p, 24, v, stride, c.natom, cudaMemcpyHostToDevice, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   return PDGPU_OK;
 }
@@ -235,7 +235,7 @@ int pdgpu_get_velocities(pdgpu_ctx* h, double* v, size_t stride) {
   Context& c = h->c;
   if (!c.md) return PDGPU_ERR_STATE;
   CK(cudaSetDevice(c.device));
-  CK(cudaMemcpy2DAsync(v, stride, c.md->d_vel.p, 24, 24, c.natom, cudaMemcpyDeviceToHost, c.stream));
+  CK(copy_xyz_rows(v, stride, c.md->d_vel.p, 24, c.natom, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   return PDGPU_OK;
 }

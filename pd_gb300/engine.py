@@ -145,8 +145,13 @@ class DeviceContext:
     def set_positions_device(self, ptr):
         ffi.check(self.lib.pdgpu_set_positions_device(self.h, ctypes.c_void_p(ptr)), "pdgpu_set_positions_device")
 
-    def get_positions(self):
-        out = np.zeros((self.natom, 3))
+    def get_positions(self, out=None):
+        """Positions (A) of every atom; `out`, if given, is a C-contiguous float64
+        (natom, 3) array filled in place (a page-locked one takes the direct DMA path)."""
+        if out is None:
+            out = np.zeros((self.natom, 3))
+        elif out.dtype != np.float64 or out.shape != (self.natom, 3) or not out.flags.c_contiguous:
+            raise ValueError("get_positions: out must be a C-contiguous float64 array of shape (%d, 3)" % self.natom)
         ffi.check(self.lib.pdgpu_get_positions(self.h, _pd(out), 24), "pdgpu_get_positions")
         return out
 
