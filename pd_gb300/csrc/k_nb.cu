@@ -87,16 +87,22 @@ __device__ __forceinline__ void nb_tile(const DevView& v, const NBConst& k, cons
     bool listed = true;
     if (MASKED) listed = !((ex >> kk) & 1u);
     bool in = r2 <= k.cut2;
-    double r2d = 0.0;
-    if (listed && (ENERGY || fabsf(r2 - k.cut2) <= 2e-6f * k.cut2 || fabsf(r2 - k.vdwcut2) <= 2e-6f * k.vdwcut2)) {
-      r2d = nb_r2_fp64(v, S, si, T.bj * 32 + ((lane + kk) & 31));
-      in = r2d <= k.cut2_dd;
+    double r2d = 0.0;  // (ENERGY) the pair's FP64 squared distance
+    if (ENERGY) {
+      if (listed) {
+        r2d = nb_r2_fp64(v, S, si, T.bj * 32 + ((lane + kk) & 31));
+        in = r2d <= k.cut2_dd;
+      }
+    } else if (listed && (fabsf(r2 - k.cut2) <= 2e-6f * k.cut2 || fabsf(r2 - k.vdwcut2) <= 2e-6f * k.vdwcut2)) {
+      // at a hard cutoff: decide, and take the distance, in FP64 (FP64 work only on this branch)
+      const double d2 = nb_r2_fp64(v, S, si, T.bj * 32 + ((lane + kk) & 31));
+      in = d2 <= k.cut2_dd;
+      r2 = (float)d2;
     }
     if (listed && in) {
       const bool is14 = MASKED && ((m14 >> kk) & 1u);
       const float eps = pi.y * pj.y * (is14 ? k.vdw14 : 1.f);
       const float qq = qi * xj.w * (is14 ? k.elec14 : 1.f);
-      if (r2d > 0.0 && !ENERGY) r2 = (float)r2d;
       const float fs = nb_force_f<ELEC>(k, r2, pi.x + pj.x, eps, qq);
       if (ENERGY) {
         // energy of this pair in FP64 from FP64 positions and parameters
