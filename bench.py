@@ -21,7 +21,6 @@ no exchange between GPUs); rank 0 prints one JSON line.
 """
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -160,11 +159,23 @@ def gb_settings(image):
                 ExpApproxThreshold=-4.0, BornRadiusOffset=0.0, P4=P[3], P5=P[4])
 
 
+NB_CUTOFF = 12.0   # FF_NonBonded Cutoff and VdwCutoff of the C1/C2 workloads (A)
+
+# DRAM bytes (read + write) per launch of the roofline kernels, from one ncu
+# capture of each workload (profiles/traffic_roofline_kernels.md)
+NCU_TRAFFIC = {
+    "c4": {"k_gb_pair": 41.33e6, "k_langevin": 23.55e6},
+    "c3": {"k_gb_pair": 0.85e6, "k_langevin": 0.50e6},
+    "c2": {"k_nb_tiles": 4.22e6, "k_langevin": 2.00e6},
+    "c1": {"k_nb_tiles": 0.30e6},
+}
+
+
 def configure(ctx, wl, image):
     """Component parameters of each workload (PD attribute names)."""
     s14v, s14e = image.scaling14
     if "NB" in wl["what"]:
-        ctx.set_nb(Cutoff=12.0, InnerCutoff=10.0, VdwCutoff=12.0, VdwInnerCutoff=10.0, Vdw14Scaling=s14v,
+        ctx.set_nb(Cutoff=NB_CUTOFF, InnerCutoff=10.0, VdwCutoff=NB_CUTOFF, VdwInnerCutoff=10.0, Vdw14Scaling=s14v,
                    Elec14Scaling=s14e, Dielectric=1.0, EnergySwitch=1, ForceSwitch=0, DoVdw=1, DoElec=1)
     if "GB" in wl["what"]:
         ctx.set_gb(**gb_settings(image))
@@ -389,6 +400,23 @@ def pairs_per_step(image, wl):
     return float((n * (n - 1) / 2).sum())
 
 
+def pairs_in_cutoff(image, pos, cutoff):
+    """Unordered atom pairs within `cutoff` (minimum image in a periodic box) at
+    these positions, counted exactly with a k-d tree: the pairs whose law the NB
+    kernel evaluates (bonded exclusions, under 1 % of them, included)."""
+    from scipy.spatial import cKDTree
+    tot = 0.0
+    for k in range(image.nsystems):
+        p = pos[image.offsets[k]:image.offsets[k + 1]]
+        box = image.box[k]
+        if np.all(box > 0):
+            tree = cKDTree(np.mod(p, box), boxsize=box)
+        else:
+            tree = cKDTree(p)
+        tot += (tree.count_neighbors(tree, cutoff) - len(p)) / 2.0
+    return tot
+
+
 def run_ours(args, key, wl, image):
     import torch
     world, rank, local = dist_env()
@@ -474,9 +502,8 @@ def run_ours(args, key, wl, image):
     if rank == 0:
         peak = fp32_peak_tflops(torch)
         pairs = pairs_per_step(image, wl) if "GB" in wl["what"] else None
-        if pairs is None:   # cutoff system: pairs inside the cutoff, from the list statistics
-            st = ctx.list_stats()
-            pairs = st["tiles"] * 1024.0 * (4.0 / 3.0 * math.pi * 12.0 ** 3) / (4.0 / 3.0 * math.pi * 14.0 ** 3) / 2
+        if pairs is None:   # cutoff system: pairs inside the cutoff at the current positions
+            pairs = pairs_in_cutoff(image, ctx.get_positions(), NB_CUTOFF)
         achieved = FLOPS[dom] * pairs / (ms_dom / 1e3) / 1e12
         peaks = {}
         pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -484,13 +511,20 @@ def run_ours(args, key, wl, image):
             peaks = json.load(open(pk))
         hbm = peaks.get("hbm_gbs", 6800.0)
         int_gbs = INTEGRATOR_BYTES * natom / (ms_int / 1e3) / 1e9
-        result["roofline"] = {"bound": "fp32", "kernel": "k_gb_pair" if dom == "gb_pair" else "k_nb_tiles",
+        kdom = "k_gb_pair" if dom == "gb_pair" else "k_nb_tiles"
+        kint = "k_langevin" if wl["integrator"] else "k_vv"
+        traffic = NCU_TRAFFIC.get(key, {})
+        result["roofline"] = {"bound": "fp32", "kernel": kdom,
                               "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                              "traffic": None, "peak_source": "measured cuBLAS SGEMM (TF32 off) on this GPU",
-                              "flops_per_pair": FLOPS[dom], "pairs_per_launch": pairs, "ms_per_launch": ms_dom}
-        result["hbm_roofline"] = {"bound": "hbm", "kernel": "k_langevin" if wl["integrator"] else "k_vv",
+                              "traffic": traffic.get(kdom), "traffic_unit": "bytes per launch (ncu)",
+                              "peak_source": "measured cuBLAS SGEMM (TF32 off) on this GPU",
+                              "flops_per_pair": FLOPS[dom], "pairs_per_launch": pairs, "ms_per_launch": ms_dom,
+                              "pairs": "all pairs" if "GB" in wl["what"] else
+                                       "pairs within the cutoff at the final positions (k-d tree count)"}
+        result["hbm_roofline"] = {"bound": "hbm", "kernel": kint,
                                   "achieved": int_gbs, "peak": hbm, "unit": "GB/s", "frac": int_gbs / hbm,
-                                  "traffic": None, "bytes_per_atom": INTEGRATOR_BYTES, "ms_per_launch": ms_int,
+                                  "traffic": traffic.get(kint), "traffic_unit": "bytes per launch (ncu)",
+                                  "bytes_per_atom": INTEGRATOR_BYTES, "ms_per_launch": ms_int,
                                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
     ctx.close()
 
