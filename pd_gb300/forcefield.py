@@ -46,8 +46,9 @@ class ForcefieldBase:
     def configure(self, ctx):
         """Push this component's parameters to the device context."""
 
-    def distribute(self, e):
-        """Add this component's share of the energies (dict, J) into wspace.ene; PD field names."""
+    def distribute(self, e, energies_only=False):
+        """Add this component's share of the energies (dict, J) into wspace.ene; PD field names.
+        energies_only: the evaluation was Forcefield::calcEnergies."""
 
     def calcForces(self):
         ff = Forcefield(self.wspace)
@@ -93,6 +94,12 @@ class FF_NonBonded_GPU(ForcefieldBase):
         self.ForceSwitch = True
         self.EnergySwitch = False
         self.UsePartialRecalc = False   # calcEnergies after small moves (nonbonded.cpp:1154-1182)
+        # long-range LJ correction, off by default (nonbonded.cpp:1009-1013)
+        self.VdwCor = False
+        self.VdwCorDensity = 0.0        # atoms per A^3
+        self.VdwCorEpsilon = 0.0        # kcal/mol
+        self.VdwCorRadius = 0.0         # A
+        self.VdwCorCutoff = 0.0         # A
         self.epot_vdw = 0.0
         self.epot_elec = 0.0
 
@@ -114,14 +121,28 @@ class FF_NonBonded_GPU(ForcefieldBase):
     def configure(self, ctx):
         ctx.set_nb(**self._nb_kwargs())
 
-    def distribute(self, e):
+    def vdw_correction(self):
+        """With VdwCor, PD's pair loop adds, for every atom i, the analytic integral of
+        the attractive LJ term from VdwCorCutoff to infinity (nonbonded.cpp:862-874):
+        -1/2 density eps (8/3) pi R^6 / Rc^3, an energy without force.  Total in J."""
+        if not self.VdwCor:
+            return 0.0
+        r3 = self.VdwCorRadius ** 3
+        per_atom = (-0.5 * self.VdwCorDensity * self.VdwCorEpsilon / _J2KCALMOL * (8.0 / 3.0) * np.pi * r3 * r3 /
+                    self.VdwCorCutoff ** 3)
+        return self.wspace.nAtoms() * per_atom
+
+    def distribute(self, e, energies_only=False):
         ene = self.wspace.ene
-        ene.epot += e["vdw"] + e["elec"]
-        ene.epot_vdw = e["vdw"]          # PD overwrites these two (nonbonded.cpp:681-682)
+        cor = self.vdw_correction()
+        vdw = e["vdw"] + cor
+        ene.epot += vdw + e["elec"]
+        ene.epot_vdw = vdw               # PD overwrites these two (nonbonded.cpp:681-682)
         ene.epot_elec = e["elec"]
+        ene.epot_vdw_att += cor
         ene.InternalVirial += e["virial"]
-        self.epot_vdw, self.epot_elec = e["vdw"], e["elec"]
-        self.epot = e["vdw"] + e["elec"]
+        self.epot_vdw, self.epot_elec = vdw, e["elec"]
+        self.epot = vdw + e["elec"]
 
     def infoLineHeader(self):
         return "%8s%8s" % ("EVdw", "Ecoul")
@@ -177,17 +198,22 @@ class FF_GeneralizedBorn_Still_GPU(FF_NonBonded_GPU):
                         ForceSwitch=int(bool(self.ForceSwitch)), DoVdw=int(bool(self.DoVdw)),
                         DoElec=int(bool(self.DoElec)))
 
-    def distribute(self, e):
+    def distribute(self, e, energies_only=False):
         ene = self.wspace.ene
-        ene.epot_vdw = e["vdw"]
+        # the vacuum part runs through FF_NonBonded (and its VdwCor) with FastMode off and
+        # in calcEnergies (gbff.cpp:178-197); FastMode's fused loop has no correction
+        cor = self.vdw_correction() if (energies_only or not self.FastMode) else 0.0
+        vdw = e["vdw"] + cor
+        ene.epot_vdw = vdw
         ene.epot_elec = e["elec"]
-        ene.epot += e["vdw"] + e["elec"] + e["pol"]
+        ene.epot_vdw_att += cor
+        ene.epot += vdw + e["elec"] + e["pol"]
         ene.epot_pol += e["pol"]
         ene.epot_pol_cross += e["pol_cross"]
         ene.epot_pol_self += e["pol_self"]
-        self.epot_vdw, self.epot_elec = e["vdw"], e["elec"]
+        self.epot_vdw, self.epot_elec = vdw, e["elec"]
         self.epot_pol, self.epot_pol_self, self.epot_pol_cross = e["pol"], e["pol_self"], e["pol_cross"]
-        self.epot = e["vdw"] + e["elec"] + e["pol"]
+        self.epot = vdw + e["elec"] + e["pol"]
 
     def infoLineHeader(self):
         return "\t%6s\t%6s\t%6s\t%6s\t%6s\t%7s" % ("EVdw", "Ecoul", "Eself", "Ecross", "Epol", "Epol+ES")
@@ -225,7 +251,7 @@ class FF_SASA_LCPO_GPU(ForcefieldBase):
         # FF_SASA_LCPO::setup, lcpo.cpp:57-63: sigma = GlobalASP / Na / J2kcal (J / A^2)
         return np.full(self.wspace.nAtoms(), self.GlobalASP / 6.0221418E23 * 4184.0)
 
-    def distribute(self, e):
+    def distribute(self, e, energies_only=False):
         ene = self.wspace.ene
         ene.epot += e["surf"]
         ene.epot_surf += e["surf"]
@@ -244,7 +270,7 @@ class FF_Bonded_GPU(ForcefieldBase):
     name = "Bonded Forcefield (GPU)"
     flag = ffi.BONDED
 
-    def distribute(self, e):
+    def distribute(self, e, energies_only=False):
         ene = self.wspace.ene
         ene.epot_bond += e["bond"]
         ene.epot_angle += e["angle"]
@@ -321,7 +347,7 @@ class Forcefield:
         tot = {k: sum(e[k] for e in energies) for k in energies[0]}
         for c in self.components:
             if c.Active:
-                c.distribute(tot)
+                c.distribute(tot, energies_only)
         if self.max_force > 0:
             mag = np.linalg.norm(ws.cur.f, axis=1)
             big = mag > self.max_force
@@ -347,7 +373,7 @@ class Forcefield:
                 energies, _ = ctx.nb_energy_update()
             ws.zeroForces()
             ws.per_system_energies = energies
-            act[0].distribute({k: sum(e[k] for e in energies) for k in energies[0]})
+            act[0].distribute({k: sum(e[k] for e in energies) for k in energies[0]}, True)
             return
         self.calcForces(energies_only=True)
 

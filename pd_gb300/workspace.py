@@ -22,7 +22,8 @@ class Hamiltonian:
     """PD's energy record (hamiltonian.h:43-66); energies in J per molecule."""
 
     FIELDS = ("etot", "epot", "ekin", "epot_vdw", "epot_elec", "epot_bond", "epot_angle", "epot_torsion",
-              "epot_surf", "epot_pol", "epot_pol_cross", "epot_pol_self", "InternalVirial")
+              "epot_surf", "epot_pol", "epot_pol_cross", "epot_pol_self", "InternalVirial", "epot_vdw_att",
+              "epot_vdw_rep")
 
     def __init__(self):
         self.zero()

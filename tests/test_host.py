@@ -57,6 +57,37 @@ def test_forcefield_defaults_mirror_pd():
     assert ws.Padding == 0.5
 
 
+def test_vdw_correction_follows_pd():
+    """FF_NonBonded's VdwCor (nonbonded.cpp:862-874): off by default; when on, every atom of
+    the pair loop adds -1/2 rho eps/(J2kcal Na) (8/3) pi R^6 / Rc^3 to epot, epot_vdw and
+    epot_vdw_att.  GB reaches it only through FF_NonBonded (FastMode off, calcEnergies)."""
+    import pd_gb300 as pdg
+    ws = pdg.WorkSpace(pdg.SystemImage._from_fixture(golden("peptide30")))
+    nb = pdg.FF_NonBonded_GPU(ws)
+    assert not nb.VdwCor and nb.vdw_correction() == 0.0
+    nb.VdwCor, nb.VdwCorDensity, nb.VdwCorEpsilon, nb.VdwCorRadius, nb.VdwCorCutoff = True, 0.0334, 0.152, 1.7682, 12.0
+    j2kcal, na = 1.0 / 4184.0, 6.0221418E23
+    per_atom = (-0.5 * 0.0334 * 0.152 / (j2kcal * na) * (8.0 / 3.0) * np.pi * 1.7682 ** 2 * 1.7682 ** 2 *
+                1.7682 ** 2 / 12.0 ** 3)
+    assert nb.vdw_correction() == pytest.approx(ws.nAtoms() * per_atom, rel=1e-14)
+    e = {"vdw": -1.0e-19, "elec": -2.0e-19, "virial": 0.0}
+    ws.ene.zero()
+    nb.distribute(e)
+    cor = nb.vdw_correction()
+    assert ws.ene.epot_vdw == pytest.approx(e["vdw"] + cor, rel=1e-14)
+    assert ws.ene.epot == pytest.approx(e["vdw"] + cor + e["elec"], rel=1e-14)
+    assert ws.ene.epot_vdw_att == pytest.approx(cor, rel=1e-14)
+    gb = pdg.FF_GeneralizedBorn_Still_GPU(ws)
+    gb.VdwCor, gb.VdwCorDensity, gb.VdwCorEpsilon, gb.VdwCorRadius, gb.VdwCorCutoff = True, 0.0334, 0.152, 1.7682, 12.0
+    g = dict(e, pol=0.0, pol_cross=0.0, pol_self=0.0)
+    ws.ene.zero()
+    gb.distribute(g)                         # FastMode forces: the fused loop has no correction
+    assert ws.ene.epot_vdw == e["vdw"]
+    ws.ene.zero()
+    gb.distribute(g, energies_only=True)     # calcEnergies goes through FF_NonBonded
+    assert ws.ene.epot_vdw == pytest.approx(e["vdw"] + cor, rel=1e-14)
+
+
 def test_maxwell_boltzmann_hits_target_temperature():
     from pd_gb300.md import KB, maxwell_boltzmann
     m = np.full(3000, 2e-26)
