@@ -217,7 +217,9 @@ def make_context(image, wl, key, seed, use_graph=True, device=0, update_nlist=10
 # ---------------------------------------------------------------------------
 # parity against the FP64 oracle on one system of the workload
 # ---------------------------------------------------------------------------
-def parity_check(image, wl, key):
+def parity_check(image, wl, key, pos=None):
+    """Energy and forces of one system (the median-size one of a batch) on the GPU
+    against the FP64 oracle, at the image's positions or at `pos` (all systems)."""
     from oracle import pdoracle as O
     from pd_gb300 import ffi
     from pd_gb300.engine import DeviceContext
@@ -225,6 +227,8 @@ def parity_check(image, wl, key):
     if image.nsystems > 1:   # the median-size system of the batch
         k = int(np.argsort(image.natoms)[image.nsystems // 2])
     sub = image.subset(k)
+    if pos is not None:
+        sub.pos = np.ascontiguousarray(pos[image.offsets[k]:image.offsets[k + 1]])
     ctx = DeviceContext(sub)
     configure(ctx, wl, sub)
     ctx.set_positions(sub.pos)
@@ -752,6 +756,62 @@ def run_adjoint(args):
     print(json.dumps(out))
 
 
+# full run lengths of the workloads (steps) and the interval of the oracle checks
+LONG = {"c1": (1000, 100), "c2": (10000, 1000), "c3": (5000, 500), "c4": (20000, 2000)}
+
+
+def run_long(args, key, wl, image):
+    """The workload's full run (C1 1,000 VV steps, C2 10,000 and C3 5,000 Langevin
+    steps, C4 20,000 steps with REMD exchange attempts every 500), with the GPU's
+    energy and forces checked against the FP64 oracle at fixed intervals on the
+    trajectory's own positions.  Not a timing run: one JSON line of the checks."""
+    ctx, temps = make_context(image, wl, key, 4242)
+    tuned = ctx.autotune(trial_steps=10)   # the list cadence and launch shape of the timed runs
+    steps, every = LONG[key]
+    exch_every = 500 if key == "c4" else 0
+    from pd_gb300 import ffi
+    checks, accepted, attempts, stale = [], 0, 0, 0
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps:
+        n = min(every, steps - done)
+        left = n
+        while left > 0:
+            chunk = left
+            if exch_every:
+                chunk = min(left, exch_every - done % exch_every)
+            due = exch_every and (done + chunk) % exch_every == 0
+            try:
+                ctx.md_run(chunk, energy_on_last=bool(due))
+            except ffi.PDGPUError as e:
+                if e.status != ffi.ERR_STALE_LIST:
+                    raise
+                stale += 1           # an atom moved past half the skin: rebuild and go on (counted)
+                ctx.rebuild_list()
+            done += chunk
+            left -= chunk
+            if due:
+                par = (done // exch_every) % 2
+                acc, _ = ctx.remd_exchange(par)
+                accepted += int(np.sum(acc[par::2]))     # rungs (par, par+1), (par+2, par+3), ...
+                attempts += len(acc[par::2])
+        ke = ctx.kinetic()
+        t_sys = 2.0 * ke / (3.0 * image.natoms * 1.380649e-23)
+        chk = parity_check(image, wl, key, pos=ctx.get_positions())
+        checks.append({"step": done, "force_rel_rms": chk["force_rel_rms"], "energy_rel_err": chk["energy_rel_err"],
+                       "mean_temperature_K": float(np.mean(t_sys))})
+    ctx.close()
+    out = {"workload": key, "steps": steps, "check_every": every, "system_atoms": chk["system_atoms"],
+           "checks": checks, "max_force_rel_rms": max(c["force_rel_rms"] for c in checks),
+           "max_energy_rel_err": max(c["energy_rel_err"] for c in checks), "wall_s": time.perf_counter() - t0,
+           "target": "force rel RMS <= 1e-5, |dE|/|E| <= 1e-6 vs the FP64 oracle", "autotune": tuned,
+           "stale_list_events": stale}
+    if exch_every:
+        out["exchange_attempts"] = attempts
+        out["exchanges_accepted"] = accepted
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -766,6 +826,8 @@ def main():
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--long", action="store_true",
+                    help="the workload's full run length with oracle checks at intervals (validation, not timing)")
     ap.add_argument("--relax-steps", type=int, default=RELAX["steps"],
                     help="untimed relaxation steps before timing (0 for short profiling runs)")
     args = ap.parse_args()
@@ -788,7 +850,10 @@ def main():
     else:
         from pd_gb300 import build as _b
         _b.build()
-        run_ours(args, args.workload, wl, image)
+        if args.long:
+            run_long(args, args.workload, wl, image)
+        else:
+            run_ours(args, args.workload, wl, image)
 
 
 if __name__ == "__main__":

@@ -18,6 +18,7 @@ ERRORS = {
     -7: "unsupported option", -8: "stale neighbour list", -9: "call sequence error",
     -10: "larger than the static scratch of the allocation-free entry point",
 }
+ERR_STALE_LIST = -8
 ERR_CAPACITY = -10
 NB, GB, SA, BONDED, ENERGY, PD_ENERGIES = 1, 2, 4, 8, 0x100, 0x200
 

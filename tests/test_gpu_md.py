@@ -1,4 +1,6 @@
 """Device dynamics against the oracle's FP64 integrators (PD md.cpp) and REMD properties."""
+import os
+
 import numpy as np
 import pytest
 
@@ -97,6 +99,52 @@ def test_langevin_thermalises_gb_peptide(goldens):
         temps.append(2 * ctx.kinetic()[0] / (3 * im.natom * 1.38065e-23))
     T = np.mean(temps[3:])
     assert 250.0 < T < 350.0, temps
+
+
+def test_langevin_temperature_matches_oracle_statistically(goldens):
+    """PD's Langevin scheme (md.cpp:923-1063) at 2 fs and its default friction reads a
+    kinetic temperature a few percent under the target on a flexible peptide (kinetic
+    energy taken after the first kick, as PD's calcKineticEnergy does).  The device
+    integrator must reproduce that stationary temperature, not just approach the
+    target: both run 3,000 steps from the same start (different random streams) and
+    their mean temperatures over the last 2,000 steps must agree within 4 combined
+    standard errors."""
+    from pd_gb300 import ffi
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.workspace import SystemImage
+    from helpers import gb_params
+    d = goldens["peptide30"]
+    im = SystemImage._from_fixture(d)
+    n, kB, dt, gamma, T0 = im.natom, 1.38065e-23, 2e-15, 1e13, 300.0
+    ctx = DeviceContext(im)
+    ctx.set_list(2.0)
+    ctx.set_gb(**gb_kwargs(d))
+    ctx.set_positions(d["pos"])
+    ctx.md_setup([T0], integrator=1, timestep=dt, fric=gamma, update_nlist=1, what=ffi.GB | ffi.BONDED, seed=3)
+    gT = []
+    for c in range(300):
+        ctx.md_run(10)
+        if c >= 100:
+            gT.append(2 * ctx.kinetic()[0] / (3 * n * kB))
+    ctx.close()
+    gp = gb_params(d)
+    bonded = (d["bond_idx"], d["bond_par"], d["angle_idx"], d["angle_par"], d["torsion_idx"], d["torsion_par"],
+              d["improper_idx"], d["improper_par"])
+    rng = np.random.default_rng(3)
+    pos, vel = d["pos"].copy(), np.zeros_like(d["pos"])
+    oT = []
+    for step in range(3000):
+        s = O.OracleSystem(pos, d["charge"], d["radius"], d["epsilon"], d["excl"], tuple(d["box"]))
+        _, f, _ = O.gb_forces(s, gp, d["gb_radius"], d["gb_vj"], d["gb_terms123"], os.cpu_count() or 1)
+        _, fb = O.bonded(pos, *bonded)
+        pos, vel, ek = O.langevin_step(pos, vel, f + fb, d["mass"], dt, gamma, T0, rng.standard_normal((n, 6)),
+                                       first_step=(step == 0))
+        if step >= 1000 and step % 10 == 0:
+            oT.append(2 * ek / (3 * n * kB))
+    sem = lambda x: np.std(x) / np.sqrt(len(x) / 10.0)   # samples 10 steps apart are correlated
+    gm, om = float(np.mean(gT)), float(np.mean(oT))
+    assert abs(gm - om) <= 4.0 * np.hypot(sem(gT), sem(oT)), (gm, om)
+    assert 0.85 * T0 < gm < 1.05 * T0, gm
 
 
 def test_remd_exchange_swaps_temperatures_and_rescales(goldens):
