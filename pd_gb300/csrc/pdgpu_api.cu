@@ -212,10 +212,15 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
   Context& c = h->c;
   c.device = device;
   auto bad = [&](int st) -> pdgpu_ctx* {
+    release_streams(c);
     delete h;
     return fail(st);
   };
-  if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) return bad(PDGPU_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming) != cudaSuccess)
+    return bad(PDGPU_ERR_CUDA);
 
   // systems and padded layout
   c.nsys = d->nsystems;
@@ -455,9 +460,17 @@ int pdgpu_destroy(pdgpu_ctx* h) {
   if (!h) return PDGPU_ERR_ARG;
   cudaSetDevice(h->c.device);
   if (h->c.stream) cudaStreamSynchronize(h->c.stream);
+  if (h->c.side) cudaStreamSynchronize(h->c.side);
   destroy_md(h->c);
-  cudaStream_t st = h->c.stream;
+  // the streams and events outlive the context's device buffers
+  cudaStream_t st = h->c.stream, side = h->c.side;
+  cudaEvent_t a = h->c.ev_fork, b = h->c.ev_join;
+  h->c.stream = h->c.side = nullptr;
+  h->c.ev_fork = h->c.ev_join = nullptr;
   delete h;
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (side) cudaStreamDestroy(side);
   if (st) cudaStreamDestroy(st);
   return PDGPU_OK;
 }
@@ -748,6 +761,16 @@ int pdgpu_rebuild_list(pdgpu_ctx* h) {
 // rebuild: rebuild the list first (else pack the positions and check the skin).
 // LCPO forces go to lcpo_f and its energy to lcpo_e (stride lcpo_e_stride) when
 // run_lcpo; dynamics points them at the cached-LCPO buffers.
+// (set-up failure) the context's streams and events
+void pdgpu::release_streams(Context& c) {
+  if (c.ev_fork) cudaEventDestroy(c.ev_fork);
+  if (c.ev_join) cudaEventDestroy(c.ev_join);
+  if (c.side) cudaStreamDestroy(c.side);
+  if (c.stream) cudaStreamDestroy(c.stream);
+  c.ev_fork = c.ev_join = nullptr;
+  c.side = c.stream = nullptr;
+}
+
 int pdgpu::enqueue_forces(Context& c, unsigned what, bool energy, bool rebuild, long long* lcpo_f,
                           long long* lcpo_e, int lcpo_e_stride, bool run_lcpo) {
   if (rebuild || !c.list_built) {
@@ -760,7 +783,24 @@ int pdgpu::enqueue_forces(Context& c, unsigned what, bool energy, bool rebuild, 
   CK(cudaMemsetAsync(c.d_facc.p, 0, sizeof(long long) * 3 * c.nslots, c.stream));
   if (energy) CK(cudaMemsetAsync(c.d_eacc.p, 0, sizeof(long long) * E_NSLOTS * c.nsys, c.stream));
   int st = PDGPU_OK;
-  if (what & PDGPU_NB) st = launch_nb(c, make_nb_const(c.nb), energy);
+  // the LCPO recalculation (positions, packed slots and tile list) and the bonded
+  // terms (positions) need nothing from the pair kernels: they run on the side
+  // stream beside them, adding into the same fixed-point accumulators (integer
+  // sums: the result does not depend on how the two streams interleave)
+  const bool side_sa = (what & PDGPU_SA) && run_lcpo, side_bonded = (what & PDGPU_BONDED) != 0;
+  const bool forked = side_sa || side_bonded;
+  if (forked) {
+    CK(cudaEventRecord(c.ev_fork, c.stream));
+    CK(cudaStreamWaitEvent(c.side, c.ev_fork, 0));
+    cudaStream_t main = c.stream;
+    c.stream = c.side;
+    if (side_sa) st = launch_lcpo(c, lcpo_f, lcpo_e, lcpo_e_stride);
+    if (st == PDGPU_OK && side_bonded) st = launch_bonded(c, energy);
+    c.stream = main;
+    // joined back below on every path, so a stream capture always closes
+    CK(cudaEventRecord(c.ev_join, c.side));
+  }
+  if (st == PDGPU_OK && (what & PDGPU_NB)) st = launch_nb(c, make_nb_const(c.nb), energy);
   if (st == PDGPU_OK && (what & PDGPU_GB)) {
     GBConst k = make_gb_const(c.gb, c.list_radius_built);
     // FastMode off, or PD's calcEnergies (gbff.cpp:178-183: calcBornEnergy, no
@@ -779,8 +819,7 @@ int pdgpu::enqueue_forces(Context& c, unsigned what, bool energy, bool rebuild, 
     double premul = -0.5 * ec * (1.0 / c.gb.DielectricSolute - 1.0 / c.gb.DielectricSolvent);
     if (st == PDGPU_OK) st = launch_gb(c, k, 0.5 * ec, c.gb.BornRadiusOffset, premul, energy);
   }
-  if (st == PDGPU_OK && (what & PDGPU_SA) && run_lcpo) st = launch_lcpo(c, lcpo_f, lcpo_e, lcpo_e_stride);
-  if (st == PDGPU_OK && (what & PDGPU_BONDED)) st = launch_bonded(c, energy);
+  if (forked) CK(cudaStreamWaitEvent(c.stream, c.ev_join, 0));
   return st;
 }
 

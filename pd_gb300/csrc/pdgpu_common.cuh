@@ -204,6 +204,7 @@ int launch_bonded(Context& c, bool energy);
 int launch_finalize_forces(Context& c, double* out, size_t stride_doubles, bool add, double scale);
 // host-side orchestration shared by the evaluation and dynamics entry points
 int rebuild_list_impl(Context& c);
+void release_streams(Context& c);
 int enqueue_forces(Context& c, unsigned what, bool energy, bool rebuild, long long* lcpo_f, long long* lcpo_e,
                    int lcpo_e_stride, bool run_lcpo);
 struct MDState;

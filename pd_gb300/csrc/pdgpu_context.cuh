@@ -28,6 +28,10 @@ struct DBuf {
 struct Context {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // work that reads positions only (bonded terms, the LCPO recalculation) runs on
+  // `side` beside the pair kernels, forked from and joined back to `stream`
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int nsys = 0, natom = 0, nslots = 0, nblocks = 0;
   long long ncand = 0;
   bool any_periodic = false, all_periodic = true;
