@@ -145,7 +145,7 @@ __global__ void k_lcpo_sort(DevView v, const float4* lc, const float4* lpos, con
 // per atom i (one warp, lanes over i's overlap partners j): SASA_i and the
 // derivative terms collected on atom i (lcpo.cpp:781-949).  Each lane sums its
 // partners' terms in FP32 (already folded with the P x sigma weights, so a lane
-// carries SA and the force only); the lanes combine in FP64.
+// carries SA and the force only); the lanes combine in 64-bit fixed point.
 __global__ void __launch_bounds__(256) k_lcpo_main(DevView v, const float4* lc, const float4* lpos, const float4* psig,
                                                    const int* nl_n, const int2* nl_e2, const float4* nl_ent,
                                                    const double* P, const double* sigma, double* sasa_out,
@@ -222,20 +222,22 @@ __global__ void __launch_bounds__(256) k_lcpo_main(DevView v, const float4* lc, 
     }
     sa += pa2 * Si2_t + pa3 * Si3_t + pa4 * (Si3_t * Si2_t);
   }
-  double SAp = warp_sum_d((double)sa);
-  double f[3];
+  // the lanes combine in 64-bit fixed point (2^32 per unit, exact integer sums;
+  // the force scale is the accumulators' own)
+  const long long sum_sa = warp_sum_ll(fx32(sa));
+  long long f[3];
 #pragma unroll
-  for (int c = 0; c < 3; c++) f[c] = warp_sum_d((double)fl[c]);
+  for (int c = 0; c < 3; c++) f[c] = warp_sum_ll(fx32(fl[c]));
   if (lane == 0) {
     const double Si = 4.0 * 3.14159265358979323846 * (double)ri * ri;
-    double SA = P[4 * a] * Si + SAp;
+    double SA = P[4 * a] * Si + (double)sum_sa * (1.0 / 4294967296.0);
     if (SA < 0) {
       SA = 0;
       f[0] = f[1] = f[2] = 0;
     }
     sasa_out[a] = SA;
     // PD adds SASAderiv / Angstrom; the derivative terms already hold d(sigma*SA)
-    for (int c = 0; c < 3; c++) atomic_add_ll(&facc_out[3 * s + c], __double2ll_rn(f[c] * kForceScale));
+    for (int c = 0; c < 3; c++) atomic_add_ll(&facc_out[3 * s + c], f[c]);
     int sys = v.slot_sys[s >> 5];
     if (esurf_out) atomic_add_ll(&esurf_out[(size_t)sys * esurf_stride], fix_energy_d(SA * sigma[a]));
   }
