@@ -491,7 +491,7 @@ __device__ __forceinline__ void gb_pair_full2(const DevView& v, const GBConst& k
 }
 
 template <bool ENERGY>
-__global__ void __launch_bounds__(256, ENERGY ? 2 : 3) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
+__global__ void __launch_bounds__(256, 3) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int ni = *v.nitems;
