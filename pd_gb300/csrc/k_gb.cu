@@ -6,13 +6,16 @@
 //   Born-radius chain     calcForcesIncludingVacuo loop2 :1768-1825
 // GB uses plain Euclidean distances, as PD does.
 //
-// Work decomposition: one warp per 32x32 tile (grid-stride over the tile list);
-// lane l holds i atom l, the j block is rotated through the warp by shuffles,
-// and both sides' FP32 sums are converted to 64-bit fixed point and added
-// atomically once per tile (so a slot's total does not depend on the order in
-// which tiles run).  Tiles without bonded pairs take a path without mask tests.
-// Registers decide the occupancy of these kernels: the i side is re-read per
-// tile rather than kept across tiles.
+// Work decomposition: one warp per GB work item (grid-stride over the item list
+// the list build writes): a single 32x32 tile, or a tile pair (bi, bj),
+// (bi, bj + 1) of one row.  In a single tile lane l holds i atom l and the j
+// block rotates through the warp by shuffles; in a tile pair each lane holds
+// one atom of each j block and the shared bi block rotates, so one rotation
+// serves two pairs (the Born and chain bodies also run the two pairs on packed
+// f32x2 arithmetic).  Every FP32 sum is converted to 64-bit fixed point and
+// added atomically once per item (so a slot's total does not depend on the
+// order in which items run).  Tiles without bonded pairs take a path without
+// mask tests.  Registers decide the occupancy of these kernels.
 #include "pdgpu_tile.cuh"
 
 namespace pdgpu {
