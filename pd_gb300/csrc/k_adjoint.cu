@@ -20,7 +20,8 @@
 // FP32 sums do not resolve to the 1e-4 a parameter fit checks against.  The GB
 // kernels therefore sum per tile in compensated FP32 (value plus running
 // rounding error, about 48 significant bits, on the FP32 pipe: GB300's FP64 rate
-// is a small fraction of its FP32 rate), the NB kernel in FP64.  Per-tile sums
+// is a small fraction of its FP32 rate), fed by plain FP32 sums over 8 rotation
+// steps; the NB kernel sums in FP64.  Per-tile sums
 // enter 64-bit fixed point (2^32 per kcal/mol per parameter unit), so the result
 // does not depend on scheduling.
 #include "pdgpu_tile.cuh"
@@ -64,6 +65,26 @@ __device__ __forceinline__ Acc3 cacc_value(const CAcc3& x) {
   ROT(x.hi);        \
   ROT(x.lo)
 
+// plain FP32 sums over 8 rotation steps, entered into the compensated sums at
+// the end of each run of 8 (a short FP32 run adds only a few roundings of its
+// own terms; the compensated sum then carries the long total)
+struct Chunk3 {
+  float a, b, c;
+};
+
+__device__ __forceinline__ void chunk_into(CAcc3& A, Chunk3& C) {
+  csum_add(A.a, C.a);
+  csum_add(A.b, C.b);
+  csum_add(A.c, C.c);
+  C.a = C.b = C.c = 0.f;
+}
+
+__device__ __forceinline__ void chunk_into2(CAcc3& A, Chunk3& C) {  // components a and b only
+  csum_add(A.a, C.a);
+  csum_add(A.b, C.b);
+  C.a = C.b = 0.f;
+}
+
 __device__ __forceinline__ void acc_flush(const DevView& v, long long* g0, long long* g1, long long* g2, int s,
                                           const Acc3& x) {
   const double m = fabs(x.a) + fabs(x.b) + fabs(x.c);
@@ -94,6 +115,7 @@ __device__ __forceinline__ void adj_gb_tile(const DevView& v, const GBConst& k, 
   float4 xj = j_in_i_frame(v, T, lane);
   float4 pj = v.par[T.bj * 32 + lane];
   float aj = born[T.bj * 32 + lane];
+  Chunk3 IC = {0.f, 0.f, 0.f}, JC = {0.f, 0.f, 0.f};  // JC rotates with its j atom
 #pragma unroll 2
   for (int kk = 0; kk < 32; kk++) {
     const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
@@ -129,8 +151,8 @@ __device__ __forceinline__ void adj_gb_tile(const DevView& v, const GBConst& k, 
       } else if (!excl) {
         phi = k.econv_out * s14 * invr * S;
       }
-      csum_add(I.a, phi * xj.w);
-      csum_add(J.a, phi * xi.w);
+      IC.a += phi * xj.w;
+      JC.a += phi * xi.w;
       if (!excl && r < k.vdwcut) {
         const float R = pi.x + pj.x;
         const float t = R * invr;
@@ -144,14 +166,19 @@ __device__ __forceinline__ void adj_gb_tile(const DevView& v, const GBConst& k, 
         }
         const float e1 = (B * B - 2.f * B) * Sv;  // energy per unit sqrt(eps_i) sqrt(eps_j)
         const float dR = lj_dR(R, invr) * Sv * pi.y * pj.y;
-        csum_add(I.b, dR);
-        csum_add(J.b, dR);
-        csum_add(I.c, e1 * pj.y);
-        csum_add(J.c, e1 * pi.y);
+        IC.b += dR;
+        JC.b += dR;
+        IC.c += e1 * pj.y;
+        JC.c += e1 * pi.y;
       }
+    }
+    if ((kk & 7) == 7) {
+      chunk_into(I, IC);
+      chunk_into(J, JC);
     }
     ROT(xj.x); ROT(xj.y); ROT(xj.z); ROT(xj.w); ROT(pj.x); ROT(pj.y); ROT(aj);
     ROT_CSUM(J.a); ROT_CSUM(J.b); ROT_CSUM(J.c);
+    ROT(JC.a); ROT(JC.b); ROT(JC.c);
   }
 }
 
@@ -187,6 +214,7 @@ __device__ __forceinline__ void adj_born_tile(const DevView& v, const GBConst& k
   float4 xj = j_in_i_frame(v, T, lane);
   float4 pj = v.par[T.bj * 32 + lane];
   float wj = w[T.bj * 32 + lane];
+  Chunk3 IC = {0.f, 0.f, 0.f}, JC = {0.f, 0.f, 0.f};  // (a, b used) JC rotates with its j atom
 #pragma unroll 4
   for (int kk = 0; kk < 32; kk++) {
     const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
@@ -208,13 +236,18 @@ __device__ __forceinline__ void adj_born_tile(const DevView& v, const GBConst& k
       }
       const float ir2 = __fdividef(1.f, r2);
       const float h4 = k.P4 * ir2 * ir2;
-      csum_add(I.b, wj * h4 * ccf);  // dE/dV_i from Gpol_j
-      csum_add(J.b, wi * h4 * ccf);  // dE/dV_j from Gpol_i
+      IC.b += wj * h4 * ccf;  // dE/dV_i from Gpol_j
+      JC.b += wi * h4 * ccf;  // dE/dV_j from Gpol_i
       const float gR = (wi * pj.w + wj * pi.w) * h4 * dccf * (-2.f * __fdividef(x, rs));
-      csum_add(I.a, gR);
-      csum_add(J.a, gR);
+      IC.a += gR;
+      JC.a += gR;
+    }
+    if ((kk & 7) == 7) {
+      chunk_into2(I, IC);
+      chunk_into2(J, JC);
     }
     ROT(xj.x); ROT(xj.y); ROT(xj.z); ROT(pj.z); ROT(pj.w); ROT(wj); ROT_CSUM(J.a); ROT_CSUM(J.b);
+    ROT(JC.a); ROT(JC.b);
   }
 }
 
