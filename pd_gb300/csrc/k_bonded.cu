@@ -25,9 +25,9 @@ struct BondedView {
 
 __device__ __forceinline__ void add_force(const BondedView& b, int atom, float fx, float fy, float fz) {
   int s = b.slot_of[atom];
-  atomic_add_ll(&b.facc[3 * s], fix_force(fx));
-  atomic_add_ll(&b.facc[3 * s + 1], fix_force(fy));
-  atomic_add_ll(&b.facc[3 * s + 2], fix_force(fz));
+  atomic_add_ll(&b.facc[3 * s], fx32(fx));
+  atomic_add_ll(&b.facc[3 * s + 1], fx32(fy));
+  atomic_add_ll(&b.facc[3 * s + 2], fx32(fz));
 }
 
 __device__ __forceinline__ float3 dvec(const double* pos, int a, int b) {

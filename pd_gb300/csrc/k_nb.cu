@@ -240,7 +240,7 @@ __global__ void k_finalize_forces(DevView v, double* out, size_t stride, int add
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     long long q = v.facc[3 * s + c];
-    if (q > (1ll << 62) || q < -(1ll << 62)) atomicOr(v.status, (unsigned)ST_FIXED_OVERFLOW);
+    if (q >= (1ll << 62) || q <= -(1ll << 62)) atomicOr(v.status, (unsigned)ST_FIXED_OVERFLOW);
     double f = (double)q * (1.0 / kForceScale) * scale;
     if (add) out[a * stride + c] += f;
     else out[a * stride + c] = f;

@@ -133,10 +133,7 @@ struct DevView {
 // ---------------------------------------------------------------------------
 // fixed point helpers
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ long long fix_force(float x) { return __float2ll_rn(x * 4294967296.0f); }
-__device__ __forceinline__ long long fix_energy(float x) { return __float2ll_rn(x * 16777216.0f); }
 __device__ __forceinline__ long long fix_energy_d(double x) { return __double2ll_rn(x * 16777216.0); }
-__device__ __forceinline__ long long fix_sum(float x) { return __float2ll_rn(x * 4294967296.0f); }
 // float -> 64-bit fixed point with 32 fractional bits using integer operations
 // only (|x| < 2^31; larger magnitudes saturate near 2^62 so the overflow check
 // trips).  Rounds half away from zero.  The hardware float->int64 conversion
@@ -159,11 +156,6 @@ __device__ __forceinline__ void atomic_add_ll(long long* p, long long v) {
   atomicAdd(reinterpret_cast<unsigned long long*>(p), static_cast<unsigned long long>(v));
 }
 __device__ __forceinline__ long long warp_sum_ll(long long v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-__device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
