@@ -41,7 +41,7 @@ extern "C" {
 #define PDGPU_GB 2u      /* FF_GeneralizedBorn_Still, FastMode (incl. vacuum LJ/Coulomb) */
 #define PDGPU_SA 4u      /* FF_SASA_LCPO                                        */
 #define PDGPU_BONDED 8u  /* FF_Bonded: bonds, angles, torsions, impropers       */
-#define PDGPU_ENERGY 0x100u /* pdgpu_compute_device: also form the energies (in FP64) */
+#define PDGPU_ENERGY 0x100u /* pdgpu_compute_device: also form the energies        */
 /* with PDGPU_GB: the energies as FF_GeneralizedBorn_Still::calcEnergies forms them
  * (gbff.cpp:178-183: Born radii, FF_NonBonded::calcEnergies with the GB object's
  * own settings, calcBornEnergy without ExpApproxThreshold, gbff.cpp:537-596);
@@ -162,8 +162,9 @@ int pdgpu_compute(pdgpu_ctx *ctx, unsigned what, pdgpu_energies *out, double *f,
 /* Device variant: forces in N written (not added) to d_f (packed xyz, device
  * memory) without any host synchronisation.  Energies are formed only when
  * `what` includes PDGPU_ENERGY and stay on the device until pdgpu_get_energies().
- * Forces are FP32 pair math with 64-bit fixed-point sums; energies, when
- * requested, are formed per pair in FP64. */
+ * Forces are FP32 pair math with 64-bit fixed-point sums.  Energies, when
+ * requested: GB pair energies from the force path's FP32 terms, summed in FP64
+ * and fixed point; FF_NonBonded pair energies in FP64. */
 int pdgpu_compute_device(pdgpu_ctx *ctx, unsigned what, double *d_f);
 int pdgpu_get_energies(pdgpu_ctx *ctx, pdgpu_energies *out);
 /* Born radii (Angstrom, original atom order) and LCPO per-atom SASA (A^2) from
