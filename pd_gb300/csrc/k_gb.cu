@@ -587,21 +587,27 @@ __global__ void __launch_bounds__(256) k_gb_pair_born_only(DevView v, GBConst k,
 
 // self term, total dE/da and the chain-rule prefactor a^2/166 * dE/da * P4
 __global__ void k_gb_self(DevView v, const double* charge, GBConst k, double premul, const long long* deda,
-                          const double* born_d, float* chain) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= v.nslots) return;
-  int a = v.sorted_atom[s];
-  if (a < 0) {
-    chain[s] = 0.f;
-    return;
+                          const double* born_d, float* chain, int energy) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  long long e = 0;
+  if (s < v.nslots) {  // nslots is a multiple of 32: warps are whole
+    const int a = v.sorted_atom[s];
+    if (a < 0) {
+      chain[s] = 0.f;
+    } else {
+      const double ai = born_d[a], q = charge[a];
+      const double inv = 1.0 / ai;
+      const double self = premul * q * q * inv;
+      const double da = (double)deda[s] * (1.0 / kSumScale) - self * inv;
+      chain[s] = (float)(ai * ai * (1.0 / 166.0) * da * (double)k.P4);
+      if (energy) e = fix_energy_d(self);
+    }
   }
-  double ai = born_d[a];
-  double q = charge[a];
-  double self = premul * q * q / ai;
-  double da = (double)deda[s] * (1.0 / kSumScale) - self / ai;
-  chain[s] = (float)(ai * ai / 166.0 * da * (double)k.P4);
-  int sys = v.slot_sys[s >> 5];
-  atomic_add_ll(&v.eacc[(size_t)sys * E_NSLOTS + E_POL_SELF], fix_energy_d(self));
+  if (energy) {  // a warp's slots are one block of one system: one atomic per warp
+    e = warp_sum_ll(e);
+    if ((threadIdx.x & 31) == 0 && s < v.nslots)
+      atomic_add_ll(&v.eacc[(size_t)v.slot_sys[s >> 5] * E_NSLOTS + E_POL_SELF], e);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -768,7 +774,8 @@ int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset
   } else {
     k_gb_pair<false><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
   }
-  k_gb_self<<<nb, 256, 0, st>>>(v, c.d_charge.p, k, premul, c.d_deda.p, c.d_born_d.p, c.d_chain_f.p);
+  k_gb_self<<<nb, 256, 0, st>>>(v, c.d_charge.p, k, premul, c.d_deda.p, c.d_born_d.p, c.d_chain_f.p,
+                                energy ? 1 : 0);
   if (c.gb_no_chain) c.kernel_launches -= 1;
   else k_gb_chain<<<g, 256, 0, st>>>(v, k, c.d_chain_f.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
