@@ -291,17 +291,26 @@ int pdgpu_md_checkpoint(pdgpu_ctx *ctx);
 int pdgpu_md_set_trajectory(pdgpu_ctx *ctx, int every, double *host_ring, int nslots);
 long long pdgpu_md_trajectory_frames(pdgpu_ctx *ctx);
 int pdgpu_md_rescue(pdgpu_ctx *ctx, unsigned long long seed, int *rescued, int *count);
-/* Project autotuner (state restored afterwards): first the launch shape of the
- * tile kernels (CTAs per SM of their grid-stride grid), timed on force
- * evaluations of the current state; then the list-rebuild cadence, timed on
- * short trial runs, keeping the fastest whose list never goes stale.
- * Outputs may be NULL. */
+/* Project autotuner (state restored afterwards): first the GB work-item size
+ * (pdgpu_set_work_items) and the launch shape of the tile kernels (CTAs per SM
+ * of their grid-stride grid), timed together on force evaluations of the
+ * current state; then the list-rebuild cadence, timed on short trial runs,
+ * keeping the fastest whose list never goes stale.  Outputs may be NULL; the
+ * chosen work-item size is read with pdgpu_get_work_items. */
 int pdgpu_md_autotune(pdgpu_ctx *ctx, int trial_steps, int *update_nlist, int *ctas_per_sm);
 /* Launch shape of the pair-tile kernels (what the autotuner sets): CTAs per SM
  * of their grid (1..64).  Results do not depend on it (per-tile sums enter
  * fixed point). */
 int pdgpu_set_launch_shape(pdgpu_ctx *ctx, int ctas_per_sm);
 int pdgpu_get_launch_shape(pdgpu_ctx *ctx, int *ctas_per_sm);
+/* Work-item size of the GB tile kernels (what the autotuner sets): 1 = one
+ * 32x32 tile per warp item, 2 = two tiles of one row that share their i block
+ * where the list allows (one rotation of that block serves both: fewer shuffles
+ * per pair, half as many items).  No counterpart in PD.  The item list is
+ * rewritten at the next list build; results agree to FP32 rounding of the
+ * per-item sums. */
+int pdgpu_set_work_items(pdgpu_ctx *ctx, int tiles_per_item);
+int pdgpu_get_work_items(pdgpu_ctx *ctx, int *tiles_per_item);
 
 /* ---- diagnostics ---------------------------------------------------------- */
 /* Tile / pair counts of the current list: ntiles, nmasked tiles, slots. */

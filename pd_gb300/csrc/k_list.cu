@@ -406,19 +406,20 @@ __device__ __forceinline__ bool tile_pairable(const DevView& v, int t, int nt) {
          tile_full(A) == tile_full(B) && !((A.flags | B.flags) & 1);
 }
 
-__global__ void k_item_flags(DevView v, long long ncand, int* flag) {
+// pairs: 0 makes every item a single tile
+__global__ void k_item_flags(DevView v, long long ncand, int pairs, int* flag) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ncand) return;
   const int nt = *v.ntiles;
-  flag[t] = (t < nt && !tile_pairable(v, (int)t - 1, nt)) ? 1 : 0;
+  flag[t] = (t < nt && !(pairs && tile_pairable(v, (int)t - 1, nt))) ? 1 : 0;
 }
 
-__global__ void k_item_write(DevView v, long long ncand, const int* flag, const int* pos) {
+__global__ void k_item_write(DevView v, long long ncand, int pairs, const int* flag, const int* pos) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ncand) return;
   if (t == ncand - 1) *v.nitems = pos[t] + flag[t];
   if (!flag[t]) return;
-  v.items[pos[t]] = (unsigned)t | (tile_pairable(v, (int)t, *v.ntiles) ? 0x80000000u : 0u);
+  v.items[pos[t]] = (unsigned)t | ((pairs && tile_pairable(v, (int)t, *v.ntiles)) ? 0x80000000u : 0u);
 }
 
 static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
@@ -466,11 +467,12 @@ int launch_list_build(Context& c, float list_radius, float full_radius) {
   if (c.has_gb) {
     c.kernel_launches += 5;
     int nb2 = nblk(c.ncand, 1024);
-    k_item_flags<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, c.d_tile_flag.p);
+    const int pairs = c.gb_item_tiles == 2 ? 1 : 0;
+    k_item_flags<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, pairs, c.d_tile_flag.p);
     k_scan_block<<<nb2, 1024, 0, st>>>(c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
     k_scan_sums<<<1, 1024, 0, st>>>(c.d_scan_tmp2.p, nb2);
     k_scan_add<<<nb2, 1024, 0, st>>>(c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
-    k_item_write<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, c.d_tile_flag.p, c.d_tile_pos.p);
+    k_item_write<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, pairs, c.d_tile_flag.p, c.d_tile_pos.p);
   }
   k_pack<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_charge.p, 0.f, 0.f, 1, c.ncand);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;

@@ -55,6 +55,7 @@ struct Context {
   // position at the build (checked every step by the position pack)
   float full_margin() const { return (float)(lp.Padding > 10.0 ? lp.Padding : 10.0); }
   int tile_ctas_per_sm = 8;    // launch shape of the tile kernels (autotuned)
+  int gb_item_tiles = 2;       // GB work items: 1 single tiles, 2 tile pairs where the list allows (autotuned)
   long long kernel_launches = 0;  // kernels this context has put on its stream (graph replays included)
 
   // static per-atom data (original order)

@@ -430,6 +430,23 @@ int pdgpu_get_launch_shape(pdgpu_ctx* h, int* ctas_per_sm) {
   return PDGPU_OK;
 }
 
+int pdgpu_set_work_items(pdgpu_ctx* h, int tiles_per_item) {
+  if (!h || (tiles_per_item != 1 && tiles_per_item != 2)) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (c.gb_item_tiles != tiles_per_item) {
+    c.gb_item_tiles = tiles_per_item;
+    c.list_built = false;  // the item list is written by the list build
+    if (c.md) invalidate_graphs(*c.md);
+  }
+  return PDGPU_OK;
+}
+
+int pdgpu_get_work_items(pdgpu_ctx* h, int* tiles_per_item) {
+  if (!h || !tiles_per_item) return PDGPU_ERR_ARG;
+  *tiles_per_item = h->c.gb_item_tiles;
+  return PDGPU_OK;
+}
+
 int pdgpu_md_autotune(pdgpu_ctx* h, int trial_steps, int* update_nlist, int* ctas_per_sm) {
   if (!h || trial_steps < 1) return PDGPU_ERR_ARG;
   Context& c = h->c;
@@ -449,40 +466,48 @@ int pdgpu_md_autotune(pdgpu_ctx* h, int trial_steps, int* update_nlist, int* cta
   CK(cudaMemcpyAsync(sa0.data(), md.d_facc_sa.p, sa0.size() * 8, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
 
-  // 1. launch shape of the tile kernels (grid = CTAs per SM x SMs): force
-  //    evaluations on the saved state (the list does not change), timed with events
+  // 1. work-item size of the GB kernels (single tiles or tile pairs) and launch
+  //    shape of the tile kernels (grid = CTAs per SM x SMs): force evaluations on
+  //    the saved state, timed with events
   const int shapes[] = {2, 4, 8, 16};
   const unsigned pair_what = md.p.what & (PDGPU_NB | PDGPU_GB);
-  int best_s = c.tile_ctas_per_sm;
+  int best_s = c.tile_ctas_per_sm, best_items = c.gb_item_tiles;
   if (pair_what) {
-    c.list_built = false;
-    if (rebuild_list_impl(c) != PDGPU_OK) return PDGPU_ERR_CUDA;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     float best_ms = 1e30f;
-    for (int shape : shapes) {
-      c.tile_ctas_per_sm = shape;
-      float ms = 0.f;
-      bool ok = true;
-      for (int rep = 0; rep < 3 && ok; rep++) {  // first repetition warms up
-        CK(cudaEventRecord(e0, c.stream));
-        ok = enqueue_forces(c, pair_what, false, false, c.d_facc.p, nullptr, 0, false) == PDGPU_OK;
-        CK(cudaEventRecord(e1, c.stream));
-        CK(cudaEventSynchronize(e1));
-        float t = 0.f;
-        CK(cudaEventElapsedTime(&t, e0, e1));
-        if (rep) ms += t;
-      }
-      if (ok && ms < best_ms) {
-        best_ms = ms;
-        best_s = shape;
+    const int n_items = (pair_what & PDGPU_GB) ? 2 : 1;
+    for (int ii = 0; ii < n_items; ii++) {
+      if (pair_what & PDGPU_GB) c.gb_item_tiles = 2 - ii;
+      c.list_built = false;
+      if (rebuild_list_impl(c) != PDGPU_OK) return PDGPU_ERR_CUDA;
+      for (int shape : shapes) {
+        c.tile_ctas_per_sm = shape;
+        float ms = 0.f;
+        bool ok = true;
+        for (int rep = 0; rep < 3 && ok; rep++) {  // first repetition warms up
+          CK(cudaEventRecord(e0, c.stream));
+          ok = enqueue_forces(c, pair_what, false, false, c.d_facc.p, nullptr, 0, false) == PDGPU_OK;
+          CK(cudaEventRecord(e1, c.stream));
+          CK(cudaEventSynchronize(e1));
+          float t = 0.f;
+          CK(cudaEventElapsedTime(&t, e0, e1));
+          if (rep) ms += t;
+        }
+        if (ok && ms < best_ms) {
+          best_ms = ms;
+          best_s = shape;
+          best_items = c.gb_item_tiles;
+        }
       }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
   }
   c.tile_ctas_per_sm = best_s;
+  c.gb_item_tiles = best_items;
+  c.list_built = false;
 
   // 2. list cadence with that shape: short dynamics from the saved state
   const int cadences[] = {1, 2, 3, 5, 10, 20, 40, 80};

@@ -286,7 +286,7 @@ class DeviceContext:
         a, b = ctypes.c_int(), ctypes.c_int()
         ffi.check(self.lib.pdgpu_md_autotune(self.h, int(trial_steps), ctypes.byref(a), ctypes.byref(b)),
                   "pdgpu_md_autotune")
-        return {"UpdateNList": a.value, "ctas_per_sm": b.value}
+        return {"UpdateNList": a.value, "ctas_per_sm": b.value, "gb_tiles_per_item": self.work_items()}
 
     def set_launch_shape(self, ctas_per_sm):
         ffi.check(self.lib.pdgpu_set_launch_shape(self.h, int(ctas_per_sm)), "pdgpu_set_launch_shape")
@@ -294,4 +294,13 @@ class DeviceContext:
     def launch_shape(self):
         a = ctypes.c_int()
         ffi.check(self.lib.pdgpu_get_launch_shape(self.h, ctypes.byref(a)), "pdgpu_get_launch_shape")
+        return a.value
+
+    def set_work_items(self, tiles_per_item):
+        """GB work-item size: 1 single tiles, 2 tile pairs (rewritten at the next list build)."""
+        ffi.check(self.lib.pdgpu_set_work_items(self.h, int(tiles_per_item)), "pdgpu_set_work_items")
+
+    def work_items(self):
+        a = ctypes.c_int()
+        ffi.check(self.lib.pdgpu_get_work_items(self.h, ctypes.byref(a)), "pdgpu_get_work_items")
         return a.value

@@ -122,6 +122,8 @@ SIGNATURES = {
     "pdgpu_md_rescue": ([ctypes.c_void_p, ctypes.c_ulonglong, _ip, _ip], ctypes.c_int),
     "pdgpu_set_launch_shape": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "pdgpu_get_launch_shape": ([ctypes.c_void_p, _ip], ctypes.c_int),
+    "pdgpu_set_work_items": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "pdgpu_get_work_items": ([ctypes.c_void_p, _ip], ctypes.c_int),
     "pdgpu_md_enqueue": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "pdgpu_synchronize": ([ctypes.c_void_p], ctypes.c_int),
     "pdgpu_kernel_launches": ([ctypes.c_void_p], ctypes.c_longlong),

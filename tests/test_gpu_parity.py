@@ -60,6 +60,29 @@ def test_gb_matches_pd(goldens, name):
     assert rel_rms(f, d["gb_f"]) <= F_TOL
 
 
+@pytest.mark.parametrize("name", ["peptide30_ap", "peptide120"])
+def test_gb_work_item_sizes_agree(goldens, name):
+    """Single tiles and tile pairs as GB work items (pdgpu_set_work_items) give the
+    same energies and forces to FP32 rounding of the per-item sums, both PD's."""
+    from pd_gb300 import ffi
+    d = goldens[name]
+    out = {}
+    for tiles in (1, 2):
+        ctx = make_ctx(d)
+        ctx.set_gb(**gb_kwargs(d))
+        ctx.set_work_items(tiles)
+        assert ctx.work_items() == tiles
+        f = np.zeros((len(d["pos"]), 3))
+        out[tiles] = (ctx.compute(ffi.GB, f)[0], f)
+        ctx.close()
+    (e1, f1), (e2, f2) = out[1], out[2]
+    assert rel_rms(f2, f1) <= 1e-6
+    for k in ("vdw", "elec", "pol", "epot"):
+        assert rel_err(e2[k], e1[k]) <= 1e-7, (k, e1[k], e2[k])
+        assert rel_err(e2[k], ref_energy(d, "gb", k)) <= E_TOL
+    assert rel_rms(f2, d["gb_f"]) <= F_TOL and rel_rms(f1, d["gb_f"]) <= F_TOL
+
+
 @pytest.mark.parametrize("name", ["peptide30", "peptide120"])
 def test_lcpo_matches_pd(goldens, name):
     from pd_gb300 import ffi
