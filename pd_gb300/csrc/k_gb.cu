@@ -210,10 +210,12 @@ __device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, 
     float g = 0.f;  // scalar multiplying (xj - xi) in the force on i
     float elec = 0.f, delec = 0.f;
     const float s14 = is14 ? k.elec14 : 1.f;
-    const bool sw_on = !FULL && r >= k.inner;  // FULL: inside the inner cutoff
+    // switching (FULL: the tile lies inside the inner cutoff) without a branch:
+    // below the inner cutoff w = 0 gives S = 1 and dS = 0 exactly
+    const bool sw_on = !FULL;
     float S = 1.f, dS = 0.f;
     if (sw_on) {
-      const float w = r - k.inner;
+      const float w = fmaxf(r - k.inner, 0.f);
       const float sw = 1.f - w * w * k.invw2;
       dS = -4.f * k.invw2 * w * sw;
       S = sw * sw;
@@ -251,24 +253,23 @@ __device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, 
     if (FAST && !excl) {
       if (ENERGY) ce += elec * S;
       if (sw_on) delec = S * delec + elec * dS;
-      float dvdw = 0.f;
-      if (FULL || r < k.vdwcut) {
-        const float t = (pix + pjx) * invr;
-        float B = t * t;
-        B = B * B * B;
-        const float A = B * B;
-        const float eps = piy * pjy * (is14 ? k.vdw14 : 1.f);
-        dvdw = -12.f * eps * invr * (A - B);
-        float Ev = ENERGY ? eps * (A - 2.f * B) : 0.f;
-        if (!FULL && r > k.vdwinner) {
-          if (!ENERGY) Ev = eps * (A - 2.f * B);
-          const float w = r - k.vdwinner;
-          const float sw = 1.f - w * w * k.vdwinvw2;
-          dvdw = sw * sw * dvdw + Ev * (-4.f * k.vdwinvw2 * w * sw);
-          if (ENERGY) Ev *= sw * sw;
-        }
-        if (ENERGY) cv += Ev;
+      const float t = (pix + pjx) * invr;
+      float B = t * t;
+      B = B * B * B;
+      const float A = B * B;
+      const float eps = piy * pjy * (is14 ? k.vdw14 : 1.f);
+      float dvdw = -12.f * eps * invr * (A - B);
+      float Ev = (ENERGY || !FULL) ? eps * (A - 2.f * B) : 0.f;
+      if (!FULL) {
+        const float w = fmaxf(r - k.vdwinner, 0.f);
+        const float sw = 1.f - w * w * k.vdwinvw2;
+        dvdw = sw * sw * dvdw + Ev * (-4.f * k.vdwinvw2 * w * sw);
+        if (ENERGY) Ev *= sw * sw;
+        const bool vin = r < k.vdwcut;
+        dvdw = vin ? dvdw : 0.f;
+        Ev = vin ? Ev : 0.f;
       }
+      if (ENERGY) cv += Ev;
       g += (dvdw + delec) * invr;
     }
     I.fx += g * dx; I.fy += g * dy; I.fz += g * dz;

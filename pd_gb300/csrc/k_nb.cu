@@ -24,28 +24,26 @@ __device__ __forceinline__ float nb_force_f(const NBConst& k, float r2, float rs
   const float invr = rsqrtf(r2), ir2 = invr * invr;
   const float r = r2 * invr;
   float g = 0.f;
-  if (k.dovdw && r < k.vdwcut_f) {
+  // switching without a branch: below the inner cutoff u = 0, so sw = 1 and the
+  // derivative term is exactly 0 (same value as the unswitched law); a branch
+  // here splits warps across the switching shell, which holds ~40% of the pairs
+  if (k.dovdw) {
     const float t2 = rsum * rsum * ir2;
     const float B = t2 * t2 * t2, A = B * B;
-    float gv = -12.f * eps * ir2 * (A - B);
-    if (r > k.vdwinner_f) {
-      const float u = r - k.vdwinner_f;
-      const float sw = 1.f - u * u * k.vdwinvw2_f;
-      gv = sw * sw * gv + eps * (A - 2.f * B) * (-4.f * k.vdwinvw2_f * u * sw) * invr;
-    }
-    g += gv;
+    const float gv = -12.f * eps * ir2 * (A - B);
+    const float u = fmaxf(r - k.vdwinner_f, 0.f);
+    const float sw = 1.f - u * u * k.vdwinvw2_f;
+    const float gs = sw * sw * gv + eps * (A - 2.f * B) * (-4.f * k.vdwinvw2_f * u * sw) * invr;
+    g += r < k.vdwcut_f ? gs : 0.f;
   }
   if (ELEC == 1) {
     g -= qq * invr * ir2;
   } else if (ELEC == 3) {
     const float Ee = qq * invr;
-    float ge = -Ee * ir2;
-    if (r > k.inner_f) {
-      const float u = r - k.inner_f;
-      const float sw = 1.f - u * u * k.invw2_f;
-      ge = sw * sw * ge + Ee * (-4.f * k.invw2_f * u * sw) * invr;
-    }
-    g += ge;
+    const float ge = -Ee * ir2;
+    const float u = fmaxf(r - k.inner_f, 0.f);
+    const float sw = 1.f - u * u * k.invw2_f;
+    g += sw * sw * ge + Ee * (-4.f * k.invw2_f * u * sw) * invr;
   } else if (ELEC == 4) {
     // Steinbach & Brooks force switch, nonbonded.cpp:798-819
     if (r > k.inner_f) {
@@ -180,7 +178,7 @@ __device__ __forceinline__ void nb_flush_energy(const DevView& v, int lane, int 
 
 // One warp per tile, grid-stride over the tile list.
 template <int ELEC, bool ENERGY>
-__global__ void __launch_bounds__(256) k_nb_tiles(DevView v, NBConst k) {
+__global__ void __launch_bounds__(256, ENERGY ? 0 : 4) k_nb_tiles(DevView v, NBConst k) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nt = *v.ntiles;
