@@ -294,9 +294,12 @@ int pdgpu_md_rescue(pdgpu_ctx *ctx, unsigned long long seed, int *rescued, int *
 /* Project autotuner (state restored afterwards): first the GB work-item size
  * (pdgpu_set_work_items) and the launch shape of the tile kernels (CTAs per SM
  * of their grid-stride grid), timed together on force evaluations of the
- * current state; then the list-rebuild cadence, timed on short trial runs,
- * keeping the fastest whose list never goes stale.  Outputs may be NULL; the
- * chosen work-item size is read with pdgpu_get_work_items. */
+ * current state; then the list-rebuild cadence together with the LJ/Coulomb
+ * j-atom groups on or off (pdgpu_set_nb_groups), timed per step on short
+ * trial runs of whole rebuild windows (at least trial_steps steps), keeping
+ * the fastest whose list never goes stale.  Outputs may be NULL; the chosen
+ * work-item size and groups setting are read with pdgpu_get_work_items and
+ * pdgpu_get_nb_groups. */
 int pdgpu_md_autotune(pdgpu_ctx *ctx, int trial_steps, int *update_nlist, int *ctas_per_sm);
 /* Launch shape of the pair-tile kernels (what the autotuner sets): CTAs per SM
  * of their grid (1..64).  Results do not depend on it (per-tile sums enter
@@ -311,6 +314,17 @@ int pdgpu_get_launch_shape(pdgpu_ctx *ctx, int *ctas_per_sm);
  * per-item sums. */
 int pdgpu_set_work_items(pdgpu_ctx *ctx, int tiles_per_item);
 int pdgpu_get_work_items(pdgpu_ctx *ctx, int *tiles_per_item);
+/* LJ/Coulomb j-atom groups (on by default; what the autotuner sets): at each
+ * list build, the j atoms of a row's plain tiles (no exclusions, off-diagonal,
+ * one periodic image) that lie within the list radius of the i block's box are
+ * packed 32 to a work item, so the pair kernel skips most out-of-cutoff pairs
+ * of a 32x32 tile.  Used only with the per-step displacement check
+ * (pdgpu_list_params.check_skin), which it keeps on in open space too.  No
+ * counterpart in PD.  Results agree with the tile path to FP32 rounding of the
+ * per-item sums.  get: the setting, and the groups and tiles the last list build
+ * left to the kernel (0 and -1 when it wrote no groups or they did not fit). */
+int pdgpu_set_nb_groups(pdgpu_ctx *ctx, int on);
+int pdgpu_get_nb_groups(pdgpu_ctx *ctx, int *on, long long *ngroups, long long *nrest_tiles);
 
 /* ---- diagnostics ---------------------------------------------------------- */
 /* Tile / pair counts of the current list: ntiles, nmasked tiles, slots. */

@@ -60,19 +60,40 @@ __global__ void k_bbox_init(int* lo, int* hi, int n) {
   }
 }
 
+// bounding box of each open-space system (periodic systems key on the box);
+// a warp whose atoms share one system reduces first and adds one atomic per
+// coordinate (a whole system's atoms otherwise meet on the same six words)
 __global__ void k_bbox(DevView v, const int* atom_sys, int* lo, int* hi) {
-  int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= v.natom) return;
-  int s = atom_sys[a];
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int s = a < v.natom ? atom_sys[a] : -1;
+  const bool use = s >= 0 && !v.sys[s].periodic;
+  const unsigned act = __ballot_sync(0xffffffffu, use);
+  if (!act) return;
+  const int s0 = __shfl_sync(0xffffffffu, s, __ffs(act) - 1);
+  const bool uniform = __all_sync(0xffffffffu, !use || s == s0);
 #pragma unroll
   for (int c = 0; c < 3; c++) {
-    float x = (float)v.pos[3 * a + c];
-    atomicMin(&lo[3 * s + c], f2ord(x));
-    atomicMax(&hi[3 * s + c], f2ord(x));
+    const int x = use ? f2ord((float)v.pos[3 * a + c]) : 0;
+    if (uniform) {
+      int mn = use ? x : f2ord(3.0e38f), mx = use ? x : f2ord(-3.0e38f);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      }
+      if (lane == __ffs(act) - 1) {
+        atomicMin(&lo[3 * s0 + c], mn);
+        atomicMax(&hi[3 * s0 + c], mx);
+      }
+    } else if (use) {
+      atomicMin(&lo[3 * s + c], x);
+      atomicMax(&hi[3 * s + c], x);
+    }
   }
 }
 
-__device__ __forceinline__ double wrap_coord(double x, double L) { return x - L * floor(x / L); }
+__device__ __forceinline__ double wrap_coord(double x, double L, double iL) { return x - L * floor(x * iL); }
 
 __global__ void k_keys(DevView v, const int* atom_sys, const int* lo, const int* hi, int* bucket, int* count) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -85,7 +106,7 @@ __global__ void k_keys(DevView v, const int* atom_sys, const int* lo, const int*
     double x = v.pos[3 * a + c];
     double f;
     if (S.periodic) {
-      f = wrap_coord(x, S.box[c]) / S.box[c];
+      f = wrap_coord(x, S.box[c], S.ibox[c]) * S.ibox[c];
     } else {
       double l = ord2f(lo[3 * s + c]), h = ord2f(hi[3 * s + c]);
       f = (x - l) / (h - l + 1e-3);
@@ -196,7 +217,7 @@ __global__ void k_blocks(DevView v) {
     double x = 0;
     if (a >= 0) {
       x = v.pos[3 * a + c];
-      if (S.periodic) x = wrap_coord(x, S.box[c]);
+      if (S.periodic) x = wrap_coord(x, S.box[c], S.ibox[c]);
     }
     lo[c] = a >= 0 ? x : 1e300;
     hi[c] = a >= 0 ? x : -1e300;
@@ -254,8 +275,10 @@ __device__ __forceinline__ bool candidate_pair(const DevView& v, long long t, in
   const SystemInfo& S = v.sys[lo];
   long long l = t - S.cand_start;
   long long nb = S.nblocks;
-  // row bi starts at bi*nb - bi*(bi-1)/2 and holds nb-bi entries
-  double fb = (2.0 * nb + 1.0 - sqrt((2.0 * nb + 1.0) * (2.0 * nb + 1.0) - 8.0 * (double)l)) * 0.5;
+  // row bi starts at bi*nb - bi*(bi-1)/2 and holds nb-bi entries (FP32 estimate,
+  // corrected by the integer tests below)
+  const float q = 2.f * (float)nb + 1.f;
+  float fb = (q - sqrtf(fmaxf(q * q - 8.f * (float)l, 0.f))) * 0.5f;
   long long bi = (long long)fb;
   if (bi < 0) bi = 0;
   if (bi > nb - 1) bi = nb - 1;
@@ -266,25 +289,30 @@ __device__ __forceinline__ bool candidate_pair(const DevView& v, long long t, in
   gj = S.block_start + (int)bj;
   float4 hi4 = v.half[gi], hj4 = v.half[gj];
   float hs[3] = {hi4.x + hj4.x, hi4.y + hj4.y, hi4.z + hj4.z};
-  double dist2 = 0, dmax2 = 0;
+  // FP32 geometry (the FP64 pipe is narrow on this GPU), every decision taken
+  // 1e-3 A on the safe side: include, per-pair image, not all-inside
+  constexpr float kSafe = 1e-3f;
+  float dist2 = 0.f, dmax2 = 0.f;
   bool need_mi = false;
 #pragma unroll
   for (int c = 0; c < 3; c++) {
-    double d = v.center[3 * gj + c] - v.center[3 * gi + c];
+    float d = (float)(v.center[3 * gj + c] - v.center[3 * gi + c]);
     if (S.periodic) {
-      d -= S.box[c] * rint(d / S.box[c]);
-      if (fabs(d) + hs[c] + margin >= 0.5 * S.box[c]) need_mi = true;
+      const float L = (float)S.box[c];
+      d -= L * rintf(d * (float)S.ibox[c]);
+      if (fabsf(d) + hs[c] + margin >= 0.5f * L - kSafe) need_mi = true;
     }
-    double g = fabs(d) - hs[c];
-    if (g > 0) dist2 += g * g;
-    const double m = fabs(d) + hs[c];
+    const float g = fabsf(d) - hs[c];
+    if (g > 0.f) dist2 += g * g;
+    const float m = fabsf(d) + hs[c];
     dmax2 += m * m;
   }
   // full: the farthest pair of the two boxes, grown by the displacement margin,
   // stays inside every cutoff and switch radius
-  const bool full = full_R > 0.f && !need_mi && sqrt(dmax2) + (double)full_margin < (double)full_R;
+  const bool full = full_R > 0.f && !need_mi && sqrtf(dmax2) + full_margin + kSafe < full_R;
   flags = (need_mi ? 1 : 0) | (gi == gj ? 2 : 0) | (full ? 4 : 0);
-  return dist2 <= (double)R * R;
+  const float Rs = R + kSafe;
+  return dist2 <= Rs * Rs;
 }
 
 __global__ void k_tile_flags(DevView v, long long ncand, float R, float margin, int* flag) {
@@ -316,7 +344,7 @@ __global__ void k_tile_write(DevView v, long long ncand, float R, float margin, 
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       o[c] = v.center[3 * gj + c] - v.center[3 * gi + c];
-      if (S.periodic) o[c] -= S.box[c] * rint(o[c] / S.box[c]);
+      if (S.periodic) o[c] -= S.box[c] * rint(o[c] * S.ibox[c]);
     }
     T.ox = (float)o[0];
     T.oy = (float)o[1];
@@ -336,14 +364,46 @@ __global__ void k_masks(DevView v) {
   int ai = v.sorted_atom[T.bi * 32 + lane];
   int aj0 = v.sorted_atom[T.bj * 32 + lane];
   bool diag = T.flags & 2;
+  // each atom's band words and far-partner range, loaded once per lane (the
+  // lower index of a pair holds them, as in pair_bondorder); j's are shuffled in
+  unsigned long long exi = 0ull, b14i = 0ull, exj0 = 0ull, b14j0 = 0ull;
+  int fsi = 0, fei = 0, fsj0 = 0, fej0 = 0;
+  if (ai >= 0) {
+    exi = v.band_excl[ai];
+    b14i = v.band_14[ai];
+    fsi = v.far_start[ai];
+    fei = v.far_start[ai + 1];
+  }
+  if (aj0 >= 0) {
+    exj0 = v.band_excl[aj0];
+    b14j0 = v.band_14[aj0];
+    fsj0 = v.far_start[aj0];
+    fej0 = v.far_start[aj0 + 1];
+  }
   unsigned ex = 0, m14 = 0;
   for (int k = 0; k < 32; k++) {
-    int aj = __shfl_sync(0xffffffffu, aj0, (lane + k) & 31);
-    if (ai < 0 || aj < 0 || (diag && k == 0)) {
+    const int src = (lane + k) & 31;
+    const int aj = __shfl_sync(0xffffffffu, aj0, src);
+    const unsigned long long exj = __shfl_sync(0xffffffffu, exj0, src);
+    const unsigned long long b14j = __shfl_sync(0xffffffffu, b14j0, src);
+    const int fsj = __shfl_sync(0xffffffffu, fsj0, src);
+    const int fej = __shfl_sync(0xffffffffu, fej0, src);
+    if (ai < 0 || aj < 0 || ai == aj) {
       ex |= 1u << k;
       continue;
     }
-    int bo = pair_bondorder(v, ai, aj);
+    const bool lo_i = ai < aj;
+    const int hi = lo_i ? aj : ai;
+    const int d = lo_i ? aj - ai : ai - aj;
+    int bo = 7;
+    if (d <= kBandWidth) {
+      const unsigned long long bit = 1ull << (d - 1);
+      if ((lo_i ? exi : exj) & bit) bo = 2;
+      else if ((lo_i ? b14i : b14j) & bit) bo = 3;
+    } else {
+      for (int q = lo_i ? fsi : fsj, e = lo_i ? fei : fej; q < e; q++)
+        if (v.far_idx[q] == hi && v.far_bo[q] < bo) bo = v.far_bo[q];
+    }
     if (bo <= 2) ex |= 1u << k;
     else if (bo == 3) m14 |= 1u << k;
   }
@@ -359,7 +419,9 @@ __global__ void k_masks(DevView v) {
 // per-evaluation pack: FP64 positions -> float offsets from the block centre
 // check2: squared skin limit (0 = no skin check); full2: squared limit that keeps
 // tiles flagged full valid (0 = none flagged), checked where the skin check is not
-__global__ void k_pack(DevView v, const double* charge, float check2, float full2, int store_ref, long long ncand) {
+// cull: the NB j-atom groups are in use (the displacement check always runs)
+__global__ void k_pack(DevView v, const double* charge, float check2, float full2, int store_ref, long long ncand,
+                       int cull) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= v.nslots) return;
   int a = v.sorted_atom[s];
@@ -374,7 +436,7 @@ __global__ void k_pack(DevView v, const double* charge, float check2, float full
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       double d = v.pos[3 * a + c] - v.center[3 * b + c];
-      if (S.periodic) d -= S.box[c] * rint(d / S.box[c]);
+      if (S.periodic) d -= S.box[c] * rint(d * S.ibox[c]);
       r[c] = d;
     }
     o = make_float4((float)r[0], (float)r[1], (float)r[2], (float)charge[a]);
@@ -383,7 +445,7 @@ __global__ void k_pack(DevView v, const double* charge, float check2, float full
     } else {
       // (in open space, when every block pair of every system is a tile, no pair
       // can leave the list; in a periodic box the tile images still depend on it)
-      const bool skin = check2 > 0.f && (S.periodic || (long long)*v.ntiles < ncand);
+      const bool skin = check2 > 0.f && (S.periodic || (long long)*v.ntiles < ncand || cull);
       const float lim = skin ? check2 : full2;
       if (lim > 0.f) {
         float4 q = v.rel0[s];
@@ -422,7 +484,115 @@ __global__ void k_item_write(DevView v, long long ncand, int pairs, const int* f
   v.items[pos[t]] = (unsigned)t | ((pairs && tile_pairable(v, (int)t, *v.ntiles)) ? 0x80000000u : 0u);
 }
 
+// ---------------------------------------------------------------------------
+// NB j-atom groups.  A 32x32 tile at list radius R holds ~12 % pairs inside a
+// 12 A cutoff (dense solvent, 7.5 A blocks); most of its j atoms lie beyond R
+// of the whole i block.  Per i-block row, the j atoms of the row's plain tiles
+// (no exclusion mask, off-diagonal, one periodic image) that lie within R of the
+// i block's box are packed into groups of 32; the pair kernel rotates a group
+// like a tile's j block.  Valid while every atom stays within half the skin of
+// its build position (the per-step displacement check, forced on with groups):
+// a pair inside the cutoff then had its j atom within R of the i box at build.
+// row: [0, nb) kept j atoms, [nb, 2nb) first tile, [2nb, 3nb) groups,
+// [3nb, 4nb) first group (exclusive scan).
+// ---------------------------------------------------------------------------
+__global__ void k_cull_mask(DevView v, long long ncand, float R2, unsigned* jmask, int* cnt, int* row) {
+  const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (t >= ncand) return;
+  const int nt = *v.ntiles;
+  if (t >= nt) {
+    if (lane == 0) cnt[t] = 0;
+    return;
+  }
+  const Tile T = v.tiles[t];
+  const bool plain = T.mask < 0 && !(T.flags & 3);
+  unsigned m = 0u;
+  if (plain) {
+    const int sj = T.bj * 32 + lane;
+    const float4 x = v.xq[sj];
+    const float4 h = v.half[T.bi];
+    const float gx = fmaxf(fabsf(x.x + T.ox) - h.x, 0.f);
+    const float gy = fmaxf(fabsf(x.y + T.oy) - h.y, 0.f);
+    const float gz = fmaxf(fabsf(x.z + T.oz) - h.z, 0.f);
+    m = __ballot_sync(0xffffffffu, v.sorted_atom[sj] >= 0 && gx * gx + gy * gy + gz * gz <= R2);
+  }
+  if (lane == 0) {
+    jmask[t] = m;
+    cnt[t] = __popc(m);
+    const int nb = v.nblocks;
+    if (m) atomicAdd(&row[T.bi], __popc(m));
+    atomicMin(&row[nb + T.bi], (int)t);
+    if (!plain) v.cull_rest[atomicAdd(&v.cull_n[0], 1)] = (int)t;
+  }
+}
+
+__global__ void k_cull_groups(int nb, int* row) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < nb) row[2 * nb + b] = (row[b] + 31) >> 5;
+}
+
+// pos: exclusive scan of the kept counts over the tile list (row-major, so a
+// row's entries keep tile order, then lane order)
+__global__ void k_cull_write(DevView v, long long ncand, const unsigned* jmask, const int* pos, const int* row) {
+  const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (t >= ncand || t >= *v.ntiles) return;
+  const unsigned m = jmask[t];
+  if (!((m >> lane) & 1u)) return;
+  const Tile T = v.tiles[t];
+  const int nb = v.nblocks;
+  const long long e = (long long)row[3 * nb + T.bi] * 32 + (pos[t] - pos[row[nb + T.bi]]) +
+                      __popc(m & ((1u << lane) - 1u));
+  if (e < v.cull_cap) v.cull_ent[e] = make_float4(T.ox, T.oy, T.oz, __int_as_float(T.bj * 32 + lane));
+}
+
+// one warp per row: group -> row, empty entries closing the row's last group,
+// and (last row) the group count and whether it fits the capacity
+__global__ void k_cull_rows(DevView v, const int* row) {
+  const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nb = v.nblocks;
+  if (b >= nb) return;
+  const int n = row[b], G = row[2 * nb + b], base = row[3 * nb + b];
+  const long long gcap = v.cull_cap / 32;
+  for (int g = lane; g < G; g += 32)
+    if (base + g < gcap) v.cull_bi[base + g] = b;
+  for (int i = n + lane; i < G * 32; i += 32) {
+    const long long e = (long long)base * 32 + i;
+    if (e < v.cull_cap) v.cull_ent[e] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+  }
+  if (b == nb - 1 && lane == 0) {
+    v.cull_n[1] = base + G;
+    v.cull_n[2] = (long long)(base + G) * 32 <= v.cull_cap ? 1 : 0;
+  }
+}
+
 static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+static void launch_cull(Context& c, float list_radius) {
+  c.kernel_launches += 10;
+  DevView v = c.view();
+  cudaStream_t st = c.stream;
+  const int nb = c.nblocks;
+  int* row = c.d_cull_row.p;
+  cudaMemsetAsync(row, 0, sizeof(int) * nb, st);
+  cudaMemsetAsync(row + nb, 0x7f, sizeof(int) * nb, st);
+  const float R = list_radius + 1e-3f;
+  // the kept counts and their scan reuse the tile-compaction arrays
+  k_cull_mask<<<nblk(c.ncand * 32, 256), 256, 0, st>>>(v, c.ncand, R * R, c.d_cull_mask.p, c.d_tile_flag.p, row);
+  const int nb2 = nblk(c.ncand, 1024);
+  k_scan_block<<<nb2, 1024, 0, st>>>(c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
+  k_scan_sums<<<1, 1024, 0, st>>>(c.d_scan_tmp2.p, nb2);
+  k_scan_add<<<nb2, 1024, 0, st>>>(c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
+  k_cull_groups<<<nblk(nb, 256), 256, 0, st>>>(nb, row);
+  const int nb3 = nblk(nb, 1024);
+  k_scan_block<<<nb3, 1024, 0, st>>>(row + 2 * nb, row + 3 * nb, c.d_cull_scan_tmp.p, nb);
+  k_scan_sums<<<1, 1024, 0, st>>>(c.d_cull_scan_tmp.p, nb3);
+  k_scan_add<<<nb3, 1024, 0, st>>>(row + 3 * nb, c.d_cull_scan_tmp.p, nb);
+  k_cull_write<<<nblk(c.ncand * 32, 256), 256, 0, st>>>(v, c.ncand, c.d_cull_mask.p, c.d_tile_pos.p, row);
+  k_cull_rows<<<nblk((long long)nb * 32, 256), 256, 0, st>>>(v, row);
+}
 
 int launch_list_build(Context& c, float list_radius, float full_radius) {
   c.kernel_launches += 18;
@@ -452,7 +622,7 @@ int launch_list_build(Context& c, float list_radius, float full_radius) {
                                                       c.has_sa ? c.d_lcpoR.p : nullptr,
                                                       c.has_sa ? c.d_lcpoUse.p : nullptr,
                                                       c.has_sa ? c.d_lc_par.p : nullptr);
-  cudaMemsetAsync(c.d_counters.p, 0, sizeof(int) * 3, st);
+  cudaMemsetAsync(c.d_counters.p, 0, sizeof(int) * 6, st);
   k_tile_flags<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, list_radius, (float)c.lp.Padding, c.d_tile_flag.p);
   {
     int nb2 = nblk(c.ncand, 1024);
@@ -474,7 +644,10 @@ int launch_list_build(Context& c, float list_radius, float full_radius) {
     k_scan_add<<<nb2, 1024, 0, st>>>(c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
     k_item_write<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, pairs, c.d_tile_flag.p, c.d_tile_pos.p);
   }
-  k_pack<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_charge.p, 0.f, 0.f, 1, c.ncand);
+  k_pack<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_charge.p, 0.f, 0.f, 1, c.ncand, 0);
+  // NB j-atom groups: only where the per-step displacement check runs
+  c.cull_built = c.nb_set && c.nb_cull && c.lp.check_skin && c.cull_cap > 0;
+  if (c.cull_built) launch_cull(c, list_radius);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 
@@ -499,7 +672,7 @@ int launch_pack(Context& c, float check_disp) {
     const float h = 0.5f * c.full_margin();
     f2 = h * h;
   }
-  k_pack<<<nblk(c.nslots, 256), 256, 0, c.stream>>>(v, c.d_charge.p, c2, f2, 0, c.ncand);
+  k_pack<<<nblk(c.nslots, 256), 256, 0, c.stream>>>(v, c.d_charge.p, c2, f2, 0, c.ncand, c.cull_built ? 1 : 0);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

@@ -24,7 +24,7 @@ __device__ __forceinline__ double mc_r2(const double* p, const SystemInfo& S, in
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     double d = p[3 * b + c] - p[3 * a + c];
-    if (S.periodic) d -= S.box[c] * rint(d / S.box[c]);
+    if (S.periodic) d -= S.box[c] * rint(d * S.ibox[c]);
     r2 += d * d;
   }
   return r2;

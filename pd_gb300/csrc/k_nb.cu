@@ -56,22 +56,20 @@ __device__ __forceinline__ float nb_force_f(const NBConst& k, float r2, float rs
   return g;
 }
 
-template <int ELEC, bool MASKED, bool ENERGY>
-__device__ __forceinline__ void nb_tile(const DevView& v, const NBConst& k, const Tile& T, const SystemInfo& S,
-                                        int lane, int si, int ai, const float4& xi, const float4& pi, float qi,
-                                        unsigned ex, unsigned m14, NBAcc& I, NBAcc& J, double& ev, double& ee,
-                                        double& vir) {
-  float4 xj = v.xq[T.bj * 32 + lane];
-  float4 pj = v.par[T.bj * 32 + lane];
-  // j positions moved into i's frame (the tile's centre offset, periodic image included)
+// 32 rotation steps of one work item: lane i holds an i atom, (xj, pj) the
+// lane's j atom already in i's frame.  Tiles: j slot jb + lane, per-pair image
+// when mi.  GROUP: the j atoms of a group (slots in gent[].w, -1 = empty lane,
+// parked far away), never masked, one image.
+template <int ELEC, bool MASKED, bool ENERGY, bool GROUP>
+__device__ __forceinline__ void nb_rot(const DevView& v, const NBConst& k, const SystemInfo& S, int lane, int si,
+                                       int ai, const float4& xi, const float4& pi, float qi, unsigned ex, unsigned m14,
+                                       float4 xj, float4 pj, bool mi_tile, int jb, const float4* gent, NBAcc& I,
+                                       NBAcc& J, double& ev, double& ee, double& vir) {
+  const bool mi = !GROUP && mi_tile;
   float Lx = 1.f, Ly = 1.f, Lz = 1.f;
-  if (S.periodic) {
+  if (!GROUP && S.periodic) {
     Lx = (float)S.box[0]; Ly = (float)S.box[1]; Lz = (float)S.box[2];
   }
-  xj.x += T.ox;
-  xj.y += T.oy;
-  xj.z += T.oz;
-  const bool mi = T.flags & 1;
   const float iLx = 1.f / Lx, iLy = 1.f / Ly, iLz = 1.f / Lz;
 #pragma unroll 4
   for (int kk = 0; kk < 32; kk++) {
@@ -86,14 +84,19 @@ __device__ __forceinline__ void nb_tile(const DevView& v, const NBConst& k, cons
     if (MASKED) listed = !((ex >> kk) & 1u);
     bool in = r2 <= k.cut2;
     double r2d = 0.0;  // (ENERGY) the pair's FP64 squared distance
+    int sj = 0;        // (ENERGY) the j slot
     if (ENERGY) {
-      if (listed) {
-        r2d = nb_r2_fp64(v, S, si, T.bj * 32 + ((lane + kk) & 31));
-        in = r2d <= k.cut2_dd;
+      if (listed && (!GROUP || in || r2 <= 1.01f * k.cut2)) {
+        sj = GROUP ? __float_as_int(gent[(lane + kk) & 31].w) : jb + ((lane + kk) & 31);
+        if (sj >= 0) {
+          r2d = nb_r2_fp64(v, S, si, sj);
+          in = r2d <= k.cut2_dd;
+        }
       }
     } else if (listed && (fabsf(r2 - k.cut2) <= 2e-6f * k.cut2 || fabsf(r2 - k.vdwcut2) <= 2e-6f * k.vdwcut2)) {
       // at a hard cutoff: decide, and take the distance, in FP64 (FP64 work only on this branch)
-      const double d2 = nb_r2_fp64(v, S, si, T.bj * 32 + ((lane + kk) & 31));
+      const int sjr = GROUP ? __float_as_int(gent[(lane + kk) & 31].w) : jb + ((lane + kk) & 31);
+      const double d2 = nb_r2_fp64(v, S, si, sjr);
       in = d2 <= k.cut2_dd;
       r2 = (float)d2;
     }
@@ -104,7 +107,7 @@ __device__ __forceinline__ void nb_tile(const DevView& v, const NBConst& k, cons
       const float fs = nb_force_f<ELEC>(k, r2, pi.x + pj.x, eps, qq);
       if (ENERGY) {
         // energy of this pair in FP64 from FP64 positions and parameters
-        const int aj = v.sorted_atom[T.bj * 32 + ((lane + kk) & 31)];
+        const int aj = v.sorted_atom[sj];
         double fsd, rdd;
         double epsd = v.sqeps[ai] * v.sqeps[aj] * (is14 ? k.vdw14_d : 1.0);
         double qqd = v.charge[ai] * v.charge[aj] * k.econv_diel_d * (is14 ? k.elec14_d : 1.0);
@@ -176,36 +179,77 @@ __device__ __forceinline__ void nb_flush_energy(const DevView& v, int lane, int 
   F = {0, 0, 0};
 }
 
-// One warp per tile, grid-stride over the tile list.
+// One warp per work item, grid-stride: the tiles left on the tile path, then the
+// j-atom groups (cull: the last list build wrote them and they fit)
 template <int ELEC, bool ENERGY>
-__global__ void __launch_bounds__(256, ENERGY ? 0 : 4) k_nb_tiles(DevView v, NBConst k) {
+__global__ void __launch_bounds__(256, ENERGY ? 0 : 4) k_nb_tiles(DevView v, NBConst k, int cull) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const int nt = *v.ntiles;
-  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
-    const Tile T = v.tiles[t];
-    const int si = T.bi * 32 + lane;
-    const float4 xi = v.xq[si], pi = v.par[si];
-    const float qi = xi.w * k.econv_diel;
-    const int ai = ENERGY ? v.sorted_atom[si] : 0;
-    const SystemInfo& S = v.sys[v.slot_sys[T.bi]];
-    unsigned ex = 0u, m14 = 0u;
-    if (T.mask >= 0) {
-      uint2 m = v.masks[T.mask * 32 + lane];
-      ex = m.x;
-      m14 = m.y;
-    }
-    if (T.flags & 2) ex |= diag_exclusion(lane);
+  const bool grouped = cull && v.cull_n[2];
+  const int nrest = grouped ? v.cull_n[0] : *v.ntiles;
+  const int nitem = nrest + (grouped ? v.cull_n[1] : 0);
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nitem; w += nwarps) {
     NBAcc I = {0.f, 0.f, 0.f}, J = {0.f, 0.f, 0.f};
     double ev = 0.0, ee = 0.0, vir = 0.0;
-    if (tile_masked(T)) nb_tile<ELEC, true, ENERGY>(v, k, T, S, lane, si, ai, xi, pi, qi, ex, m14, I, J, ev, ee, vir);
-    else nb_tile<ELEC, false, ENERGY>(v, k, T, S, lane, si, ai, xi, pi, qi, ex, m14, I, J, ev, ee, vir);
-    nb_flush(v, si, I);
-    nb_flush(v, T.bj * 32 + lane, J);
+    int bi, sjl;
+    if (w < nrest) {
+      const Tile T = v.tiles[grouped ? v.cull_rest[w] : w];
+      bi = T.bi;
+      sjl = T.bj * 32 + lane;
+      const int si = T.bi * 32 + lane;
+      const float4 xi = v.xq[si], pi = v.par[si];
+      const float qi = xi.w * k.econv_diel;
+      const int ai = ENERGY ? v.sorted_atom[si] : 0;
+      const SystemInfo& S = v.sys[v.slot_sys[T.bi]];
+      unsigned ex = 0u, m14 = 0u;
+      if (T.mask >= 0) {
+        uint2 m = v.masks[T.mask * 32 + lane];
+        ex = m.x;
+        m14 = m.y;
+      }
+      if (T.flags & 2) ex |= diag_exclusion(lane);
+      // j positions moved into i's frame (the tile's centre offset, periodic image included)
+      float4 xj = v.xq[sjl];
+      const float4 pj = v.par[sjl];
+      xj.x += T.ox;
+      xj.y += T.oy;
+      xj.z += T.oz;
+      const bool mi = T.flags & 1;
+      if (tile_masked(T))
+        nb_rot<ELEC, true, ENERGY, false>(v, k, S, lane, si, ai, xi, pi, qi, ex, m14, xj, pj, mi, T.bj * 32,
+                                          nullptr, I, J, ev, ee, vir);
+      else
+        nb_rot<ELEC, false, ENERGY, false>(v, k, S, lane, si, ai, xi, pi, qi, ex, m14, xj, pj, mi, T.bj * 32,
+                                           nullptr, I, J, ev, ee, vir);
+      nb_flush(v, si, I);
+    } else {
+      const int g = w - nrest;
+      bi = v.cull_bi[g];
+      const float4* gent = v.cull_ent + (size_t)g * 32;
+      const float4 e = gent[lane];
+      sjl = __float_as_int(e.w);
+      const int si = bi * 32 + lane;
+      const float4 xi = v.xq[si], pi = v.par[si];
+      const float qi = xi.w * k.econv_diel;
+      const int ai = ENERGY ? v.sorted_atom[si] : 0;
+      const SystemInfo& S = v.sys[v.slot_sys[bi]];
+      float4 xj = make_float4(1.0e15f, 1.0e15f, 1.0e15f, 0.f), pj = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (sjl >= 0) {
+        xj = v.xq[sjl];
+        pj = v.par[sjl];
+        xj.x += e.x;
+        xj.y += e.y;
+        xj.z += e.z;
+      }
+      nb_rot<ELEC, false, ENERGY, true>(v, k, S, lane, si, ai, xi, pi, qi, 0u, 0u, xj, pj, false, 0, gent, I, J,
+                                        ev, ee, vir);
+      nb_flush(v, si, I);
+    }
+    if (sjl >= 0) nb_flush(v, sjl, J);
     if (ENERGY) {
       NBEFix EF = {0, 0, 0};
       nb_efix_in(EF, ev, ee, vir);
-      nb_flush_energy(v, lane, T.bi, EF);
+      nb_flush_energy(v, lane, bi, EF);
     }
   }
 }
@@ -213,11 +257,12 @@ __global__ void __launch_bounds__(256, ENERGY ? 0 : 4) k_nb_tiles(DevView v, NBC
 template <bool E>
 static void launch_nb_mode(Context& c, const NBConst& k, int g) {
   DevView v = c.view();
+  const int cull = c.cull_built ? 1 : 0;
   switch (k.elecmode) {
-    case 0: k_nb_tiles<0, E><<<g, 256, 0, c.stream>>>(v, k); break;
-    case 1: k_nb_tiles<1, E><<<g, 256, 0, c.stream>>>(v, k); break;
-    case 3: k_nb_tiles<3, E><<<g, 256, 0, c.stream>>>(v, k); break;
-    default: k_nb_tiles<4, E><<<g, 256, 0, c.stream>>>(v, k); break;
+    case 0: k_nb_tiles<0, E><<<g, 256, 0, c.stream>>>(v, k, cull); break;
+    case 1: k_nb_tiles<1, E><<<g, 256, 0, c.stream>>>(v, k, cull); break;
+    case 3: k_nb_tiles<3, E><<<g, 256, 0, c.stream>>>(v, k, cull); break;
+    default: k_nb_tiles<4, E><<<g, 256, 0, c.stream>>>(v, k, cull); break;
   }
 }
 

@@ -241,6 +241,7 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
     int per = 0;
     for (int k = 0; k < 3; k++) {
       S.box[k] = d->box[3 * s + k];
+      S.ibox[k] = S.box[k] > 0 ? 1.0 / S.box[k] : 0.0;
       if (S.box[k] > 0) per++;
     }
     if (per != 0 && per != 3) return bad(PDGPU_ERR_ARG);
@@ -412,7 +413,7 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
   if (e == cudaSuccess) e = c.d_center.alloc(3 * (size_t)c.nblocks);
   if (e == cudaSuccess) e = c.d_half.alloc(c.nblocks);
   if (e == cudaSuccess) e = c.d_tiles.alloc(c.ncand);
-  if (e == cudaSuccess) e = c.d_counters.alloc(3);
+  if (e == cudaSuccess) e = c.d_counters.alloc(6);
   if (e == cudaSuccess && c.has_gb) e = c.d_items.alloc(c.ncand);
   if (e == cudaSuccess) e = c.d_tile_flag.alloc(c.ncand);
   if (e == cudaSuccess) e = c.d_tile_pos.alloc(c.ncand);
@@ -475,10 +476,43 @@ int pdgpu_destroy(pdgpu_ctx* h) {
   return PDGPU_OK;
 }
 
+}  // extern "C"
+
+// NB j-atom group buffers, made with the NB parameters (never inside a stream
+// capture): at most 32 entries per candidate tile plus one open group per row,
+// held to 8192 entries per row (a list that needs more keeps the tile path)
+static int alloc_cull(Context& c) {
+  if (c.cull_cap > 0 || c.ncand == 0) return PDGPU_OK;
+  const long long cap = std::min(32LL * c.ncand + 32LL * c.nblocks, 8192LL * c.nblocks);
+  cudaError_t e = cudaSetDevice(c.device);
+  if (e == cudaSuccess) e = c.d_cull_mask.alloc(c.ncand);
+  if (e == cudaSuccess) e = c.d_cull_rest.alloc(c.ncand);
+  if (e == cudaSuccess) e = c.d_cull_row.alloc(4 * (size_t)c.nblocks);
+  if (e == cudaSuccess) e = c.d_cull_scan_tmp.alloc((c.nblocks + 1023) / 1024 + 1);
+  if (e == cudaSuccess) e = c.d_cull_ent.alloc(cap);
+  if (e == cudaSuccess) e = c.d_cull_bi.alloc(cap / 32);
+  if (e != cudaSuccess) {
+    c.d_cull_mask.release();
+    c.d_cull_rest.release();
+    c.d_cull_row.release();
+    c.d_cull_scan_tmp.release();
+    c.d_cull_ent.release();
+    c.d_cull_bi.release();
+    cudaGetLastError();
+    return PDGPU_ERR_CUDA;
+  }
+  c.cull_cap = cap;
+  return PDGPU_OK;
+}
+
+extern "C" {
+
 int pdgpu_set_nb_params(pdgpu_ctx* h, const pdgpu_nb_params* p) {
   if (!h || !p || p->Cutoff <= 0 || p->InnerCutoff > p->Cutoff || p->VdwInnerCutoff > p->VdwCutoff ||
       p->Dielectric == 0)
     return PDGPU_ERR_ARG;
+  const int st = alloc_cull(h->c);
+  if (st != PDGPU_OK) return st;
   h->c.nb = *p;
   h->c.nb_set = true;
   h->c.list_built = false;

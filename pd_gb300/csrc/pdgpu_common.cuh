@@ -54,6 +54,7 @@ struct SystemInfo {
   long long cand_start;  // first candidate block pair of this system
   int periodic;
   double box[3];
+  double ibox[3];   // 1 / box (periodic systems)
 };
 
 struct __align__(16) Tile {
@@ -125,6 +126,14 @@ struct DevView {
   int* nitems;
   uint2* masks;              // [nmask*32] per lane: (excluded bits, 1-4 bits) in rotation order
   int* nmasks;
+  // NB j-atom groups: per i-block row, the j atoms of its unmasked, off-diagonal,
+  // single-image tiles that lie within the list radius of the i block's box,
+  // packed 32 to a group; the other tiles stay on the tile path (cull_rest)
+  float4* cull_ent;          // [cull_cap] j offset into the i block's frame (x, y, z), j slot (int bits; -1 empty)
+  int* cull_bi;              // [cull_cap / 32] i block of each group
+  int* cull_rest;            // [ncand] tiles left on the tile path (any order)
+  int* cull_n;               // [0] rest tiles, [1] groups, [2] 1 when the groups fit the capacity
+  long long cull_cap;        // entries
   long long* facc;           // [nslots*3]
   long long* eacc;           // [nsys*E_NSLOTS]
   unsigned* status;

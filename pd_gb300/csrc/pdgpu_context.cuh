@@ -54,6 +54,8 @@ struct Context {
   // displacement margin of full tiles: every atom stays within half of it of its
   // position at the build (checked every step by the position pack)
   float full_margin() const { return (float)(lp.Padding > 10.0 ? lp.Padding : 10.0); }
+  bool nb_cull = true;         // NB j-atom groups (needs the per-step skin check)
+  bool cull_built = false;     // the last list build wrote the groups
   int tile_ctas_per_sm = 8;    // launch shape of the tile kernels (autotuned)
   int gb_item_tiles = 2;       // GB work items: 1 single tiles, 2 tile pairs where the list allows (autotuned)
   long long kernel_launches = 0;  // kernels this context has put on its stream (graph replays included)
@@ -86,10 +88,18 @@ struct Context {
   DBuf<float4> d_half;         // [nblocks]
   DBuf<Tile> d_tiles;          // [ncand] row-major tile list
   DBuf<int> d_tile_flag, d_tile_pos, d_scan_tmp2;  // tile-list compaction
-  DBuf<int> d_counters;        // [0] ntiles, [1] nmasks, [2] nitems
+  DBuf<int> d_counters;        // [0] ntiles, [1] nmasks, [2] nitems, [3..5] NB groups (rest tiles, groups, fit)
   DBuf<unsigned> d_items;      // [ncand] GB work items (with GB only)
   DBuf<uint2> d_masks;         // [ncand*32] worst case
   DBuf<float4> d_xq, d_par, d_rel0;  // [nslots]
+  // NB j-atom groups (allocated with the NB parameters)
+  DBuf<unsigned> d_cull_mask;        // [ncand] j lanes kept per tile
+  DBuf<int> d_cull_rest;             // [ncand]
+  DBuf<int> d_cull_row;              // [4*nblocks] per row: kept j atoms, first tile, groups, first group
+  DBuf<int> d_cull_scan_tmp;
+  DBuf<float4> d_cull_ent;           // [cull_cap]
+  DBuf<int> d_cull_bi;               // [cull_cap / 32]
+  long long cull_cap = 0;
 
   // accumulators
   DBuf<long long> d_facc;      // [nslots*3]
@@ -167,6 +177,11 @@ struct Context {
     v.nitems = d_counters.p + 2;
     v.masks = d_masks.p;
     v.nmasks = d_counters.p + 1;
+    v.cull_ent = d_cull_ent.p;
+    v.cull_bi = d_cull_bi.p;
+    v.cull_rest = d_cull_rest.p;
+    v.cull_n = d_counters.p + 3;
+    v.cull_cap = cull_cap;
     v.facc = d_facc.p;
     v.eacc = d_eacc.p;
     v.status = d_status.p;

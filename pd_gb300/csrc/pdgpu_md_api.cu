@@ -447,6 +447,37 @@ int pdgpu_get_work_items(pdgpu_ctx* h, int* tiles_per_item) {
   return PDGPU_OK;
 }
 
+int pdgpu_set_nb_groups(pdgpu_ctx* h, int on) {
+  if (!h || (on != 0 && on != 1)) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (c.nb_cull != (on != 0)) {
+    c.nb_cull = on != 0;
+    c.list_built = false;  // the groups are written by the list build
+    if (c.md) invalidate_graphs(*c.md);
+  }
+  return PDGPU_OK;
+}
+
+int pdgpu_get_nb_groups(pdgpu_ctx* h, int* on, long long* ngroups, long long* nrest) {
+  if (!h || !on) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  *on = c.nb_cull ? 1 : 0;
+  long long g = 0, r = -1;
+  if (c.list_built && c.cull_built) {
+    CK(cudaSetDevice(c.device));
+    int n[6];
+    CK(cudaMemcpyAsync(n, c.d_counters.p, sizeof(n), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    if (n[5]) {
+      g = n[4];
+      r = n[3];
+    }
+  }
+  if (ngroups) *ngroups = g;
+  if (nrest) *nrest = r;
+  return PDGPU_OK;
+}
+
 int pdgpu_md_autotune(pdgpu_ctx* h, int trial_steps, int* update_nlist, int* ctas_per_sm) {
   if (!h || trial_steps < 1) return PDGPU_ERR_ARG;
   Context& c = h->c;
@@ -509,32 +540,43 @@ int pdgpu_md_autotune(pdgpu_ctx* h, int trial_steps, int* update_nlist, int* cta
   c.gb_item_tiles = best_items;
   c.list_built = false;
 
-  // 2. list cadence with that shape: short dynamics from the saved state
+  // 2. list cadence with that shape, with and without the NB j-atom groups (their
+  //    build cost counts, per rebuild): short dynamics from the saved state
   const int cadences[] = {1, 2, 3, 5, 10, 20, 40, 80};
+  const bool cull0 = c.nb_cull;
+  const bool try_groups = (md.p.what & PDGPU_NB) && c.nb_set && c.cull_cap > 0 && c.lp.check_skin;
   double best = 1e300;
   int best_n = p0.UpdateNList;
-  for (int n : cadences) {
-    md.p.UpdateNList = n;
-    invalidate_graphs(md);
-    CK(cudaMemcpyAsync(c.d_pos.p, pos0.p, N3 * 8, cudaMemcpyDeviceToDevice, c.stream));
-    CK(cudaMemcpyAsync(md.d_vel.p, vel0.p, N3 * 8, cudaMemcpyDeviceToDevice, c.stream));
-    md.step = step0;
-    md.trajectory_started = started0;
-    c.list_built = false;
-    int warm = std::min(trial_steps, n);
-    if (md_run_impl(c, md, warm, false) != PDGPU_OK) continue;
-    auto t0 = std::chrono::steady_clock::now();
-    int st = md_run_impl(c, md, trial_steps, false);
-    auto t1 = std::chrono::steady_clock::now();
-    if (st != PDGPU_OK) continue;  // stale list (or worse): cadence too long
-    // the cadence must also survive a longer stretch (4 rebuild windows)
-    if (md_run_impl(c, md, 4 * n, false) != PDGPU_OK) continue;
-    double dt = std::chrono::duration<double>(t1 - t0).count();
-    if (dt < best) {
-      best = dt;
-      best_n = n;
+  bool best_cull = cull0;
+  for (int gi = 0; gi < (try_groups ? 2 : 1); gi++) {
+    if (try_groups) c.nb_cull = gi == 0;
+    for (int n : cadences) {
+      md.p.UpdateNList = n;
+      invalidate_graphs(md);
+      CK(cudaMemcpyAsync(c.d_pos.p, pos0.p, N3 * 8, cudaMemcpyDeviceToDevice, c.stream));
+      CK(cudaMemcpyAsync(md.d_vel.p, vel0.p, N3 * 8, cudaMemcpyDeviceToDevice, c.stream));
+      md.step = step0;
+      md.trajectory_started = started0;
+      c.list_built = false;
+      int warm = std::min(trial_steps, n);
+      if (md_run_impl(c, md, warm, false) != PDGPU_OK) continue;
+      // whole rebuild windows, so every cadence pays its list builds; per step
+      const int timed = (trial_steps + n - 1) / n * n;
+      auto t0 = std::chrono::steady_clock::now();
+      int st = md_run_impl(c, md, timed, false);
+      auto t1 = std::chrono::steady_clock::now();
+      if (st != PDGPU_OK) continue;  // stale list (or worse): cadence too long
+      // the cadence must also survive a longer stretch (4 rebuild windows)
+      if (md_run_impl(c, md, 4 * n, false) != PDGPU_OK) continue;
+      double dt = std::chrono::duration<double>(t1 - t0).count() / timed;
+      if (dt < best) {
+        best = dt;
+        best_n = n;
+        best_cull = c.nb_cull;
+      }
     }
   }
+  c.nb_cull = best >= 1e300 ? cull0 : best_cull;
   // restore the state and keep the winner
   md.p = p0;
   md.p.UpdateNList = best_n;

@@ -137,7 +137,7 @@ __device__ __forceinline__ double r2_fp64(const DevView& v, const SystemInfo& S,
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     double d = v.pos[3 * b + c] - v.pos[3 * a + c];
-    if (S.periodic) d -= S.box[c] * rint(d / S.box[c]);
+    if (S.periodic) d -= S.box[c] * rint(d * S.ibox[c]);
     r2 += d * d;
   }
   return r2;

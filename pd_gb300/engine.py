@@ -286,7 +286,8 @@ class DeviceContext:
         a, b = ctypes.c_int(), ctypes.c_int()
         ffi.check(self.lib.pdgpu_md_autotune(self.h, int(trial_steps), ctypes.byref(a), ctypes.byref(b)),
                   "pdgpu_md_autotune")
-        return {"UpdateNList": a.value, "ctas_per_sm": b.value, "gb_tiles_per_item": self.work_items()}
+        return {"UpdateNList": a.value, "ctas_per_sm": b.value, "gb_tiles_per_item": self.work_items(),
+                "nb_groups": self.nb_groups()[0]}
 
     def set_launch_shape(self, ctas_per_sm):
         ffi.check(self.lib.pdgpu_set_launch_shape(self.h, int(ctas_per_sm)), "pdgpu_set_launch_shape")
@@ -304,3 +305,14 @@ class DeviceContext:
         a = ctypes.c_int()
         ffi.check(self.lib.pdgpu_get_work_items(self.h, ctypes.byref(a)), "pdgpu_get_work_items")
         return a.value
+
+    def set_nb_groups(self, on):
+        """LJ/Coulomb j-atom groups on or off (rewritten at the next list build)."""
+        ffi.check(self.lib.pdgpu_set_nb_groups(self.h, int(bool(on))), "pdgpu_set_nb_groups")
+
+    def nb_groups(self):
+        """(setting, groups, tiles left on the tile path) of the last list build."""
+        a, g, r = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_longlong()
+        ffi.check(self.lib.pdgpu_get_nb_groups(self.h, ctypes.byref(a), ctypes.byref(g), ctypes.byref(r)),
+                  "pdgpu_get_nb_groups")
+        return bool(a.value), g.value, r.value

@@ -124,6 +124,9 @@ SIGNATURES = {
     "pdgpu_get_launch_shape": ([ctypes.c_void_p, _ip], ctypes.c_int),
     "pdgpu_set_work_items": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "pdgpu_get_work_items": ([ctypes.c_void_p, _ip], ctypes.c_int),
+    "pdgpu_set_nb_groups": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "pdgpu_get_nb_groups": ([ctypes.c_void_p, _ip, ctypes.POINTER(ctypes.c_longlong),
+                             ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
     "pdgpu_md_enqueue": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "pdgpu_synchronize": ([ctypes.c_void_p], ctypes.c_int),
     "pdgpu_kernel_launches": ([ctypes.c_void_p], ctypes.c_longlong),

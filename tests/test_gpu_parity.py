@@ -83,6 +83,71 @@ def test_gb_work_item_sizes_agree(goldens, name):
     assert rel_rms(f2, d["gb_f"]) <= F_TOL and rel_rms(f1, d["gb_f"]) <= F_TOL
 
 
+@pytest.mark.parametrize("name,tag", [("peptide120", "nb"), ("peptide30_ap", "nb"), ("water_c1", "nb"),
+                                      ("water_c1", "nbfswitch")])
+def test_nb_groups_match_pd(goldens, name, tag):
+    """LJ/Coulomb j-atom groups (pdgpu_set_nb_groups): the force-only kernel (the
+    one dynamics runs) and the energy kernel, groups on and off, against PD's
+    forces and energies and against each other."""
+    torch = pytest.importorskip("torch")
+    from pd_gb300 import ffi
+    d = goldens[name]
+    n = len(d["pos"])
+    out = {}
+    for on in (1, 0):
+        ctx = make_ctx(d)
+        ctx.set_nb(**nb_kwargs(d, tag))
+        ctx.set_nb_groups(on)
+        f = np.zeros((n, 3))
+        e = ctx.compute(ffi.NB, f)[0]
+        setting, ngroups, nrest = ctx.nb_groups()
+        assert setting == bool(on)
+        if on and name.startswith("peptide"):
+            assert ngroups > 0 and nrest >= 0
+        if not on:
+            assert ngroups == 0
+        fd = torch.zeros((n, 3), dtype=torch.float64, device="cuda")
+        ctx.compute_device(ffi.NB, fd.data_ptr())
+        ctx.synchronize()
+        out[on] = (e, f, fd.cpu().numpy())
+        ctx.close()
+    ref_f = d[tag + "_f"]
+    for on in (1, 0):
+        e, f, ff = out[on]
+        for k in ("vdw", "elec", "epot"):
+            assert rel_err(e[k], ref_energy(d, tag, k)) <= E_TOL, (on, k, e[k], ref_energy(d, tag, k))
+        assert rel_rms(f, ref_f) <= F_TOL
+        assert rel_rms(ff, ref_f) <= F_TOL
+    assert rel_rms(out[1][2], out[0][2]) <= 1e-6
+    assert rel_rms(out[1][1], out[0][1]) <= 1e-6
+
+
+def test_nb_groups_keep_the_displacement_check(goldens):
+    """With the groups on, a move beyond half the skin is reported as a stale list
+    even in open space where every block pair is a tile (the groups drop j atoms
+    beyond the list radius); with them off such a list cannot go stale."""
+    from pd_gb300 import ffi
+    d = goldens["peptide30"]
+    pos = np.array(d["pos"], dtype=np.float64)
+    for on in (1, 0):
+        ctx = make_ctx(d, padding=1.0)
+        ctx.set_nb(**nb_kwargs(d, "nb"))
+        ctx.set_nb_groups(on)
+        ctx.compute(ffi.NB, np.zeros((len(pos), 3)))
+        ntiles = ctx.list_stats()["tiles"]
+        nb = (len(pos) + 31) // 32
+        moved = pos.copy()
+        moved[0] += np.array([0.8, 0.0, 0.0])
+        ctx.set_positions(moved)
+        if on:
+            with pytest.raises(ffi.PDGPUError) as ex:
+                ctx.compute(ffi.NB, np.zeros((len(pos), 3)))
+            assert ex.value.status == ffi.ERR_STALE_LIST
+        elif ntiles == nb * (nb + 1) // 2:
+            ctx.compute(ffi.NB, np.zeros((len(pos), 3)))
+        ctx.close()
+
+
 @pytest.mark.parametrize("name", ["peptide30", "peptide120"])
 def test_lcpo_matches_pd(goldens, name):
     from pd_gb300 import ffi
