@@ -355,65 +355,94 @@ __global__ void k_tile_write(DevView v, long long ncand, float R, float margin, 
 }
 
 // exclusion masks in rotation order (bit k <-> j slot (lane+k)&31); one warp per tile
-__global__ void k_masks(DevView v) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  int nt = *v.ntiles;
-  if (warp >= nt) return;
-  Tile T = v.tiles[warp];
-  int ai = v.sorted_atom[T.bi * 32 + lane];
-  int aj0 = v.sorted_atom[T.bj * 32 + lane];
-  bool diag = T.flags & 2;
-  // each atom's band words and far-partner range, loaded once per lane (the
-  // lower index of a pair holds them, as in pair_bondorder); j's are shuffled in
-  unsigned long long exi = 0ull, b14i = 0ull, exj0 = 0ull, b14j0 = 0ull;
-  int fsi = 0, fei = 0, fsj0 = 0, fej0 = 0;
-  if (ai >= 0) {
-    exi = v.band_excl[ai];
-    b14i = v.band_14[ai];
-    fsi = v.far_start[ai];
-    fei = v.far_start[ai + 1];
-  }
-  if (aj0 >= 0) {
-    exj0 = v.band_excl[aj0];
-    b14j0 = v.band_14[aj0];
-    fsj0 = v.far_start[aj0];
-    fej0 = v.far_start[aj0 + 1];
-  }
-  unsigned ex = 0, m14 = 0;
-  for (int k = 0; k < 32; k++) {
-    const int src = (lane + k) & 31;
-    const int aj = __shfl_sync(0xffffffffu, aj0, src);
-    const unsigned long long exj = __shfl_sync(0xffffffffu, exj0, src);
-    const unsigned long long b14j = __shfl_sync(0xffffffffu, b14j0, src);
-    const int fsj = __shfl_sync(0xffffffffu, fsj0, src);
-    const int fej = __shfl_sync(0xffffffffu, fej0, src);
-    if (ai < 0 || aj < 0 || ai == aj) {
-      ex |= 1u << k;
-      continue;
+// tiles holding a bonded pair (bond order <= 3: excluded or 1-4), marked from
+// each atom's partners (band words, far list) through the candidate index of its
+// block pair: need[tile] = 1.  flag / pos: the tile-compaction scan (candidate ->
+// tile).  Diagonal tiles and tiles with padding slots are recognised in k_masks.
+__global__ void k_mask_mark(DevView v, const int* slot_of, const int* flag, const int* pos, unsigned char* need) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= v.natom) return;
+  const unsigned long long w = v.band_excl[a] | v.band_14[a];
+  const int fs = v.far_start[a], fe = v.far_start[a + 1];
+  if (!w && fs == fe) return;
+  const int sa = slot_of[a];
+  const int ga = sa >> 5;
+  const SystemInfo& S = v.sys[v.slot_sys[ga]];
+  auto mark = [&](int b) {
+    const int gb = slot_of[b] >> 5;
+    const long long bi = (ga < gb ? ga : gb) - S.block_start, bj = (ga < gb ? gb : ga) - S.block_start;
+    const long long nb = S.nblocks;
+    const long long l = S.cand_start + bi * nb - bi * (bi - 1) / 2 + (bj - bi);
+    if (flag[l]) need[pos[l]] = 1;
+  };
+  for (unsigned long long m = w; m; m &= m - 1) mark(a + __ffsll((long long)m));
+  for (int q = fs; q < fe; q++)
+    if (v.far_bo[q] <= 3) mark(v.far_idx[q]);
+}
+
+// grid-stride over the tiles, one warp per tile; tiles without a bonded pair,
+// padding slot or diagonal get no mask and skip the pair loop
+__global__ void k_masks(DevView v, const unsigned char* need) {
+  const int lane = threadIdx.x & 31;
+  const int nt = *v.ntiles;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < nt; warp += nwarps) {
+    Tile T = v.tiles[warp];
+    int ai = v.sorted_atom[T.bi * 32 + lane];
+    int aj0 = v.sorted_atom[T.bj * 32 + lane];
+    bool diag = T.flags & 2;
+    if (!need[warp] && !diag && __all_sync(0xffffffffu, ai >= 0 && aj0 >= 0)) continue;
+    // each atom's band words and far-partner range, loaded once per lane (the
+    // lower index of a pair holds them, as in pair_bondorder); j's are shuffled in
+    unsigned long long exi = 0ull, b14i = 0ull, exj0 = 0ull, b14j0 = 0ull;
+    int fsi = 0, fei = 0, fsj0 = 0, fej0 = 0;
+    if (ai >= 0) {
+      exi = v.band_excl[ai];
+      b14i = v.band_14[ai];
+      fsi = v.far_start[ai];
+      fei = v.far_start[ai + 1];
     }
-    const bool lo_i = ai < aj;
-    const int hi = lo_i ? aj : ai;
-    const int d = lo_i ? aj - ai : ai - aj;
-    int bo = 7;
-    if (d <= kBandWidth) {
-      const unsigned long long bit = 1ull << (d - 1);
-      if ((lo_i ? exi : exj) & bit) bo = 2;
-      else if ((lo_i ? b14i : b14j) & bit) bo = 3;
-    } else {
-      for (int q = lo_i ? fsi : fsj, e = lo_i ? fei : fej; q < e; q++)
-        if (v.far_idx[q] == hi && v.far_bo[q] < bo) bo = v.far_bo[q];
+    if (aj0 >= 0) {
+      exj0 = v.band_excl[aj0];
+      b14j0 = v.band_14[aj0];
+      fsj0 = v.far_start[aj0];
+      fej0 = v.far_start[aj0 + 1];
     }
-    if (bo <= 2) ex |= 1u << k;
-    else if (bo == 3) m14 |= 1u << k;
+    unsigned ex = 0, m14 = 0;
+    for (int k = 0; k < 32; k++) {
+      const int src = (lane + k) & 31;
+      const int aj = __shfl_sync(0xffffffffu, aj0, src);
+      const unsigned long long exj = __shfl_sync(0xffffffffu, exj0, src);
+      const unsigned long long b14j = __shfl_sync(0xffffffffu, b14j0, src);
+      const int fsj = __shfl_sync(0xffffffffu, fsj0, src);
+      const int fej = __shfl_sync(0xffffffffu, fej0, src);
+      if (ai < 0 || aj < 0 || ai == aj) {
+        ex |= 1u << k;
+        continue;
+      }
+      const bool lo_i = ai < aj;
+      const int hi = lo_i ? aj : ai;
+      const int d = lo_i ? aj - ai : ai - aj;
+      int bo = 7;
+      if (d <= kBandWidth) {
+        const unsigned long long bit = 1ull << (d - 1);
+        if ((lo_i ? exi : exj) & bit) bo = 2;
+        else if ((lo_i ? b14i : b14j) & bit) bo = 3;
+      } else {
+        for (int q = lo_i ? fsi : fsj, e = lo_i ? fei : fej; q < e; q++)
+          if (v.far_idx[q] == hi && v.far_bo[q] < bo) bo = v.far_bo[q];
+      }
+      if (bo <= 2) ex |= 1u << k;
+      else if (bo == 3) m14 |= 1u << k;
+    }
+    bool any = __any_sync(0xffffffffu, (ex | m14) != 0);
+    if (!any) continue;
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(v.nmasks, 1);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    v.masks[idx * 32 + lane] = make_uint2(ex, m14);
+    if (lane == 0) v.tiles[warp].mask = idx;
   }
-  bool any = __any_sync(0xffffffffu, (ex | m14) != 0);
-  if (!any) return;
-  int idx = 0;
-  if (lane == 0) idx = atomicAdd(v.nmasks, 1);
-  idx = __shfl_sync(0xffffffffu, idx, 0);
-  v.masks[idx * 32 + lane] = make_uint2(ex, m14);
-  if (lane == 0) v.tiles[warp].mask = idx;
 }
 
 // per-evaluation pack: FP64 positions -> float offsets from the block centre
@@ -496,34 +525,32 @@ __global__ void k_item_write(DevView v, long long ncand, int pairs, const int* f
 // row: [0, nb) kept j atoms, [nb, 2nb) first tile, [2nb, 3nb) groups,
 // [3nb, 4nb) first group (exclusive scan).
 // ---------------------------------------------------------------------------
-__global__ void k_cull_mask(DevView v, long long ncand, float R2, unsigned* jmask, int* cnt, int* row) {
-  const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// cnt: zeroed beforehand over all candidates (the scan runs over them)
+__global__ void k_cull_mask(DevView v, float R2, unsigned* jmask, int* cnt, int* row) {
   const int lane = threadIdx.x & 31;
-  if (t >= ncand) return;
   const int nt = *v.ntiles;
-  if (t >= nt) {
-    if (lane == 0) cnt[t] = 0;
-    return;
-  }
-  const Tile T = v.tiles[t];
-  const bool plain = T.mask < 0 && !(T.flags & 3);
-  unsigned m = 0u;
-  if (plain) {
-    const int sj = T.bj * 32 + lane;
-    const float4 x = v.xq[sj];
-    const float4 h = v.half[T.bi];
-    const float gx = fmaxf(fabsf(x.x + T.ox) - h.x, 0.f);
-    const float gy = fmaxf(fabsf(x.y + T.oy) - h.y, 0.f);
-    const float gz = fmaxf(fabsf(x.z + T.oz) - h.z, 0.f);
-    m = __ballot_sync(0xffffffffu, v.sorted_atom[sj] >= 0 && gx * gx + gy * gy + gz * gz <= R2);
-  }
-  if (lane == 0) {
-    jmask[t] = m;
-    cnt[t] = __popc(m);
-    const int nb = v.nblocks;
-    if (m) atomicAdd(&row[T.bi], __popc(m));
-    atomicMin(&row[nb + T.bi], (int)t);
-    if (!plain) v.cull_rest[atomicAdd(&v.cull_n[0], 1)] = (int)t;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
+    const Tile T = v.tiles[t];
+    const bool plain = T.mask < 0 && !(T.flags & 3);
+    unsigned m = 0u;
+    if (plain) {
+      const int sj = T.bj * 32 + lane;
+      const float4 x = v.xq[sj];
+      const float4 h = v.half[T.bi];
+      const float gx = fmaxf(fabsf(x.x + T.ox) - h.x, 0.f);
+      const float gy = fmaxf(fabsf(x.y + T.oy) - h.y, 0.f);
+      const float gz = fmaxf(fabsf(x.z + T.oz) - h.z, 0.f);
+      m = __ballot_sync(0xffffffffu, v.sorted_atom[sj] >= 0 && gx * gx + gy * gy + gz * gz <= R2);
+    }
+    if (lane == 0) {
+      jmask[t] = m;
+      cnt[t] = __popc(m);
+      const int nb = v.nblocks;
+      if (m) atomicAdd(&row[T.bi], __popc(m));
+      atomicMin(&row[nb + T.bi], t);
+      if (!plain) v.cull_rest[atomicAdd(&v.cull_n[0], 1)] = t;
+    }
   }
 }
 
@@ -534,17 +561,19 @@ __global__ void k_cull_groups(int nb, int* row) {
 
 // pos: exclusive scan of the kept counts over the tile list (row-major, so a
 // row's entries keep tile order, then lane order)
-__global__ void k_cull_write(DevView v, long long ncand, const unsigned* jmask, const int* pos, const int* row) {
-  const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void k_cull_write(DevView v, const unsigned* jmask, const int* pos, const int* row) {
   const int lane = threadIdx.x & 31;
-  if (t >= ncand || t >= *v.ntiles) return;
-  const unsigned m = jmask[t];
-  if (!((m >> lane) & 1u)) return;
-  const Tile T = v.tiles[t];
+  const int nt = *v.ntiles;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nb = v.nblocks;
-  const long long e = (long long)row[3 * nb + T.bi] * 32 + (pos[t] - pos[row[nb + T.bi]]) +
-                      __popc(m & ((1u << lane) - 1u));
-  if (e < v.cull_cap) v.cull_ent[e] = make_float4(T.ox, T.oy, T.oz, __int_as_float(T.bj * 32 + lane));
+  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nwarps) {
+    const unsigned m = jmask[t];
+    if (!((m >> lane) & 1u)) continue;
+    const Tile T = v.tiles[t];
+    const long long e = (long long)row[3 * nb + T.bi] * 32 + (pos[t] - pos[row[nb + T.bi]]) +
+                        __popc(m & ((1u << lane) - 1u));
+    if (e < v.cull_cap) v.cull_ent[e] = make_float4(T.ox, T.oy, T.oz, __int_as_float(T.bj * 32 + lane));
+  }
 }
 
 // one warp per row: group -> row, empty entries closing the row's last group,
@@ -570,6 +599,14 @@ __global__ void k_cull_rows(DevView v, const int* row) {
 
 static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
+// grid of the warp-per-tile list kernels (grid-stride; 16 CTAs of 8 warps per SM)
+static int list_tile_grid(const Context& c) {
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
+  const long long want = (c.ncand + 7) / 8, g = 16LL * (sms > 0 ? sms : 1);
+  return (int)(want < g ? (want > 0 ? want : 1) : g);
+}
+
 static void launch_cull(Context& c, float list_radius) {
   c.kernel_launches += 10;
   DevView v = c.view();
@@ -580,7 +617,8 @@ static void launch_cull(Context& c, float list_radius) {
   cudaMemsetAsync(row + nb, 0x7f, sizeof(int) * nb, st);
   const float R = list_radius + 1e-3f;
   // the kept counts and their scan reuse the tile-compaction arrays
-  k_cull_mask<<<nblk(c.ncand * 32, 256), 256, 0, st>>>(v, c.ncand, R * R, c.d_cull_mask.p, c.d_tile_flag.p, row);
+  cudaMemsetAsync(c.d_tile_flag.p, 0, sizeof(int) * c.ncand, st);
+  k_cull_mask<<<list_tile_grid(c), 256, 0, st>>>(v, R * R, c.d_cull_mask.p, c.d_tile_flag.p, row);
   const int nb2 = nblk(c.ncand, 1024);
   k_scan_block<<<nb2, 1024, 0, st>>>(c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
   k_scan_sums<<<1, 1024, 0, st>>>(c.d_scan_tmp2.p, nb2);
@@ -590,12 +628,12 @@ static void launch_cull(Context& c, float list_radius) {
   k_scan_block<<<nb3, 1024, 0, st>>>(row + 2 * nb, row + 3 * nb, c.d_cull_scan_tmp.p, nb);
   k_scan_sums<<<1, 1024, 0, st>>>(c.d_cull_scan_tmp.p, nb3);
   k_scan_add<<<nb3, 1024, 0, st>>>(row + 3 * nb, c.d_cull_scan_tmp.p, nb);
-  k_cull_write<<<nblk(c.ncand * 32, 256), 256, 0, st>>>(v, c.ncand, c.d_cull_mask.p, c.d_tile_pos.p, row);
+  k_cull_write<<<list_tile_grid(c), 256, 0, st>>>(v, c.d_cull_mask.p, c.d_tile_pos.p, row);
   k_cull_rows<<<nblk((long long)nb * 32, 256), 256, 0, st>>>(v, row);
 }
 
 int launch_list_build(Context& c, float list_radius, float full_radius) {
-  c.kernel_launches += 18;
+  c.kernel_launches += 19;
   DevView v = c.view();
   cudaStream_t st = c.stream;
   int ncells = c.nsys * kCellsPerSystem;
@@ -632,8 +670,10 @@ int launch_list_build(Context& c, float list_radius, float full_radius) {
   }
   k_tile_write<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, list_radius, (float)c.lp.Padding, full_radius,
                                                     c.full_margin(), c.d_tile_flag.p, c.d_tile_pos.p);
-  // masks: launched over the worst case; warps beyond *ntiles return at once
-  k_masks<<<nblk(c.ncand * 32, 256), 256, 0, st>>>(v);
+  cudaMemsetAsync(c.d_tile_need.p, 0, c.ncand, st);
+  k_mask_mark<<<nblk(c.natom, 256), 256, 0, st>>>(v, c.d_slot_of.p, c.d_tile_flag.p, c.d_tile_pos.p,
+                                                   c.d_tile_need.p);
+  k_masks<<<list_tile_grid(c), 256, 0, st>>>(v, c.d_tile_need.p);
   if (c.has_gb) {
     c.kernel_launches += 5;
     int nb2 = nblk(c.ncand, 1024);

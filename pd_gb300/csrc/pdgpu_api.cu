@@ -417,6 +417,7 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
   if (e == cudaSuccess && c.has_gb) e = c.d_items.alloc(c.ncand);
   if (e == cudaSuccess) e = c.d_tile_flag.alloc(c.ncand);
   if (e == cudaSuccess) e = c.d_tile_pos.alloc(c.ncand);
+  if (e == cudaSuccess) e = c.d_tile_need.alloc(c.ncand);
   if (e == cudaSuccess) e = c.d_scan_tmp2.alloc((c.ncand + 1023) / 1024 + 1);
   if (e == cudaSuccess) e = c.d_masks.alloc((size_t)c.ncand * 32);
   if (e == cudaSuccess) e = c.d_xq.alloc(c.nslots);

@@ -88,6 +88,7 @@ struct Context {
   DBuf<float4> d_half;         // [nblocks]
   DBuf<Tile> d_tiles;          // [ncand] row-major tile list
   DBuf<int> d_tile_flag, d_tile_pos, d_scan_tmp2;  // tile-list compaction
+  DBuf<unsigned char> d_tile_need;                  // [ncand] tile holds a bonded pair (mask build)
   DBuf<int> d_counters;        // [0] ntiles, [1] nmasks, [2] nitems, [3..5] NB groups (rest tiles, groups, fit)
   DBuf<unsigned> d_items;      // [ncand] GB work items (with GB only)
   DBuf<uint2> d_masks;         // [ncand*32] worst case
