@@ -342,3 +342,36 @@ def test_trajectory_frames_without_host_sync(goldens, tmp_path):
     w.append(ring)
     back = read_pdb_models(path)
     assert back.shape == (4, im.natom, 3) and np.allclose(back, ring, atol=6e-4)
+
+
+def test_autotune_restores_the_state_and_picks_listed_settings(goldens):
+    """pdgpu_md_autotune runs trial dynamics from a saved state and puts it back:
+    positions and velocities bit-identical, and the next step (the step counter
+    keys the Langevin noise) the same as on a context that never tuned, to the
+    FP32 rounding the chosen list settings allow.  Every setting comes from the
+    tuner's candidate sets."""
+    from pd_gb300 import ffi
+    from pd_gb300.md import maxwell_boltzmann
+    d = goldens["water_c1"]
+    v_init = maxwell_boltzmann(d["mass"], 300.0, 5)
+    ctxs = []
+    for _ in range(2):
+        ctx = water_ctx(d, 1, ffi.NB | ffi.BONDED)
+        ctx.set_velocities(v_init)
+        ctx.md_run(5)
+        ctxs.append(ctx)
+    tuned_ctx, plain_ctx = ctxs
+    p0, v0 = tuned_ctx.get_positions(), tuned_ctx.get_velocities()
+    tuned = tuned_ctx.autotune(trial_steps=10)
+    assert tuned["UpdateNList"] in (1, 2, 3, 5, 10, 20, 40, 80)
+    assert tuned["ctas_per_sm"] in (2, 4, 8, 16)
+    assert tuned["gb_tiles_per_item"] in (1, 2)
+    assert tuned["nb_groups"] in (True, False)
+    assert np.array_equal(tuned_ctx.get_positions(), p0)
+    assert np.array_equal(tuned_ctx.get_velocities(), v0)
+    tuned_ctx.md_run(1)
+    plain_ctx.md_run(1)
+    assert np.allclose(tuned_ctx.get_positions(), plain_ctx.get_positions(), rtol=0, atol=1e-9)
+    assert rel_rms(tuned_ctx.get_velocities(), plain_ctx.get_velocities()) <= 1e-6
+    for c in ctxs:
+        c.close()
