@@ -33,13 +33,23 @@ __device__ __forceinline__ bool still_in(const DevView& v, const GBConst& k, flo
   return in;
 }
 
-// P4 CCF / r^4 of one pair (rs = R_i + R_j, raw type radii)
-__device__ __forceinline__ float born_w(const GBConst& k, float r2, float rs) {
-  const float rdivR = __fdividef(r2, rs * rs);
+// Close contact, r^2 / (R_i + R_j)^2 <= 1 / P5, where the CCF switches on.  Tested
+// as r^2 <= rs^2 / P5 (no division); the CCF is continuous there (h = 1), so
+// the rounding of the test does not matter.  Rare in a tile: the bodies take
+// the branch only when some lane of the warp needs it (a warp vote), so the
+// trigonometric code is skipped, not predicated, on nearly every step.
+__device__ __forceinline__ bool gb_contact(const GBConst& k, float r2, float rs2) { return r2 <= rs2 * k.invP5; }
+
+// P4 CCF / r^4 of one pair (rs = R_i + R_j, raw type radii); any_contact: the
+// warp vote over gb_contact
+__device__ __forceinline__ float born_w(const GBConst& k, float r2, float rs, bool any_contact) {
+  const float rs2 = rs * rs;
   float ccf = 1.f;
-  if (rdivR <= k.invP5) {
-    const float h = 0.5f - 0.5f * cospif(rdivR * k.P5);
-    ccf = h * h;
+  if (any_contact) {
+    if (gb_contact(k, r2, rs2)) {
+      const float h = 0.5f - 0.5f * cospif(__fdividef(r2, rs2) * k.P5);
+      ccf = h * h;
+    }
   }
   const float ir2 = __fdividef(1.f, r2);
   return k.P4 * ccf * ir2 * ir2;
@@ -56,8 +66,10 @@ __device__ __forceinline__ void born_tile(const DevView& v, const GBConst& k, co
     const float r2 = dx * dx + dy * dy + dz * dz;
     bool in = still_in<FULL>(v, k, r2, si, T.bj * 32 + ((lane + kk) & 31));
     if (MASKED) in = in && !((ex >> kk) & 1u);
+    const float rs = pi.z + pj.z;
+    const bool anyc = __any_sync(0xffffffffu, in && gb_contact(k, r2, rs * rs));
     if (in) {
-      const float w = born_w(k, r2, pi.z + pj.z);
+      const float w = born_w(k, r2, rs, anyc);
       gi += w * pj.w;
       gj += w * pi.w;
     }
@@ -91,15 +103,18 @@ __device__ __forceinline__ void born_tile2(const DevView& v, const GBConst& k, c
     const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
     const float2 rs = __fadd2_rn(RS, f2(pr.z));
     const float2 rs2 = __fmul2_rn(rs, rs);
-    const float qa = __fdividef(r2.x, rs2.x), qb = __fdividef(r2.y, rs2.y);
+    const float2 lim = __fmul2_rn(rs2, f2(k.invP5));
+    const bool ca = r2.x <= lim.x, cb = r2.y <= lim.y;
     float2 ccf = f2(1.f);
-    if (qa <= k.invP5) {
-      const float h = 0.5f - 0.5f * cospif(qa * k.P5);
-      ccf.x = h * h;
-    }
-    if (qb <= k.invP5) {
-      const float h = 0.5f - 0.5f * cospif(qb * k.P5);
-      ccf.y = h * h;
+    if (__any_sync(0xffffffffu, ca || cb)) {
+      if (ca) {
+        const float h = 0.5f - 0.5f * cospif(__fdividef(r2.x, rs2.x) * k.P5);
+        ccf.x = h * h;
+      }
+      if (cb) {
+        const float h = 0.5f - 0.5f * cospif(__fdividef(r2.y, rs2.y) * k.P5);
+        ccf.y = h * h;
+      }
     }
     const float2 ir2 = make_float2(__fdividef(1.f, r2.x), __fdividef(1.f, r2.y));
     float2 w = __fmul2_rn(__fmul2_rn(P4, ccf), __fmul2_rn(ir2, ir2));
@@ -615,16 +630,18 @@ __global__ void k_gb_self(DevView v, const double* charge, GBConst k, double pre
 // pass 3: dE/da chain rule through the Born radii, both directions of a pair
 // ---------------------------------------------------------------------------
 // (c_i V_j + c_j V_i) (4 CCF - dCCF) / r^6 of one pair: the chain-rule force per unit d
-__device__ __forceinline__ float chain_w(const GBConst& k, float r2, float rs, float cv) {
-  const float rdivR = __fdividef(r2, rs * rs);
+__device__ __forceinline__ float chain_w(const GBConst& k, float r2, float rs, float cv, bool any_contact) {
+  const float rs2 = rs * rs;
   float ccf = 1.f, dccf = 0.f;
-  if (rdivR <= k.invP5) {
-    float sn, cs;
-    const float x = rdivR * k.P5;
-    sincospif(x, &sn, &cs);
-    const float h = 0.5f - 0.5f * cs;
-    ccf = h * h;
-    dccf = 2.f * h * sn * (x * 3.14159265358979f);
+  if (any_contact) {
+    if (gb_contact(k, r2, rs2)) {
+      float sn, cs;
+      const float x = __fdividef(r2, rs2) * k.P5;
+      sincospif(x, &sn, &cs);
+      const float h = 0.5f - 0.5f * cs;
+      ccf = h * h;
+      dccf = 2.f * h * sn * (x * 3.14159265358979f);
+    }
   }
   const float ir2 = __fdividef(1.f, r2);
   return cv * (4.f * ccf - dccf) * ir2 * ir2 * ir2;
@@ -643,8 +660,10 @@ __device__ __forceinline__ void chain_tile(const DevView& v, const GBConst& k, c
     const float r2 = dx * dx + dy * dy + dz * dz;
     bool in = still_in<FULL>(v, k, r2, si, T.bj * 32 + ((lane + kk) & 31));
     if (MASKED) in = in && !((ex >> kk) & 1u);
+    const float rs = pi.z + pj.z;
+    const bool anyc = __any_sync(0xffffffffu, in && gb_contact(k, r2, rs * rs));
     if (in) {
-      const float w = chain_w(k, r2, pi.z + pj.z, ci * pj.w + cj * pi.w);
+      const float w = chain_w(k, r2, rs, ci * pj.w + cj * pi.w, anyc);
       I.fx -= w * dx; I.fy -= w * dy; I.fz -= w * dz;
       J.fx += w * dx; J.fy += w * dy; J.fz += w * dz;
     }
@@ -678,21 +697,24 @@ __device__ __forceinline__ void chain_tile2(const DevView& v, const GBConst& k, 
     const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
     const float2 rs = __fadd2_rn(RS, f2(pr.z));
     const float2 rs2 = __fmul2_rn(rs, rs);
-    const float qa = __fdividef(r2.x, rs2.x), qb = __fdividef(r2.y, rs2.y);
+    const float2 lim = __fmul2_rn(rs2, f2(k.invP5));
+    const bool ca = r2.x <= lim.x, cb = r2.y <= lim.y;
     float2 fac = f2(4.f);  // 4 CCF - dCCF
-    if (qa <= k.invP5) {
-      float sn, cs;
-      const float x = qa * k.P5;
-      sincospif(x, &sn, &cs);
-      const float h = 0.5f - 0.5f * cs;
-      fac.x = 4.f * h * h - 2.f * h * sn * (x * 3.14159265358979f);
-    }
-    if (qb <= k.invP5) {
-      float sn, cs;
-      const float x = qb * k.P5;
-      sincospif(x, &sn, &cs);
-      const float h = 0.5f - 0.5f * cs;
-      fac.y = 4.f * h * h - 2.f * h * sn * (x * 3.14159265358979f);
+    if (__any_sync(0xffffffffu, ca || cb)) {
+      if (ca) {
+        float sn, cs;
+        const float x = __fdividef(r2.x, rs2.x) * k.P5;
+        sincospif(x, &sn, &cs);
+        const float h = 0.5f - 0.5f * cs;
+        fac.x = 4.f * h * h - 2.f * h * sn * (x * 3.14159265358979f);
+      }
+      if (cb) {
+        float sn, cs;
+        const float x = __fdividef(r2.y, rs2.y) * k.P5;
+        sincospif(x, &sn, &cs);
+        const float h = 0.5f - 0.5f * cs;
+        fac.y = 4.f * h * h - 2.f * h * sn * (x * 3.14159265358979f);
+      }
     }
     const float2 ir2 = make_float2(__fdividef(1.f, r2.x), __fdividef(1.f, r2.y));
     const float2 cvv = __ffma2_rn(CS, f2(pr.w), __fmul2_rn(f2(cr), VS));
