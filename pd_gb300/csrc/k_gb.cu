@@ -205,23 +205,35 @@ struct PairAcc {
   float fx, fy, fz, da;
 };
 
+// u = -r^2 / (4 a_i a_j) of a pair, and whether the pair may lie above the exp
+// threshold (the FP64 tie-break band included): the warp votes on it, and the
+// GB term's code runs only when some lane needs it (in the all-pairs case most
+// warp steps have none)
+__device__ __forceinline__ float gb_u(float r2, float ai, float aj) { return -0.25f * __fdividef(r2, ai * aj); }
+__device__ __forceinline__ bool gb_maybe_on(const GBConst& k, float u) {
+  return u >= k.thresh - 4e-6f * fabsf(k.thresh);
+}
+
 // One pair of the fused law: i = (xi.w, pix, piy, ai), j = (qj, pjx, pjy, aj),
-// (dx, dy, dz) = x_j - x_i.  Adds the force on i along d to I and its opposite to
-// J, dE/da to both, and (ENERGY) the pair energies to cv, ce, cp.  si, sj: slots
-// for the FP64 threshold tie-break.
+// (dx, dy, dz) = x_j - x_i, u = gb_u.  Adds the force on i along d to I and its
+// opposite to J, dE/da to both, and (ENERGY) the pair energies to cv, ce, cp.
+// si, sj: slots for the FP64 threshold tie-break; any_gb: the warp's vote on
+// gb_maybe_on (warp-uniform).
 template <bool ENERGY, bool FULL, bool FAST>
 __device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, float dx, float dy, float dz,
-                                            float r2, float qi, float qj, float pix, float piy, float pjx,
-                                            float pjy, float ai, float aj, bool excl, bool is14, int si, int sj,
-                                            PairAcc& I, PairAcc& J, float& cv, float& ce, float& cp) {
+                                            float r2, float u, bool any_gb, float qi, float qj, float pix, float piy,
+                                            float pjx, float pjy, float ai, float aj, bool excl, bool is14, int si,
+                                            int sj, PairAcc& I, PairAcc& J, float& cv, float& ce, float& cp) {
     const float invr = rsqrtf(r2);
     const float r = r2 * invr;
     const float qiqj = qi * qj;
     const float aiaj = ai * aj;
-    const float u = -0.25f * __fdividef(r2, aiaj);
-    bool gbon = u > k.thresh;
-    if (fabsf(u - k.thresh) <= 2e-6f * fabsf(k.thresh))
-      gbon = gb_on_fp64(v, si, sj, k.thresh_d);
+    bool gbon = false;
+    if (any_gb) {
+      gbon = u > k.thresh;
+      if (fabsf(u - k.thresh) <= 2e-6f * fabsf(k.thresh))
+        gbon = gb_on_fp64(v, si, sj, k.thresh_d);
+    }
     float g = 0.f;  // scalar multiplying (xj - xi) in the force on i
     float elec = 0.f, delec = 0.f;
     const float s14 = is14 ? k.elec14 : 1.f;
@@ -235,7 +247,7 @@ __device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, 
       dS = -4.f * k.invw2 * w * sw;
       S = sw * sw;
     }
-    if (gbon) {
+    if (any_gb && gbon) {
       const float tg = __expf(u);
       const float fgb = rsqrtf(r2 + tg * aiaj);
       const float l = fgb * fgb;
@@ -311,9 +323,12 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
       excl = (ex >> kk) & 1u;  // bond order <= 2: GB term only
       is14 = (m14 >> kk) & 1u;
     }
-    if ((FULL || r2 <= k.cut2) && pair)
-      gb_pair_one<ENERGY, FULL, FAST>(v, k, dx, dy, dz, r2, xi.w, xj.w, pi.x, pi.y, pj.x, pj.y, ai, aj, excl, is14,
-                                      si, T.bj * 32 + ((lane + kk) & 31), I, J, cv, ce, cp);
+    const bool in = (FULL || r2 <= k.cut2) && pair;
+    const float u = gb_u(r2, ai, aj);
+    const bool any_gb = __any_sync(0xffffffffu, in && gb_maybe_on(k, u));
+    if (in)
+      gb_pair_one<ENERGY, FULL, FAST>(v, k, dx, dy, dz, r2, u, any_gb, xi.w, xj.w, pi.x, pi.y, pj.x, pj.y, ai, aj,
+                                      excl, is14, si, T.bj * 32 + ((lane + kk) & 31), I, J, cv, ce, cp);
     if (ENERGY && (kk & 7) == 7) {
       evdw += (double)cv;
       eel += (double)ce;
@@ -397,16 +412,22 @@ __device__ __forceinline__ void gb_pair_tile2(const DevView& v, const GBConst& k
     {
       const float dx = xr.x - xa.x, dy = xr.y - xa.y, dz = xr.z - xa.z;
       const float r2 = dx * dx + dy * dy + dz * dz;
-      if (FULL || r2 <= k.cut2)
-        gb_pair_one<ENERGY, FULL, true>(v, k, dx, dy, dz, r2, xa.w, xr.w, pa.x, pa.y, pr.x, pr.y, aa, ar, false,
-                                        false, sa, sr, IA, R, cv, ce, cp);
+      const bool in = FULL || r2 <= k.cut2;
+      const float u = gb_u(r2, aa, ar);
+      const bool any_gb = __any_sync(0xffffffffu, in && gb_maybe_on(k, u));
+      if (in)
+        gb_pair_one<ENERGY, FULL, true>(v, k, dx, dy, dz, r2, u, any_gb, xa.w, xr.w, pa.x, pa.y, pr.x, pr.y, aa, ar,
+                                        false, false, sa, sr, IA, R, cv, ce, cp);
     }
     {
       const float dx = xr.x - xb.x, dy = xr.y - xb.y, dz = xr.z - xb.z;
       const float r2 = dx * dx + dy * dy + dz * dz;
-      if (FULL || r2 <= k.cut2)
-        gb_pair_one<ENERGY, FULL, true>(v, k, dx, dy, dz, r2, xb.w, xr.w, pb.x, pb.y, pr.x, pr.y, ab, ar, false,
-                                        false, sb, sr, IB, R, cv, ce, cp);
+      const bool in = FULL || r2 <= k.cut2;
+      const float u = gb_u(r2, ab, ar);
+      const bool any_gb = __any_sync(0xffffffffu, in && gb_maybe_on(k, u));
+      if (in)
+        gb_pair_one<ENERGY, FULL, true>(v, k, dx, dy, dz, r2, u, any_gb, xb.w, xr.w, pb.x, pb.y, pr.x, pr.y, ab, ar,
+                                        false, false, sb, sr, IB, R, cv, ce, cp);
     }
     if (ENERGY && (kk & 7) == 7) {
       evdw += (double)cv;
