@@ -126,15 +126,22 @@ __device__ __forceinline__ void adj_gb_tile(const DevView& v, const GBConst& k, 
       excl = (ex >> kk) & 1u;
       is14 = (m14 >> kk) & 1u;
     }
-    if (r2 <= k.cut2 && pair) {
+    // the GB term's code runs only when some lane may lie above the exp
+    // threshold (warp vote, FP64 tie-break band included)
+    const bool in = r2 <= k.cut2 && pair;
+    const float u = -0.25f * __fdividef(r2, ai * aj);
+    const bool any_gb = __any_sync(0xffffffffu, in && u >= k.thresh - 4e-6f * fabsf(k.thresh));
+    if (in) {
       const float invr = rsqrtf(r2);
       const float r = r2 * invr;
-      const float u = -0.25f * __fdividef(r2, ai * aj);
-      bool gbon = u > k.thresh;
-      if (fabsf(u - k.thresh) <= 2e-6f * fabsf(k.thresh)) {
-        const int a = v.sorted_atom[si], b = v.sorted_atom[T.bj * 32 + ((lane + kk) & 31)];
-        gbon = a >= 0 && b >= 0 && -0.25 * r2_slots_fp64(v, si, T.bj * 32 + ((lane + kk) & 31)) /
-                                           (v.born[a] * v.born[b]) > k.thresh_d;
+      bool gbon = false;
+      if (any_gb) {
+        gbon = u > k.thresh;
+        if (fabsf(u - k.thresh) <= 2e-6f * fabsf(k.thresh)) {
+          const int a = v.sorted_atom[si], b = v.sorted_atom[T.bj * 32 + ((lane + kk) & 31)];
+          gbon = a >= 0 && b >= 0 && -0.25 * r2_slots_fp64(v, si, T.bj * 32 + ((lane + kk) & 31)) /
+                                             (v.born[a] * v.born[b]) > k.thresh_d;
+        }
       }
       float S = 1.f;
       if (r >= k.inner) {
@@ -144,7 +151,7 @@ __device__ __forceinline__ void adj_gb_tile(const DevView& v, const GBConst& k, 
       }
       const float s14 = is14 ? k.elec14 : 1.f;
       float phi = 0.f;  // energy per unit q_i q_j
-      if (gbon) {
+      if (any_gb && gbon) {
         const float fgb = rsqrtf(r2 + __expf(u) * ai * aj);
         phi = 2.f * k.premul * fgb * S;
         if (!excl) phi += k.econv_in * s14 * invr * S;
@@ -223,22 +230,27 @@ __device__ __forceinline__ void adj_born_tile(const DevView& v, const GBConst& k
     if (fabsf(r2 - k.still2) <= 2e-6f * k.still2)
       in = r2_slots_fp64(v, si, T.bj * 32 + ((lane + kk) & 31)) <= k.still2_d;
     if (MASKED) in = in && !((ex >> kk) & 1u);
+    // close contact (r^2 <= rs^2 / P5, where the CCF switches on) is rare: its
+    // branch runs on a warp vote
+    const float rs = pi.z + pj.z, rs2 = rs * rs;
+    const bool anyc = __any_sync(0xffffffffu, in && r2 <= rs2 * k.invP5);
     if (in) {
-      const float rs = pi.z + pj.z;
-      const float x = __fdividef(r2, rs * rs);
-      float ccf = 1.f, dccf = 0.f;  // CCF and dCCF/dx
-      if (x <= k.invP5) {
-        float sn, cs;
-        sincospif(x * k.P5, &sn, &cs);
-        const float h = 0.5f - 0.5f * cs;
-        ccf = h * h;
-        dccf = h * sn * (k.P5 * 3.14159265358979f);
+      float ccf = 1.f, gx = 0.f;  // CCF, and dCCF/dx * dx/dR (0 outside contact)
+      if (anyc) {
+        if (r2 <= rs2 * k.invP5) {
+          const float x = __fdividef(r2, rs2);
+          float sn, cs;
+          sincospif(x * k.P5, &sn, &cs);
+          const float h = 0.5f - 0.5f * cs;
+          ccf = h * h;
+          gx = h * sn * (k.P5 * 3.14159265358979f) * (-2.f * __fdividef(x, rs));
+        }
       }
       const float ir2 = __fdividef(1.f, r2);
       const float h4 = k.P4 * ir2 * ir2;
       IC.b += wj * h4 * ccf;  // dE/dV_i from Gpol_j
       JC.b += wi * h4 * ccf;  // dE/dV_j from Gpol_i
-      const float gR = (wi * pj.w + wj * pi.w) * h4 * dccf * (-2.f * __fdividef(x, rs));
+      const float gR = (wi * pj.w + wj * pi.w) * h4 * gx;
       IC.a += gR;
       JC.a += gR;
     }
