@@ -162,7 +162,7 @@ def gb_settings(image):
 NB_CUTOFF = 12.0   # FF_NonBonded Cutoff and VdwCutoff of the C1/C2 workloads (A)
 
 # DRAM bytes (read + write) per launch of the roofline kernels, from one ncu
-# capture of each workload (profiles/traffic_roofline_kernels.md)
+# capture of each workload (the DRAM traffic summary under profiles/)
 NCU_TRAFFIC = {
     "c4": {"k_gb_pair": 41.33e6, "k_langevin": 23.55e6},
     "c3": {"k_gb_pair": 0.85e6, "k_langevin": 0.50e6},
@@ -365,7 +365,7 @@ def run_reference(args, key, wl, image):
     v = statistics.median(vals)
     out = {"metric": METRIC, "value": v, "unit": "atom-steps/s", "impl": "reference", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic (systems built by PD, see DESIGN.md)",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (systems built by PD: NewProtein + seeded compaction, TIP3P lattice)",
            "config": {"workload": key, "description": wl["desc"]},
            "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": cb.threads, "kind": "port",
                             "sample": "median over %d samples of %.2f s: %s" % (args.steps, per_step,
@@ -548,7 +548,7 @@ def run_ours(args, key, wl, image):
     out = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math / int64 fixed-point sums / f64 state",
-           "data": "synthetic systems built by PD (NewProtein + seeded compaction, TIP3P lattice), see DESIGN.md",
+           "data": "synthetic systems built by PD (NewProtein + seeded compaction, TIP3P lattice)",
            "config": {"workload": key, "description": wl["desc"], "atoms": int(natom),
                       "preparation": "untimed relaxation: %d Langevin steps at %.1f fs, friction %.0e/s, then "
                                      "Maxwell-Boltzmann velocities" % (RELAX["steps"], RELAX["dt"] * 1e15,
