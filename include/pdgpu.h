@@ -340,6 +340,20 @@ long long pdgpu_kernel_launches(pdgpu_ctx *ctx);
 int pdgpu_time_kernel(pdgpu_ctx *ctx, int kernel, int reps, int flush_l2, double *avg_ms);
 /* Stream the context launches on (cudaStream_t as void*), for event timing. */
 void *pdgpu_stream(pdgpu_ctx *ctx);
+/* Device memory of the library in this process, over all contexts: cudaMalloc
+ * calls made so far (count, never decreases) and bytes held now (either may be
+ * NULL).  No counterpart in PD; a diagnostic (e.g. to check that a call
+ * allocated nothing). */
+int pdgpu_device_allocations(long long *count, long long *bytes);
+
+/* ---- host memory ------------------------------------------------------------ */
+/* Page-locked host memory for buffers the library fills asynchronously (the
+ * trajectory ring of pdgpu_md_set_trajectory), so callers need no CUDA runtime
+ * of their own.  No counterpart in PD (its trajectory writer reads ordinary
+ * host memory).  PDGPU_ERR_CUDA when the runtime cannot provide it (e.g. no
+ * GPU): ordinary memory also works, with copies that wait for the step. */
+int pdgpu_host_alloc(size_t bytes, void **ptr);
+int pdgpu_host_free(void *ptr);
 
 #ifdef __cplusplus
 }

@@ -480,20 +480,19 @@ int launch_adjoint(Context& c, unsigned what, double* d_q, double* d_r, double* 
 // ---------------------------------------------------------------------------
 static __device__ __align__(256) unsigned char g_adj_scratch[(size_t)kNoAllocMaxSlots *
                                                              (G_NACC * sizeof(long long) + sizeof(float))];
-static void* g_adj_scratch_addr[kNoAllocMaxDevices] = {};
 
 int launch_adjoint_static(Context& c, unsigned what, double* d_q, double* d_r, double* d_e, double* d_R, double* d_V,
                           double* d_T) {
   if (c.nslots > kNoAllocMaxSlots) return PDGPU_ERR_CAPACITY;
-  if (c.device < 0 || c.device >= kNoAllocMaxDevices) return PDGPU_ERR_ARG;
-  if (!g_adj_scratch_addr[c.device]) {
-    // once per device, with that device current: the array's device address
-    // (in host code its name only stands in for the symbol)
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_adj_scratch) != cudaSuccess || !p) return PDGPU_ERR_CUDA;
-    g_adj_scratch_addr[c.device] = p;
-  }
-  unsigned char* base = static_cast<unsigned char*>(g_adj_scratch_addr[c.device]);
+  // The array's device address on the current device (the caller made the
+  // context's device current).  In host code the array's name only stands in
+  // for the symbol.  Looked up on every call: the lookup is cheap once the
+  // module is loaded, keeps no host-side cache (nothing to go stale after a
+  // device reset, nothing shared between host threads), and the first call on
+  // a device may load the library's device code there.
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_adj_scratch) != cudaSuccess || !p) return PDGPU_ERR_CUDA;
+  unsigned char* base = static_cast<unsigned char*>(p);
   long long* g = reinterpret_cast<long long*>(base);
   float* w = reinterpret_cast<float*>(base + (size_t)kNoAllocMaxSlots * G_NACC * sizeof(long long));
   return launch_adjoint_into(c, what, g, w, d_q, d_r, d_e, d_R, d_V, d_T);

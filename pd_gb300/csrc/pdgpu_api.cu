@@ -966,3 +966,25 @@ int pdgpu_list_stats(pdgpu_ctx* h, long long* ntiles, long long* nmasked, long l
 void* pdgpu_stream(pdgpu_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
 
 }  // extern "C"
+
+int pdgpu_device_allocations(long long* count, long long* bytes) {
+  if (count) *count = g_device_allocs.load();
+  if (bytes) *bytes = g_device_bytes.load();
+  return PDGPU_OK;
+}
+
+int pdgpu_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr || bytes == 0) return PDGPU_ERR_ARG;
+  *ptr = nullptr;
+  if (cudaHostAlloc(ptr, bytes, cudaHostAllocDefault) != cudaSuccess) {
+    *ptr = nullptr;
+    cudaGetLastError();  // leave no pending error for the caller's next runtime call
+    return PDGPU_ERR_CUDA;
+  }
+  return PDGPU_OK;
+}
+
+int pdgpu_host_free(void* ptr) {
+  if (!ptr) return PDGPU_OK;
+  return cudaFreeHost(ptr) == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
+}

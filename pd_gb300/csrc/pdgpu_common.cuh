@@ -190,7 +190,6 @@ int launch_adjoint(Context& c, unsigned what, double* d_q, double* d_r, double* 
 // the same into a static device array: no allocation during the call (at most
 // kNoAllocMaxSlots sorted slots; one scratch per device shared by all contexts)
 constexpr int kNoAllocMaxSlots = 65536;
-constexpr int kNoAllocMaxDevices = 64;
 int launch_adjoint_static(Context& c, unsigned what, double* d_q, double* d_r, double* d_e, double* d_R, double* d_V,
                           double* d_T);
 // Monte Carlo partial NB energies: take the reference from the last energy

@@ -1,5 +1,6 @@
 // pdgpu_context.cuh — host-side context: device buffers, parameters, stream.
 #pragma once
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -7,18 +8,33 @@
 
 namespace pdgpu {
 
+// Every device allocation of the library goes through DBuf; these process-wide
+// counters (cudaMalloc calls made, bytes held) back pdgpu_device_allocations.
+inline std::atomic<long long> g_device_allocs{0};
+inline std::atomic<long long> g_device_bytes{0};
+
 template <typename T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
   cudaError_t alloc(size_t count) {
     release();
-    n = count;
     if (count == 0) return cudaSuccess;
-    return cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    n = count;
+    g_device_allocs.fetch_add(1);
+    g_device_bytes.fetch_add((long long)(count * sizeof(T)));
+    return cudaSuccess;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      g_device_bytes.fetch_sub((long long)(n * sizeof(T)));
+    }
     p = nullptr;
     n = 0;
   }

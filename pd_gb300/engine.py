@@ -257,12 +257,9 @@ class DeviceContext:
             ffi.check(self.lib.pdgpu_md_set_trajectory(self.h, 0, None, 0), "pdgpu_md_set_trajectory")
             self._traj_ring = None
             return None
-        try:
-            import torch
-            ring = torch.zeros((nslots, self.natom, 3), dtype=torch.float64, pin_memory=True).numpy()
-        except Exception:       # no CUDA torch: pageable memory (the copy then waits for the step)
-            ring = np.zeros((nslots, self.natom, 3))
-        self._traj_ring = ring   # kept alive with the context
+        # page-locked through the library (pdgpu_host_alloc), so the copies stay
+        # asynchronous; kept alive with the context
+        ring = self._traj_ring = ffi.host_array((nslots, self.natom, 3))
         ffi.check(self.lib.pdgpu_md_set_trajectory(self.h, int(every), _pd(ring), int(nslots)),
                   "pdgpu_md_set_trajectory")
         return ring

@@ -131,6 +131,10 @@ SIGNATURES = {
     "pdgpu_synchronize": ([ctypes.c_void_p], ctypes.c_int),
     "pdgpu_kernel_launches": ([ctypes.c_void_p], ctypes.c_longlong),
     "pdgpu_time_kernel": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp], ctypes.c_int),
+    "pdgpu_device_allocations": ([ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
+                                 ctypes.c_int),
+    "pdgpu_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "pdgpu_host_free": ([ctypes.c_void_p], ctypes.c_int),
 }
 
 _lib = None
@@ -164,6 +168,32 @@ def load(build_if_missing=True):
         fn.restype = res
     _lib = L
     return L
+
+
+def device_allocations():
+    """(cudaMalloc calls the library made so far, device bytes it holds now)."""
+    n, b = ctypes.c_longlong(), ctypes.c_longlong()
+    check(load().pdgpu_device_allocations(ctypes.byref(n), ctypes.byref(b)), "pdgpu_device_allocations")
+    return n.value, b.value
+
+
+def host_array(shape):
+    """A float64 numpy array in page-locked host memory from pdgpu_host_alloc
+    (ordinary memory when the runtime cannot provide it).  The memory is freed
+    by pdgpu_host_free once the array and every view of it are gone."""
+    import weakref
+
+    import numpy as np
+    count = int(np.prod(shape))
+    L = load()
+    ptr = ctypes.c_void_p()
+    if L.pdgpu_host_alloc(8 * count, ctypes.byref(ptr)) != OK:
+        return np.zeros(shape)
+    buf = (ctypes.c_double * count).from_address(ptr.value)
+    weakref.finalize(buf, L.pdgpu_host_free, ctypes.c_void_p(ptr.value))
+    arr = np.frombuffer(buf, dtype=np.float64).reshape(shape)   # keeps buf (and the memory) alive
+    arr[...] = 0.0
+    return arr
 
 
 def check(status, where):

@@ -2,8 +2,11 @@
 
 Runs here only (it needs the PD sources to build ``oracle/_ref/ref_driver``):
 
-    make -C oracle ref
-    PD_PARAM_PATH=<pd>/param python tests/golden/make_golden.py [--fixtures] [--workloads]
+    make -C oracle ref REF=<PD checkout>
+    PD_SOURCES=<PD checkout> python tests/golden/make_golden.py [--fixtures] [--workloads] [--configs]
+
+``PD_SOURCES`` names the PD checkout (its ``param/`` directory holds the force
+field files); ``PD_PARAM_PATH`` may name the parameter directory directly.
 
 Outputs
 -------
@@ -11,6 +14,13 @@ tests/golden/<case>.npz
     System description plus PD's own FP64 energies (J), forces (N), Born radii,
     per-atom SASA, neighbour-list checksums and pair-law scans for that system.
     These pin the C restatement in ``oracle/`` and the CUDA path.
+tests/golden/cfg_<workload>.npz
+    PD's FP64 energies, forces (stored as float32, a relative rounding of
+    6e-8, far inside the 1e-5 force tolerance), Born radii and per-atom SASA
+    for the benchmark workloads themselves: the solvated C2 box, the C3
+    peptide and the smallest and largest C4 peptides, evaluated by PD at the
+    very positions stored in the workload images (checked by a hash of their
+    float32 bytes).
 pd_gb300/workloads/<name>.npz
     Compact system images (float32-exact positions, per-atom parameter classes,
     exclusion table, bonded terms) for the benchmark workloads.  Positions were
@@ -67,12 +77,22 @@ C4_SYSTEMS = 64
 C4_SEED = 4
 
 
+def param_path():
+    """PD's parameter directory: PD_PARAM_PATH, else $PD_SOURCES/param."""
+    if os.environ.get("PD_PARAM_PATH"):
+        return os.environ["PD_PARAM_PATH"]
+    src = os.environ.get("PD_SOURCES")
+    if not src:
+        sys.exit("set PD_SOURCES to the PD checkout (or PD_PARAM_PATH to its param/ directory)")
+    return os.path.join(src, "param")
+
+
 def run_driver(kind, opts):
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "out.bin")
         args = [DRIVER, kind, out] + ["%s=%s" % (k, v) for k, v in opts.items()]
         env = dict(os.environ)
-        env.setdefault("PD_PARAM_PATH", "/root/reference/param")
+        env.setdefault("PD_PARAM_PATH", param_path())
         subprocess.run(args, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, env=env)
         return read_container(out)
 
@@ -242,17 +262,80 @@ def make_c4():
     print("%-14s natoms=%6d  %7.1f kB" % ("c4_remd64", len(img["pos"]), os.path.getsize(path) / 1024))
 
 
+# ---------------------------------------------------------------------------
+# goldens at the benchmark workloads' own sizes
+# ---------------------------------------------------------------------------
+def c4_system_opts(k):
+    counts = c4_residue_counts()
+    return dict(seed=4000 + k, nres=int(counts[k]), padding=2, gbcutoff=999, gbinner=998, gbsastill=999,
+                cutoff=999, inner=998, nb=0, gb=1, sasa=1)
+
+
+def config_golden_specs():
+    """name -> (driver kind, driver options, workload image, system index or None)."""
+    counts = c4_residue_counts()
+    return {
+        "cfg_c2": ("solvated", WORKLOAD_SPECS["c2_solvated"][1], "c2_solvated", None),
+        "cfg_c3": ("peptide", WORKLOAD_SPECS["c3_gb256"][1], "c3_gb256", None),
+        "cfg_c4_small": ("peptide", c4_system_opts(int(counts.argmin())), "c4_remd64", int(counts.argmin())),
+        "cfg_c4_large": ("peptide", c4_system_opts(int(counts.argmax())), "c4_remd64", int(counts.argmax())),
+    }
+
+
+def pos_hash(pos):
+    """sha256 of the positions as float32 (the workload images store them so)."""
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(pos, dtype=np.float32).tobytes()).hexdigest()
+
+
+def make_config_goldens(which):
+    sys.path.insert(0, ROOT)
+    from pd_gb300.workspace import load_workload
+    for name, (kind, opts, image, k) in config_golden_specs().items():
+        if which and name not in which:
+            continue
+        d = run_driver(kind, opts)
+        im = load_workload(image)
+        sub = im if k is None else im.subset(k)
+        assert len(d["pos"]) == sub.natom and np.array_equal(d["pos"], sub.pos.astype(np.float64)), name
+        out = {"natoms": np.array([sub.natom]), "pos_sha256": np.array(pos_hash(sub.pos)),
+               "image": np.array(image), "system": np.array([-1 if k is None else k]),
+               "cfg_list_cutoff": d["cfg_list_cutoff"], "cfg_padding": d["cfg_padding"],
+               "gen_kind": np.array(kind), "gen_opts": np.array(repr(sorted(opts.items())))}
+        for tag in ("bonded", "nb", "gb", "sasa", "gbslow"):
+            if tag + "_ene" in d:
+                out[tag + "_ene"] = d[tag + "_ene"]
+        for tag in ("nb", "gb", "sasa"):
+            if tag + "_f" in d:
+                out[tag + "_f"] = d[tag + "_f"].astype(np.float32)
+        for key in d:
+            if (key.startswith("nb_") or key.startswith("gb_")) and d[key].size == 1:
+                out[key] = d[key]
+        if "gb_P" in d:
+            out["gb_P"] = d["gb_P"]
+            out["gb_born"] = d["gb_born"].astype(np.float32)
+        if "lcpo_sasa" in d:
+            out["lcpo_sasa"] = d["lcpo_sasa"].astype(np.float32)
+            out["lcpo_GlobalASP"] = d["lcpo_GlobalASP"]
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **out)
+        print("%-14s natoms=%6d  %7.1f kB" % (name, sub.natom, os.path.getsize(path) / 1024))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--fixtures", action="store_true")
     ap.add_argument("--workloads", nargs="*")
+    ap.add_argument("--configs", nargs="*", help="goldens at the workloads' own sizes (cfg_*.npz)")
     a = ap.parse_args()
     if not os.path.exists(DRIVER):
         sys.exit("build the reference first: make -C oracle ref")
-    if a.fixtures or a.workloads is None:
+    if a.fixtures or (a.workloads is None and a.configs is None):
         make_fixtures()
     if a.workloads is not None:
         make_workloads(a.workloads)
+    if a.configs is not None:
+        make_config_goldens(a.configs)
 
 
 if __name__ == "__main__":

@@ -3,10 +3,13 @@ a call allocate device memory (cudaMalloc synchronises the whole device, or
 their own pool holds the free memory), against pdgpu_param_grad_device, two
 calls in a row, through the C ABI.
 
-The file name sorts last, so a run that stops at the first failure has run
-every other test before this one; it also passes alone in a fresh process.
-Tolerance: both entry points run the same kernels on the same list, so the
-gradients agree to 1e-12 relative (in practice bit for bit)."""
+The allocation-free calls run first, on a fresh context of their own, and the
+library's allocation counter (pdgpu_device_allocations) must not move across
+them; the allocating entry point then runs on a second context of the same
+system.  The file name sorts last, so a run that stops at the first failure
+has run every other test before this one; it also passes alone in a fresh
+process.  Tolerance: both entry points run the same kernels on the same list,
+so the gradients agree to 1e-12 relative (in practice bit for bit)."""
 import ctypes
 
 import numpy as np
@@ -39,8 +42,7 @@ def _grads(ctx, what, entry):
     return {n: t.cpu().numpy() for n, t in out.items()}, E
 
 
-@pytest.mark.parametrize("case", ["gb", "nb"])
-def test_noalloc_matches_allocating_entry(goldens, case):
+def _setup(goldens, case):
     from pd_gb300 import ffi
     if case == "gb":
         d = goldens["peptide30"]
@@ -53,16 +55,32 @@ def test_noalloc_matches_allocating_entry(goldens, case):
         ctx.set_nb(**nb_kwargs(d, "nbfswitch"))
         what = ffi.NB
     ctx.set_positions(d["pos"])
-    ref, e_ref = _grads(ctx, what, "pdgpu_param_grad_device")
+    return ctx, what
+
+
+@pytest.mark.parametrize("case", ["gb", "nb"])
+def test_noalloc_matches_allocating_entry(goldens, case):
+    from pd_gb300 import ffi
+    fresh, what = _setup(goldens, case)
+    got = []
     for _ in range(2):
-        got, e = _grads(ctx, what, "pdgpu_param_grad_device_noalloc")
+        import torch
+        torch.cuda.synchronize()
+        n0, b0 = ffi.device_allocations()
+        got.append(_grads(fresh, what, "pdgpu_param_grad_device_noalloc"))
+        n1, b1 = ffi.device_allocations()
+        assert (n1, b1) == (n0, b0), "the allocation-free entry point allocated device memory"
+    fresh.close()
+    other, _ = _setup(goldens, case)
+    ref, e_ref = _grads(other, what, "pdgpu_param_grad_device")
+    other.close()
+    for g, e in got:
         for n in NAMES:
-            assert np.all(np.isfinite(got[n])), n
+            assert np.all(np.isfinite(g[n])), n
             scale = max(float(np.max(np.abs(ref[n]))), 1e-300)
-            assert np.max(np.abs(got[n] - ref[n])) <= 1e-12 * scale, n
+            assert np.max(np.abs(g[n] - ref[n])) <= 1e-12 * scale, n
         for k in ("vdw", "elec", "pol", "epot"):
             assert e[0][k] == e_ref[0][k], k
-    ctx.close()
 
 
 def test_noalloc_rejects_contexts_beyond_its_scratch(goldens):
