@@ -18,6 +18,7 @@ struct BondedView {
   const double* pos;
   long long* facc;
   long long* eacc;
+  unsigned* status;
   int nbond, nangle, ntors, nimpr;
   const int *bidx, *aidx, *tidx, *iidx;
   const double *bpar, *apar, *tpar, *ipar;   // kcal/mol units
@@ -25,6 +26,7 @@ struct BondedView {
 
 __device__ __forceinline__ void add_force(const BondedView& b, int atom, float fx, float fy, float fz) {
   int s = b.slot_of[atom];
+  fix_range(b.status, fabsf(fx) + fabsf(fy) + fabsf(fz));
   atomic_add_ll(&b.facc[3 * s], fx32(fx));
   atomic_add_ll(&b.facc[3 * s + 1], fx32(fy));
   atomic_add_ll(&b.facc[3 * s + 2], fx32(fz));
@@ -192,6 +194,7 @@ int launch_bonded(Context& c, bool energy) {
   b.atom_sys = c.d_atom_sys.p;
   b.pos = c.d_pos.p;
   b.facc = c.d_facc.p;
+  b.status = c.d_status.p;
   b.eacc = c.d_eacc.p;
   b.nbond = c.nbond; b.nangle = c.nangle; b.ntors = c.ntors; b.nimpr = c.nimpr;
   b.bidx = c.d_bidx.p; b.aidx = c.d_aidx.p; b.tidx = c.d_tidx.p; b.iidx = c.d_iidx.p;

@@ -127,6 +127,7 @@ __device__ __forceinline__ void born_tile2(const DevView& v, const GBConst& k, c
     gr = fmaf(w.y, pb.w, gr);
     ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(pr.z); ROT(pr.w); ROT(gr);
   }
+  fix_range(v.status, fabsf(G.x) + fabsf(G.y) + fabsf(gr));
   atomic_add_ll(&gpol[sa], fx32(G.x));
   atomic_add_ll(&gpol[sb], fx32(G.y));
   atomic_add_ll(&gpol[r0 + lane], fx32(gr));
@@ -167,6 +168,7 @@ __global__ void __launch_bounds__(256) k_gb_born(DevView v, GBConst k, long long
       if (full) born_tile<false, true>(v, k, T, lane, si, xi, pi, ex, gi, gj);
       else born_tile<false, false>(v, k, T, lane, si, xi, pi, ex, gi, gj);
     }
+    fix_range(v.status, fabsf(gi) + fabsf(gj));
     atomic_add_ll(&gpol[si], fx32(gi));
     atomic_add_ll(&gpol[T.bj * 32 + lane], fx32(gj));
   }
@@ -340,10 +342,6 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
   }
 }
 
-__device__ __forceinline__ bool finite_acc(const PairAcc& a) {
-  return fabsf(a.fx) + fabsf(a.fy) + fabsf(a.fz) + fabsf(a.da) < 1.0e18f;
-}
-
 // per-tile FP32 sums enter 64-bit fixed point before they are combined, so a
 // slot's total does not depend on how its tiles were grouped into work items
 struct FixAcc {
@@ -351,7 +349,7 @@ struct FixAcc {
 };
 
 __device__ __forceinline__ void fix_in(const DevView& v, FixAcc& F, const PairAcc& a) {
-  if (!finite_acc(a)) atomicOr(v.status, (unsigned)ST_NAN);
+  fix_range(v.status, fabsf(a.fx) + fabsf(a.fy) + fabsf(a.fz) + fabsf(a.da));
   F.fx += fx32(a.fx);
   F.fy += fx32(a.fy);
   F.fz += fx32(a.fz);

@@ -224,6 +224,7 @@ __global__ void __launch_bounds__(256) k_lcpo_main(DevView v, const float4* lc, 
   }
   // the lanes combine in 64-bit fixed point (2^32 per unit, exact integer sums;
   // the force scale is the accumulators' own)
+  fix_range(v.status, fabsf(sa) + fabsf(fl[0]) + fabsf(fl[1]) + fabsf(fl[2]));
   const long long sum_sa = warp_sum_ll(fx32(sa));
   long long f[3];
 #pragma unroll

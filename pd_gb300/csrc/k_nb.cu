@@ -138,7 +138,7 @@ struct NBFix {
 };
 
 __device__ __forceinline__ void nb_fix_in(const DevView& v, NBFix& F, const NBAcc& a) {
-  if (!(fabsf(a.fx) + fabsf(a.fy) + fabsf(a.fz) < 1.0e18f)) atomicOr(v.status, (unsigned)ST_NAN);
+  fix_range(v.status, fabsf(a.fx) + fabsf(a.fy) + fabsf(a.fz));
   F.fx += fx32(a.fx);
   F.fy += fx32(a.fy);
   F.fz += fx32(a.fz);

@@ -161,6 +161,16 @@ __device__ __forceinline__ long long fx32(float x) {
   return (b >> 31) ? -(long long)r : (long long)r;
 }
 
+// Range of FP32 partial sums about to enter 64-bit fixed point (2^32 per unit):
+// m is the sum of their magnitudes.  NaN or infinity sets ST_NAN; 2^28 or more
+// sets ST_FIXED_OVERFLOW.  One conversion holds up to 2^30 and a slot's total
+// up to 2^31, so flagging every partial sum at 2^28 keeps a few large ones
+// from wrapping a total past the final check unnoticed.  (PD has no such
+// limit; 2^28 kcal/mol/A lies far beyond any physical force.)
+__device__ __forceinline__ void fix_range(unsigned* status, float m) {
+  if (!(m < 268435456.f)) atomicOr(status, !(m < 1.0e18f) ? (unsigned)ST_NAN : (unsigned)ST_FIXED_OVERFLOW);
+}
+
 __device__ __forceinline__ void atomic_add_ll(long long* p, long long v) {
   atomicAdd(reinterpret_cast<unsigned long long*>(p), static_cast<unsigned long long>(v));
 }

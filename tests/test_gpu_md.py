@@ -177,6 +177,102 @@ def test_remd_exchange_swaps_temperatures_and_rescales(goldens):
         assert np.array_equal(v_after, v_before)
 
 
+def _philox4x32(ctr, key):
+    """Philox4x32-10 (Salmon et al., SC'11), the generator of the exchange draws."""
+    M = 0xFFFFFFFF
+    c0, c1, c2, c3 = ctr
+    k0, k1 = key
+    for _ in range(10):
+        p0, p1 = 0xD2511F53 * c0, 0xCD9E8D57 * c2
+        c0, c1, c2, c3 = ((p1 >> 32) ^ c1 ^ k0) & M, p1 & M, ((p0 >> 32) ^ c3 ^ k1) & M, p0 & M
+        k0, k1 = (k0 + 0x9E3779B9) & M, (k1 + 0xBB67AE85) & M
+    return c0, c1, c2, c3
+
+
+def _exchange_uniform(seed, rnd, rung):
+    """The uniform draw of rung `rung` in exchange round `rnd` (counter (round, rung, 7))."""
+    x = _philox4x32((rnd & 0xFFFFFFFF, rnd >> 32, rung, 7),
+                    ((seed & 0xFFFFFFFF) ^ 0x5BD1E995, seed >> 32))[0]
+    return (x + 0.5) / 4294967296.0
+
+
+def test_remd_metropolis_decision_matches_pd_criterion(goldens):
+    """REX_Local::exchangeCriterion (remd.cpp:349-356): delta = (E_lo - E_hi)
+    (1/kT_hi - 1/kT_lo), accept when delta <= 0 or exp(-delta) > u.  Four
+    systems of unequal energy on a ladder chosen so the first sweep's rungs have
+    delta = 0.3, 1.0 and 2.5, then 24 sweeps of alternating parity: every device
+    decision, the temperatures and the velocity rescaling against the host's
+    own evaluation of the criterion with the same Philox uniforms."""
+    from pd_gb300 import ffi
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.workspace import SystemImage
+    kB = 1.38065E-23
+    d = goldens["peptide30"]
+    rng = np.random.default_rng(11)
+    pos = [d["pos"] + rng.normal(0.0, 0.05, d["pos"].shape) for _ in range(4)]
+    im = SystemImage.concat([SystemImage._from_fixture(d)] * 4)
+    n = im.natoms[0]
+    what = ffi.GB | ffi.BONDED
+
+    def energies(ctx):
+        return np.array([e["epot"] for e in ctx.compute(what)])
+
+    probe = DeviceContext(im)
+    probe.set_list(2.0)
+    probe.set_gb(**gb_kwargs(d))
+    probe.set_positions(np.concatenate(pos))
+    E = energies(probe)
+    probe.close()
+    order = np.argsort(E)                     # rung r starts with the r-th lowest energy
+    pos = [pos[i] for i in order]
+    E = E[order]
+    T = [300.0]
+    for r, target in enumerate((0.3, 1.0, 2.5)):
+        dE = E[r] - E[r + 1]                  # < 0: the lower rung holds the lower energy
+        target = min(target, 0.5 * abs(dE) / (kB * T[r]))
+        T.append(1.0 / (1.0 / T[r] - target * kB / abs(dE)))
+    T = np.array(T)
+    seed = 0x1234ABCD5678
+    ctx = DeviceContext(im)
+    ctx.set_list(2.0)
+    ctx.set_gb(**gb_kwargs(d))
+    ctx.set_positions(np.concatenate(pos))
+    ctx.md_setup(T, integrator=0, timestep=1e-15, what=what, seed=seed)
+    v0 = np.tile(np.arange(1.0, 4.0), (im.natom, 1))
+    ctx.set_velocities(v0)
+    Edev = energies(ctx)                      # the energies the exchange reads
+    assert np.allclose(Edev, E, rtol=1e-12, atol=0)
+    holder = list(range(4))                   # system at each rung
+    temp = dict(zip(range(4), T))             # target temperature of each system
+    vscale = np.ones(4)
+    decided, draws_on = 0, 0
+    for rnd in range(24):
+        parity = rnd % 2
+        acc, temps = ctx.remd_exchange(parity)
+        for r in range(parity, 3, 2):
+            lo, hi = holder[r], holder[r + 1]
+            delta = (Edev[lo] - Edev[hi]) * (1.0 / (kB * T[r + 1]) - 1.0 / (kB * T[r]))
+            u = _exchange_uniform(seed, rnd, r)
+            want = delta <= 0 or np.exp(-delta) > u
+            if delta > 0 and abs(np.exp(-delta) - u) < 1e-9:
+                want = bool(acc[r])          # a draw within rounding of the boundary decides nothing
+            assert bool(acc[r]) == want, (rnd, r, delta, u)
+            decided += 1
+            draws_on += int(delta > 0)
+            if want:
+                f = np.sqrt(T[r + 1] / T[r])
+                holder[r], holder[r + 1] = hi, lo
+                temp[lo], temp[hi] = T[r + 1], T[r]
+                vscale[lo] *= f
+                vscale[hi] /= f
+        assert np.allclose(temps, [temp[s] for s in range(4)], rtol=0, atol=1e-12)
+    v = ctx.get_velocities()
+    for s in range(4):
+        assert np.allclose(v[s * n:(s + 1) * n], v0[s * n:(s + 1) * n] * vscale[s], rtol=1e-12)
+    assert draws_on >= 10 and decided == 36
+    ctx.close()
+
+
 def test_md_is_deterministic(goldens):
     from pd_gb300 import ffi
     d = goldens["water_c1"]

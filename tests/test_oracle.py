@@ -119,3 +119,44 @@ def test_gb_slow_mode_and_calc_energies_match_pd(goldens, name):
     p.ExpApproxThreshold = -1e300
     e2, _, _ = O.gb_forces(s, p, d["gb_radius"], d["gb_vj"], d["gb_terms123"])
     assert abs(e2[0] + en[0] - d["gbene_ene"][0]) <= 1e-12 * abs(d["gbene_ene"][0])
+
+
+def _cfg_system(name):
+    """A workload image (or one of its systems) with the PD outputs for it."""
+    import hashlib
+
+    from conftest import golden
+    from pd_gb300.workspace import load_workload
+    d = golden(name)
+    im = load_workload(str(d["image"]))
+    k = int(d["system"][0])
+    sub = im if k < 0 else im.subset(k)
+    h = hashlib.sha256(np.ascontiguousarray(sub.pos, dtype=np.float32).tobytes()).hexdigest()
+    assert h == str(d["pos_sha256"])
+    s = O.OracleSystem(sub.pos, sub.charge, sub.radius, sub.epsilon, sub.excl, tuple(sub.box[0]))
+    return d, sub, s
+
+
+def test_oracle_matches_pd_on_the_solvated_workload():
+    """The 22,489-atom periodic C2 box (solute + water): PD's forces are stored as
+    float32 (relative rounding 6e-8), energies in FP64."""
+    d, sub, s = _cfg_system("cfg_c2")
+    e, f = O.nonbonded(s, nb_params(d), nthreads=8)
+    for i, k in enumerate(("epot", "vdw", "elec")):
+        assert rel_err(e[i], ref_energy(d, "nb", k)) < 1e-12
+    assert rel_rms(f, d["nb_f"]) < 1e-7
+
+
+@pytest.mark.parametrize("name", ["cfg_c3", "cfg_c4_small", "cfg_c4_large"])
+def test_oracle_matches_pd_on_the_gb_workloads(name):
+    d, sub, s = _cfg_system(name)
+    e, f, born = O.gb_forces(s, gb_params(d), sub.gb_radius, sub.gb_vj, sub.gb_terms123, nthreads=8)
+    assert np.max(np.abs(born / d["gb_born"] - 1)) < 1e-6
+    for i, k in enumerate(("epot", "vdw", "elec", "pol", "pol_self", "pol_cross")):
+        assert rel_err(e[i], ref_energy(d, "gb", k)) < 1e-12, k
+    assert rel_rms(f, d["gb_f"]) < 1e-7
+    e, f, sa = O.lcpo_forces(s, list_cutoff(d), sub.lcpo_radius, sub.lcpo_p, sub.lcpo_sigma, sub.lcpo_use,
+                             nthreads=8)
+    assert rel_err(e[6], ref_energy(d, "sasa", "surf")) < 1e-12
+    assert np.max(np.abs(sa - d["lcpo_sasa"])) <= 1e-4
+    assert rel_rms(f, d["sasa_f"]) < 1e-7
