@@ -149,11 +149,13 @@ def test_oracle_matches_pd_on_the_solvated_workload():
 
 @pytest.mark.parametrize("name", ["cfg_c3", "cfg_c4_small", "cfg_c4_large"])
 def test_oracle_matches_pd_on_the_gb_workloads(name):
+    """Energies to 1e-11: over the 30 M pairs of the largest peptide the threaded
+    oracle and PD's sequential loop sum in different orders."""
     d, sub, s = _cfg_system(name)
     e, f, born = O.gb_forces(s, gb_params(d), sub.gb_radius, sub.gb_vj, sub.gb_terms123, nthreads=8)
     assert np.max(np.abs(born / d["gb_born"] - 1)) < 1e-6
     for i, k in enumerate(("epot", "vdw", "elec", "pol", "pol_self", "pol_cross")):
-        assert rel_err(e[i], ref_energy(d, "gb", k)) < 1e-12, k
+        assert rel_err(e[i], ref_energy(d, "gb", k)) < 1e-11, k
     assert rel_rms(f, d["gb_f"]) < 1e-7
     e, f, sa = O.lcpo_forces(s, list_cutoff(d), sub.lcpo_radius, sub.lcpo_p, sub.lcpo_sigma, sub.lcpo_use,
                              nthreads=8)
