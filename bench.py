@@ -36,8 +36,24 @@ sys.path.insert(0, ROOT)
 KB = 1.38065E-23
 METRIC = "atom-steps/s batched vs plain GPU at force rel err <=1e-5 vs FP64; % HBM roofline"
 
-# flops per pair of the pair kernels (FP32, FMA = 2 flops), frozen planning figures
-FLOPS = {"gb_born": 40, "gb_pair": 120, "gb_chain": 60, "nb": 77}
+# FP32 flops per pair of the pair kernels by the branch the pair takes (FMA =
+# 2 flops, each MUFU operation = 1), counted from the pair law each kernel
+# evaluates; pairs per branch come from pdgpu_pair_census at the final state.
+#   GB fused pair (k_gb_pair), every pair inside the GB cutoff: d (3), r^2 (5),
+#     u = -r^2/(4 a_i a_j) for the threshold test (4), 1/r (1), q_i q_j (1),
+#     Coulomb energy and dE/dr (3), LJ 12-6 (12), dE/dr / r (3), forces on both
+#     atoms (12): 44.  Above ExpApproxThreshold the GB cross term adds exp,
+#     f_GB = 1/sqrt(r^2 + a_i a_j e^u), E, dE/dr, dE/da for both atoms: +23.
+#   FF_NonBonded pair inside the cutoff (k_nb_tiles, energy-switched LJ and
+#     Coulomb): d (3), r^2 (5), 1/r and r (2), LJ (12), both switches (22),
+#     sum and 1/r (2), forces (12): 58.
+#   Born-radius pair (k_gb_born, both directions): d, r^2 (8), R_i + R_j and
+#     the contact test (3), 1/r^2 (1), P4 / r^4 (3), two sums (4): 19; in close
+#     contact the CCF adds 7.
+#   Chain-rule pair (k_gb_chain, both directions): d, r^2 (8), contact test
+#     (3), 1/r^2 (1), c_i V_j + c_j V_i (3), the factor over r^6 (4), forces
+#     (12): 31; in close contact the CCF and its derivative add 13.
+FLOPS = {"gb_pair": 44, "gb_term": 23, "nb": 58, "born": 19, "born_contact": 7, "chain": 31, "chain_contact": 13}
 # bytes per atom-step of the integrator: read p, v, f (24 B each) + mass (8 B), write p, v
 INTEGRATOR_BYTES = 80 + 48
 
@@ -270,24 +286,21 @@ def parity_check(image, wl, key, pos=None):
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle's FP64 restatement of PD's path on the host cores
 # ---------------------------------------------------------------------------
-class CPUBaseline:
-    """The oracle's FP64 restatement of PD's path stepping one system of the
-    workload on the host cores (OpenMP over every host thread).  State (positions,
-    velocities, PD's stored list and its 10-step cadence) carries over between
-    samples, so short samples amortise list builds as a long run does."""
+class CPUSystem:
+    """The oracle's FP64 restatement of PD's path stepping one system of a
+    workload: forces of the workload's components (PD's O(N^2) list kept for
+    UpdateNList = 10 steps for cutoff systems, LCPO every 5 steps), then the
+    FP64 integrator.  State (positions, velocities, stored list) carries over
+    between steps."""
 
-    def __init__(self, image, wl, key):
-        from oracle import pdoracle as O
-        self.O = O
-        self.wl = wl
-        self.threads = os.cpu_count() or 1
-        self.k = int(np.argsort(image.natoms)[image.nsystems // 2]) if image.nsystems > 1 else 0
-        self.sub = image.subset(self.k)
-        self.pos = self.sub.pos.copy()
+    def __init__(self, O, sub, wl, threads, seed):
+        self.O, self.sub, self.wl, self.threads = O, sub, wl, threads
+        self.pos = sub.pos.copy()
         self.vel = np.zeros_like(self.pos)
-        self.rng = np.random.default_rng(1)
+        self.rng = np.random.default_rng(seed)
         self.steps = 0
         self.nlist = None
+        self.f_sa = np.zeros_like(self.pos)
 
     def step(self):
         O, wl, sub, threads = self.O, self.wl, self.sub, self.threads
@@ -297,10 +310,10 @@ class CPUBaseline:
         if "NB" in wl["what"]:
             # PD keeps the list for UpdateNList = 10 steps (protocolbase.cpp:135-144)
             if self.steps % 10 == 0:
-                self.nlist = O.StoredList(s, 12 + wl["padding"], threads)
-            _, ff = O.nonbonded_list(s, self.nlist, O.nb_params(Cutoff=12, InnerCutoff=10, Vdw14Scaling=s14v,
-                                                                Elec14Scaling=s14e, ListCutoff=12 + wl["padding"]),
-                                     threads)
+                self.nlist = O.StoredList(s, NB_CUTOFF + wl["padding"], threads)
+            _, ff = O.nonbonded_list(s, self.nlist, O.nb_params(Cutoff=NB_CUTOFF, InnerCutoff=10, Vdw14Scaling=s14v,
+                                                                Elec14Scaling=s14e,
+                                                                ListCutoff=NB_CUTOFF + wl["padding"]), threads)
             f += ff
         if "GB" in wl["what"]:
             P = sub.gb_P
@@ -309,10 +322,11 @@ class CPUBaseline:
                              ListCutoff=999 + wl["padding"])
             _, ff, _ = O.gb_forces(s, gp, sub.gb_radius, sub.gb_vj, sub.gb_terms123, threads)
             f += ff
-        if "SA" in wl["what"] and self.steps % 5 == 0:
-            _, ff, _ = O.lcpo_forces(s, 999 + wl["padding"], sub.lcpo_radius, sub.lcpo_p, sub.lcpo_sigma,
-                                     sub.lcpo_use, threads)
-            f += ff
+        if "SA" in wl["what"]:
+            if self.steps % 5 == 0:     # FF_SASA_LCPO::UpdateSasa (lcpo.cpp:193-206): cached between
+                _, self.f_sa, _ = O.lcpo_forces(s, 999 + wl["padding"], sub.lcpo_radius, sub.lcpo_p, sub.lcpo_sigma,
+                                                sub.lcpo_use, threads)
+            f += self.f_sa
         if "BONDED" in wl["what"]:
             _, ff = O.bonded(self.pos, *sub.bonds, *sub.angles, *sub.torsions, *sub.impropers)
             f += ff
@@ -324,30 +338,114 @@ class CPUBaseline:
             self.pos, self.vel, _ = O.vv_step(self.pos, self.vel, f, sub.mass, wl["dt"])
         self.steps += 1
 
-    def run(self, budget_s):
-        """At least one MD step, then more until budget_s of wall clock; atom-steps/s."""
+
+def _cpu_worker(conn, key, systems, threads):
+    """One host process: loads the workload itself and steps its systems on
+    every 'step' message, answering with the seconds it took."""
+    sys.path.insert(0, ROOT)
+    from oracle import pdoracle as O
+    from pd_gb300.workspace import load_workload
+    wl = WORKLOADS[key]
+    image = load_workload(wl["image"])
+    mine = [CPUSystem(O, image.subset(k) if image.nsystems > 1 else image, wl, threads, 1 + k) for k in systems]
+    conn.send("ready")
+    while True:
+        msg = conn.recv()
+        if msg != "step":
+            break
         t0 = time.perf_counter()
-        n = 0
-        while True:
-            self.step()
-            n += 1
-            el = time.perf_counter() - t0
-            if el >= budget_s or n >= 10000:
-                break
-        self.last = (n, el)
-        return self.sub.natom * n / el
-
-    def describe(self):
-        n, el = self.last
-        return ("MD steps (forces + FP64 integrator; PD's O(N^2) list rebuilt every 10 steps for cutoff "
-                "systems, all pairs for GB) of system %d (%d atoms) of the workload, OpenMP over %d host threads; "
-                "last sample %d steps in %.2f s" % (self.k, self.sub.natom, self.threads, n, el))
+        for c in mine:
+            c.step()
+        conn.send(time.perf_counter() - t0)
+    conn.close()
 
 
-def cpu_baseline(image, wl, key, budget_s=20.0):
-    cb = CPUBaseline(image, wl, key)
-    v = cb.run(budget_s)
-    return {"value": v, "unit": "atom-steps/s", "cores": cb.threads, "kind": "port", "sample": cb.describe()}
+class CPUWorkload:
+    """PD's FP64 path (the oracle restatement) stepping EVERY system of the
+    workload on the host cores: one worker process per core (PD is single-
+    threaded; one independent process per core is how it runs a batch), systems
+    dealt to workers largest cost first (n^2 for all-pairs GB, n for cutoff
+    systems).  A single-system workload runs in one process over every host
+    thread (the oracle's OpenMP loops).  One step = one MD step of every
+    system; its time is the wall clock until the slowest worker is done.
+    Workers are started with 'spawn', never forked from a process holding a
+    CUDA context."""
+
+    def __init__(self, image, wl, key):
+        import multiprocessing as mp
+        self.cores = os.cpu_count() or 1
+        n = image.nsystems
+        self.natom = image.natom
+        self.nsystems = n
+        if n == 1:
+            groups, threads = [[0]], self.cores
+        else:
+            w = min(self.cores, n)
+            cost = image.natoms.astype(np.float64) ** (2 if "GB" in wl["what"] else 1)
+            load = np.zeros(w)
+            groups = [[] for _ in range(w)]
+            for k in np.argsort(-cost):
+                j = int(np.argmin(load))
+                groups[j].append(int(k))
+                load[j] += cost[k]
+            threads = 1
+        self.threads_used = len(groups) * threads
+        ctx = mp.get_context("spawn")
+        self.conns, self.procs = [], []
+        for g in groups:
+            a, b = ctx.Pipe()
+            p = ctx.Process(target=_cpu_worker, args=(b, key, g, threads), daemon=True)
+            p.start()
+            self.conns.append(a)
+            self.procs.append(p)
+        for c in self.conns:
+            assert c.recv() == "ready"
+
+    def step(self):
+        t0 = time.perf_counter()
+        for c in self.conns:
+            c.send("step")
+        for c in self.conns:
+            c.recv()
+        return time.perf_counter() - t0
+
+    def close(self):
+        for c in self.conns:
+            try:
+                c.send("stop")
+            except (OSError, BrokenPipeError):
+                pass
+        for p in self.procs:
+            p.join(timeout=10)
+
+    def describe(self, steps, seconds):
+        how = ("one process per host core (%d processes, one thread each), systems dealt largest first" %
+               len(self.procs) if self.nsystems > 1 else "one process, OpenMP over %d host threads" % self.threads_used)
+        return ("MD steps of every system of the workload (%d systems, %d atoms): forces (PD's O(N^2) list kept "
+                "10 steps for cutoff systems, all pairs for GB, LCPO every 5 steps) + FP64 integrator; %s; %d "
+                "timed steps in %.2f s" % (self.nsystems, self.natom, how, steps, seconds))
+
+
+def cpu_baseline(image, wl, key, steps=2, warmup=1):
+    """A bounded sample of the same workload on the host cores: `warmup` + `steps`
+    MD steps of every system (a few to tens of seconds)."""
+    cw = CPUWorkload(image, wl, key)
+    try:
+        for _ in range(warmup):
+            cw.step()
+        ts = [cw.step() for _ in range(steps)]
+    finally:
+        cw.close()
+    return {"value": image.natom * steps / sum(ts), "unit": "atom-steps/s", "cores": cw.threads_used,
+            "kind": "port", "sample": cw.describe(steps, sum(ts))}
+
+
+def workload_config(key, wl, image):
+    """The `config` object of both arms: the workload and nothing about how an
+    arm measured it."""
+    return {"workload": key, "description": wl["desc"], "atoms": int(image.natom), "systems": int(image.nsystems),
+            "l2": "flushed before every timed GPU step (256 MB write); host arm: not applicable",
+            "parallelism": "replicas only"}
 
 
 # ---------------------------------------------------------------------------
@@ -358,67 +456,61 @@ def run_reference(args, key, wl, image):
     if rank != 0:
         return
     from oracle import pdoracle as O  # noqa: F401  (builds the C restatement if needed)
-    # the whole arm (warm-up included) stays near two minutes of host time
-    per_step = max(0.25, 120.0 / max(args.steps + args.warmup, 1))
-    cb = CPUBaseline(image, wl, key)
-    vals = [cb.run(per_step) for _ in range(args.warmup + args.steps)][args.warmup:]
-    v = statistics.median(vals)
+    cw = CPUWorkload(image, wl, key)
+    try:
+        for _ in range(args.warmup):
+            cw.step()
+        ts = [cw.step() for _ in range(args.steps)]
+    finally:
+        cw.close()
+    t = float(np.median(ts))
+    v = image.natom / t
     out = {"metric": METRIC, "value": v, "unit": "atom-steps/s", "impl": "reference", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic (systems built by PD: NewProtein + seeded compaction, TIP3P lattice)",
-           "config": {"workload": key, "description": wl["desc"]},
-           "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": cb.threads, "kind": "port",
-                            "sample": "median over %d samples of %.2f s: %s" % (args.steps, per_step,
-                                                                               cb.describe())},
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic systems built by PD (NewProtein + seeded compaction, TIP3P lattice)",
+           "config": workload_config(key, wl, image),
+           "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": cw.threads_used, "kind": "port",
+                            "sample": "median step of " + cw.describe(args.steps, sum(ts)),
+                            "cpu": cpu_model()},
            "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
+
+
+def cpu_model():
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith(("model name", "cpu model", "hardware")):
+                return ln.split(":", 1)[1].strip()
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return "unknown"
 
 
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
-def fp32_peak_tflops(torch):
-    """Measured FP32 FMA ceiling: cuBLAS SGEMM with TF32 off, best of 5."""
-    torch.backends.cuda.matmul.allow_tf32 = False
-    n = 8192
-    a = torch.randn(n, n, device="cuda", dtype=torch.float32)
-    b = torch.randn(n, n, device="cuda", dtype=torch.float32)
-    for _ in range(2):
-        a @ b
-    torch.cuda.synchronize()
-    best = 1e9
-    for _ in range(5):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        a @ b
-        e1.record()
-        e1.synchronize()
-        best = min(best, e0.elapsed_time(e1) / 1e3)
-    del a, b
-    return 2.0 * n ** 3 / best / 1e12
+def roofline_flops(census, dom):
+    """Algorithmic FP32 flops of one launch of the dominant pair kernel, from the
+    pair census (counts of each branch) and FLOPS."""
+    if dom == "gb_pair":
+        return FLOPS["gb_pair"] * census["gb"] + FLOPS["gb_term"] * census["gb_term"]
+    return FLOPS["nb"] * census["nb"]
 
 
-def pairs_per_step(image, wl):
-    """Unordered atom pairs each pair kernel visits per step (all pairs for GB)."""
-    n = image.natoms.astype(np.float64)
-    return float((n * (n - 1) / 2).sum())
-
-
-def pairs_in_cutoff(image, pos, cutoff):
-    """Unordered atom pairs within `cutoff` (minimum image in a periodic box) at
-    these positions, counted exactly with a k-d tree: the pairs whose law the NB
-    kernel evaluates (bonded exclusions, under 1 % of them, included)."""
-    from scipy.spatial import cKDTree
-    tot = 0.0
-    for k in range(image.nsystems):
-        p = pos[image.offsets[k]:image.offsets[k + 1]]
-        box = image.box[k]
-        if np.all(box > 0):
-            tree = cKDTree(np.mod(p, box), boxsize=box)
-        else:
-            tree = cKDTree(p)
-        tot += (tree.count_neighbors(tree, cutoff) - len(p)) / 2.0
-    return tot
+def list_build_bytes(image, stats, groups):
+    """Algorithmic DRAM bytes of one list build: per atom the FP64 position read
+    (24 B), the sorted-slot record written and read back (16 B position + 16 B
+    parameters + 4 B index), the cell key written and read (8 B); per tile its
+    32 B record written (and the candidate flag + scan, 8 B); per masked tile
+    32 lanes x 8 B of exclusion masks; per NB j-atom group 32 x 16 B entries."""
+    n = image.natom
+    ngroups = max(groups[1], 0)
+    return n * (24 + 36 + 8) + stats["tiles"] * (32 + 8) + stats["masked_tiles"] * 256 + ngroups * 32 * 16
 
 
 def run_ours(args, key, wl, image):
@@ -493,22 +585,38 @@ def run_ours(args, key, wl, image):
                                          "added %.2f times (steps / %d minus attempts in the window)" % (
                                              owed, exch_every)})
     launches = ctx.kernel_launches() - launches0
+    # list rebuilds belong to the workload at one per UpdateNList steps (the
+    # autotuned cadence; steps s with s % UpdateNList == 0 rebuild).  The window
+    # holds however many fall inside it; the difference from its share is
+    # charged (or credited) at the measured cost of one list build.
+    nl = tuned["UpdateNList"] if tuned else 10
+    rebuilds = sum(1 for s in range(step0, step0 + args.steps) if s % nl == 0)
+    ms_build = ctx.time_kernel("list", reps=10)
+    ctx.compute(flags(wl["what"]))   # Born radii etc. in the order of the list just built
+    owed_builds = args.steps / nl - rebuilds
+    t_dev += owed_builds * ms_build / 1e3
+    rebuild_info = {"update_nlist": nl, "in_window": rebuilds, "share": args.steps / nl,
+                    "build_ms": ms_build, "charged_ms": owed_builds * ms_build,
+                    "how": "(steps / UpdateNList - rebuilds in the window) x the measured list-build time"}
     if dist is not None:
         dist.barrier()
     t_max, units = reduce_max_sum(dist, t_dev, float(natom) * args.steps)
     value = units / t_max
 
-    # kernel roofline (dominant kernel measured on the live state, L2 flushed before each launch)
+    # kernel rooflines (measured on the live state, L2 flushed before each launch)
     dom = "gb_pair" if "GB" in wl["what"] else "nb"
     ms_dom = ctx.time_kernel(dom, reps=10)
+    census = ctx.pair_census()
     ms_int = ctx.time_kernel("integrate", reps=10)
+    ms_list = ms_build
+    list_stats = ctx.list_stats()
+    groups = ctx.nb_groups()
     result = {}
     if rank == 0:
-        peak = fp32_peak_tflops(torch)
-        pairs = pairs_per_step(image, wl) if "GB" in wl["what"] else None
-        if pairs is None:   # cutoff system: pairs inside the cutoff at the current positions
-            pairs = pairs_in_cutoff(image, ctx.get_positions(), NB_CUTOFF)
-        achieved = FLOPS[dom] * pairs / (ms_dom / 1e3) / 1e12
+        fp32 = ffi.fp32_peak(local)
+        peak = max(fp32["ffma_tflops"], fp32["ffma2_tflops"])
+        flops = roofline_flops(census, dom)
+        achieved = flops / (ms_dom / 1e3) / 1e12
         peaks = {}
         pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
         if os.path.exists(pk):
@@ -518,21 +626,33 @@ def run_ours(args, key, wl, image):
         kdom = "k_gb_pair" if dom == "gb_pair" else "k_nb_tiles"
         kint = "k_langevin" if wl["integrator"] else "k_vv"
         traffic = NCU_TRAFFIC.get(key, {})
-        result["roofline"] = {"bound": "fp32", "kernel": kdom,
-                              "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                              "traffic": traffic.get(kdom), "traffic_unit": "bytes per launch (ncu)",
-                              "peak_source": "measured cuBLAS SGEMM (TF32 off) on this GPU",
-                              "flops_per_pair": FLOPS[dom], "pairs_per_launch": pairs, "ms_per_launch": ms_dom,
-                              "pairs": "all pairs" if "GB" in wl["what"] else
-                                       "pairs within the cutoff at the final positions (k-d tree count)"}
+        roof = {"bound": "fp32", "kernel": kdom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": traffic.get(kdom), "traffic_unit": "bytes per launch (ncu)",
+                "peak_source": "measured: FP32 FMA probe on this GPU (pdgpu_fp32_peak, best of FFMA %.1f / "
+                               "FFMA2 %.1f TFLOP/s at %.0f MHz)" % (fp32["ffma_tflops"], fp32["ffma2_tflops"],
+                                                                   fp32["sm_mhz"]),
+                "flops_per_launch": flops, "ms_per_launch": ms_dom, "census": census}
+        if dom == "gb_pair":
+            roof["flops"] = ("%d per pair inside the GB cutoff + %d per pair above ExpApproxThreshold "
+                             "(GB cross term)" % (FLOPS["gb_pair"], FLOPS["gb_term"]))
+        else:
+            visited = 1024 * (max(groups[1], 0) + (groups[2] if groups[2] >= 0 else list_stats["tiles"]))
+            roof["flops"] = "%d per pair inside the cutoff" % FLOPS["nb"]
+            roof["visited_pairs"] = visited
+            roof["in_cutoff_over_visited"] = census["nb"] / visited if visited else None
+        result["roofline"] = roof
         result["hbm_roofline"] = {"bound": "hbm", "kernel": kint,
                                   "achieved": int_gbs, "peak": hbm, "unit": "GB/s", "frac": int_gbs / hbm,
                                   "traffic": traffic.get(kint), "traffic_unit": "bytes per launch (ncu)",
                                   "bytes_per_atom": INTEGRATOR_BYTES, "ms_per_launch": ms_int,
                                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+        lb = list_build_bytes(image, list_stats, groups)
+        result["list_roofline"] = {"bound": "hbm", "kernel": "list build (all its kernels)", "bytes": lb,
+                                   "ms_per_build": ms_list, "achieved": lb / (ms_list / 1e3) / 1e9, "peak": hbm,
+                                   "unit": "GB/s", "frac": lb / (ms_list / 1e3) / 1e9 / hbm,
+                                   "tiles": list_stats["tiles"], "masked_tiles": list_stats["masked_tiles"]}
     ctx.close()
 
-    nl = tuned["UpdateNList"] if tuned else 10
     # plain single-system path on the same systems (rank 0, N=1 semantics per rank)
     plain = None
     if rank == 0 and image.nsystems > 1 and not args.no_plain:
@@ -549,14 +669,11 @@ def run_ours(args, key, wl, image):
            "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math / int64 fixed-point sums / f64 state",
            "data": "synthetic systems built by PD (NewProtein + seeded compaction, TIP3P lattice)",
-           "config": {"workload": key, "description": wl["desc"], "atoms": int(natom),
-                      "preparation": "untimed relaxation: %d Langevin steps at %.1f fs, friction %.0e/s, then "
-                                     "Maxwell-Boltzmann velocities" % (RELAX["steps"], RELAX["dt"] * 1e15,
-                                                                       RELAX["fric"]),
-                      "systems": int(image.nsystems), "l2": "flushed before every timed step (256 MB write)",
-                      "graphs": True, "exchanges_in_timed_region": exchanges, "exchange": exchange_info,
-                      "autotune": tuned,
-                      "parallelism": "replicas only (%d GPU%s)" % (world, "s" if world > 1 else "")},
+           "config": workload_config(key, wl, image),
+           "preparation": "untimed relaxation: %d Langevin steps at %.1f fs, friction %.0e/s, then "
+                          "Maxwell-Boltzmann velocities" % (RELAX["steps"], RELAX["dt"] * 1e15, RELAX["fric"]),
+           "timing": {"graphs": True, "exchanges_in_timed_region": exchanges, "exchange": exchange_info,
+                      "rebuilds": rebuild_info, "autotune": tuned, "ranks": world},
            "gpu_launches": int(launches), "clocks": clocks}
     out.update(result)
     if plain:
@@ -566,7 +683,7 @@ def run_ours(args, key, wl, image):
     if not args.no_parity:
         out["parity"] = parity_check(image, wl, key)
     if not args.no_cpu and world == 1:
-        out["cpu_baseline"] = cpu_baseline(image, wl, key, budget_s=args.cpu_seconds)
+        out["cpu_baseline"] = cpu_baseline(image, wl, key, steps=args.cpu_steps)
     print(json.dumps(out))
 
 
@@ -603,7 +720,9 @@ def run_e2e(args, key, wl, image, torch, update_nlist):
     ctx, _ = make_context(image, wl, key, 3000, use_graph=True, update_nlist=update_nlist)
     n = image.natom
     pos_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    # each timed stretch is whole list-rebuild windows, so it holds its share of rebuilds
     steps = max(3, min(args.steps, 100))
+    steps = -(-steps // update_nlist) * update_nlist
     ctx.get_positions(out=pos_h)
 
     def run(k):
@@ -622,6 +741,7 @@ def run_e2e(args, key, wl, image, torch, update_nlist):
     ctx.close()
     return {"value": float(np.median(rates)), "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * n,
             "d2h_bytes_per_step": 24 * n + 8 * image.nsystems, "steps": steps, "repeats": 3,
+            "rebuilds_per_stretch": steps // update_nlist,
             "spread": [float(min(rates)), float(max(rates))]}
 
 
@@ -832,7 +952,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-steps", type=int, default=2, help="timed steps of the CPU baseline sample")
     ap.add_argument("--long", action="store_true",
                     help="the workload's full run length with oracle checks at intervals (validation, not timing)")
     ap.add_argument("--relax-steps", type=int, default=RELAX["steps"],

@@ -340,6 +340,22 @@ long long pdgpu_kernel_launches(pdgpu_ctx *ctx);
 int pdgpu_time_kernel(pdgpu_ctx *ctx, int kernel, int reps, int flush_l2, double *avg_ms);
 /* Stream the context launches on (cudaStream_t as void*), for event timing. */
 void *pdgpu_stream(pdgpu_ctx *ctx);
+/* Pair census of the current list at the positions of the last evaluation, by
+ * the branch each pair takes in the pair kernels (FP32 decisions, as they take
+ * them): counts[0] FF_NonBonded pairs inside Cutoff (bond order > 2);
+ * counts[1] GB pairs inside the GB Cutoff; counts[2] of those, the pairs above
+ * ExpApproxThreshold (GB cross term evaluated, gbff.cpp:1592-1678; Born radii
+ * of the last GB evaluation); counts[3] Born-radius pairs inside
+ * GbsaStillCutoff (bond order > 2, gbff.cpp:432-483); counts[4] of those, the
+ * close-contact pairs (CCF < 1).  No counterpart in PD; the benchmark's
+ * roofline counts flops per branch with it. */
+int pdgpu_pair_census(pdgpu_ctx *ctx, long long counts[5]);
+/* FP32 FMA throughput of a device, measured: kernels of independent FFMA (and
+ * packed FFMA2) chains, best of 5 launches timed with CUDA events, in TFLOP/s
+ * (FMA = 2 flops), and the SM clock over the FFMA launch from the SM cycle
+ * counter (MHz).  Outputs may be NULL.  No counterpart in PD; the ceiling the
+ * benchmark's pair-kernel roofline divides by. */
+int pdgpu_fp32_peak(int device, double *tflops_ffma, double *tflops_ffma2, double *sm_mhz);
 /* Device memory of the library in this process, over all contexts: cudaMalloc
  * calls made so far (count, never decreases) and bytes held now (either may be
  * NULL).  No counterpart in PD; a diagnostic (e.g. to check that a call

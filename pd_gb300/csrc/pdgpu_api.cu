@@ -988,3 +988,26 @@ int pdgpu_host_free(void* ptr) {
   if (!ptr) return PDGPU_OK;
   return cudaFreeHost(ptr) == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
+
+int pdgpu_pair_census(pdgpu_ctx* h, long long* counts) {
+  if (!h || !counts) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.list_built) return PDGPU_ERR_STATE;
+  CK(cudaSetDevice(c.device));
+  DBuf<unsigned long long> d;
+  CK(d.alloc(5));
+  CK(cudaMemsetAsync(d.p, 0, 5 * sizeof(unsigned long long), c.stream));
+  const bool gb = c.gb_set && c.has_gb;
+  int st = launch_census(c, make_nb_const(c.nb), make_gb_const(c.gb, c.list_radius_built), c.nb_set, gb, d.p);
+  if (st != PDGPU_OK) return st;
+  unsigned long long h_out[5];
+  CK(cudaMemcpyAsync(h_out, d.p, sizeof(h_out), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  for (int k = 0; k < 5; k++) counts[k] = (long long)h_out[k];
+  return PDGPU_OK;
+}
+
+int pdgpu_fp32_peak(int device, double* tflops_ffma, double* tflops_ffma2, double* sm_mhz) {
+  if (device < 0) return PDGPU_ERR_ARG;
+  return measure_fp32_peak(device, tflops_ffma, tflops_ffma2, sm_mhz);
+}

@@ -193,6 +193,14 @@ class DeviceContext:
                   "pdgpu_list_stats")
         return {"tiles": a.value, "masked_tiles": b.value, "slots": c.value}
 
+    def pair_census(self):
+        """Pairs of the current list by the branch the pair kernels take
+        (pdgpu_pair_census): NB in cutoff, GB in cutoff, GB term on, Born sums,
+        Born close contacts."""
+        out = (ctypes.c_longlong * 5)()
+        ffi.check(self.lib.pdgpu_pair_census(self.h, out), "pdgpu_pair_census")
+        return dict(zip(("nb", "gb", "gb_term", "born", "born_contact"), (int(x) for x in out)))
+
     def stream(self):
         return self.lib.pdgpu_stream(self.h)
 
