@@ -629,8 +629,8 @@ def run_ours(args, key, wl, image):
         roof = {"bound": "fp32", "kernel": kdom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": traffic.get(kdom), "traffic_unit": "bytes per launch (ncu)",
                 "peak_source": "measured: FP32 FMA probe on this GPU (pdgpu_fp32_peak, best of FFMA %.1f / "
-                               "FFMA2 %.1f TFLOP/s at %.0f MHz)" % (fp32["ffma_tflops"], fp32["ffma2_tflops"],
-                                                                   fp32["sm_mhz"]),
+                               "FFMA2 %.1f TFLOP/s; SM clock in `clocks`)" % (fp32["ffma_tflops"],
+                                                                              fp32["ffma2_tflops"]),
                 "flops_per_launch": flops, "ms_per_launch": ms_dom, "census": census}
         if dom == "gb_pair":
             roof["flops"] = ("%d per pair inside the GB cutoff + %d per pair above ExpApproxThreshold "

@@ -352,10 +352,9 @@ void *pdgpu_stream(pdgpu_ctx *ctx);
 int pdgpu_pair_census(pdgpu_ctx *ctx, long long counts[5]);
 /* FP32 FMA throughput of a device, measured: kernels of independent FFMA (and
  * packed FFMA2) chains, best of 5 launches timed with CUDA events, in TFLOP/s
- * (FMA = 2 flops), and the SM clock over the FFMA launch from the SM cycle
- * counter (MHz).  Outputs may be NULL.  No counterpart in PD; the ceiling the
+ * (FMA = 2 flops).  Outputs may be NULL.  No counterpart in PD; the ceiling the
  * benchmark's pair-kernel roofline divides by. */
-int pdgpu_fp32_peak(int device, double *tflops_ffma, double *tflops_ffma2, double *sm_mhz);
+int pdgpu_fp32_peak(int device, double *tflops_ffma, double *tflops_ffma2);
 /* Device memory of the library in this process, over all contexts: cudaMalloc
  * calls made so far (count, never decreases) and bytes held now (either may be
  * NULL).  No counterpart in PD; a diagnostic (e.g. to check that a call

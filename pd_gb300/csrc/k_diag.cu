@@ -10,14 +10,12 @@ namespace pdgpu {
 // ---------------------------------------------------------------------------
 // FP32 FMA ceiling: kChains independent FMA chains per thread (FFMA, or FFMA2
 // on float2 pairs), enough warps per scheduler to cover the FMA latency.  The
-// result is written so the chains are not removed.  Thread 0 of block 0 reads
-// the SM cycle counter at start and end for the clock over the launch.
+// result is written so the chains are not removed.
 // ---------------------------------------------------------------------------
 constexpr int kChains = 8;
 
 template <bool PACKED>
-__global__ void __launch_bounds__(256) k_fma_probe(float* out, long long* cycles, int iters, float b, float c) {
-  const long long t0 = clock64();
+__global__ void __launch_bounds__(256) k_fma_probe(float* out, int iters, float b, float c) {
   float s = 0.f;
   if (PACKED) {
     float2 a[kChains];
@@ -42,7 +40,6 @@ __global__ void __launch_bounds__(256) k_fma_probe(float* out, long long* cycles
     for (int k = 0; k < kChains; k++) s += a[k];
   }
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
-  if (blockIdx.x == 0 && threadIdx.x == 0) *cycles = clock64() - t0;
 }
 
 // ---------------------------------------------------------------------------
@@ -118,35 +115,29 @@ int launch_census(Context& c, const NBConst& nk, const GBConst& gk, bool do_nb, 
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 
-int measure_fp32_peak(int device, double* tflops_ffma, double* tflops_ffma2, double* sm_mhz) {
+int measure_fp32_peak(int device, double* tflops_ffma, double* tflops_ffma2) {
   if (cudaSetDevice(device) != cudaSuccess) return PDGPU_ERR_CUDA;
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return PDGPU_ERR_CUDA;
   const int blocks = sms * 4, threads = 256, iters = 1 << 14;
   DBuf<float> out;
-  DBuf<long long> cyc;
-  if (out.alloc((size_t)blocks * threads) != cudaSuccess || cyc.alloc(1) != cudaSuccess) return PDGPU_ERR_CUDA;
+  if (out.alloc((size_t)blocks * threads) != cudaSuccess) return PDGPU_ERR_CUDA;
   cudaStream_t st;
   cudaEvent_t e0, e1;
   if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return PDGPU_ERR_CUDA;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  double best[2] = {1e30, 1e30}, mhz = 0.0;
+  double best[2] = {1e30, 1e30};
   for (int packed = 0; packed < 2; packed++) {
     for (int rep = 0; rep < 6; rep++) {  // the first launch warms up and is not counted
       cudaEventRecord(e0, st);
-      if (packed) k_fma_probe<true><<<blocks, threads, 0, st>>>(out.p, cyc.p, iters, 0.999999f, 1e-6f);
-      else k_fma_probe<false><<<blocks, threads, 0, st>>>(out.p, cyc.p, iters, 0.999999f, 1e-6f);
+      if (packed) k_fma_probe<true><<<blocks, threads, 0, st>>>(out.p, iters, 0.999999f, 1e-6f);
+      else k_fma_probe<false><<<blocks, threads, 0, st>>>(out.p, iters, 0.999999f, 1e-6f);
       cudaEventRecord(e1, st);
       cudaEventSynchronize(e1);
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
-      if (rep > 0 && ms < best[packed]) {
-        best[packed] = ms;
-        long long cycles = 0;
-        cudaMemcpy(&cycles, cyc.p, sizeof(long long), cudaMemcpyDeviceToHost);
-        if (!packed) mhz = (double)cycles / (ms * 1e3);
-      }
+      if (rep > 0 && ms < best[packed]) best[packed] = ms;
     }
   }
   const cudaError_t err = cudaGetLastError();
@@ -157,7 +148,6 @@ int measure_fp32_peak(int device, double* tflops_ffma, double* tflops_ffma2, dou
   const double fmas = (double)blocks * threads * iters * kChains;  // per launch (FFMA2 does two per chain step)
   if (tflops_ffma) *tflops_ffma = 2.0 * fmas / (best[0] * 1e-3) / 1e12;
   if (tflops_ffma2) *tflops_ffma2 = 4.0 * fmas / (best[1] * 1e-3) / 1e12;
-  if (sm_mhz) *sm_mhz = mhz;
   return PDGPU_OK;
 }
 

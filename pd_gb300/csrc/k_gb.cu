@@ -200,8 +200,14 @@ __device__ __noinline__ bool gb_on_fp64(const DevView& v, int si, int sj, double
 
 // ---------------------------------------------------------------------------
 // pass 2: GB cross term fused with vacuum LJ + Coulomb, i > j pairs within Cutoff
-// (forces, dE/da and, with ENERGY, the pair energies in FP32; energies are summed
-// in FP32 over 8 rotation steps, then in FP64, then per tile in fixed point)
+// (forces, dE/da and, with ENERGY, the pair energies).  With ENERGY each pair's
+// displacement is formed in FP64 from the FP64 positions and rounded once, its
+// energies are evaluated in FP32 from it and summed in FP64, then per tile in
+// fixed point: the vdW and Coulomb totals are sums of large terms of both
+// signs, and FP32 positions (rounded relative to their block centres) or FP32
+// partial sums leave ~1e-6 of such a total.  Energy evaluations are rare (an
+// exchange attempt, an explicit energy call), so the FP64 work stays off the
+// force-only dynamics step.
 // ---------------------------------------------------------------------------
 struct PairAcc {
   float fx, fy, fz, da;
@@ -225,7 +231,7 @@ template <bool ENERGY, bool FULL, bool FAST>
 __device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, float dx, float dy, float dz,
                                             float r2, float u, bool any_gb, float qi, float qj, float pix, float piy,
                                             float pjx, float pjy, float ai, float aj, bool excl, bool is14, int si,
-                                            int sj, PairAcc& I, PairAcc& J, float& cv, float& ce, float& cp) {
+                                            int sj, PairAcc& I, PairAcc& J, double& cv, double& ce, double& cp) {
     const float invr = rsqrtf(r2);
     const float r = r2 * invr;
     const float qiqj = qi * qj;
@@ -256,7 +262,7 @@ __device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, 
       const float ep = k.premul * qiqj * fgb;
       float dedr = -ep * (r - 0.25f * r * tg) * l;
       float dalpha = -ep * tg * (1.f - u) * l;
-      if (ENERGY) cp += 2.f * ep * S;
+      if (ENERGY) cp += (double)(2.f * ep * S);
       if (FAST && !excl) {
         elec = k.econv_in * s14 * qiqj * invr;
         delec = -elec * invr;
@@ -275,12 +281,12 @@ __device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, 
       // calcBornForces below the threshold (gbff.cpp:1308-1325): premul q_i q_j / r
       const float ep = k.premul * qiqj * invr;
       float dedr = -ep * invr;
-      if (ENERGY) cp += 2.f * ep * S;
+      if (ENERGY) cp += (double)(2.f * ep * S);
       if (sw_on) dedr = S * dedr + dS * ep;
       g += 2.f * dedr * invr;
     }
     if (FAST && !excl) {
-      if (ENERGY) ce += elec * S;
+      if (ENERGY) ce += (double)(elec * S);
       if (sw_on) delec = S * delec + elec * dS;
       const float t = (pix + pjx) * invr;
       float B = t * t;
@@ -298,12 +304,37 @@ __device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, 
         dvdw = vin ? dvdw : 0.f;
         Ev = vin ? Ev : 0.f;
       }
-      if (ENERGY) cv += Ev;
+      if (ENERGY) cv += (double)Ev;
       g += (dvdw + delec) * invr;
     }
     I.fx += g * dx; I.fy += g * dy; I.fz += g * dz;
     J.fx -= g * dx; J.fy -= g * dy; J.fz -= g * dz;
   
+}
+
+// (ENERGY) the displacement x_b - x_a of two atoms from the FP64 positions,
+// rounded once to FP32; false (nothing written) for a padding slot
+__device__ __forceinline__ bool disp_fp64(const DevView& v, int a, const double* pa, int sb, float& dx, float& dy,
+                                          float& dz, float& r2) {
+  const int b = v.sorted_atom[sb];
+  if (a < 0 || b < 0) return false;
+  const double ex = v.pos[3 * b] - pa[0], ey = v.pos[3 * b + 1] - pa[1], ez = v.pos[3 * b + 2] - pa[2];
+  dx = (float)ex;
+  dy = (float)ey;
+  dz = (float)ez;
+  r2 = (float)(ex * ex + ey * ey + ez * ez);
+  return true;
+}
+
+__device__ __forceinline__ int own_atom_fp64(const DevView& v, int s, double* p) {
+  const int a = v.sorted_atom[s];
+  p[0] = p[1] = p[2] = 0.0;
+  if (a >= 0) {
+    p[0] = v.pos[3 * a];
+    p[1] = v.pos[3 * a + 1];
+    p[2] = v.pos[3 * a + 2];
+  }
+  return a;
 }
 
 template <bool MASKED, bool ENERGY, bool FULL, bool FAST = true>
@@ -314,11 +345,13 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
   float4 xj = j_in_i_frame(v, T, lane);
   float4 pj = v.par[T.bj * 32 + lane];
   float aj = born[T.bj * 32 + lane];
-  float cv = 0.f, ce = 0.f, cp = 0.f;  // (ENERGY) vdW, Coulomb, GB cross over the current 8 steps
+  double pos_i[3];
+  const int atom_i = ENERGY ? own_atom_fp64(v, si, pos_i) : 0;
 #pragma unroll 2
   for (int kk = 0; kk < 32; kk++) {
-    const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
-    const float r2 = dx * dx + dy * dy + dz * dz;
+    float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+    float r2 = dx * dx + dy * dy + dz * dz;
+    if (ENERGY) disp_fp64(v, atom_i, pos_i, T.bj * 32 + ((lane + kk) & 31), dx, dy, dz, r2);
     bool pair = true, excl = false, is14 = false;
     if (MASKED) {
       pair = !((dmask >> kk) & 1u);
@@ -330,13 +363,7 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
     const bool any_gb = __any_sync(0xffffffffu, in && gb_maybe_on(k, u));
     if (in)
       gb_pair_one<ENERGY, FULL, FAST>(v, k, dx, dy, dz, r2, u, any_gb, xi.w, xj.w, pi.x, pi.y, pj.x, pj.y, ai, aj,
-                                      excl, is14, si, T.bj * 32 + ((lane + kk) & 31), I, J, cv, ce, cp);
-    if (ENERGY && (kk & 7) == 7) {
-      evdw += (double)cv;
-      eel += (double)ce;
-      epol += (double)cp;
-      cv = ce = cp = 0.f;
-    }
+                                      excl, is14, si, T.bj * 32 + ((lane + kk) & 31), I, J, evdw, eel, epol);
     ROT(xj.x); ROT(xj.y); ROT(xj.z); ROT(xj.w); ROT(pj.x); ROT(pj.y); ROT(aj);
     ROT(J.fx); ROT(J.fy); ROT(J.fz); ROT(J.da);
   }
@@ -402,129 +429,40 @@ __device__ __forceinline__ void gb_pair_tile2(const DevView& v, const GBConst& k
   const float aa = born[sa], ab = born[sb];
   float4 xr = v.xq[r0 + lane], pr = v.par[r0 + lane];
   float ar = born[r0 + lane];
+  double pos_a[3], pos_b[3];
+  const int atom_a = ENERGY ? own_atom_fp64(v, sa, pos_a) : 0;
+  const int atom_b = ENERGY ? own_atom_fp64(v, sb, pos_b) : 0;
   PairAcc IA = {0.f, 0.f, 0.f, 0.f}, IB = {0.f, 0.f, 0.f, 0.f}, R = {0.f, 0.f, 0.f, 0.f};
-  float cv = 0.f, ce = 0.f, cp = 0.f;
 #pragma unroll 2
   for (int kk = 0; kk < 32; kk++) {
     const int sr = r0 + ((lane + kk) & 31);
     {
-      const float dx = xr.x - xa.x, dy = xr.y - xa.y, dz = xr.z - xa.z;
-      const float r2 = dx * dx + dy * dy + dz * dz;
+      float dx = xr.x - xa.x, dy = xr.y - xa.y, dz = xr.z - xa.z;
+      float r2 = dx * dx + dy * dy + dz * dz;
+      if (ENERGY) disp_fp64(v, atom_a, pos_a, sr, dx, dy, dz, r2);
       const bool in = FULL || r2 <= k.cut2;
       const float u = gb_u(r2, aa, ar);
       const bool any_gb = __any_sync(0xffffffffu, in && gb_maybe_on(k, u));
       if (in)
         gb_pair_one<ENERGY, FULL, true>(v, k, dx, dy, dz, r2, u, any_gb, xa.w, xr.w, pa.x, pa.y, pr.x, pr.y, aa, ar,
-                                        false, false, sa, sr, IA, R, cv, ce, cp);
+                                        false, false, sa, sr, IA, R, evdw, eel, epol);
     }
     {
-      const float dx = xr.x - xb.x, dy = xr.y - xb.y, dz = xr.z - xb.z;
-      const float r2 = dx * dx + dy * dy + dz * dz;
+      float dx = xr.x - xb.x, dy = xr.y - xb.y, dz = xr.z - xb.z;
+      float r2 = dx * dx + dy * dy + dz * dz;
+      if (ENERGY) disp_fp64(v, atom_b, pos_b, sr, dx, dy, dz, r2);
       const bool in = FULL || r2 <= k.cut2;
       const float u = gb_u(r2, ab, ar);
       const bool any_gb = __any_sync(0xffffffffu, in && gb_maybe_on(k, u));
       if (in)
         gb_pair_one<ENERGY, FULL, true>(v, k, dx, dy, dz, r2, u, any_gb, xb.w, xr.w, pb.x, pb.y, pr.x, pr.y, ab, ar,
-                                        false, false, sb, sr, IB, R, cv, ce, cp);
-    }
-    if (ENERGY && (kk & 7) == 7) {
-      evdw += (double)cv;
-      eel += (double)ce;
-      epol += (double)cp;
-      cv = ce = cp = 0.f;
+                                        false, false, sb, sr, IB, R, evdw, eel, epol);
     }
     ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(xr.w); ROT(pr.x); ROT(pr.y); ROT(ar);
     ROT(R.fx); ROT(R.fy); ROT(R.fz); ROT(R.da);
   }
   flush_pair(v, deda, sa, IA);
   flush_pair(v, deda, sb, IB);
-  flush_pair(v, deda, r0 + lane, R);
-}
-
-// gb_pair_tile2 for a tile pair whose pairs all lie inside every cutoff and switch
-// radius (no switching, LJ everywhere; unmasked: no exclusions, no 1-4 scaling),
-// the all-pairs case, on packed FP32x2 arithmetic, used for the energy variant.
-// The GB part runs when either pair of the lane is above the exp threshold and is
-// kept per pair by a select.
-template <bool ENERGY>
-__device__ __forceinline__ void gb_pair_full2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B,
-                                              int lane, const float* born, long long* deda, double& evdw,
-                                              double& eel, double& epol) {
-  const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
-  const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
-  const float4 pa = v.par[sa], pb = v.par[sb];
-  const float2 nx = make_float2(-xa.x, -xb.x), ny = make_float2(-xa.y, -xb.y), nz = make_float2(-xa.z, -xb.z);
-  const float2 QS = make_float2(xa.w, xb.w), SG = make_float2(pa.x, pb.x), EP = make_float2(pa.y, pb.y);
-  const float2 AS = make_float2(born[sa], born[sb]);
-  const float tol = 2e-6f * fabsf(k.thresh);
-  float4 xr = v.xq[r0 + lane], pr = v.par[r0 + lane];
-  float ar = born[r0 + lane];
-  float2 FX = f2(0.f), FY = f2(0.f), FZ = f2(0.f), DA = f2(0.f);  // the two j atoms' sums
-  PairAcc R = {0.f, 0.f, 0.f, 0.f};                                 // the rotating atom's sums
-  float2 CV = f2(0.f), CE = f2(0.f), CP = f2(0.f);                  // (ENERGY) over 8 steps
-#pragma unroll 2
-  for (int kk = 0; kk < 32; kk++) {
-    const float2 dx = __fadd2_rn(f2(xr.x), nx), dy = __fadd2_rn(f2(xr.y), ny), dz = __fadd2_rn(f2(xr.z), nz);
-    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
-    const float2 invr = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
-    const float2 qq = __fmul2_rn(QS, f2(xr.w));
-    const float2 aa = __fmul2_rn(AS, f2(ar));
-    const float2 u = __fmul2_rn(f2(-0.25f), make_float2(__fdividef(r2.x, aa.x), __fdividef(r2.y, aa.y)));
-    bool gx = u.x > k.thresh, gy = u.y > k.thresh;
-    const float2 du = __fadd2_rn(u, f2(-k.thresh));
-    if (fabsf(du.x) <= tol) gx = gb_on_fp64(v, sa, r0 + ((lane + kk) & 31), k.thresh_d);
-    if (fabsf(du.y) <= tol) gy = gb_on_fp64(v, sb, r0 + ((lane + kk) & 31), k.thresh_d);
-    // Coulomb with eps_in above the threshold, eps_out below; en = -E_elec
-    const float2 en = __fmul2_rn(__fmul2_rn(make_float2(gx ? -k.econv_in : -k.econv_out,
-                                                        gy ? -k.econv_in : -k.econv_out), qq), invr);
-    float2 g = f2(0.f), dal = f2(0.f);
-    if (gx || gy) {
-      const float2 r = __fmul2_rn(r2, invr);
-      const float2 tg = make_float2(__expf(u.x), __expf(u.y));
-      const float2 t = __ffma2_rn(tg, aa, r2);
-      const float2 fgb = make_float2(rsqrtf(t.x), rsqrtf(t.y));
-      const float2 l = __fmul2_rn(fgb, fgb);
-      const float2 nep = __fmul2_rn(__fmul2_rn(f2(-k.premul), qq), fgb);  // -E_GB pair factor
-      const float2 dedr = __fmul2_rn(__fmul2_rn(nep, __fmul2_rn(r, __ffma2_rn(f2(-0.25f), tg, f2(1.f)))), l);
-      const float2 da = __fmul2_rn(__fmul2_rn(__fmul2_rn(nep, tg), __ffma2_rn(u, f2(-1.f), f2(1.f))), l);
-      const float2 gg = __fmul2_rn(__fmul2_rn(f2(2.f), dedr), invr);
-      g = make_float2(gx ? gg.x : 0.f, gy ? gg.y : 0.f);
-      dal = make_float2(gx ? da.x : 0.f, gy ? da.y : 0.f);
-      if (ENERGY) CP = __ffma2_rn(f2(-2.f), make_float2(gx ? nep.x : 0.f, gy ? nep.y : 0.f), CP);
-    }
-    // LJ
-    const float2 tt = __fmul2_rn(__fadd2_rn(SG, f2(pr.x)), invr);
-    const float2 b2 = __fmul2_rn(tt, tt);
-    const float2 b6 = __fmul2_rn(__fmul2_rn(b2, b2), b2);
-    const float2 a12 = __fmul2_rn(b6, b6);
-    const float2 eps = __fmul2_rn(EP, f2(pr.y));
-    const float2 dv = __fmul2_rn(__fmul2_rn(__fmul2_rn(f2(-12.f), eps), invr), __ffma2_rn(b6, f2(-1.f), a12));
-    if (ENERGY) {
-      CV = __ffma2_rn(eps, __ffma2_rn(b6, f2(-2.f), a12), CV);
-      CE = __ffma2_rn(en, f2(-1.f), CE);
-    }
-    // g: dE/dr / r;  dE_elec/dr = -E_elec / r = en / r
-    g = __ffma2_rn(__ffma2_rn(en, invr, dv), invr, g);
-    FX = __ffma2_rn(g, dx, FX);
-    FY = __ffma2_rn(g, dy, FY);
-    FZ = __ffma2_rn(g, dz, FZ);
-    R.fx = fmaf(-g.x, dx.x, R.fx); R.fx = fmaf(-g.y, dx.y, R.fx);
-    R.fy = fmaf(-g.x, dy.x, R.fy); R.fy = fmaf(-g.y, dy.y, R.fy);
-    R.fz = fmaf(-g.x, dz.x, R.fz); R.fz = fmaf(-g.y, dz.y, R.fz);
-    DA = __ffma2_rn(dal, f2(ar), DA);
-    R.da = fmaf(dal.x, AS.x, R.da);
-    R.da = fmaf(dal.y, AS.y, R.da);
-    if (ENERGY && (kk & 7) == 7) {
-      evdw += (double)CV.x + (double)CV.y;
-      eel += (double)CE.x + (double)CE.y;
-      epol += (double)CP.x + (double)CP.y;
-      CV = CE = CP = f2(0.f);
-    }
-    ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(xr.w); ROT(pr.x); ROT(pr.y); ROT(ar);
-    ROT(R.fx); ROT(R.fy); ROT(R.fz); ROT(R.da);
-  }
-  flush_pair(v, deda, sa, PairAcc{FX.x, FY.x, FZ.x, DA.x});
-  flush_pair(v, deda, sb, PairAcc{FX.y, FY.y, FZ.y, DA.y});
   flush_pair(v, deda, r0 + lane, R);
 }
 
@@ -540,13 +478,8 @@ __global__ void __launch_bounds__(256, 3) k_gb_pair(DevView v, GBConst k, const 
     if (two) {
       const Tile U = v.tiles[t + 1];
       double evdw = 0.0, eel = 0.0, epol = 0.0;
-      // (the packed body issues fewer instructions only where the energies ride along)
-      if (tile_full(T)) {
-        if (ENERGY) gb_pair_full2<true>(v, k, T, U, lane, born, deda, evdw, eel, epol);
-        else gb_pair_tile2<false, true>(v, k, T, U, lane, born, deda, evdw, eel, epol);
-      } else {
-        gb_pair_tile2<ENERGY, false>(v, k, T, U, lane, born, deda, evdw, eel, epol);
-      }
+      if (tile_full(T)) gb_pair_tile2<ENERGY, true>(v, k, T, U, lane, born, deda, evdw, eel, epol);
+      else gb_pair_tile2<ENERGY, false>(v, k, T, U, lane, born, deda, evdw, eel, epol);
       if (ENERGY) {
         EFix EF = {0, 0, 0};
         efix_in(EF, evdw, eel, epol);

@@ -1007,7 +1007,7 @@ int pdgpu_pair_census(pdgpu_ctx* h, long long* counts) {
   return PDGPU_OK;
 }
 
-int pdgpu_fp32_peak(int device, double* tflops_ffma, double* tflops_ffma2, double* sm_mhz) {
+int pdgpu_fp32_peak(int device, double* tflops_ffma, double* tflops_ffma2) {
   if (device < 0) return PDGPU_ERR_ARG;
-  return measure_fp32_peak(device, tflops_ffma, tflops_ffma2, sm_mhz);
+  return measure_fp32_peak(device, tflops_ffma, tflops_ffma2);
 }

@@ -211,7 +211,7 @@ int launch_slot_params(Context& c);
 // measurement aids (k_diag.cu): the pair census of the current list into out[5]
 // (device, zeroed by the caller) and the FP32 FMA ceiling of a device
 int launch_census(Context& c, const NBConst& nk, const GBConst& gk, bool do_nb, bool do_gb, unsigned long long* out);
-int measure_fp32_peak(int device, double* tflops_ffma, double* tflops_ffma2, double* sm_mhz);
+int measure_fp32_peak(int device, double* tflops_ffma, double* tflops_ffma2);
 NBConst make_nb_const(const pdgpu_nb_params& p);
 GBConst make_gb_const(const pdgpu_gb_params& p, double listR);
 int launch_bonded(Context& c, bool energy);

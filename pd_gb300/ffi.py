@@ -132,7 +132,7 @@ SIGNATURES = {
     "pdgpu_kernel_launches": ([ctypes.c_void_p], ctypes.c_longlong),
     "pdgpu_time_kernel": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp], ctypes.c_int),
     "pdgpu_pair_census": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
-    "pdgpu_fp32_peak": ([ctypes.c_int, _dp, _dp, _dp], ctypes.c_int),
+    "pdgpu_fp32_peak": ([ctypes.c_int, _dp, _dp], ctypes.c_int),
     "pdgpu_device_allocations": ([ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
                                  ctypes.c_int),
     "pdgpu_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
@@ -173,11 +173,10 @@ def load(build_if_missing=True):
 
 
 def fp32_peak(device=0):
-    """Measured FP32 FMA throughput (TFLOP/s, FFMA and packed FFMA2) and the SM
-    clock (MHz) over the FFMA probe (pdgpu_fp32_peak)."""
-    a, b, m = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
-    check(load().pdgpu_fp32_peak(int(device), ctypes.byref(a), ctypes.byref(b), ctypes.byref(m)), "pdgpu_fp32_peak")
-    return {"ffma_tflops": a.value, "ffma2_tflops": b.value, "sm_mhz": m.value}
+    """Measured FP32 FMA throughput (TFLOP/s, FFMA and packed FFMA2; pdgpu_fp32_peak)."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    check(load().pdgpu_fp32_peak(int(device), ctypes.byref(a), ctypes.byref(b)), "pdgpu_fp32_peak")
+    return {"ffma_tflops": a.value, "ffma2_tflops": b.value}
 
 
 def device_allocations():

@@ -45,9 +45,11 @@ def test_fixed_point_overflow_is_reported_and_the_context_recovers():
     with pytest.raises(ffi.PDGPUError) as err:
         ctx.compute(ffi.NB, f)
     assert err.value.status == -4          # PDGPU_ERR_FIXED_OVERFLOW
-    # the same context, atoms 4 A apart: plain Coulomb (no switching inside 10 A)
+    # the same context, atoms 4 A apart (moved past the skin: new list, as PD's
+    # calcNewList): plain Coulomb (no switching inside 10 A)
     far = np.array([[0.0, 0.0, 0.0], [4.0, 0.0, 0.0]])
     ctx.set_positions(far)
+    ctx.rebuild_list()
     f = np.zeros((2, 3))
     e = ctx.compute(ffi.NB, f)[0]
     kcal = 4184.0 / 6.0221418E23
@@ -74,6 +76,7 @@ def test_lcpo_candidate_overflow_is_reported_and_the_context_recovers():
     assert err.value.status == -3          # PDGPU_ERR_LIST_OVERFLOW
     # the same atoms 8 A apart: no overlaps, every atom keeps its full sphere
     ctx.set_positions(dense * 16.0)
+    ctx.rebuild_list()
     e = ctx.compute(ffi.SA)[0]
     sasa = ctx.sasa()
     r = lcpo[0]
