@@ -163,8 +163,9 @@ int pdgpu_compute(pdgpu_ctx *ctx, unsigned what, pdgpu_energies *out, double *f,
  * memory) without any host synchronisation.  Energies are formed only when
  * `what` includes PDGPU_ENERGY and stay on the device until pdgpu_get_energies().
  * Forces are FP32 pair math with 64-bit fixed-point sums.  Energies, when
- * requested: GB pair energies from the force path's FP32 terms, summed in FP64
- * and fixed point; FF_NonBonded pair energies in FP64. */
+ * requested: GB pair energies in FP64 from FP64 positions and parameters for
+ * pairs closer than 4.5 A, from FP32 terms beyond, summed in FP64 and fixed
+ * point; FF_NonBonded pair energies in FP64. */
 int pdgpu_compute_device(pdgpu_ctx *ctx, unsigned what, double *d_f);
 int pdgpu_get_energies(pdgpu_ctx *ctx, pdgpu_energies *out);
 /* Born radii (Angstrom, original atom order) and LCPO per-atom SASA (A^2) from
@@ -190,7 +191,9 @@ int pdgpu_nb_energy_update(pdgpu_ctx *ctx, pdgpu_energies *out, int *nmoved);
  * PD has no counterpart: its parameter derivatives are finite differences of
  * Forcefield::calcEnergies with setup() re-run after each edit
  * (src/mmlib/forcefields/nonbonded.cpp:1078-1084).  One call evaluates the
- * energies (FP64 per pair) and dE/dp for every per-atom parameter array of
+ * energies (GB pairs from FP32 terms summed in FP64, |dE|/|E| ~ 1e-6: they
+ * weight a loss; pdgpu_compute gives the closer ones) and dE/dp for every
+ * per-atom parameter array of
  * pdgpu_system_desc, in original atom order, J per unit of the parameter as
  * it is given there (charge e, radius A, epsilon sqrt(J), gb_radius A, gb_vj
  * A^3, gb_terms123 its own unit); E is the system's own energy, so atoms of

@@ -133,6 +133,66 @@ __device__ __forceinline__ void born_tile2(const DevView& v, const GBConst& k, c
   atomic_add_ll(&gpol[r0 + lane], fx32(gr));
 }
 
+// ---------------------------------------------------------------------------
+// All-inside tile pairs (every pair inside every cutoff, no exclusions: the
+// all-pairs case) take lean Born and chain-rule bodies: per-atom factors are
+// folded into the values loaded once per item, and the close-contact (CCF)
+// branch is entered on a warp vote over a coarse bound of the item,
+// (max R_i + max R_j)^2 / P5, instead of each pair's own limit.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float warp_max(float x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+  return x;
+}
+
+// an upper bound of (R_i + R_j)^2 / P5 over the pairs of a tile pair: held raw
+// GB radii RS, the rotating block's Rr
+__device__ __forceinline__ float pair_contact2(const GBConst& k, float2 RS, float Rr) {
+  const float m = warp_max(fmaxf(RS.x, RS.y)) + warp_max(Rr);
+  return m * m * k.invP5 * 1.0001f;
+}
+
+__device__ __forceinline__ void born_full2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B, int lane,
+                                           long long* gpol) {
+  const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
+  const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
+  const float4 pa = v.par[sa], pb = v.par[sb];
+  const float2 nx = make_float2(-xa.x, -xb.x), ny = make_float2(-xa.y, -xb.y), nz = make_float2(-xa.z, -xb.z);
+  const float2 RS = make_float2(pa.z, pb.z), VP = make_float2(k.P4 * pa.w, k.P4 * pb.w);
+  float4 xr = v.xq[r0 + lane];
+  const float4 pr = v.par[r0 + lane];
+  float Rr = pr.z, VPr = k.P4 * pr.w, gr = 0.f;
+  const float c2 = pair_contact2(k, RS, Rr);
+  float2 G = f2(0.f);
+#pragma unroll 4
+  for (int kk = 0; kk < 32; kk++) {
+    const float2 dx = __fadd2_rn(f2(xr.x), nx), dy = __fadd2_rn(f2(xr.y), ny), dz = __fadd2_rn(f2(xr.z), nz);
+    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    const float2 ir2 = make_float2(__fdividef(1.f, r2.x), __fdividef(1.f, r2.y));
+    float2 w = __fmul2_rn(ir2, ir2);
+    if (__any_sync(0xffffffffu, r2.x <= c2 || r2.y <= c2)) {
+      const float2 rs = __fadd2_rn(RS, f2(Rr)), rs2 = __fmul2_rn(rs, rs);
+      if (gb_contact(k, r2.x, rs2.x)) {
+        const float h = 0.5f - 0.5f * cospif(__fdividef(r2.x, rs2.x) * k.P5);
+        w.x *= h * h;
+      }
+      if (gb_contact(k, r2.y, rs2.y)) {
+        const float h = 0.5f - 0.5f * cospif(__fdividef(r2.y, rs2.y) * k.P5);
+        w.y *= h * h;
+      }
+    }
+    G = __ffma2_rn(w, f2(VPr), G);
+    gr = fmaf(w.x, VP.x, gr);
+    gr = fmaf(w.y, VP.y, gr);
+    ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(Rr); ROT(VPr); ROT(gr);
+  }
+  fix_range(v.status, fabsf(G.x) + fabsf(G.y) + fabsf(gr));
+  atomic_add_ll(&gpol[sa], fx32(G.x));
+  atomic_add_ll(&gpol[sb], fx32(G.y));
+  atomic_add_ll(&gpol[r0 + lane], fx32(gr));
+}
+
 // the warp's next work item: a tile (t) or a tile pair (t, t + 1)
 __device__ __forceinline__ int item_tile(const DevView& v, int it, bool& two) {
   const unsigned code = v.items[it];
@@ -150,7 +210,7 @@ __global__ void __launch_bounds__(256) k_gb_born(DevView v, GBConst k, long long
     const Tile T = v.tiles[t];
     if (two) {
       const Tile U = v.tiles[t + 1];
-      if (tile_full(T)) born_tile2<true>(v, k, T, U, lane, gpol);
+      if (tile_full(T)) born_full2(v, k, T, U, lane, gpol);
       else born_tile2<false>(v, k, T, U, lane, gpol);
       continue;
     }
@@ -200,18 +260,56 @@ __device__ __noinline__ bool gb_on_fp64(const DevView& v, int si, int sj, double
 
 // ---------------------------------------------------------------------------
 // pass 2: GB cross term fused with vacuum LJ + Coulomb, i > j pairs within Cutoff
-// (forces, dE/da and, with ENERGY, the pair energies).  With ENERGY each pair's
-// displacement is formed in FP64 from the FP64 positions and rounded once, its
-// energies are evaluated in FP32 from it and summed in FP64, then per tile in
-// fixed point: the vdW and Coulomb totals are sums of large terms of both
-// signs, and FP32 positions (rounded relative to their block centres) or FP32
-// partial sums leave ~1e-6 of such a total.  Energy evaluations are rare (an
-// exchange attempt, an explicit energy call), so the FP64 work stays off the
-// force-only dynamics step.
+// (forces, dE/da and, with ENERGY, the pair energies).  With ENERGY every pair
+// closer than sqrt(GBConst::e64_r2) (4.5 A: the close contacts that carry the
+// large repulsive terms) takes its displacement from FP64 slot records (rounded
+// once to FP32 for the force) and its energies in FP64 from FP64 per-atom
+// parameters; the other pairs' energies are FP32, in partial sums moved to FP64
+// every 8 rotation steps; a work item's sums then go over the warp in FP64 and
+// enter fixed point once.  The vdW total is a small difference of large
+// repulsive and attractive sums: FP32 positions (rounded relative to their
+// block centres) on the close contacts, or FP32 sums, leave ~1e-6 of it.
+// Energy evaluations are rare (an exchange attempt, an explicit energy call),
+// so this FP64 work stays off the force-only step; the energy pass of a
+// parameter-gradient call sets e64_r2 = 0 (its energies only weight the loss).
 // ---------------------------------------------------------------------------
 struct PairAcc {
   float fx, fy, fz, da;
 };
+
+// FP64 records of every sorted slot for the energy pass (DevView::epos, epar)
+__global__ void k_energy_records(DevView v, double4* epos, double2* epar) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= v.nslots) return;
+  const int a = v.sorted_atom[s];
+  if (a < 0) {
+    epos[s] = make_double4(1e6, 1e6, 1e6, 0.0);
+    epar[s] = make_double2(-1.0, 0.0);
+    return;
+  }
+  epos[s] = make_double4(v.pos[3 * a], v.pos[3 * a + 1], v.pos[3 * a + 2], v.charge[a]);
+  epar[s] = make_double2(v.radius[a], v.sqeps[a]);
+}
+
+// (ENERGY) pair energies of a work item: close pairs in FP64, the others in
+// FP32 partial sums moved to FP64 every 8 rotation steps
+struct EAcc {
+  double v = 0.0, e = 0.0, p = 0.0;
+  float fv = 0.f, fe = 0.f, fp = 0.f;
+  __device__ __forceinline__ void flush() {
+    v += (double)fv;
+    e += (double)fe;
+    p += (double)fp;
+    fv = fe = fp = 0.f;
+  }
+};
+
+// 1 / sqrt(x) in FP64 from the FP32 approximation and one Newton step
+// (relative error ~1e-13), without the FP64 square-root sequence
+__device__ __forceinline__ double rsqrt_fp64(double x) {
+  const double y = (double)rsqrtf((float)x);
+  return y * fma(-0.5 * x * y, y, 1.5);
+}
 
 // u = -r^2 / (4 a_i a_j) of a pair, and whether the pair may lie above the exp
 // threshold (the FP64 tie-break band included): the warp votes on it, and the
@@ -224,14 +322,69 @@ __device__ __forceinline__ bool gb_maybe_on(const GBConst& k, float u) {
 
 // One pair of the fused law: i = (xi.w, pix, piy, ai), j = (qj, pjx, pjy, aj),
 // (dx, dy, dz) = x_j - x_i, u = gb_u.  Adds the force on i along d to I and its
-// opposite to J, dE/da to both, and (ENERGY) the pair energies to cv, ce, cp.
-// si, sj: slots for the FP64 threshold tie-break; any_gb: the warp's vote on
-// gb_maybe_on (warp-uniform).
+// opposite to J, dE/da to both.  si, sj:
+// slots for the FP64 threshold tie-break; any_gb: the warp's vote on
+// gb_maybe_on (warp-uniform).  (ENERGY) pe: the pair's energies for
+// add_pair_energy.
+// (ENERGY) what a pair's energies need beyond r^2: its FP32 energies (vdW,
+// Coulomb, GB cross term) and, for the FP64 path of a close pair, whether the
+// GB term is on, fgb S, the Coulomb switch S and the vdW switch (0 beyond
+// VdwCutoff)
+struct PairE {
+  float v, e, p, fgbS, S, vsw;
+  bool gbon;
+};
+
+// FP64 energies of a close pair from the slot records (the caller enters this
+// on a warp vote, so the FP64 code is not issued for warps without a close
+// pair); returned, not accumulated, so the accumulators stay in registers
+struct E3 {
+  double v, e, p;
+};
+template <bool FAST>
+__device__ __noinline__ E3 close_energy(const DevView& v, const GBConst& k, double r2d, double4 ei, double4 ej,
+                                        double2 pi_e, int sj, bool excl, bool is14, PairE pe) {
+  E3 r = {0.0, 0.0, 0.0};
+  const double qq = ei.w * ej.w, ir = rsqrt_fp64(r2d);
+  if (pe.gbon) r.p = 2.0 * k.premul_d * qq * (double)pe.fgbS;
+  else if (!FAST) r.p = 2.0 * k.premul_d * qq * ir * (double)pe.S;
+  if (FAST && !excl) {
+    r.e = (pe.gbon ? k.econv_in_d : k.econv_out_d) * (is14 ? k.elec14_d : 1.0) * qq * ir * (double)pe.S;
+    const double2 pj_e = v.epar[sj];
+    const double sd = pi_e.x + pj_e.x, t2 = sd * sd * (ir * ir), B6 = t2 * t2 * t2;
+    r.v = pi_e.y * pj_e.y * (is14 ? k.vdw14_d : 1.0) * (B6 * B6 - 2.0 * B6) * (double)pe.vsw;
+  }
+  return r;
+}
+
+// (ENERGY) a pair's energies into the item's sums: the FP64 path for a close
+// pair (warp-voted; PRECISE passes only), the FP32 sums otherwise
+template <bool FAST, bool PRECISE>
+__device__ __forceinline__ void add_pair_energy(const DevView& v, const GBConst& k, bool in, bool close, double r2d,
+                                                const double4& ei, const double4& ej, const double2& pi_e, int sj,
+                                                bool excl, bool is14, const PairE& pe, EAcc& ea) {
+  bool fp32 = in;
+  if (PRECISE && __any_sync(0xffffffffu, in && close)) {
+    if (in && close) {
+      const E3 c = close_energy<FAST>(v, k, r2d, ei, ej, pi_e, sj, excl, is14, pe);
+      ea.v += c.v;
+      ea.e += c.e;
+      ea.p += c.p;
+      fp32 = false;
+    }
+  }
+  if (fp32) {
+    ea.fv += pe.v;
+    ea.fe += pe.e;
+    ea.fp += pe.p;
+  }
+}
+
 template <bool ENERGY, bool FULL, bool FAST>
 __device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, float dx, float dy, float dz,
                                             float r2, float u, bool any_gb, float qi, float qj, float pix, float piy,
                                             float pjx, float pjy, float ai, float aj, bool excl, bool is14, int si,
-                                            int sj, PairAcc& I, PairAcc& J, double& cv, double& ce, double& cp) {
+                                            int sj, PairAcc& I, PairAcc& J, PairE& pe) {
     const float invr = rsqrtf(r2);
     const float r = r2 * invr;
     const float qiqj = qi * qj;
@@ -255,6 +408,7 @@ __device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, 
       dS = -4.f * k.invw2 * w * sw;
       S = sw * sw;
     }
+    if (ENERGY) pe = PairE{0.f, 0.f, 0.f, 0.f, S, 0.f, any_gb && gbon};
     if (any_gb && gbon) {
       const float tg = __expf(u);
       const float fgb = rsqrtf(r2 + tg * aiaj);
@@ -262,7 +416,10 @@ __device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, 
       const float ep = k.premul * qiqj * fgb;
       float dedr = -ep * (r - 0.25f * r * tg) * l;
       float dalpha = -ep * tg * (1.f - u) * l;
-      if (ENERGY) cp += (double)(2.f * ep * S);
+      if (ENERGY) {
+        pe.p = 2.f * ep * S;
+        pe.fgbS = fgb * S;
+      }
       if (FAST && !excl) {
         elec = k.econv_in * s14 * qiqj * invr;
         delec = -elec * invr;
@@ -281,12 +438,12 @@ __device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, 
       // calcBornForces below the threshold (gbff.cpp:1308-1325): premul q_i q_j / r
       const float ep = k.premul * qiqj * invr;
       float dedr = -ep * invr;
-      if (ENERGY) cp += (double)(2.f * ep * S);
+      if (ENERGY) pe.p = 2.f * ep * S;
       if (sw_on) dedr = S * dedr + dS * ep;
       g += 2.f * dedr * invr;
     }
     if (FAST && !excl) {
-      if (ENERGY) ce += (double)(elec * S);
+      if (ENERGY) pe.e = elec * S;
       if (sw_on) delec = S * delec + elec * dS;
       const float t = (pix + pjx) * invr;
       float B = t * t;
@@ -295,63 +452,63 @@ __device__ __forceinline__ void gb_pair_one(const DevView& v, const GBConst& k, 
       const float eps = piy * pjy * (is14 ? k.vdw14 : 1.f);
       float dvdw = -12.f * eps * invr * (A - B);
       float Ev = (ENERGY || !FULL) ? eps * (A - 2.f * B) : 0.f;
+      float vsw = 1.f;
       if (!FULL) {
         const float w = fmaxf(r - k.vdwinner, 0.f);
         const float sw = 1.f - w * w * k.vdwinvw2;
         dvdw = sw * sw * dvdw + Ev * (-4.f * k.vdwinvw2 * w * sw);
-        if (ENERGY) Ev *= sw * sw;
         const bool vin = r < k.vdwcut;
+        vsw = vin ? sw * sw : 0.f;
         dvdw = vin ? dvdw : 0.f;
-        Ev = vin ? Ev : 0.f;
       }
-      if (ENERGY) cv += (double)Ev;
+      if (ENERGY) {
+        pe.v = Ev * vsw;
+        pe.vsw = vsw;
+      }
       g += (dvdw + delec) * invr;
     }
     I.fx += g * dx; I.fy += g * dy; I.fz += g * dz;
     J.fx -= g * dx; J.fy -= g * dy; J.fz -= g * dz;
-  
 }
 
-// (ENERGY) the displacement x_b - x_a of two atoms from the FP64 positions,
-// rounded once to FP32; false (nothing written) for a padding slot
-__device__ __forceinline__ bool disp_fp64(const DevView& v, int a, const double* pa, int sb, float& dx, float& dy,
-                                          float& dz, float& r2) {
-  const int b = v.sorted_atom[sb];
-  if (a < 0 || b < 0) return false;
-  const double ex = v.pos[3 * b] - pa[0], ey = v.pos[3 * b + 1] - pa[1], ez = v.pos[3 * b + 2] - pa[2];
+// (ENERGY) for a pair closer than sqrt(k.e64_r2): the displacement x_b - x_a
+// from the FP64 slot records (rounded once to FP32 for the force) and r^2 in
+// FP64; false (nothing written) for a farther pair or a padding slot
+__device__ __forceinline__ bool disp_fp64(const DevView& v, const GBConst& k, const double4& ea_, int sb, double4& eb,
+                                          float& dx, float& dy, float& dz, float& r2, double& r2d) {
+  if (!(r2 < k.e64_r2) || ea_.x > 1e5) return false;
+  eb = v.epos[sb];
+  if (eb.x > 1e5) return false;
+  const double ex = eb.x - ea_.x, ey = eb.y - ea_.y, ez = eb.z - ea_.z;
   dx = (float)ex;
   dy = (float)ey;
   dz = (float)ez;
-  r2 = (float)(ex * ex + ey * ey + ez * ez);
+  r2d = ex * ex + ey * ey + ez * ez;
+  r2 = (float)r2d;
   return true;
 }
 
-__device__ __forceinline__ int own_atom_fp64(const DevView& v, int s, double* p) {
-  const int a = v.sorted_atom[s];
-  p[0] = p[1] = p[2] = 0.0;
-  if (a >= 0) {
-    p[0] = v.pos[3 * a];
-    p[1] = v.pos[3 * a + 1];
-    p[2] = v.pos[3 * a + 2];
-  }
-  return a;
-}
-
-template <bool MASKED, bool ENERGY, bool FULL, bool FAST = true>
+template <bool MASKED, bool ENERGY, bool FULL, bool FAST = true, bool PRECISE = true>
 __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k, const Tile& T, int lane, int si,
                                              const float4& xi, const float4& pi, float ai, unsigned ex,
                                              unsigned m14, unsigned dmask, const float* born, PairAcc& I, PairAcc& J,
-                                             double& evdw, double& eel, double& epol) {
+                                             EAcc& ea) {
   float4 xj = j_in_i_frame(v, T, lane);
   float4 pj = v.par[T.bj * 32 + lane];
   float aj = born[T.bj * 32 + lane];
-  double pos_i[3];
-  const int atom_i = ENERGY ? own_atom_fp64(v, si, pos_i) : 0;
+  double4 e_i = make_double4(0.0, 0.0, 0.0, 0.0), e_j = e_i;
+  double2 p_i = make_double2(0.0, 0.0);
+  if (ENERGY && PRECISE) {
+    e_i = v.epos[si];
+    p_i = v.epar[si];
+  }
 #pragma unroll 2
   for (int kk = 0; kk < 32; kk++) {
     float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
     float r2 = dx * dx + dy * dy + dz * dz;
-    if (ENERGY) disp_fp64(v, atom_i, pos_i, T.bj * 32 + ((lane + kk) & 31), dx, dy, dz, r2);
+    double r2d = 0.0;
+    const bool close =
+        ENERGY && PRECISE && disp_fp64(v, k, e_i, T.bj * 32 + ((lane + kk) & 31), e_j, dx, dy, dz, r2, r2d);
     bool pair = true, excl = false, is14 = false;
     if (MASKED) {
       pair = !((dmask >> kk) & 1u);
@@ -361,9 +518,14 @@ __device__ __forceinline__ void gb_pair_tile(const DevView& v, const GBConst& k,
     const bool in = (FULL || r2 <= k.cut2) && pair;
     const float u = gb_u(r2, ai, aj);
     const bool any_gb = __any_sync(0xffffffffu, in && gb_maybe_on(k, u));
+    PairE pe;
     if (in)
       gb_pair_one<ENERGY, FULL, FAST>(v, k, dx, dy, dz, r2, u, any_gb, xi.w, xj.w, pi.x, pi.y, pj.x, pj.y, ai, aj,
-                                      excl, is14, si, T.bj * 32 + ((lane + kk) & 31), I, J, evdw, eel, epol);
+                                      excl, is14, si, T.bj * 32 + ((lane + kk) & 31), I, J, pe);
+    if (ENERGY)
+      add_pair_energy<FAST, PRECISE>(v, k, in, close, r2d, e_i, e_j, p_i, T.bj * 32 + ((lane + kk) & 31), excl,
+                                     is14, pe, ea);
+    if (ENERGY && (kk & 7) == 7) ea.flush();
     ROT(xj.x); ROT(xj.y); ROT(xj.z); ROT(xj.w); ROT(pj.x); ROT(pj.y); ROT(aj);
     ROT(J.fx); ROT(J.fy); ROT(J.fz); ROT(J.da);
   }
@@ -396,42 +558,42 @@ __device__ __forceinline__ void flush_pair(const DevView& v, long long* deda, in
   flush_fix(v, deda, s, F);
 }
 
-// per-tile FP64 energy sums in fixed point, combined per run of tiles
-struct EFix {
-  long long vdw, elec, pol;
-};
-
-__device__ __forceinline__ void efix_in(EFix& F, double& evdw, double& eel, double& epol) {
-  F.vdw += fix_energy_d(evdw);
-  F.elec += fix_energy_d(eel);
-  F.pol += fix_energy_d(epol);
-  evdw = eel = epol = 0.0;
+__device__ __forceinline__ double warp_sum_d(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
 }
 
-__device__ __forceinline__ void flush_gb_energy(const DevView& v, int lane, int bi, EFix& F) {
-  long long e0 = warp_sum_ll(F.vdw), e1 = warp_sum_ll(F.elec), e2 = warp_sum_ll(F.pol);
+// (ENERGY) a work item's pair energies: summed over the warp in FP64 (a fixed
+// butterfly order), entered in fixed point once per item
+__device__ __forceinline__ void flush_gb_energy(const DevView& v, int lane, int bi, EAcc& ea) {
+  ea.flush();
+  const double e0 = warp_sum_d(ea.v), e1 = warp_sum_d(ea.e), e2 = warp_sum_d(ea.p);
   if (lane == 0) {
     long long* E = v.eacc + (size_t)v.slot_sys[bi] * E_NSLOTS;
-    atomic_add_ll(&E[E_VDW], e0);
-    atomic_add_ll(&E[E_ELEC], e1);
-    atomic_add_ll(&E[E_POL_CROSS], e2);
+    atomic_add_ll(&E[E_VDW], fix_energy_d(e0));
+    atomic_add_ll(&E[E_ELEC], fix_energy_d(e1));
+    atomic_add_ll(&E[E_POL_CROSS], fix_energy_d(e2));
   }
-  F = {0, 0, 0};
 }
 
-template <bool ENERGY, bool FULL>
+template <bool ENERGY, bool FULL, bool PRECISE = true>
 __device__ __forceinline__ void gb_pair_tile2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B,
-                                              int lane, const float* born, long long* deda, double& evdw,
-                                              double& eel, double& epol) {
+                                              int lane, const float* born, long long* deda, EAcc& ea) {
   const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
   const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
   const float4 pa = v.par[sa], pb = v.par[sb];
   const float aa = born[sa], ab = born[sb];
   float4 xr = v.xq[r0 + lane], pr = v.par[r0 + lane];
   float ar = born[r0 + lane];
-  double pos_a[3], pos_b[3];
-  const int atom_a = ENERGY ? own_atom_fp64(v, sa, pos_a) : 0;
-  const int atom_b = ENERGY ? own_atom_fp64(v, sb, pos_b) : 0;
+  double4 e_a = make_double4(0.0, 0.0, 0.0, 0.0), e_b = e_a, e_r = e_a;
+  double2 p_a = make_double2(0.0, 0.0), p_b = p_a;
+  if (ENERGY && PRECISE) {
+    e_a = v.epos[sa];
+    e_b = v.epos[sb];
+    p_a = v.epar[sa];
+    p_b = v.epar[sb];
+  }
   PairAcc IA = {0.f, 0.f, 0.f, 0.f}, IB = {0.f, 0.f, 0.f, 0.f}, R = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 2
   for (int kk = 0; kk < 32; kk++) {
@@ -439,25 +601,32 @@ __device__ __forceinline__ void gb_pair_tile2(const DevView& v, const GBConst& k
     {
       float dx = xr.x - xa.x, dy = xr.y - xa.y, dz = xr.z - xa.z;
       float r2 = dx * dx + dy * dy + dz * dz;
-      if (ENERGY) disp_fp64(v, atom_a, pos_a, sr, dx, dy, dz, r2);
+      double r2d = 0.0;
+      const bool close = ENERGY && PRECISE && disp_fp64(v, k, e_a, sr, e_r, dx, dy, dz, r2, r2d);
       const bool in = FULL || r2 <= k.cut2;
       const float u = gb_u(r2, aa, ar);
       const bool any_gb = __any_sync(0xffffffffu, in && gb_maybe_on(k, u));
+      PairE pe;
       if (in)
         gb_pair_one<ENERGY, FULL, true>(v, k, dx, dy, dz, r2, u, any_gb, xa.w, xr.w, pa.x, pa.y, pr.x, pr.y, aa, ar,
-                                        false, false, sa, sr, IA, R, evdw, eel, epol);
+                                        false, false, sa, sr, IA, R, pe);
+      if (ENERGY) add_pair_energy<true, PRECISE>(v, k, in, close, r2d, e_a, e_r, p_a, sr, false, false, pe, ea);
     }
     {
       float dx = xr.x - xb.x, dy = xr.y - xb.y, dz = xr.z - xb.z;
       float r2 = dx * dx + dy * dy + dz * dz;
-      if (ENERGY) disp_fp64(v, atom_b, pos_b, sr, dx, dy, dz, r2);
+      double r2d = 0.0;
+      const bool close = ENERGY && PRECISE && disp_fp64(v, k, e_b, sr, e_r, dx, dy, dz, r2, r2d);
       const bool in = FULL || r2 <= k.cut2;
       const float u = gb_u(r2, ab, ar);
       const bool any_gb = __any_sync(0xffffffffu, in && gb_maybe_on(k, u));
+      PairE pe;
       if (in)
         gb_pair_one<ENERGY, FULL, true>(v, k, dx, dy, dz, r2, u, any_gb, xb.w, xr.w, pb.x, pb.y, pr.x, pr.y, ab, ar,
-                                        false, false, sb, sr, IB, R, evdw, eel, epol);
+                                        false, false, sb, sr, IB, R, pe);
+      if (ENERGY) add_pair_energy<true, PRECISE>(v, k, in, close, r2d, e_b, e_r, p_b, sr, false, false, pe, ea);
     }
+    if (ENERGY && (kk & 7) == 7) ea.flush();
     ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(xr.w); ROT(pr.x); ROT(pr.y); ROT(ar);
     ROT(R.fx); ROT(R.fy); ROT(R.fz); ROT(R.da);
   }
@@ -466,8 +635,11 @@ __device__ __forceinline__ void gb_pair_tile2(const DevView& v, const GBConst& k
   flush_pair(v, deda, r0 + lane, R);
 }
 
-template <bool ENERGY>
-__global__ void __launch_bounds__(256, 3) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
+// EMODE 0: forces and dE/da only; 1: with energies (close pairs in FP64);
+// 2: with energies from FP32 pair terms (a gradient call's energy pass)
+template <int EMODE>
+__device__ __forceinline__ void gb_pair_items(const DevView& v, const GBConst& k, const float* born, long long* deda) {
+  constexpr bool ENERGY = EMODE != 0, PRECISE = EMODE == 1;
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int ni = *v.nitems;
@@ -477,14 +649,10 @@ __global__ void __launch_bounds__(256, 3) k_gb_pair(DevView v, GBConst k, const 
     const Tile T = v.tiles[t];
     if (two) {
       const Tile U = v.tiles[t + 1];
-      double evdw = 0.0, eel = 0.0, epol = 0.0;
-      if (tile_full(T)) gb_pair_tile2<ENERGY, true>(v, k, T, U, lane, born, deda, evdw, eel, epol);
-      else gb_pair_tile2<ENERGY, false>(v, k, T, U, lane, born, deda, evdw, eel, epol);
-      if (ENERGY) {
-        EFix EF = {0, 0, 0};
-        efix_in(EF, evdw, eel, epol);
-        flush_gb_energy(v, lane, T.bi, EF);
-      }
+      EAcc ea;
+      if (tile_full(T)) gb_pair_tile2<ENERGY, true, PRECISE>(v, k, T, U, lane, born, deda, ea);
+      else gb_pair_tile2<ENERGY, false, PRECISE>(v, k, T, U, lane, born, deda, ea);
+      if (ENERGY) flush_gb_energy(v, lane, T.bi, ea);
       continue;
     }
     const int si = T.bi * 32 + lane;
@@ -494,31 +662,41 @@ __global__ void __launch_bounds__(256, 3) k_gb_pair(DevView v, GBConst k, const 
     tile_masks(v, T, lane, ex, m14);
     const unsigned dmask = (T.flags & 2) ? diag_exclusion(lane) : 0u;
     PairAcc I = {0.f, 0.f, 0.f, 0.f}, J = {0.f, 0.f, 0.f, 0.f};
-    double evdw = 0.0, eel = 0.0, epol = 0.0;
+    EAcc ea;
     const bool full = tile_full(T);
     if (tile_masked(T)) {
       if (full)
-        gb_pair_tile<true, ENERGY, true>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
-                                         eel, epol);
+        gb_pair_tile<true, ENERGY, true, true, PRECISE>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J,
+                                                         ea);
       else
-        gb_pair_tile<true, ENERGY, false>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
-                                          eel, epol);
+        gb_pair_tile<true, ENERGY, false, true, PRECISE>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J,
+                                                         ea);
     } else {
       if (full)
-        gb_pair_tile<false, ENERGY, true>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
-                                          eel, epol);
+        gb_pair_tile<false, ENERGY, true, true, PRECISE>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J,
+                                                         ea);
       else
-        gb_pair_tile<false, ENERGY, false>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J, evdw,
-                                           eel, epol);
+        gb_pair_tile<false, ENERGY, false, true, PRECISE>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J,
+                                                         ea);
     }
     flush_pair(v, deda, si, I);
     flush_pair(v, deda, T.bj * 32 + lane, J);
-    if (ENERGY) {
-      EFix EF = {0, 0, 0};
-      efix_in(EF, evdw, eel, epol);
-      flush_gb_energy(v, lane, T.bi, EF);
-    }
+    if (ENERGY) flush_gb_energy(v, lane, T.bi, ea);
   }
+}
+
+// the force-only pass (every dynamics step) keeps three CTAs per SM; the energy
+// pass carries FP64 records of its close pairs and gets more registers
+__global__ void __launch_bounds__(256, 3) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
+  gb_pair_items<0>(v, k, born, deda);
+}
+__global__ void __launch_bounds__(256, 2) k_gb_pair_energy(DevView v, GBConst k, const float* born,
+                                                           long long* deda) {
+  gb_pair_items<1>(v, k, born, deda);
+}
+__global__ void __launch_bounds__(256, 3) k_gb_pair_energy32(DevView v, GBConst k, const float* born,
+                                                             long long* deda) {
+  gb_pair_items<2>(v, k, born, deda);
 }
 
 // FastMode off (calcBornForces, gbff.cpp:1189-1340): the GB term of every pair
@@ -540,16 +718,11 @@ __global__ void __launch_bounds__(256) k_gb_pair_born_only(DevView v, GBConst k,
     tile_masks(v, T, lane, ex, m14);
     const unsigned dmask = (T.flags & 2) ? diag_exclusion(lane) : 0u;
     PairAcc I = {0.f, 0.f, 0.f, 0.f}, J = {0.f, 0.f, 0.f, 0.f};
-    double evdw = 0.0, eel = 0.0, epol = 0.0;
-    gb_pair_tile<true, ENERGY, false, false>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J,
-                                             evdw, eel, epol);
+    EAcc ea;
+    gb_pair_tile<true, ENERGY, false, false>(v, k, T, lane, si, xi, pi, ai, ex, m14, dmask, born, I, J, ea);
     flush_pair(v, deda, si, I);
     flush_pair(v, deda, T.bj * 32 + lane, J);
-    if (ENERGY) {
-      EFix EF = {0, 0, 0};
-      efix_in(EF, evdw, eel, epol);
-      flush_gb_energy(v, lane, T.bi, EF);
-    }
+    if (ENERGY) flush_gb_energy(v, lane, T.bi, ea);
   }
 }
 
@@ -689,6 +862,60 @@ __device__ __forceinline__ void chain_tile2(const DevView& v, const GBConst& k, 
   flush_force(v, r0 + lane, FR);
 }
 
+// Born chain rule of an all-inside tile pair: (c_i V_j + c_j V_i)(4 CCF - dCCF) / r^6
+// along d, with -4 folded into c (w then carries the held atom's sign and the
+// factor 4 of the no-contact case); the CCF branch on the coarse-bound vote.
+__device__ __forceinline__ void chain_full2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B, int lane,
+                                            const float* chain) {
+  const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
+  const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
+  const float4 pa = v.par[sa], pb = v.par[sb];
+  const float2 nx = make_float2(-xa.x, -xb.x), ny = make_float2(-xa.y, -xb.y), nz = make_float2(-xa.z, -xb.z);
+  const float2 RS = make_float2(pa.z, pb.z), VS = make_float2(pa.w, pb.w);
+  const float2 CS = make_float2(-4.f * chain[sa], -4.f * chain[sb]);
+  float4 xr = v.xq[r0 + lane];
+  const float4 pr = v.par[r0 + lane];
+  float Rr = pr.z, Vr = pr.w, Cr = -4.f * chain[r0 + lane];
+  const float c2 = pair_contact2(k, RS, Rr);
+  float2 FX = f2(0.f), FY = f2(0.f), FZ = f2(0.f);
+  PairAcc FR = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+  for (int kk = 0; kk < 32; kk++) {
+    const float2 dx = __fadd2_rn(f2(xr.x), nx), dy = __fadd2_rn(f2(xr.y), ny), dz = __fadd2_rn(f2(xr.z), nz);
+    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    const float2 ir2 = make_float2(__fdividef(1.f, r2.x), __fdividef(1.f, r2.y));
+    const float2 ir6 = __fmul2_rn(__fmul2_rn(ir2, ir2), ir2);
+    float2 w = __fmul2_rn(__ffma2_rn(CS, f2(Vr), __fmul2_rn(f2(Cr), VS)), ir6);   // -w of the plain law
+    if (__any_sync(0xffffffffu, r2.x <= c2 || r2.y <= c2)) {
+      const float2 rs = __fadd2_rn(RS, f2(Rr)), rs2 = __fmul2_rn(rs, rs);
+      if (gb_contact(k, r2.x, rs2.x)) {
+        float sn, cs;
+        const float x = __fdividef(r2.x, rs2.x) * k.P5;
+        sincospif(x, &sn, &cs);
+        const float h = 0.5f - 0.5f * cs;
+        w.x *= 0.25f * (4.f * h * h - 2.f * h * sn * (x * 3.14159265358979f));
+      }
+      if (gb_contact(k, r2.y, rs2.y)) {
+        float sn, cs;
+        const float x = __fdividef(r2.y, rs2.y) * k.P5;
+        sincospif(x, &sn, &cs);
+        const float h = 0.5f - 0.5f * cs;
+        w.y *= 0.25f * (4.f * h * h - 2.f * h * sn * (x * 3.14159265358979f));
+      }
+    }
+    FX = __ffma2_rn(w, dx, FX);
+    FY = __ffma2_rn(w, dy, FY);
+    FZ = __ffma2_rn(w, dz, FZ);
+    FR.fx = fmaf(-w.x, dx.x, FR.fx); FR.fx = fmaf(-w.y, dx.y, FR.fx);
+    FR.fy = fmaf(-w.x, dy.x, FR.fy); FR.fy = fmaf(-w.y, dy.y, FR.fy);
+    FR.fz = fmaf(-w.x, dz.x, FR.fz); FR.fz = fmaf(-w.y, dz.y, FR.fz);
+    ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(Rr); ROT(Vr); ROT(Cr); ROT(FR.fx); ROT(FR.fy); ROT(FR.fz);
+  }
+  flush_force(v, sa, PairAcc{FX.x, FY.x, FZ.x, 0.f});
+  flush_force(v, sb, PairAcc{FX.y, FY.y, FZ.y, 0.f});
+  flush_force(v, r0 + lane, FR);
+}
+
 __global__ void __launch_bounds__(256) k_gb_chain(DevView v, GBConst k, const float* chain) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -699,7 +926,7 @@ __global__ void __launch_bounds__(256) k_gb_chain(DevView v, GBConst k, const fl
     const Tile T = v.tiles[t];
     if (two) {
       const Tile U = v.tiles[t + 1];
-      if (tile_full(T)) chain_tile2<true>(v, k, T, U, lane, chain);
+      if (tile_full(T)) chain_full2(v, k, T, U, lane, chain);
       else chain_tile2<false>(v, k, T, U, lane, chain);
       continue;
     }
@@ -741,13 +968,20 @@ int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset
   cudaMemsetAsync(c.d_deda.p, 0, sizeof(long long) * c.nslots, st);
   k_gb_born<<<g, 256, 0, st>>>(v, k, c.d_gpol.p);
   k_gb_radii<<<nb, 256, 0, st>>>(v, c.d_gbT.p, c.d_gpol.p, halfeconv, born_offset, c.d_born_f.p, c.d_born_d.p);
+  GBConst ke = k;
+  if (c.gb_no_chain) ke.e64_r2 = 0.f;  // a gradient call's energy pass: FP32 pair energies
+  if (energy && ke.e64_r2 > 0.f) {
+    c.kernel_launches += 1;
+    k_energy_records<<<nb, 256, 0, st>>>(v, c.d_epos.p, c.d_epar.p);
+  }
   if (!k.fast) {
     if (energy) k_gb_pair_born_only<true><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
     else k_gb_pair_born_only<false><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
   } else if (energy) {
-    k_gb_pair<true><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
+    if (ke.e64_r2 > 0.f) k_gb_pair_energy<<<g, 256, 0, st>>>(v, ke, c.d_born_f.p, c.d_deda.p);
+    else k_gb_pair_energy32<<<g, 256, 0, st>>>(v, ke, c.d_born_f.p, c.d_deda.p);
   } else {
-    k_gb_pair<false><<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
+    k_gb_pair<<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
   }
   k_gb_self<<<nb, 256, 0, st>>>(v, c.d_charge.p, k, premul, c.d_deda.p, c.d_born_d.p, c.d_chain_f.p,
                                 energy ? 1 : 0);
@@ -762,7 +996,7 @@ int launch_gb_stage(Context& c, const GBConst& k, int stage) {
   int g = tile_grid(c);
   c.kernel_launches += 1;
   if (stage == 1) k_gb_born<<<g, 256, 0, c.stream>>>(v, k, c.d_gpol.p);
-  else if (stage == 2) k_gb_pair<false><<<g, 256, 0, c.stream>>>(v, k, c.d_born_f.p, c.d_deda.p);
+  else if (stage == 2) k_gb_pair<<<g, 256, 0, c.stream>>>(v, k, c.d_born_f.p, c.d_deda.p);
   else k_gb_chain<<<g, 256, 0, c.stream>>>(v, k, c.d_chain_f.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }

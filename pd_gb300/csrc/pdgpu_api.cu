@@ -175,6 +175,7 @@ GBConst pdgpu::make_gb_const(const pdgpu_gb_params& p, double listR) {
   k.elec14_d = p.Elec14Scaling;
   k.thresh_d = p.ExpApproxThreshold;
   k.fast = 1;
+  k.e64_r2 = 4.5f * 4.5f;
   return k;
 }
 
@@ -432,6 +433,8 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
     if (e == cudaSuccess) e = c.d_born_f.alloc(c.nslots);
     if (e == cudaSuccess) e = c.d_chain_f.alloc(c.nslots);
     if (e == cudaSuccess) e = c.d_born_d.alloc(N);
+    if (e == cudaSuccess) e = c.d_epos.alloc(c.nslots);
+    if (e == cudaSuccess) e = c.d_epar.alloc(c.nslots);
   }
   if (c.has_sa) {
     if (e == cudaSuccess) e = c.d_lc_ncand.alloc(c.nslots);

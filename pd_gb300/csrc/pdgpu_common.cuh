@@ -30,7 +30,7 @@ constexpr int kLcpoCand = 160;                        // candidate capacity befo
 
 // fixed-point scales
 constexpr double kForceScale = 4294967296.0;          // 2^32 per kcal/mol/A
-constexpr double kEnergyScale = 16777216.0;           // 2^24 per kcal/mol
+constexpr double kEnergyScale = 4294967296.0;         // 2^32 per kcal/mol (|E| < 2^31 kcal/mol per slot)
 constexpr double kSumScale = 4294967296.0;            // 2^32 per unit (Born sums, dE/da)
 
 // per-system energy slots (fixed point)
@@ -93,6 +93,9 @@ struct GBConst {
   // 1: FastMode (GB fused with LJ + Coulomb, εout Coulomb below the threshold);
   // 0: calcBornForces (GB term alone for every pair, premul q q / r below it)
   int fast;
+  // energy passes: pairs closer than sqrt(e64_r2) take their energies in FP64
+  // from FP64 positions and parameters (0: none, every pair in FP32)
+  float e64_r2;
 };
 
 // Device-side view of a context, passed by value to kernels.
@@ -106,6 +109,11 @@ struct DevView {
   const double* radius;      // natom, LJ Rmin/2
   const double* sqeps;       // natom, sqrt(kcal/mol)
   const double* born;        // natom, Born radii of the last GB pass (FP64)
+  // (GB energy evaluations) FP64 records per sorted slot, written by
+  // k_energy_records before the energy pass: (x, y, z, charge) and (LJ radius,
+  // sqrt(eps kcal/mol)); padding slots: far away, radius -1
+  const double4* epos;
+  const double2* epar;
   // sorted order
   const int* sorted_atom;    // [nslots]
   float4* xq;                // rel pos + charge
@@ -142,7 +150,10 @@ struct DevView {
 // ---------------------------------------------------------------------------
 // fixed point helpers
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ long long fix_energy_d(double x) { return __double2ll_rn(x * 16777216.0); }
+// energies: 2^32 per kcal/mol.  The resolution matters: a converted partial
+// sum keeps only whole units, so many small partial sums of one sign (the far
+// attractive LJ tail, per lane and tile) would be lost at a coarse scale.
+__device__ __forceinline__ long long fix_energy_d(double x) { return __double2ll_rn(x * 4294967296.0); }
 // float -> 64-bit fixed point with 32 fractional bits using integer operations
 // only (|x| < 2^31; larger magnitudes saturate near 2^62 so the overflow check
 // trips).  Rounds half away from zero.  The hardware float->int64 conversion

@@ -128,6 +128,8 @@ struct Context {
   DBuf<float> d_born_f;             // [nslots]
   DBuf<float> d_chain_f;            // [nslots] a^2/166 * dE/da * P4
   DBuf<double> d_born_d;            // [natom] original order
+  DBuf<double4> d_epos;             // [nslots] FP64 position + charge per slot (energy evaluations)
+  DBuf<double2> d_epar;             // [nslots] FP64 LJ radius + sqrt(eps) per slot
   // Monte Carlo partial energy updates (allocated on first use)
   DBuf<double> d_mc_ref;            // [natom*3] positions of the reference evaluation
   DBuf<long long> d_mc_eref;        // [nsys*2] reference vdw, elec (fixed point, energy scale)
@@ -177,6 +179,8 @@ struct Context {
     v.radius = d_radius.p;
     v.sqeps = d_sqeps.p;
     v.born = d_born_d.p;
+    v.epos = d_epos.p;
+    v.epar = d_epar.p;
     v.sorted_atom = d_sorted_atom.p;
     v.xq = d_xq.p;
     v.par = d_par.p;

@@ -82,15 +82,24 @@ def test_c2_solvated_nonbonded_matches_pd():
 
 
 @pytest.mark.parametrize("name", ["cfg_c3", "cfg_c4_small", "cfg_c4_large"])
-def test_gb_sa_workloads_match_pd(name):
+@pytest.mark.parametrize("tiles", [1, 2])
+def test_gb_sa_workloads_match_pd(name, tiles):
+    """Energy evaluation, and the force-only evaluation the dynamics step runs,
+    against PD, with single tiles and with tile pairs as GB work items."""
+    torch = pytest.importorskip("torch")
     from pd_gb300 import ffi
     d = golden(name)
     im = _image(d)
     ctx = _ctx(im, d)
     ctx.set_gb(**gb_kwargs(d))
+    ctx.set_work_items(tiles)
     f = np.zeros((im.natom, 3))
     e = ctx.compute(ffi.GB, f)[0]
     _check_gb(d, e, f, ctx.born_radii())
+    fd = torch.zeros((im.natom, 3), dtype=torch.float64, device="cuda")
+    ctx.compute_device(ffi.GB, fd.data_ptr())
+    ctx.synchronize()
+    assert rel_rms(fd.cpu().numpy(), d["gb_f"]) <= F_TOL
     f = np.zeros((im.natom, 3))
     e = ctx.compute(ffi.SA, f)[0]
     assert rel_err(e["surf"], ref_energy(d, "sasa", "surf")) <= E_TOL

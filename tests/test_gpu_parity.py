@@ -62,25 +62,35 @@ def test_gb_matches_pd(goldens, name):
 
 @pytest.mark.parametrize("name", ["peptide30_ap", "peptide120"])
 def test_gb_work_item_sizes_agree(goldens, name):
-    """Single tiles and tile pairs as GB work items (pdgpu_set_work_items) give the
-    same energies and forces to FP32 rounding of the per-item sums, both PD's."""
+    """Single tiles and tile pairs as GB work items (pdgpu_set_work_items) give
+    the same energies and forces to FP32 rounding of the per-item sums, all
+    PD's: the energy evaluation and the force-only evaluation the dynamics step
+    runs (its own bodies for all-inside tile pairs)."""
+    torch = pytest.importorskip("torch")
     from pd_gb300 import ffi
     d = goldens[name]
+    n = len(d["pos"])
     out = {}
     for tiles in (1, 2):
         ctx = make_ctx(d)
         ctx.set_gb(**gb_kwargs(d))
         ctx.set_work_items(tiles)
         assert ctx.work_items() == tiles
-        f = np.zeros((len(d["pos"]), 3))
-        out[tiles] = (ctx.compute(ffi.GB, f)[0], f)
+        f = np.zeros((n, 3))
+        e = ctx.compute(ffi.GB, f)[0]
+        fd = torch.zeros((n, 3), dtype=torch.float64, device="cuda")
+        ctx.compute_device(ffi.GB, fd.data_ptr())
+        ctx.synchronize()
+        out[tiles] = (e, f, fd.cpu().numpy())
         ctx.close()
-    (e1, f1), (e2, f2) = out[1], out[2]
-    assert rel_rms(f2, f1) <= 1e-6
-    for k in ("vdw", "elec", "pol", "epot"):
-        assert rel_err(e2[k], e1[k]) <= 1e-7, (k, e1[k], e2[k])
-        assert rel_err(e2[k], ref_energy(d, "gb", k)) <= E_TOL
-    assert rel_rms(f2, d["gb_f"]) <= F_TOL and rel_rms(f1, d["gb_f"]) <= F_TOL
+    e1, f1, _ = out[1]
+    for tiles in (1, 2):
+        e, f, ff = out[tiles]
+        assert rel_rms(f, f1) <= 1e-6 and rel_rms(ff, f1) <= 1e-6
+        for k in ("vdw", "elec", "pol", "epot"):
+            assert rel_err(e[k], e1[k]) <= 1e-7, (tiles, k, e1[k], e[k])
+            assert rel_err(e[k], ref_energy(d, "gb", k)) <= E_TOL
+        assert rel_rms(f, d["gb_f"]) <= F_TOL and rel_rms(ff, d["gb_f"]) <= F_TOL
 
 
 @pytest.mark.parametrize("name,tag", [("peptide120", "nb"), ("peptide30_ap", "nb"), ("water_c1", "nb"),
