@@ -635,6 +635,88 @@ __device__ __forceinline__ void gb_pair_tile2(const DevView& v, const GBConst& k
   flush_pair(v, deda, r0 + lane, R);
 }
 
+// The GB cross term of an all-inside pair the threshold test may switch on:
+// the exact decision (FP64 within rounding of the threshold, as gb_pair_one)
+// and, above it, the GB term (gbff.cpp:1592-1678) with Coulomb at eps_in in
+// place of eps_out.  akh, akr: Born radii times sqrtK; e1: the pair's eps_out
+// Coulomb energy; ir = 1/r; g: dE/dr / r.
+__device__ __noinline__ void gb_full_term(const DevView& v, const GBConst& k, float r2, float ir, float e1, float akh,
+                                          float akr, int sh, int sr, float& g, float& dah, float& dar) {
+  const float ah = akh * k.inv_sqrtK, ar = akr * k.inv_sqrtK;
+  const float aiaj = ah * ar;
+  const float u = -0.25f * __fdividef(r2, aiaj);
+  bool on = u > k.thresh;
+  if (fabsf(u - k.thresh) <= 2e-6f * fabsf(k.thresh)) on = gb_on_fp64(v, sh, sr, k.thresh_d);
+  if (!on) return;
+  const float r = r2 * ir;
+  const float qq = e1 * r * k.inv_eout;
+  const float tg = __expf(u);
+  const float fgb = rsqrtf(fmaf(tg, aiaj, r2));
+  const float l = fgb * fgb;
+  const float ep = k.premul * qq * fgb;
+  const float dedr = -ep * (r - 0.25f * r * tg) * l;
+  const float dalpha = -ep * tg * (1.f - u) * l;
+  g += 2.f * dedr * ir - k.in_over_out_m1 * e1 * ir * ir;
+  dah += dalpha * ar;
+  dar += dalpha * ah;
+}
+
+// Force-only GB fused pair of an all-inside tile pair (the dynamics step's
+// body), the two held atoms on packed FP32x2 arithmetic.  Common pair: vacuum
+// LJ + Coulomb at eps_out,  dE/dr / r = -(12 eps (A - B) + E_out) / r^2,  with
+// the held atoms' charges scaled by -sqrt(econv_out) and sqrt(eps) by
+// -sqrt(12) (the rotating atom's by the positive factors), so one FFMA forms
+// the bracket with its sign.  A pair with r^2 <= K a_i a_j may lie above the
+// exp threshold; when any lane has one, gb_full_term runs for those pairs.
+__device__ __forceinline__ void gb_pair_full2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B,
+                                              int lane, const float* born, long long* deda) {
+  const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
+  const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
+  const float4 pa = v.par[sa], pb = v.par[sb];
+  const float2 nx = make_float2(-xa.x, -xb.x), ny = make_float2(-xa.y, -xb.y), nz = make_float2(-xa.z, -xb.z);
+  const float2 QN = make_float2(-k.sq_eout * xa.w, -k.sq_eout * xb.w);
+  const float2 S = make_float2(pa.x, pb.x);
+  const float2 EN = make_float2(-k.sqrt12 * pa.y, -k.sqrt12 * pb.y);
+  const float2 AK = make_float2(k.sqrtK * born[sa], k.sqrtK * born[sb]);
+  const float2 M1 = f2(-1.f);
+  float4 xr = v.xq[r0 + lane];
+  const float4 pr = v.par[r0 + lane];
+  float qr = k.sq_eout * xr.w, sgr = pr.x, er = k.sqrt12 * pr.y, akr = k.sqrtK * born[r0 + lane];
+  float2 FX = f2(0.f), FY = f2(0.f), FZ = f2(0.f), DA = f2(0.f);
+  PairAcc R = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 2
+  for (int kk = 0; kk < 32; kk++) {
+    const float2 dx = __fadd2_rn(f2(xr.x), nx), dy = __fadd2_rn(f2(xr.y), ny), dz = __fadd2_rn(f2(xr.z), nz);
+    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    const float2 lim = __fmul2_rn(AK, f2(akr));
+    const bool na = r2.x <= lim.x, nb = r2.y <= lim.y;
+    const float2 ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+    const float2 ir2 = __fmul2_rn(ir, ir);
+    const float2 e1n = __fmul2_rn(__fmul2_rn(QN, f2(qr)), ir);   // -E_out
+    const float2 s = __fadd2_rn(S, f2(sgr));
+    const float2 t2 = __fmul2_rn(__fmul2_rn(s, s), ir2);
+    const float2 b6 = __fmul2_rn(__fmul2_rn(t2, t2), t2);
+    const float2 amb = __ffma2_rn(b6, b6, __fmul2_rn(b6, M1));    // A - B
+    float2 g = __fmul2_rn(__ffma2_rn(__fmul2_rn(EN, f2(er)), amb, e1n), ir2);
+    if (__any_sync(0xffffffffu, na || nb)) {
+      const int sr = r0 + ((lane + kk) & 31);
+      if (na) gb_full_term(v, k, r2.x, ir.x, -e1n.x, AK.x, akr, sa, sr, g.x, DA.x, R.da);
+      if (nb) gb_full_term(v, k, r2.y, ir.y, -e1n.y, AK.y, akr, sb, sr, g.y, DA.y, R.da);
+    }
+    FX = __ffma2_rn(g, dx, FX);
+    FY = __ffma2_rn(g, dy, FY);
+    FZ = __ffma2_rn(g, dz, FZ);
+    R.fx = fmaf(-g.x, dx.x, R.fx); R.fx = fmaf(-g.y, dx.y, R.fx);
+    R.fy = fmaf(-g.x, dy.x, R.fy); R.fy = fmaf(-g.y, dy.y, R.fy);
+    R.fz = fmaf(-g.x, dz.x, R.fz); R.fz = fmaf(-g.y, dz.y, R.fz);
+    ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(qr); ROT(sgr); ROT(er); ROT(akr);
+    ROT(R.fx); ROT(R.fy); ROT(R.fz); ROT(R.da);
+  }
+  flush_pair(v, deda, sa, PairAcc{FX.x, FY.x, FZ.x, DA.x});
+  flush_pair(v, deda, sb, PairAcc{FX.y, FY.y, FZ.y, DA.y});
+  flush_pair(v, deda, r0 + lane, R);
+}
+
 // EMODE 0: forces and dE/da only; 1: with energies (close pairs in FP64);
 // 2: with energies from FP32 pair terms (a gradient call's energy pass)
 template <int EMODE>
@@ -650,7 +732,10 @@ __device__ __forceinline__ void gb_pair_items(const DevView& v, const GBConst& k
     if (two) {
       const Tile U = v.tiles[t + 1];
       EAcc ea;
-      if (tile_full(T)) gb_pair_tile2<ENERGY, true, PRECISE>(v, k, T, U, lane, born, deda, ea);
+      if (tile_full(T)) {
+        if (ENERGY) gb_pair_tile2<true, true, PRECISE>(v, k, T, U, lane, born, deda, ea);
+        else gb_pair_full2(v, k, T, U, lane, born, deda);
+      }
       else gb_pair_tile2<ENERGY, false, PRECISE>(v, k, T, U, lane, born, deda, ea);
       if (ENERGY) flush_gb_energy(v, lane, T.bi, ea);
       continue;

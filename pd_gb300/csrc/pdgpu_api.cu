@@ -176,6 +176,13 @@ GBConst pdgpu::make_gb_const(const pdgpu_gb_params& p, double listR) {
   k.thresh_d = p.ExpApproxThreshold;
   k.fast = 1;
   k.e64_r2 = 4.5f * 4.5f;
+  const double K = -4.0 * (p.ExpApproxThreshold - 4e-6 * std::fabs(p.ExpApproxThreshold));
+  k.sqrtK = K > 0 ? (float)std::sqrt(std::min(K, 1e36)) : 0.f;
+  k.inv_sqrtK = K > 0 ? (float)(1.0 / std::sqrt(std::min(K, 1e36))) : 0.f;
+  k.sq_eout = (float)std::sqrt(ec / p.DielectricSolvent);
+  k.inv_eout = (float)(p.DielectricSolvent / ec);
+  k.in_over_out_m1 = (float)(p.DielectricSolvent / p.DielectricSolute - 1.0);
+  k.sqrt12 = (float)std::sqrt(12.0);
   return k;
 }
 

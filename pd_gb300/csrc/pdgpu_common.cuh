@@ -96,6 +96,11 @@ struct GBConst {
   // energy passes: pairs closer than sqrt(e64_r2) take their energies in FP64
   // from FP64 positions and parameters (0: none, every pair in FP32)
   float e64_r2;
+  // the force-only all-inside body: Born radii scaled by sqrtK, so that
+  // a_i a_j K >= r^2 holds for every pair the threshold test may switch on
+  // (K = -4 x the threshold widened by 4e-6 relative); charges scaled by
+  // sqrt(econv_out), sqrt(eps) by sqrt(12)
+  float sqrtK, inv_sqrtK, sq_eout, inv_eout, in_over_out_m1, sqrt12;
 };
 
 // Device-side view of a context, passed by value to kernels.
