@@ -505,12 +505,46 @@ def roofline_flops(census, dom):
 def list_build_bytes(image, stats, groups):
     """Algorithmic DRAM bytes of one list build: per atom the FP64 position read
     (24 B), the sorted-slot record written and read back (16 B position + 16 B
-    parameters + 4 B index), the cell key written and read (8 B); per tile its
-    32 B record written (and the candidate flag + scan, 8 B); per masked tile
-    32 lanes x 8 B of exclusion masks; per NB j-atom group 32 x 16 B entries."""
+    parameters + 4 B index), the cell key written and read (8 B); per block its
+    centre, extent, grid cell and row count (48 B); per tile its 32 B record
+    written; per masked tile 32 lanes x 8 B of exclusion masks; per NB j-atom
+    group 32 x 16 B entries."""
     n = image.natom
     ngroups = max(groups[1], 0)
-    return n * (24 + 36 + 8) + stats["tiles"] * (32 + 8) + stats["masked_tiles"] * 256 + ngroups * 32 * 16
+    nblocks = stats["slots"] // 32
+    return (n * (24 + 36 + 8) + nblocks * 48 + stats["tiles"] * 32 + stats["masked_tiles"] * 256 +
+            ngroups * 32 * 16)
+
+
+def run_list_scaling(args):
+    """List build of the C2 box (peptide in TIP3P, 22,489 atoms, 62 A) replicated
+    1x, 2x, 4x and 8x at the same density, one JSON line: per size the tiles, the
+    bytes of the list arrays, the device memory the context holds, the build time
+    (CUDA events, L2 flushed, mean of 10) and, for comparison, what arrays sized
+    by every block pair (candidate flags, tiles, masks, NB groups) would hold."""
+    from pd_gb300 import ffi
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.workspace import load_workload
+    wl = WORKLOADS["c2"]
+    base = load_workload(wl["image"])
+    rows = []
+    for reps in ((1, 1, 1), (2, 1, 1), (2, 2, 1), (2, 2, 2)):
+        image = base.replicate(reps)
+        b0 = ffi.device_allocations()[1]
+        ctx = DeviceContext(image)
+        configure(ctx, wl, image)
+        ctx.set_positions(image.pos)
+        held = ffi.device_allocations()[1] - b0
+        ms = ctx.time_kernel("list", reps=10)
+        tiles, cap, lbytes = ctx.list_tiles()
+        nb = (image.natom + 31) // 32
+        pairs = nb * (nb + 1) // 2
+        all_pairs = pairs * (32 + 4 + 4 + 1 + 8 + 256) + min(32 * pairs + 32 * nb, 8192 * nb) * 16
+        rows.append({"replicas": int(np.prod(reps)), "atoms": image.natom, "blocks": nb, "tiles": int(len(tiles)),
+                     "tile_capacity": int(cap), "list_bytes": int(lbytes), "context_bytes": int(held),
+                     "build_ms": ms, "block_pairs": pairs, "all_pairs_list_bytes": int(all_pairs)})
+        ctx.close()
+    print(json.dumps({"list_scaling": rows, "workload": "c2 replicated", "radius": NB_CUTOFF + wl["padding"]}))
 
 
 def run_ours(args, key, wl, image):
@@ -955,12 +989,19 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2, help="timed steps of the CPU baseline sample")
     ap.add_argument("--long", action="store_true",
                     help="the workload's full run length with oracle checks at intervals (validation, not timing)")
+    ap.add_argument("--list-scaling", action="store_true",
+                    help="list build memory and time on the C2 box replicated 1x-8x (one JSON line)")
     ap.add_argument("--relax-steps", type=int, default=RELAX["steps"],
                     help="untimed relaxation steps before timing (0 for short profiling runs)")
     args = ap.parse_args()
     RELAX["steps"] = args.relax_steps
     args.warmup = max(args.warmup, 3)
     from pd_gb300.workspace import load_workload
+    if args.list_scaling:
+        from pd_gb300 import build as _b
+        _b.build()
+        run_list_scaling(args)
+        return
     if args.workload == "c5":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "PD has no parameter gradient; its derivative is "

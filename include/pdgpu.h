@@ -332,6 +332,15 @@ int pdgpu_get_nb_groups(pdgpu_ctx *ctx, int *on, long long *ngroups, long long *
 /* ---- diagnostics ---------------------------------------------------------- */
 /* Tile / pair counts of the current list: ntiles, nmasked tiles, slots. */
 int pdgpu_list_stats(pdgpu_ctx *ctx, long long *ntiles, long long *nmasked, long long *nslots);
+/* The current tile list as (bi, bj, flags) per tile, rows ascending and
+ * columns ascending within a row (block b holds sorted slots 32b..32b+31);
+ * at most `cap` tiles are written, *ntiles gets the list length.  Flags: bit 0
+ * per-pair minimum image, bit 1 diagonal, bit 2 every pair inside all cutoffs.
+ * Also the device memory the list arrays hold (tile capacity, bytes). */
+int pdgpu_list_tiles(pdgpu_ctx *ctx, int *tiles, long long cap, long long *ntiles, long long *tile_cap,
+                     long long *list_bytes);
+/* The atom in each sorted slot of the current list (-1 for a padding slot). */
+int pdgpu_list_slots(pdgpu_ctx *ctx, int *atom_of_slot);
 /* Number of kernels this context has launched so far (graph replays count
  * every kernel node they run). */
 long long pdgpu_kernel_launches(pdgpu_ctx *ctx);

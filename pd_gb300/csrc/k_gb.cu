@@ -200,7 +200,7 @@ __device__ __forceinline__ int item_tile(const DevView& v, int it, bool& two) {
   return (int)(code & 0x7fffffffu);
 }
 
-__global__ void __launch_bounds__(256) k_gb_born(DevView v, GBConst k, long long* gpol) {
+__global__ void __launch_bounds__(256) k_gb_born(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, long long* gpol) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int ni = *v.nitems;
@@ -639,15 +639,20 @@ __device__ __forceinline__ void gb_pair_tile2(const DevView& v, const GBConst& k
 // the exact decision (FP64 within rounding of the threshold, as gb_pair_one)
 // and, above it, the GB term (gbff.cpp:1592-1678) with Coulomb at eps_in in
 // place of eps_out.  akh, akr: Born radii times sqrtK; e1: the pair's eps_out
-// Coulomb energy; ir = 1/r; g: dE/dr / r.
-__device__ __noinline__ void gb_full_term(const DevView& v, const GBConst& k, float r2, float ir, float e1, float akh,
-                                          float akr, int sh, int sr, float& g, float& dah, float& dar) {
+// Coulomb energy; ir = 1/r.  Returns what the pair adds to dE/dr / r and to
+// the two atoms' dE/da (by value: the caller's accumulators stay in registers).
+struct GBTerm {
+  float g, dah, dar;
+};
+__device__ __noinline__ GBTerm gb_full_term(const DevView& v, const GBConst& k, float r2, float ir, float e1,
+                                            float akh, float akr, int sh, int sr) {
+  GBTerm t = {0.f, 0.f, 0.f};
   const float ah = akh * k.inv_sqrtK, ar = akr * k.inv_sqrtK;
   const float aiaj = ah * ar;
   const float u = -0.25f * __fdividef(r2, aiaj);
   bool on = u > k.thresh;
   if (fabsf(u - k.thresh) <= 2e-6f * fabsf(k.thresh)) on = gb_on_fp64(v, sh, sr, k.thresh_d);
-  if (!on) return;
+  if (!on) return t;
   const float r = r2 * ir;
   const float qq = e1 * r * k.inv_eout;
   const float tg = __expf(u);
@@ -656,9 +661,10 @@ __device__ __noinline__ void gb_full_term(const DevView& v, const GBConst& k, fl
   const float ep = k.premul * qq * fgb;
   const float dedr = -ep * (r - 0.25f * r * tg) * l;
   const float dalpha = -ep * tg * (1.f - u) * l;
-  g += 2.f * dedr * ir - k.in_over_out_m1 * e1 * ir * ir;
-  dah += dalpha * ar;
-  dar += dalpha * ah;
+  t.g = 2.f * dedr * ir - k.in_over_out_m1 * e1 * ir * ir;
+  t.dah = dalpha * ar;
+  t.dar = dalpha * ah;
+  return t;
 }
 
 // Force-only GB fused pair of an all-inside tile pair (the dynamics step's
@@ -700,8 +706,18 @@ __device__ __forceinline__ void gb_pair_full2(const DevView& v, const GBConst& k
     float2 g = __fmul2_rn(__ffma2_rn(__fmul2_rn(EN, f2(er)), amb, e1n), ir2);
     if (__any_sync(0xffffffffu, na || nb)) {
       const int sr = r0 + ((lane + kk) & 31);
-      if (na) gb_full_term(v, k, r2.x, ir.x, -e1n.x, AK.x, akr, sa, sr, g.x, DA.x, R.da);
-      if (nb) gb_full_term(v, k, r2.y, ir.y, -e1n.y, AK.y, akr, sb, sr, g.y, DA.y, R.da);
+      if (na) {
+        const GBTerm t = gb_full_term(v, k, r2.x, ir.x, -e1n.x, AK.x, akr, sa, sr);
+        g.x += t.g;
+        DA.x += t.dah;
+        R.da += t.dar;
+      }
+      if (nb) {
+        const GBTerm t = gb_full_term(v, k, r2.y, ir.y, -e1n.y, AK.y, akr, sb, sr);
+        g.y += t.g;
+        DA.y += t.dah;
+        R.da += t.dar;
+      }
     }
     FX = __ffma2_rn(g, dx, FX);
     FY = __ffma2_rn(g, dy, FY);
@@ -772,14 +788,14 @@ __device__ __forceinline__ void gb_pair_items(const DevView& v, const GBConst& k
 
 // the force-only pass (every dynamics step) keeps three CTAs per SM; the energy
 // pass carries FP64 records of its close pairs and gets more registers
-__global__ void __launch_bounds__(256, 3) k_gb_pair(DevView v, GBConst k, const float* born, long long* deda) {
+__global__ void __launch_bounds__(256, 3) k_gb_pair(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* born, long long* deda) {
   gb_pair_items<0>(v, k, born, deda);
 }
-__global__ void __launch_bounds__(256, 2) k_gb_pair_energy(DevView v, GBConst k, const float* born,
+__global__ void __launch_bounds__(256, 2) k_gb_pair_energy(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* born,
                                                            long long* deda) {
   gb_pair_items<1>(v, k, born, deda);
 }
-__global__ void __launch_bounds__(256, 3) k_gb_pair_energy32(DevView v, GBConst k, const float* born,
+__global__ void __launch_bounds__(256, 3) k_gb_pair_energy32(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* born,
                                                              long long* deda) {
   gb_pair_items<2>(v, k, born, deda);
 }
@@ -789,7 +805,7 @@ __global__ void __launch_bounds__(256, 3) k_gb_pair_energy32(DevView v, GBConst 
 // the NB kernel with the GB object's own FF_NonBonded settings.  One masked body
 // serves every tile: this mode exists for parity with PD, not for speed.
 template <bool ENERGY>
-__global__ void __launch_bounds__(256) k_gb_pair_born_only(DevView v, GBConst k, const float* born,
+__global__ void __launch_bounds__(256) k_gb_pair_born_only(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* born,
                                                            long long* deda) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -1001,7 +1017,7 @@ __device__ __forceinline__ void chain_full2(const DevView& v, const GBConst& k, 
   flush_force(v, r0 + lane, FR);
 }
 
-__global__ void __launch_bounds__(256) k_gb_chain(DevView v, GBConst k, const float* chain) {
+__global__ void __launch_bounds__(256) k_gb_chain(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* chain) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int ni = *v.nitems;
@@ -1038,7 +1054,7 @@ __global__ void __launch_bounds__(256) k_gb_chain(DevView v, GBConst k, const fl
 int tile_grid(Context& c) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
-  long long want = (c.ncand + 7) / 8;
+  long long want = (c.tile_cap + 7) / 8;
   long long g = (long long)sms * c.tile_ctas_per_sm;
   return (int)(want < g ? (want > 0 ? want : 1) : g);
 }

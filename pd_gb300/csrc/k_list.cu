@@ -3,7 +3,9 @@
 // (PD src/mmlib/workspace/neighbourlist.cpp:222-439): PD scans all j < i at
 // minimum image; here atoms are binned on a 32^3 grid ordered along a Hilbert
 // curve, grouped into 32-atom blocks, and block pairs whose bounding boxes come
-// within max(cutoffs)+Padding form the tile list.  The bond order PD packs into
+// within max(cutoffs)+Padding form the tile list, found through a grid over the
+// block centres (work and memory follow the tiles, not the square of the block
+// count).  The bond order PD packs into
 // each list entry (neighbourlist.cpp:398-422, 179-220) becomes a per-tile
 // exclusion / 1-4 bit mask.
 #include <cstdio>
@@ -52,11 +54,12 @@ __device__ __forceinline__ int f2ord(float f) {
 }
 __device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
 
-__global__ void k_bbox_init(int* lo, int* hi, int n) {
+__global__ void k_bbox_init(int* lo, int* hi, int* hmax, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
     lo[i] = f2ord(3.0e38f);
     hi[i] = f2ord(-3.0e38f);
+    hmax[i] = f2ord(0.f);
   }
 }
 
@@ -203,8 +206,8 @@ __global__ void k_to_slots(DevView v, const int* atom_sys, const int* tmp, int* 
   slot_of[a] = slot;
 }
 
-// block bounding boxes; one warp per block
-__global__ void k_blocks(DevView v) {
+// block bounding boxes, and each system's largest half-extent; one warp per block
+__global__ void k_blocks(DevView v, int* hmax) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= v.nblocks) return;
@@ -235,6 +238,10 @@ __global__ void k_blocks(DevView v) {
     h.z = (float)(0.5 * (hi[2] - lo[2])) + 1e-4f;
     h.w = 0.f;
     v.half[warp] = h;
+    const int s3 = 3 * v.slot_sys[warp];
+    atomicMax(&hmax[s3], f2ord(h.x));
+    atomicMax(&hmax[s3 + 1], f2ord(h.y));
+    atomicMax(&hmax[s3 + 2], f2ord(h.z));
   }
 }
 
@@ -262,35 +269,25 @@ __global__ void k_slot_params(DevView v, const double* radius, const double* sqe
   if (lc_par) lc_par[s] = l;
 }
 
-// candidate block pairs -> include flags, in candidate order (row-major: bi, then bj >= bi)
-__device__ __forceinline__ bool candidate_pair(const DevView& v, long long t, int& gi, int& gj, int& flags, float R,
-                                               float margin, float full_R, float full_margin) {
-  // system by binary search over cand_start
-  int lo = 0, hi = v.nsys - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (v.sys[mid].cand_start <= t) lo = mid;
-    else hi = mid - 1;
-  }
-  const SystemInfo& S = v.sys[lo];
-  long long l = t - S.cand_start;
-  long long nb = S.nblocks;
-  // row bi starts at bi*nb - bi*(bi-1)/2 and holds nb-bi entries (FP32 estimate,
-  // corrected by the integer tests below)
-  const float q = 2.f * (float)nb + 1.f;
-  float fb = (q - sqrtf(fmaxf(q * q - 8.f * (float)l, 0.f))) * 0.5f;
-  long long bi = (long long)fb;
-  if (bi < 0) bi = 0;
-  if (bi > nb - 1) bi = nb - 1;
-  while (bi > 0 && bi * nb - bi * (bi - 1) / 2 > l) bi--;
-  while (bi + 1 < nb && (bi + 1) * nb - (bi + 1) * bi / 2 <= l) bi++;
-  long long bj = bi + (l - (bi * nb - bi * (bi - 1) / 2));
-  gi = S.block_start + (int)bi;
-  gj = S.block_start + (int)bj;
-  float4 hi4 = v.half[gi], hj4 = v.half[gj];
-  float hs[3] = {hi4.x + hj4.x, hi4.y + hj4.y, hi4.z + hj4.z};
-  // FP32 geometry (the FP64 pipe is narrow on this GPU), every decision taken
-  // 1e-3 A on the safe side: include, per-pair image, not all-inside
+// ---------------------------------------------------------------------------
+// Tile list.  Block pair (bi, bj), bi <= bj of one system, is a tile when the
+// two blocks' bounding boxes come within R (periodic: at the minimum image of
+// their centres).  Each build bins every system's block centres on a grid of
+// at most one cell per block; row bi visits only the cells within
+// R + h_i + hmax of its centre along each axis (h: half-extents, hmax the
+// system's largest), marks its hits in a per-warp bitmap over its columns
+// bj >= bi, and writes them in ascending bj.  The list is row-major with
+// ascending columns whatever order the cells were visited in, so every build
+// from the same positions writes the same list.  A row whose cell range spans
+// the whole grid (all pairs within reach) walks its columns directly.
+// ---------------------------------------------------------------------------
+// box test of one block pair; flags as Tile::flags.  FP32 geometry (the FP64
+// pipe is narrow on this GPU), every decision taken 1e-3 A on the safe side:
+// include, per-pair image, not all-inside
+__device__ __forceinline__ bool tile_test(const DevView& v, const SystemInfo& S, int gi, int gj, float R,
+                                          float margin, float full_R, float full_margin, int& flags) {
+  const float4 hi4 = v.half[gi], hj4 = v.half[gj];
+  const float hs[3] = {hi4.x + hj4.x, hi4.y + hj4.y, hi4.z + hj4.z};
   constexpr float kSafe = 1e-3f;
   float dist2 = 0.f, dmax2 = 0.f;
   bool need_mi = false;
@@ -315,65 +312,264 @@ __device__ __forceinline__ bool candidate_pair(const DevView& v, long long t, in
   return dist2 <= Rs * Rs;
 }
 
-__global__ void k_tile_flags(DevView v, long long ncand, float R, float margin, int* flag) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncand) return;
-  int gi, gj, fl;
-  flag[t] = candidate_pair(v, t, gi, gj, fl, R, margin, 0.f, 0.f) ? 1 : 0;
-}
-
-// write the included pairs at their scanned positions: the tile list is in
-// row-major order, so every run of tiles with one i-block is contiguous and
-// its order is the same on every build
-__global__ void k_tile_write(DevView v, long long ncand, float R, float margin, float full_R, float full_margin,
-                             const int* flag, const int* pos) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncand) return;
-  if (t == ncand - 1) *v.ntiles = pos[t] + flag[t];
-  if (!flag[t]) return;
-  int gi, gj, fl;
-  candidate_pair(v, t, gi, gj, fl, R, margin, full_R, full_margin);
+// the tile record at position t (centre offset formed in FP64, rounded once)
+__device__ __forceinline__ void write_tile(const DevView& v, const SystemInfo& S, int gi, int gj, int flags,
+                                           long long t, long long cap) {
+  if (t >= cap) return;
   Tile T;
   T.bi = gi;
   T.bj = gj;
   T.mask = -1;
-  T.flags = fl;
-  {
-    const SystemInfo& S = v.sys[v.slot_sys[gi]];
-    double o[3];
+  T.flags = flags;
+  double o[3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      o[c] = v.center[3 * gj + c] - v.center[3 * gi + c];
-      if (S.periodic) o[c] -= S.box[c] * rint(o[c] * S.ibox[c]);
-    }
-    T.ox = (float)o[0];
-    T.oy = (float)o[1];
-    T.oz = (float)o[2];
-    T.pad = 0.f;
+  for (int c = 0; c < 3; c++) {
+    o[c] = v.center[3 * gj + c] - v.center[3 * gi + c];
+    if (S.periodic) o[c] -= S.box[c] * rint(o[c] * S.ibox[c]);
   }
-  v.tiles[pos[t]] = T;
+  T.ox = (float)o[0];
+  T.oy = (float)o[1];
+  T.oz = (float)o[2];
+  T.pad = 0.f;
+  v.tiles[t] = T;
+}
+
+// one thread per system: the grid of its block centres for this build
+__global__ void k_grid_setup(DevView v, const int* lo, const int* hi, const int* hmax, BlockGrid* grid) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= v.nsys) return;
+  const SystemInfo& S = v.sys[s];
+  BlockGrid G;
+  double ext[3];
+  for (int c = 0; c < 3; c++) {
+    if (S.periodic) {
+      G.origin[c] = 0.0;
+      ext[c] = S.box[c];
+    } else {
+      const double l = ord2f(lo[3 * s + c]), h = ord2f(hi[3 * s + c]);
+      G.origin[c] = l;
+      ext[c] = fmax(h - l, 1e-3);
+    }
+    G.hmax[c] = ord2f(hmax[3 * s + c]);
+  }
+  // cells of about equal edge, at most grid_cells of them
+  const double edge = cbrt(ext[0] * ext[1] * ext[2] / (double)S.grid_cells);
+  for (int c = 0; c < 3; c++) G.dims[c] = (int)fmax(1.0, fmin(floor(ext[c] / edge), 4096.0));
+  while ((long long)G.dims[0] * G.dims[1] * G.dims[2] > S.grid_cells) {
+    const int m = G.dims[0] >= G.dims[1] ? (G.dims[0] >= G.dims[2] ? 0 : 2) : (G.dims[1] >= G.dims[2] ? 1 : 2);
+    G.dims[m]--;
+  }
+  for (int c = 0; c < 3; c++) G.cell[c] = ext[c] / G.dims[c];
+  G.start = S.grid_start;
+  G.pad = 0.f;
+  grid[s] = G;
+}
+
+// cell coordinate of x along axis c (clamped into the grid)
+__device__ __forceinline__ int grid_axis(const BlockGrid& G, int c, double x) {
+  const double q = floor((x - G.origin[c]) / G.cell[c]);
+  return (int)fmin(fmax(q, 0.0), (double)(G.dims[c] - 1));
+}
+
+__global__ void k_bgrid_count(DevView v, const BlockGrid* grid, int* bcell, int* count) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= v.nblocks) return;
+  const BlockGrid& G = grid[v.slot_sys[b]];
+  const double* x = v.center + 3 * b;
+  const int cell = G.start + (grid_axis(G, 2, x[2]) * G.dims[1] + grid_axis(G, 1, x[1])) * G.dims[0] +
+                   grid_axis(G, 0, x[0]);
+  bcell[b] = cell;
+  atomicAdd(&count[cell], 1);
+}
+
+// blocks in cell order (the order inside a cell does not matter: rows collect
+// their hits in a bitmap)
+__global__ void k_bgrid_scatter(int nblocks, const int* bcell, const int* offset, int* cursor, int* blocks) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nblocks) return;
+  const int cell = bcell[b];
+  blocks[offset[cell] + atomicAdd(&cursor[cell], 1)] = b;
+}
+
+// one warp per row bi, 4 warps per CTA, `words` bitmap words per warp in
+// dynamic shared memory.  COUNT: tiles of the row -> row_cnt.  WRITE: the row's
+// tiles from row_start[bi] (positions past `cap` are dropped; the last row
+// stores the tile count, clamped to cap, and flags an overflow)
+template <bool WRITE>
+__global__ void __launch_bounds__(128) k_tile_rows(DevView v, const BlockGrid* grid, const int* cell_off,
+                                                   const int* cell_count, const int* cell_blocks, float R,
+                                                   float margin, float full_R, float full_margin, int* row_cnt,
+                                                   const int* row_start, long long cap, int words) {
+  extern __shared__ unsigned s_bits[];
+  const int lane = threadIdx.x & 31;
+  const int bi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (bi >= v.nblocks) return;
+  unsigned* bits = s_bits + (threadIdx.x >> 5) * words;
+  const SystemInfo& S = v.sys[v.slot_sys[bi]];
+  const BlockGrid& G = grid[v.slot_sys[bi]];
+  const int end = S.block_start + S.nblocks;
+  const float4 h4 = v.half[bi];
+  const float h[3] = {h4.x, h4.y, h4.z};
+  int lo[3], hi[3];
+  bool all = true;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const double x = v.center[3 * bi + c] - G.origin[c];
+    // reach along the axis: list radius, both half-extents, and a slack far
+    // above the rounding of the centres and cell edges
+    const double r = (double)R + (double)h[c] + (double)G.hmax[c] + 0.01;
+    const int D = G.dims[c];
+    int a = (int)fmax(floor((x - r) / G.cell[c]), -1.0e9);
+    int b = (int)fmin(floor((x + r) / G.cell[c]), 1.0e9);
+    if (S.periodic) {
+      if (b - a + 1 >= D) {
+        a = 0;
+        b = D - 1;
+      } else {
+        all = false;
+      }
+    } else {
+      a = max(a, 0);
+      b = min(b, D - 1);
+      if (a > 0 || b < D - 1) all = false;
+    }
+    lo[c] = a;
+    hi[c] = b;
+  }
+  const unsigned lt = (1u << lane) - 1u;
+  long long n = 0;   // tiles of the row so far
+  const long long base = WRITE ? (long long)row_start[bi] : 0;
+  if (all) {
+#pragma unroll 2
+    for (int j0 = bi; j0 < end; j0 += 32) {
+      const int bj = j0 + lane;
+      int fl = 0;
+      const bool hit = bj < end && tile_test(v, S, bi, bj, R, margin, full_R, full_margin, fl);
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (WRITE && hit) write_tile(v, S, bi, bj, fl, base + n + __popc(m & lt), cap);
+      n += __popc(m);
+    }
+  } else {
+    const int nw = (end - bi + 31) >> 5;
+    for (int w = lane; w < nw; w += 32) bits[w] = 0u;
+    __syncwarp();
+    // the cell runs to visit: one per (y, z) cell row of the range, two where
+    // a periodic x range wraps.  Each lane reads one run's block range, then
+    // the warp deals the runs' blocks over its lanes (the reads of a row are
+    // independent of one another, not a chain of dependent loads)
+    const int Dx = G.dims[0], Dy = G.dims[1], Dz = G.dims[2];
+    const int nyr = hi[1] - lo[1] + 1, nzr = hi[2] - lo[2] + 1;
+    const bool wrapx = lo[0] < 0 || hi[0] >= Dx;
+    const int nxr = wrapx ? 2 : 1;
+    const int nrun = nyr * nzr * nxr;
+    for (int q0 = 0; q0 < nrun; q0 += 32) {
+      const int q = q0 + lane;
+      int p0 = 0, len = 0;
+      if (q < nrun) {
+        const int xr = q % nxr, yz = q / nxr;
+        const int cy = ((lo[1] + yz % nyr) % Dy + Dy) % Dy, cz = ((lo[2] + yz / nyr) % Dz + Dz) % Dz;
+        const int row0 = G.start + (cz * Dy + cy) * Dx;
+        int c0 = lo[0], c1 = hi[0];
+        if (lo[0] < 0) {
+          c0 = xr ? 0 : lo[0] + Dx;
+          c1 = xr ? hi[0] : Dx - 1;
+        } else if (hi[0] >= Dx) {
+          c0 = xr ? 0 : lo[0];
+          c1 = xr ? hi[0] - Dx : Dx - 1;
+        }
+        p0 = cell_off[row0 + c0];
+        len = cell_off[row0 + c1] + cell_count[row0 + c1] - p0;
+      }
+      int inc = len;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+      }
+      const int total = __shfl_sync(0xffffffffu, inc, 31);
+      const int excl = inc - len;
+      for (int t0 = 0; t0 < total; t0 += 32) {
+        const int t = t0 + lane;
+        // the run holding entry t: the last lane whose runs start at or before t
+        int L = 0;
+#pragma unroll
+        for (int b = 16; b > 0; b >>= 1)
+          if (__shfl_sync(0xffffffffu, excl, L + b) <= t) L += b;
+        const int p = __shfl_sync(0xffffffffu, p0, L) + t - __shfl_sync(0xffffffffu, excl, L);
+        if (t < total) {
+          const int bj = cell_blocks[p];
+          int fl;
+          if (bj >= bi && tile_test(v, S, bi, bj, R, margin, 0.f, 0.f, fl))
+            atomicOr(&bits[(bj - bi) >> 5], 1u << ((bj - bi) & 31));
+        }
+      }
+    }
+    __syncwarp();
+    for (int w0 = 0; w0 < nw; w0 += 32) {
+      const int w = w0 + lane;
+      unsigned word = w < nw ? bits[w] : 0u;
+      const int k = __popc(word);
+      int inc = k;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+      }
+      if (WRITE) {
+        long long t = base + n + inc - k;
+        while (word) {
+          const int bit = __ffs(word) - 1;
+          word &= word - 1u;
+          const int bj = bi + 32 * w + bit;
+          int fl = 0;
+          tile_test(v, S, bi, bj, R, margin, full_R, full_margin, fl);
+          write_tile(v, S, bi, bj, fl, t++, cap);
+        }
+      }
+      n += __shfl_sync(0xffffffffu, inc, 31);
+    }
+  }
+  if (lane == 0) {
+    if (!WRITE) {
+      row_cnt[bi] = (int)n;
+    } else if (bi == v.nblocks - 1) {
+      const long long total = base + n;
+      *v.ntiles = (int)(total < cap ? total : cap);
+      if (total > cap) atomicOr(v.status, (unsigned)ST_TILE_OVERFLOW);
+    }
+  }
+}
+
+// index of tile (bi, bj) in the list (rows contiguous, ascending columns), -1 if absent
+__device__ __forceinline__ int tile_index(const DevView& v, const int* row_start, const int* row_cnt, int bi, int bj) {
+  const int nt = *v.ntiles;
+  int lo = row_start[bi], hi = min(lo + row_cnt[bi], nt) - 1;
+  while (lo <= hi) {
+    const int mid = (lo + hi) >> 1;
+    const int c = v.tiles[mid].bj;
+    if (c == bj) return mid;
+    if (c < bj) lo = mid + 1;
+    else hi = mid - 1;
+  }
+  return -1;
 }
 
 // exclusion masks in rotation order (bit k <-> j slot (lane+k)&31); one warp per tile
 // tiles holding a bonded pair (bond order <= 3: excluded or 1-4), marked from
-// each atom's partners (band words, far list) through the candidate index of its
-// block pair: need[tile] = 1.  flag / pos: the tile-compaction scan (candidate ->
-// tile).  Diagonal tiles and tiles with padding slots are recognised in k_masks.
-__global__ void k_mask_mark(DevView v, const int* slot_of, const int* flag, const int* pos, unsigned char* need) {
+// each atom's partners (band words, far list): need[tile] = 1.  Diagonal tiles
+// and tiles with padding slots are recognised in k_masks.
+__global__ void k_mask_mark(DevView v, const int* slot_of, const int* row_start, const int* row_cnt,
+                            unsigned char* need) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= v.natom) return;
   const unsigned long long w = v.band_excl[a] | v.band_14[a];
   const int fs = v.far_start[a], fe = v.far_start[a + 1];
   if (!w && fs == fe) return;
-  const int sa = slot_of[a];
-  const int ga = sa >> 5;
-  const SystemInfo& S = v.sys[v.slot_sys[ga]];
+  const int ga = slot_of[a] >> 5;
   auto mark = [&](int b) {
     const int gb = slot_of[b] >> 5;
-    const long long bi = (ga < gb ? ga : gb) - S.block_start, bj = (ga < gb ? gb : ga) - S.block_start;
-    const long long nb = S.nblocks;
-    const long long l = S.cand_start + bi * nb - bi * (bi - 1) / 2 + (bj - bi);
-    if (flag[l]) need[pos[l]] = 1;
+    const int t = tile_index(v, row_start, row_cnt, ga < gb ? ga : gb, ga < gb ? gb : ga);
+    if (t >= 0) need[t] = 1;
   };
   for (unsigned long long m = w; m; m &= m - 1) mark(a + __ffsll((long long)m));
   for (int q = fs; q < fe; q++)
@@ -440,6 +636,11 @@ __global__ void k_masks(DevView v, const unsigned char* need) {
     int idx = 0;
     if (lane == 0) idx = atomicAdd(v.nmasks, 1);
     idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= v.mask_cap) {
+      // (the capacity bounds the diagonal, padded and bonded tiles: not reached)
+      if (lane == 0) atomicOr(v.status, (unsigned)ST_TILE_OVERFLOW);
+      continue;
+    }
     v.masks[idx * 32 + lane] = make_uint2(ex, m14);
     if (lane == 0) v.tiles[warp].mask = idx;
   }
@@ -449,8 +650,8 @@ __global__ void k_masks(DevView v, const unsigned char* need) {
 // check2: squared skin limit (0 = no skin check); full2: squared limit that keeps
 // tiles flagged full valid (0 = none flagged), checked where the skin check is not
 // cull: the NB j-atom groups are in use (the displacement check always runs)
-__global__ void k_pack(DevView v, const double* charge, float check2, float full2, int store_ref, long long ncand,
-                       int cull) {
+__global__ void k_pack(DevView v, const double* charge, float check2, float full2, int store_ref,
+                       long long npairs_all, int cull) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= v.nslots) return;
   int a = v.sorted_atom[s];
@@ -474,7 +675,7 @@ __global__ void k_pack(DevView v, const double* charge, float check2, float full
     } else {
       // (in open space, when every block pair of every system is a tile, no pair
       // can leave the list; in a periodic box the tile images still depend on it)
-      const bool skin = check2 > 0.f && (S.periodic || (long long)*v.ntiles < ncand || cull);
+      const bool skin = check2 > 0.f && (S.periodic || (long long)*v.ntiles < npairs_all || cull);
       const float lim = skin ? check2 : full2;
       if (lim > 0.f) {
         float4 q = v.rel0[s];
@@ -498,17 +699,17 @@ __device__ __forceinline__ bool tile_pairable(const DevView& v, int t, int nt) {
 }
 
 // pairs: 0 makes every item a single tile
-__global__ void k_item_flags(DevView v, long long ncand, int pairs, int* flag) {
+__global__ void k_item_flags(DevView v, long long cap, int pairs, int* flag) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncand) return;
+  if (t >= cap) return;
   const int nt = *v.ntiles;
   flag[t] = (t < nt && !(pairs && tile_pairable(v, (int)t - 1, nt))) ? 1 : 0;
 }
 
-__global__ void k_item_write(DevView v, long long ncand, int pairs, const int* flag, const int* pos) {
+__global__ void k_item_write(DevView v, long long cap, int pairs, const int* flag, const int* pos) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncand) return;
-  if (t == ncand - 1) *v.nitems = pos[t] + flag[t];
+  if (t >= cap) return;
+  if (t == cap - 1) *v.nitems = pos[t] + flag[t];
   if (!flag[t]) return;
   v.items[pos[t]] = (unsigned)t | ((pairs && tile_pairable(v, (int)t, *v.ntiles)) ? 0x80000000u : 0u);
 }
@@ -525,7 +726,7 @@ __global__ void k_item_write(DevView v, long long ncand, int pairs, const int* f
 // row: [0, nb) kept j atoms, [nb, 2nb) first tile, [2nb, 3nb) groups,
 // [3nb, 4nb) first group (exclusive scan).
 // ---------------------------------------------------------------------------
-// cnt: zeroed beforehand over all candidates (the scan runs over them)
+// cnt: zeroed beforehand over the tile capacity (the scan runs over it)
 __global__ void k_cull_mask(DevView v, float R2, unsigned* jmask, int* cnt, int* row) {
   const int lane = threadIdx.x & 31;
   const int nt = *v.ntiles;
@@ -603,8 +804,16 @@ static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 static int list_tile_grid(const Context& c) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
-  const long long want = (c.ncand + 7) / 8, g = 16LL * (sms > 0 ? sms : 1);
+  const long long want = (c.tile_cap + 7) / 8, g = 16LL * (sms > 0 ? sms : 1);
   return (int)(want < g ? (want > 0 ? want : 1) : g);
+}
+
+// exclusive scan of n ints (n <= 2^20) with the three-kernel scan
+static void scan_ints(const int* in, int* out, int* tmp, long long n, cudaStream_t st) {
+  const int nb = nblk(n, 1024);
+  k_scan_block<<<nb, 1024, 0, st>>>(in, out, tmp, (int)n);
+  k_scan_sums<<<1, 1024, 0, st>>>(tmp, nb);
+  k_scan_add<<<nb, 1024, 0, st>>>(out, tmp, (int)n);
 }
 
 static void launch_cull(Context& c, float list_radius) {
@@ -617,74 +826,99 @@ static void launch_cull(Context& c, float list_radius) {
   cudaMemsetAsync(row + nb, 0x7f, sizeof(int) * nb, st);
   const float R = list_radius + 1e-3f;
   // the kept counts and their scan reuse the tile-compaction arrays
-  cudaMemsetAsync(c.d_tile_flag.p, 0, sizeof(int) * c.ncand, st);
+  cudaMemsetAsync(c.d_tile_flag.p, 0, sizeof(int) * c.tile_cap, st);
   k_cull_mask<<<list_tile_grid(c), 256, 0, st>>>(v, R * R, c.d_cull_mask.p, c.d_tile_flag.p, row);
-  const int nb2 = nblk(c.ncand, 1024);
-  k_scan_block<<<nb2, 1024, 0, st>>>(c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
-  k_scan_sums<<<1, 1024, 0, st>>>(c.d_scan_tmp2.p, nb2);
-  k_scan_add<<<nb2, 1024, 0, st>>>(c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
+  scan_ints(c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, c.tile_cap, st);
   k_cull_groups<<<nblk(nb, 256), 256, 0, st>>>(nb, row);
-  const int nb3 = nblk(nb, 1024);
-  k_scan_block<<<nb3, 1024, 0, st>>>(row + 2 * nb, row + 3 * nb, c.d_cull_scan_tmp.p, nb);
-  k_scan_sums<<<1, 1024, 0, st>>>(c.d_cull_scan_tmp.p, nb3);
-  k_scan_add<<<nb3, 1024, 0, st>>>(row + 3 * nb, c.d_cull_scan_tmp.p, nb);
+  scan_ints(row + 2 * nb, row + 3 * nb, c.d_cull_scan_tmp.p, nb, st);
   k_cull_write<<<list_tile_grid(c), 256, 0, st>>>(v, c.d_cull_mask.p, c.d_tile_pos.p, row);
   k_cull_rows<<<nblk((long long)nb * 32, 256), 256, 0, st>>>(v, row);
 }
 
-int launch_list_build(Context& c, float list_radius, float full_radius) {
-  c.kernel_launches += 19;
+// rows of the tile-list build: 4 warps per CTA, a bitmap over each warp's row
+static void launch_rows(Context& c, bool write, float R, float full_radius) {
+  const int words = (c.max_sys_blocks + 31) / 32 + 1;
+  const size_t smem = (size_t)4 * words * sizeof(unsigned);
+  DevView v = c.view();
+  const int g = nblk((long long)c.nblocks * 32, 128);
+  const float pad = (float)c.lp.Padding;
+  if (write)
+    k_tile_rows<true><<<g, 128, smem, c.stream>>>(v, c.d_bgrid.p, c.d_bcell_off.p, c.d_bcell_count.p,
+                                                   c.d_bcell_blocks.p, R, pad, full_radius, c.full_margin(),
+                                                   c.d_row_cnt.p, c.d_row_start.p, c.tile_cap, words);
+  else
+    k_tile_rows<false><<<g, 128, smem, c.stream>>>(v, c.d_bgrid.p, c.d_bcell_off.p, c.d_bcell_count.p,
+                                                    c.d_bcell_blocks.p, R, pad, 0.f, 0.f, c.d_row_cnt.p,
+                                                    c.d_row_start.p, c.tile_cap, words);
+}
+
+int launch_list_build(Context& c, float list_radius, float full_radius, ListSizing sizing) {
+  c.kernel_launches += 25;
   DevView v = c.view();
   cudaStream_t st = c.stream;
   int ncells = c.nsys * kCellsPerSystem;
   int* lo = reinterpret_cast<int*>(c.d_sys_lo.p);
   int* hi = reinterpret_cast<int*>(c.d_sys_hi.p);
-  k_bbox_init<<<nblk(3 * c.nsys, 128), 128, 0, st>>>(lo, hi, 3 * c.nsys);
+  int* hmax = reinterpret_cast<int*>(c.d_sys_hmax.p);
+  k_bbox_init<<<nblk(3 * c.nsys, 128), 128, 0, st>>>(lo, hi, hmax, 3 * c.nsys);
   k_bbox<<<nblk(c.natom, 256), 256, 0, st>>>(v, c.d_atom_sys.p, lo, hi);
   cudaMemsetAsync(c.d_count.p, 0, sizeof(int) * ncells, st);
   cudaMemsetAsync(c.d_cursor.p, 0, sizeof(int) * ncells, st);
   k_keys<<<nblk(c.natom, 256), 256, 0, st>>>(v, c.d_atom_sys.p, lo, hi, c.d_bucket.p, c.d_count.p);
-  int nsb = nblk(ncells, 1024);
-  k_scan_block<<<nsb, 1024, 0, st>>>(c.d_count.p, c.d_offset.p, c.d_scan_tmp.p, ncells);
-  k_scan_sums<<<1, 1024, 0, st>>>(c.d_scan_tmp.p, nsb);
-  k_scan_add<<<nsb, 1024, 0, st>>>(c.d_offset.p, c.d_scan_tmp.p, ncells);
+  scan_ints(c.d_count.p, c.d_offset.p, c.d_scan_tmp.p, ncells, st);
   k_scatter<<<nblk(c.natom, 256), 256, 0, st>>>(c.natom, c.d_bucket.p, c.d_offset.p, c.d_cursor.p,
                                                  c.d_tmp_sorted.p);
   k_cell_sort<<<nblk(ncells, 256), 256, 0, st>>>(ncells, c.d_offset.p, c.d_count.p, c.d_tmp_sorted.p);
   cudaMemsetAsync(c.d_sorted_atom.p, 0xff, sizeof(int) * c.nslots, st);
   k_to_slots<<<nblk(c.natom, 256), 256, 0, st>>>(v, c.d_atom_sys.p, c.d_tmp_sorted.p, c.d_sorted_atom.p,
                                                   c.d_slot_of.p);
-  k_blocks<<<nblk((long long)c.nblocks * 32, 256), 256, 0, st>>>(v);
+  k_blocks<<<nblk((long long)c.nblocks * 32, 256), 256, 0, st>>>(v, hmax);
   k_slot_params<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_radius.p, c.d_sqeps.p, c.has_gb ? c.d_gbR.p : nullptr,
                                                       c.has_gb ? c.d_gbVj.p : nullptr,
                                                       c.has_sa ? c.d_lcpoR.p : nullptr,
                                                       c.has_sa ? c.d_lcpoUse.p : nullptr,
                                                       c.has_sa ? c.d_lc_par.p : nullptr);
-  cudaMemsetAsync(c.d_counters.p, 0, sizeof(int) * 6, st);
-  k_tile_flags<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, list_radius, (float)c.lp.Padding, c.d_tile_flag.p);
-  {
-    int nb2 = nblk(c.ncand, 1024);
-    k_scan_block<<<nb2, 1024, 0, st>>>(c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
-    k_scan_sums<<<1, 1024, 0, st>>>(c.d_scan_tmp2.p, nb2);
-    k_scan_add<<<nb2, 1024, 0, st>>>(c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
+  // block grid and the row counts of the tile list
+  k_grid_setup<<<nblk(c.nsys, 64), 64, 0, st>>>(v, lo, hi, hmax, c.d_bgrid.p);
+  cudaMemsetAsync(c.d_bcell_count.p, 0, sizeof(int) * c.nblocks, st);
+  cudaMemsetAsync(c.d_bcell_cursor.p, 0, sizeof(int) * c.nblocks, st);
+  k_bgrid_count<<<nblk(c.nblocks, 256), 256, 0, st>>>(v, c.d_bgrid.p, c.d_bcell.p, c.d_bcell_count.p);
+  scan_ints(c.d_bcell_count.p, c.d_bcell_off.p, c.d_bcell_scan_tmp.p, c.nblocks, st);
+  k_bgrid_scatter<<<nblk(c.nblocks, 256), 256, 0, st>>>(c.nblocks, c.d_bcell.p, c.d_bcell_off.p,
+                                                         c.d_bcell_cursor.p, c.d_bcell_blocks.p);
+  launch_rows(c, false, list_radius, full_radius);
+  scan_ints(c.d_row_cnt.p, c.d_row_start.p, c.d_row_scan_tmp.p, c.nblocks, st);
+  if (sizing != kListDevice) {
+    // the tile count (last row's start + count) against the capacity
+    int last[2] = {0, 0};
+    if (cudaMemcpyAsync(&last[0], c.d_row_start.p + c.nblocks - 1, sizeof(int), cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(&last[1], c.d_row_cnt.p + c.nblocks - 1, sizeof(int), cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return PDGPU_ERR_CUDA;
+    const long long total = (long long)last[0] + last[1];
+    if (total > c.tile_cap) {
+      if (sizing == kListCheck) return PDGPU_ERR_CAPACITY;
+      const int e = alloc_tiles(c, total);
+      if (e != PDGPU_OK) return e;
+      v = c.view();
+    }
   }
-  k_tile_write<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, list_radius, (float)c.lp.Padding, full_radius,
-                                                    c.full_margin(), c.d_tile_flag.p, c.d_tile_pos.p);
-  cudaMemsetAsync(c.d_tile_need.p, 0, c.ncand, st);
-  k_mask_mark<<<nblk(c.natom, 256), 256, 0, st>>>(v, c.d_slot_of.p, c.d_tile_flag.p, c.d_tile_pos.p,
+  cudaMemsetAsync(c.d_counters.p, 0, sizeof(int) * 6, st);
+  launch_rows(c, true, list_radius, full_radius);
+  cudaMemsetAsync(c.d_tile_need.p, 0, c.tile_cap, st);
+  k_mask_mark<<<nblk(c.natom, 256), 256, 0, st>>>(v, c.d_slot_of.p, c.d_row_start.p, c.d_row_cnt.p,
                                                    c.d_tile_need.p);
   k_masks<<<list_tile_grid(c), 256, 0, st>>>(v, c.d_tile_need.p);
   if (c.has_gb) {
     c.kernel_launches += 5;
-    int nb2 = nblk(c.ncand, 1024);
     const int pairs = c.gb_item_tiles == 2 ? 1 : 0;
-    k_item_flags<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, pairs, c.d_tile_flag.p);
-    k_scan_block<<<nb2, 1024, 0, st>>>(c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
-    k_scan_sums<<<1, 1024, 0, st>>>(c.d_scan_tmp2.p, nb2);
-    k_scan_add<<<nb2, 1024, 0, st>>>(c.d_tile_pos.p, c.d_scan_tmp2.p, (int)c.ncand);
-    k_item_write<<<nblk(c.ncand, 256), 256, 0, st>>>(v, c.ncand, pairs, c.d_tile_flag.p, c.d_tile_pos.p);
+    k_item_flags<<<nblk(c.tile_cap, 256), 256, 0, st>>>(v, c.tile_cap, pairs, c.d_tile_flag.p);
+    scan_ints(c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, c.tile_cap, st);
+    k_item_write<<<nblk(c.tile_cap, 256), 256, 0, st>>>(v, c.tile_cap, pairs, c.d_tile_flag.p, c.d_tile_pos.p);
   }
-  k_pack<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_charge.p, 0.f, 0.f, 1, c.ncand, 0);
+  k_pack<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_charge.p, 0.f, 0.f, 1, c.npairs_all, 0);
   // NB j-atom groups: only where the per-step displacement check runs
   c.cull_built = c.nb_set && c.nb_cull && c.lp.check_skin && c.cull_cap > 0;
   if (c.cull_built) launch_cull(c, list_radius);
@@ -712,7 +946,8 @@ int launch_pack(Context& c, float check_disp) {
     const float h = 0.5f * c.full_margin();
     f2 = h * h;
   }
-  k_pack<<<nblk(c.nslots, 256), 256, 0, c.stream>>>(v, c.d_charge.p, c2, f2, 0, c.ncand, c.cull_built ? 1 : 0);
+  k_pack<<<nblk(c.nslots, 256), 256, 0, c.stream>>>(v, c.d_charge.p, c2, f2, 0, c.npairs_all,
+                                                     c.cull_built ? 1 : 0);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

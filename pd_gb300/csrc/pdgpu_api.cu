@@ -86,7 +86,7 @@ int read_status(Context& c) {
   if (e != cudaSuccess) return cuda_status(e, &c, "status");
   if (st & ST_NAN) return PDGPU_ERR_NAN;
   if (st & ST_FIXED_OVERFLOW) return PDGPU_ERR_FIXED_OVERFLOW;
-  if (st & ST_LCPO_OVERFLOW) return PDGPU_ERR_LIST_OVERFLOW;
+  if (st & (ST_LCPO_OVERFLOW | ST_TILE_OVERFLOW)) return PDGPU_ERR_LIST_OVERFLOW;
   if (st & ST_STALE_LIST) return PDGPU_ERR_STALE_LIST;
   return PDGPU_OK;
 }
@@ -233,7 +233,7 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
   // systems and padded layout
   c.nsys = d->nsystems;
   int atom = 0, slot = 0, block = 0;
-  long long cand = 0;
+  long long pairs = 0;
   c.any_periodic = false;
   c.all_periodic = true;
   for (int s = 0; s < c.nsys; s++) {
@@ -245,7 +245,9 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
     S.npad = (S.natom + 31) / 32 * 32;
     S.block_start = block;
     S.nblocks = S.npad / 32;
-    S.cand_start = cand;
+    S.grid_start = block;   // one grid cell per block
+    S.grid_cells = S.nblocks;
+    if (S.nblocks > kMaxSystemBlocks) return bad(PDGPU_ERR_CAPACITY);
     int per = 0;
     for (int k = 0; k < 3; k++) {
       S.box[k] = d->box[3 * s + k];
@@ -260,12 +262,15 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
     atom += S.natom;
     slot += S.npad;
     block += S.nblocks;
-    cand += (long long)S.nblocks * (S.nblocks + 1) / 2;
+    pairs += (long long)S.nblocks * (S.nblocks + 1) / 2;
+    c.max_sys_blocks = std::max(c.max_sys_blocks, S.nblocks);
   }
   c.natom = atom;
   c.nslots = slot;
   c.nblocks = block;
-  c.ncand = cand;
+  c.npairs_all = pairs;
+  // the list build counts tiles in 32-bit integers
+  if (pairs > 2147483647LL) return bad(PDGPU_ERR_CAPACITY);
   const int N = c.natom;
 
   c.h_atom_sys.resize(N);
@@ -303,6 +308,17 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
       fidx.push_back(p.first);
       fbo.push_back(p.second);
     }
+  }
+  // exclusion-mask table: a tile gets a mask only when it is diagonal, holds a
+  // padding slot (the last block of a system) or a bonded pair, so this bounds
+  // the masks of any list
+  {
+    long long bonded = (long long)fidx.size();
+    for (int a = 0; a < N; a++) bonded += __builtin_popcountll(bex[a] | b14[a]);
+    long long cap = c.nblocks + bonded;
+    for (const SystemInfo& S : c.sys)
+      if (S.natom != S.npad) cap += S.nblocks;
+    c.mask_cap = (int)std::min(std::min(cap, c.npairs_all), 2147483647LL / 32);
   }
   if (fidx.empty()) {
     fidx.push_back(-1);
@@ -416,18 +432,25 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
   if (e == cudaSuccess) e = c.d_tmp_sorted.alloc(N);
   if (e == cudaSuccess) e = c.d_sys_lo.alloc(3 * (size_t)c.nsys);
   if (e == cudaSuccess) e = c.d_sys_hi.alloc(3 * (size_t)c.nsys);
+  if (e == cudaSuccess) e = c.d_sys_hmax.alloc(3 * (size_t)c.nsys);
+  if (e == cudaSuccess) e = c.d_bgrid.alloc(c.nsys);
+  if (e == cudaSuccess) e = c.d_bcell.alloc(c.nblocks);
+  if (e == cudaSuccess) e = c.d_bcell_count.alloc(c.nblocks);
+  if (e == cudaSuccess) e = c.d_bcell_off.alloc(c.nblocks);
+  if (e == cudaSuccess) e = c.d_bcell_cursor.alloc(c.nblocks);
+  if (e == cudaSuccess) e = c.d_bcell_scan_tmp.alloc((c.nblocks + 1023) / 1024 + 1);
+  if (e == cudaSuccess) e = c.d_bcell_blocks.alloc(c.nblocks);
+  if (e == cudaSuccess) e = c.d_row_cnt.alloc(c.nblocks);
+  if (e == cudaSuccess) e = c.d_row_start.alloc(c.nblocks);
+  if (e == cudaSuccess) e = c.d_row_scan_tmp.alloc((c.nblocks + 1023) / 1024 + 1);
   if (e == cudaSuccess) e = c.d_sorted_atom.alloc(c.nslots);
   if (e == cudaSuccess) e = c.d_slot_of.alloc(N);
   if (e == cudaSuccess) e = c.d_center.alloc(3 * (size_t)c.nblocks);
   if (e == cudaSuccess) e = c.d_half.alloc(c.nblocks);
-  if (e == cudaSuccess) e = c.d_tiles.alloc(c.ncand);
+  // (the tile arrays are sized by the first list build, from its tile count)
   if (e == cudaSuccess) e = c.d_counters.alloc(6);
-  if (e == cudaSuccess && c.has_gb) e = c.d_items.alloc(c.ncand);
-  if (e == cudaSuccess) e = c.d_tile_flag.alloc(c.ncand);
-  if (e == cudaSuccess) e = c.d_tile_pos.alloc(c.ncand);
-  if (e == cudaSuccess) e = c.d_tile_need.alloc(c.ncand);
-  if (e == cudaSuccess) e = c.d_scan_tmp2.alloc((c.ncand + 1023) / 1024 + 1);
-  if (e == cudaSuccess) e = c.d_masks.alloc((size_t)c.ncand * 32);
+  if (e == cudaSuccess) e = cudaMemset(c.d_counters.p, 0, sizeof(int) * 6);
+  if (e == cudaSuccess) e = c.d_masks.alloc((size_t)c.mask_cap * 32);
   if (e == cudaSuccess) e = c.d_xq.alloc(c.nslots);
   if (e == cudaSuccess) e = c.d_par.alloc(c.nslots);
   if (e == cudaSuccess) e = c.d_rel0.alloc(c.nslots);
@@ -489,24 +512,43 @@ int pdgpu_destroy(pdgpu_ctx* h) {
 
 }  // extern "C"
 
-// NB j-atom group buffers, made with the NB parameters (never inside a stream
-// capture): at most 32 entries per candidate tile plus one open group per row,
-// held to 8192 entries per row (a list that needs more keeps the tile path)
+// the first positions of a context with its parameters set build the list,
+// which sizes the tile arrays (later builds reuse them, growing only when the
+// tile count outgrows them), so that calls which may not allocate find them
+static int size_list(Context& c) {
+  if (c.tile_cap > 0 || (!c.nb_set && !c.gb_set && !c.has_sa)) return PDGPU_OK;
+  return rebuild_list_impl(c);
+}
+
+// NB j-atom group buffers: the per-row arrays with the NB parameters (never
+// inside a stream capture), the per-tile ones with the tile arrays
 static int alloc_cull(Context& c) {
-  if (c.cull_cap > 0 || c.ncand == 0) return PDGPU_OK;
-  const long long cap = std::min(32LL * c.ncand + 32LL * c.nblocks, 8192LL * c.nblocks);
+  if (c.d_cull_row.p) return PDGPU_OK;
   cudaError_t e = cudaSetDevice(c.device);
-  if (e == cudaSuccess) e = c.d_cull_mask.alloc(c.ncand);
-  if (e == cudaSuccess) e = c.d_cull_rest.alloc(c.ncand);
   if (e == cudaSuccess) e = c.d_cull_row.alloc(4 * (size_t)c.nblocks);
   if (e == cudaSuccess) e = c.d_cull_scan_tmp.alloc((c.nblocks + 1023) / 1024 + 1);
+  if (e != cudaSuccess) {
+    c.d_cull_row.release();
+    c.d_cull_scan_tmp.release();
+    cudaGetLastError();
+    return PDGPU_ERR_CUDA;
+  }
+  return c.tile_cap > 0 ? alloc_cull_tiles(c) : PDGPU_OK;
+}
+
+// at most 32 entries per tile plus one open group per row, held to 8192
+// entries per row (a list that needs more keeps the tile path)
+int pdgpu::alloc_cull_tiles(Context& c) {
+  c.cull_cap = 0;
+  if (!c.d_cull_row.p || c.tile_cap == 0) return PDGPU_OK;
+  const long long cap = std::min(32LL * c.tile_cap + 32LL * c.nblocks, 8192LL * c.nblocks);
+  cudaError_t e = c.d_cull_mask.alloc(c.tile_cap);
+  if (e == cudaSuccess) e = c.d_cull_rest.alloc(c.tile_cap);
   if (e == cudaSuccess) e = c.d_cull_ent.alloc(cap);
   if (e == cudaSuccess) e = c.d_cull_bi.alloc(cap / 32);
   if (e != cudaSuccess) {
     c.d_cull_mask.release();
     c.d_cull_rest.release();
-    c.d_cull_row.release();
-    c.d_cull_scan_tmp.release();
     c.d_cull_ent.release();
     c.d_cull_bi.release();
     cudaGetLastError();
@@ -514,6 +556,28 @@ static int alloc_cull(Context& c) {
   }
   c.cull_cap = cap;
   return PDGPU_OK;
+}
+
+// the tile list and everything sized by it, for `tiles` tiles with a quarter
+// of headroom (never more than every block pair); captured step graphs hold the
+// old addresses and are dropped
+int pdgpu::alloc_tiles(Context& c, long long tiles) {
+  const long long cap = std::min(c.npairs_all, std::max(tiles + tiles / 4 + 256, 1LL));
+  drop_step_graphs(c);
+  c.tile_cap = 0;
+  c.cull_cap = 0;
+  cudaError_t e = c.d_tiles.alloc(cap);
+  if (e == cudaSuccess && c.has_gb) e = c.d_items.alloc(cap);
+  if (e == cudaSuccess) e = c.d_tile_flag.alloc(cap);
+  if (e == cudaSuccess) e = c.d_tile_pos.alloc(cap);
+  if (e == cudaSuccess) e = c.d_tile_need.alloc(cap);
+  if (e == cudaSuccess) e = c.d_scan_tmp2.alloc((cap + 1023) / 1024 + 1);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return PDGPU_ERR_CUDA;
+  }
+  c.tile_cap = cap;
+  return alloc_cull_tiles(c);
 }
 
 extern "C" {
@@ -718,7 +782,9 @@ int pdgpu_param_grad_device_noalloc(pdgpu_ctx* h, unsigned what, const pdgpu_par
   if (st != PDGPU_OK) return st;
   if (c.nslots > kNoAllocMaxSlots) return PDGPU_ERR_CAPACITY;
   CK(cudaSetDevice(c.device));
+  c.no_alloc = true;
   st = enqueue_grad_energies(c, what);
+  c.no_alloc = false;
   if (st != PDGPU_OK) return st;
   return launch_adjoint_static(c, what, g->charge, g->radius, g->epsilon, g->gb_radius, g->gb_vj, g->gb_terms123);
 }
@@ -753,7 +819,7 @@ int pdgpu_set_positions(pdgpu_ctx* h, const double* xyz, size_t stride) {
   CK(copy_xyz_rows(c.d_pos.p, 24, xyz, stride, c.natom, cudaMemcpyHostToDevice, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   c.positions_set = true;
-  return PDGPU_OK;
+  return size_list(c);
 }
 
 int pdgpu_set_positions_device(pdgpu_ctx* h, const double* d_xyz) {
@@ -762,7 +828,7 @@ int pdgpu_set_positions_device(pdgpu_ctx* h, const double* d_xyz) {
   CK(cudaSetDevice(c.device));
   CK(cudaMemcpyAsync(c.d_pos.p, d_xyz, 24 * (size_t)c.natom, cudaMemcpyDeviceToDevice, c.stream));
   c.positions_set = true;
-  return PDGPU_OK;
+  return size_list(c);
 }
 
 int pdgpu_get_positions(pdgpu_ctx* h, double* xyz, size_t stride) {
@@ -782,7 +848,13 @@ int pdgpu::rebuild_list_impl(Context& c) {
   CK(cudaSetDevice(c.device));
   float R = (float)list_radius(c);
   float F = (float)std::min(full_radius(c), (double)R);
-  int st = launch_list_build(c, R, F);
+  // a captured step cannot read the tile count back; the allocation-free
+  // entry point may not resize
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(c.stream, &cs));
+  const ListSizing sizing =
+      cs != cudaStreamCaptureStatusNone ? kListDevice : (c.no_alloc ? kListCheck : kListReadback);
+  int st = launch_list_build(c, R, F, sizing);
   if (st != PDGPU_OK) return st;
   c.list_radius_built = R;
   c.full_radius_built = F;
@@ -970,6 +1042,48 @@ int pdgpu_list_stats(pdgpu_ctx* h, long long* ntiles, long long* nmasked, long l
   if (ntiles) *ntiles = cnt[0];
   if (nmasked) *nmasked = cnt[1];
   if (nslots) *nslots = c.nslots;
+  return PDGPU_OK;
+}
+
+int pdgpu_list_tiles(pdgpu_ctx* h, int* tiles, long long cap, long long* ntiles, long long* tile_cap,
+                     long long* list_bytes) {
+  if (!h || (cap > 0 && !tiles) || cap < 0) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.list_built) return PDGPU_ERR_STATE;
+  CK(cudaSetDevice(c.device));
+  int nt = 0;
+  CK(cudaMemcpyAsync(&nt, c.d_counters.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  const long long n = std::min<long long>(nt, cap);
+  if (n > 0) {
+    std::vector<Tile> t(n);
+    CK(cudaMemcpyAsync(t.data(), c.d_tiles.p, sizeof(Tile) * n, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    for (long long k = 0; k < n; k++) {
+      tiles[3 * k] = t[k].bi;
+      tiles[3 * k + 1] = t[k].bj;
+      tiles[3 * k + 2] = t[k].flags;
+    }
+  }
+  if (ntiles) *ntiles = nt;
+  if (tile_cap) *tile_cap = c.tile_cap;
+  if (list_bytes) {
+    // the arrays whose size follows the list
+    *list_bytes = (long long)(c.d_tiles.n * sizeof(Tile) + c.d_items.n * 4 + c.d_tile_flag.n * 4 +
+                              c.d_tile_pos.n * 4 + c.d_scan_tmp2.n * 4 + c.d_tile_need.n +
+                              c.d_masks.n * sizeof(uint2) + c.d_cull_mask.n * 4 + c.d_cull_rest.n * 4 +
+                              c.d_cull_ent.n * sizeof(float4) + c.d_cull_bi.n * 4);
+  }
+  return PDGPU_OK;
+}
+
+int pdgpu_list_slots(pdgpu_ctx* h, int* atom_of_slot) {
+  if (!h || !atom_of_slot) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.list_built) return PDGPU_ERR_STATE;
+  CK(cudaSetDevice(c.device));
+  CK(cudaMemcpyAsync(atom_of_slot, c.d_sorted_atom.p, sizeof(int) * c.nslots, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
   return PDGPU_OK;
 }
 

@@ -24,6 +24,7 @@ namespace pdgpu {
 constexpr int kWarp = 32;
 constexpr int kHilbertBits = 5;                       // 32 cells per dimension
 constexpr int kCellsPerSystem = 1 << (3 * kHilbertBits);
+constexpr int kMaxSystemBlocks = 65536;               // blocks of one system (2^21 atoms): the list-build bitmap
 constexpr int kBandWidth = 64;                        // bonded partners within +-64 indices use the band masks
 constexpr int kLcpoMax = 80;                          // PD caps an atom's LCPO overlap list at 80 (lcpo.h:24)
 constexpr int kLcpoCand = 160;                        // candidate capacity before the cap is applied
@@ -42,6 +43,9 @@ enum StatusBits : unsigned {
   ST_FIXED_OVERFLOW = 2u,
   ST_NAN = 4u,
   ST_STALE_LIST = 8u,
+  // the tile list or its exclusion-mask table outgrew its capacity in a build
+  // that could not resize it (a captured step); the list is incomplete
+  ST_TILE_OVERFLOW = 16u,
 };
 
 struct SystemInfo {
@@ -51,7 +55,8 @@ struct SystemInfo {
   int npad;         // multiple of 32
   int block_start;
   int nblocks;
-  long long cand_start;  // first candidate block pair of this system
+  int grid_start;   // first cell of this system's block grid (list build)
+  int grid_cells;   // its cell budget: one per block
   int periodic;
   double box[3];
   double ibox[3];   // 1 / box (periodic systems)
@@ -66,6 +71,18 @@ struct __align__(16) Tile {
   // in FP64 at the list build and rounded once: the pair kernels add it to the
   // j positions without per-tile FP64 work
   float ox, oy, oz, pad;
+};
+
+// Grid over one system's block centres (list build), remade every build: cells
+// of about equal edge over the periodic box, or over the bounding box of the
+// system's atoms in open space, at most one cell per block
+struct BlockGrid {
+  double origin[3];
+  double cell[3];   // cell edges
+  int dims[3];
+  int start;        // first cell in the context's cell arrays
+  float hmax[3];    // largest block half-extent of the system per axis
+  float pad;
 };
 
 // Pair-law constants for the LJ + Coulomb kernel (FF_NonBonded)
@@ -137,14 +154,15 @@ struct DevView {
   // tile pair (t, t + 1) (same row, adjacent columns, both unmasked off-diagonal)
   unsigned* items;
   int* nitems;
-  uint2* masks;              // [nmask*32] per lane: (excluded bits, 1-4 bits) in rotation order
+  uint2* masks;              // [mask_cap*32] per lane: (excluded bits, 1-4 bits) in rotation order
   int* nmasks;
+  int mask_cap;
   // NB j-atom groups: per i-block row, the j atoms of its unmasked, off-diagonal,
   // single-image tiles that lie within the list radius of the i block's box,
   // packed 32 to a group; the other tiles stay on the tile path (cull_rest)
   float4* cull_ent;          // [cull_cap] j offset into the i block's frame (x, y, z), j slot (int bits; -1 empty)
   int* cull_bi;              // [cull_cap / 32] i block of each group
-  int* cull_rest;            // [ncand] tiles left on the tile path (any order)
+  int* cull_rest;            // [tile capacity] tiles left on the tile path (any order)
   int* cull_n;               // [0] rest tiles, [1] groups, [2] 1 when the groups fit the capacity
   long long cull_cap;        // entries
   long long* facc;           // [nslots*3]
@@ -202,8 +220,18 @@ __device__ __forceinline__ long long warp_sum_ll(long long v) {
 struct Context;
 int tile_grid(Context& c);   // grid of the tile kernels (grid-stride, one tile per warp item)
 // full_radius: distance below which every cutoff and switch of the set
-// components is inactive (0 = never mark tiles full)
-int launch_list_build(Context& c, float list_radius, float full_radius);
+// components is inactive (0 = never mark tiles full).  sizing: how the tile
+// count meets the capacity:
+//   kListReadback  read the count back, grow the tile arrays when it exceeds them
+//   kListCheck     read it back, PDGPU_ERR_CAPACITY when it exceeds them (no allocation)
+//   kListDevice    no host round trip (a captured step): an overflow leaves the
+//                  list short and sets ST_TILE_OVERFLOW
+enum ListSizing { kListReadback = 0, kListCheck = 1, kListDevice = 2 };
+int launch_list_build(Context& c, float list_radius, float full_radius, ListSizing sizing);
+// tile arrays (and the NB group arrays sized from them) for `tiles` tiles
+int alloc_tiles(Context& c, long long tiles);
+// the NB j-atom group arrays for the current tile capacity
+int alloc_cull_tiles(Context& c);
 int launch_pack(Context& c, float check_disp);
 int launch_nb(Context& c, const NBConst& k, bool need_virial);
 int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset, double premul, bool energy);
@@ -239,5 +267,7 @@ int enqueue_forces(Context& c, unsigned what, bool energy, bool rebuild, long lo
                    int lcpo_e_stride, bool run_lcpo);
 struct MDState;
 void destroy_md(Context& c);
+// captured step graphs hold buffer addresses: dropped when a buffer is replaced
+void drop_step_graphs(Context& c);
 
 }  // namespace pdgpu

@@ -49,7 +49,11 @@ struct Context {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int nsys = 0, natom = 0, nslots = 0, nblocks = 0;
-  long long ncand = 0;
+  long long npairs_all = 0;    // block pairs bi <= bj of every system (every pair a tile)
+  long long tile_cap = 0;      // tile list capacity: sized from the count of a build, with headroom
+  int mask_cap = 0;            // exclusion-mask table: diagonal, padded and bonded tiles (a strict bound)
+  int max_sys_blocks = 0;      // blocks of the largest system
+  bool no_alloc = false;       // inside pdgpu_param_grad_device_noalloc: list builds may not resize
   bool any_periodic = false, all_periodic = true;
   bool has_gb = false, has_sa = false, has_bonded = false, has_mass = false;
   bool positions_set = false, list_built = false;
@@ -102,16 +106,22 @@ struct Context {
   DBuf<int> d_slot_of;         // [natom] sorted slot of each atom
   DBuf<double> d_center;       // [nblocks*3]
   DBuf<float4> d_half;         // [nblocks]
-  DBuf<Tile> d_tiles;          // [ncand] row-major tile list
-  DBuf<int> d_tile_flag, d_tile_pos, d_scan_tmp2;  // tile-list compaction
-  DBuf<unsigned char> d_tile_need;                  // [ncand] tile holds a bonded pair (mask build)
+  DBuf<float> d_sys_hmax;      // [nsys*3] largest block half-extent (ordered ints)
+  DBuf<BlockGrid> d_bgrid;     // [nsys]
+  DBuf<int> d_bcell;           // [nblocks] cell of each block
+  DBuf<int> d_bcell_count, d_bcell_off, d_bcell_cursor, d_bcell_scan_tmp;  // [nblocks] cells
+  DBuf<int> d_bcell_blocks;    // [nblocks] blocks in cell order
+  DBuf<int> d_row_cnt, d_row_start, d_row_scan_tmp;  // [nblocks] tiles per row, first tile of each row
+  DBuf<Tile> d_tiles;          // [tile_cap] row-major tile list, ascending columns
+  DBuf<int> d_tile_flag, d_tile_pos, d_scan_tmp2;  // [tile_cap] compaction scratch (GB items, NB groups)
+  DBuf<unsigned char> d_tile_need;                  // [tile_cap] tile holds a bonded pair (mask build)
   DBuf<int> d_counters;        // [0] ntiles, [1] nmasks, [2] nitems, [3..5] NB groups (rest tiles, groups, fit)
-  DBuf<unsigned> d_items;      // [ncand] GB work items (with GB only)
-  DBuf<uint2> d_masks;         // [ncand*32] worst case
+  DBuf<unsigned> d_items;      // [tile_cap] GB work items (with GB only)
+  DBuf<uint2> d_masks;         // [mask_cap*32]
   DBuf<float4> d_xq, d_par, d_rel0;  // [nslots]
   // NB j-atom groups (allocated with the NB parameters)
-  DBuf<unsigned> d_cull_mask;        // [ncand] j lanes kept per tile
-  DBuf<int> d_cull_rest;             // [ncand]
+  DBuf<unsigned> d_cull_mask;        // [tile_cap] j lanes kept per tile
+  DBuf<int> d_cull_rest;             // [tile_cap]
   DBuf<int> d_cull_row;              // [4*nblocks] per row: kept j atoms, first tile, groups, first group
   DBuf<int> d_cull_scan_tmp;
   DBuf<float4> d_cull_ent;           // [cull_cap]
@@ -198,6 +208,7 @@ struct Context {
     v.nitems = d_counters.p + 2;
     v.masks = d_masks.p;
     v.nmasks = d_counters.p + 1;
+    v.mask_cap = mask_cap;
     v.cull_ent = d_cull_ent.p;
     v.cull_bi = d_cull_bi.p;
     v.cull_rest = d_cull_rest.p;

@@ -28,6 +28,12 @@ void destroy_md(Context& c) {
   c.md = nullptr;
 }
 
+void drop_step_graphs(Context& c) {
+  if (!c.md) return;
+  for (auto& kv : c.md->graphs) cudaGraphExecDestroy(kv.second);
+  c.md->graphs.clear();
+}
+
 }  // namespace pdgpu
 
 namespace {
@@ -138,7 +144,7 @@ int read_status_md(Context& c) {
   CK(cudaStreamSynchronize(c.stream));
   if (st & ST_NAN) return PDGPU_ERR_NAN;
   if (st & ST_FIXED_OVERFLOW) return PDGPU_ERR_FIXED_OVERFLOW;
-  if (st & ST_LCPO_OVERFLOW) return PDGPU_ERR_LIST_OVERFLOW;
+  if (st & (ST_LCPO_OVERFLOW | ST_TILE_OVERFLOW)) return PDGPU_ERR_LIST_OVERFLOW;
   if (st & ST_STALE_LIST) return PDGPU_ERR_STALE_LIST;
   return PDGPU_OK;
 }
@@ -292,7 +298,7 @@ int pdgpu_time_kernel(pdgpu_ctx* h, int kernel, int reps, int flush_l2, double* 
       case 1: case 2: case 3: st = launch_gb_stage(c, make_gb_const(c.gb, c.list_radius_built), kernel); break;
       case 4: st = launch_lcpo(c, c.d_facc.p, nullptr, 0); break;
       case 5: st = launch_integrate(c, *c.md, false, false); break;
-      case 6: st = launch_list_build(c, c.list_radius_built, c.full_radius_built); break;
+      case 6: st = launch_list_build(c, c.list_radius_built, c.full_radius_built, kListDevice); break;
       case 7: st = launch_pack(c, 0.f); break;
       case 8: st = launch_bonded(c, false); break;
       default: st = PDGPU_ERR_ARG;

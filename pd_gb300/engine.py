@@ -193,6 +193,26 @@ class DeviceContext:
                   "pdgpu_list_stats")
         return {"tiles": a.value, "masked_tiles": b.value, "slots": c.value}
 
+    def list_tiles(self):
+        """The tile list as an (ntiles, 3) array of (bi, bj, flags), the tile
+        capacity and the bytes of the arrays sized by the list."""
+        n, cap, nbytes = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        ffi.check(self.lib.pdgpu_list_tiles(self.h, None, 0, ctypes.byref(n), ctypes.byref(cap),
+                                            ctypes.byref(nbytes)), "pdgpu_list_tiles")
+        out = np.zeros((n.value, 3), dtype=np.int32)
+        if n.value:
+            ffi.check(self.lib.pdgpu_list_tiles(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n.value,
+                                                ctypes.byref(n), None, None), "pdgpu_list_tiles")
+        return out, cap.value, nbytes.value
+
+    def list_slots(self):
+        """The atom held by each sorted slot of the current list (-1: padding)."""
+        n = self.list_stats()["slots"]
+        out = np.zeros(n, dtype=np.int32)
+        ffi.check(self.lib.pdgpu_list_slots(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))),
+                  "pdgpu_list_slots")
+        return out
+
     def pair_census(self):
         """Pairs of the current list by the branch the pair kernels take
         (pdgpu_pair_census): NB in cutoff, GB in cutoff, GB term on, Born sums,

@@ -107,6 +107,10 @@ SIGNATURES = {
     "pdgpu_get_sasa": ([ctypes.c_void_p, _dp], ctypes.c_int),
     "pdgpu_list_stats": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
                           ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+    "pdgpu_list_tiles": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_longlong,
+                          ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                          ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+    "pdgpu_list_slots": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     "pdgpu_stream": ([ctypes.c_void_p], ctypes.c_void_p),
     "pdgpu_md_setup": ([ctypes.c_void_p, ctypes.POINTER(MDParams), _dp], ctypes.c_int),
     "pdgpu_set_velocities": ([ctypes.c_void_p, _dp, ctypes.c_size_t], ctypes.c_int),

@@ -10,6 +10,7 @@ sqrt(J) epsilons) so a PD user finds the familiar fields.
 A ``SystemImage`` holds the static description of one or more systems (a
 batch); a ``WorkSpace`` adds the state and owns the device context.
 """
+import copy
 import os
 
 import numpy as np
@@ -170,6 +171,25 @@ class SystemImage:
                    impropers=catidx(lambda im: im.impropers, 4),
                    pos=None if images[0].pos is None else np.concatenate([im.pos for im in images]),
                    scaling14=images[0].scaling14, gb_P=images[0].gb_P)
+
+    def replicate(self, reps):
+        """A periodic one-system image copied reps = (nx, ny, nz) times along its
+        box axes, as one system in the enlarged box (same density, reps-fold atoms)."""
+        if self.nsystems != 1 or not self.periodic or self.pos is None:
+            raise ValueError("replicate: one periodic system with positions")
+        L = self.box[0]
+        copies = []
+        for i in range(int(reps[0])):
+            for j in range(int(reps[1])):
+                for k in range(int(reps[2])):
+                    c = copy.copy(self)
+                    c.pos = self.pos + L * np.array([i, j, k], dtype=np.float64)
+                    copies.append(c)
+        out = SystemImage.concat(copies)
+        out.natoms = np.array([out.natom], dtype=np.int32)
+        out.nsystems = 1
+        out.box = (L * np.asarray(reps, dtype=np.float64)).reshape(1, 3)
+        return out
 
     def subset(self, k):
         """System k of a batch as its own image."""

@@ -273,6 +273,36 @@ def test_remd_metropolis_decision_matches_pd_criterion(goldens):
     ctx.close()
 
 
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_list_rebuilds_follow_update_nlist(goldens, use_graph):
+    """The list is rebuilt on the steps PD's ProtocolBase::refreshNeighborList
+    rebuilds it (protocolbase.cpp:135-144: a call counter that starts at 0 and
+    rebuilds when counter % UpdateNList == 0, one call per MD step, md.cpp:232),
+    counted across md_run calls as PD's counter lives with the protocol.  A
+    rebuild step launches the list build's kernels on top of a plain step's."""
+    from pd_gb300 import ffi
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.workspace import SystemImage
+    d = goldens["water_c1"]
+    ctx = DeviceContext(SystemImage._from_fixture(d))
+    ctx.set_list(2.0)
+    ctx.set_nb(**nb_kwargs(d, "nb"))
+    ctx.set_positions(d["pos"])
+    ctx.md_setup([300.0], integrator=1, timestep=1e-15, fric=1e13, update_nlist=3, what=ffi.NB | ffi.BONDED,
+                 seed=7, use_graph=use_graph)
+    counts = []
+    for n in (2, 3, 2, 4):   # runs of different lengths: the cadence carries across them
+        for _ in range(n):
+            k1 = ctx.kernel_launches()
+            ctx.md_enqueue(1)
+            counts.append(ctx.kernel_launches() - k1)
+        ctx.synchronize()
+    plain = min(counts)
+    rebuilt = [s for s, k in enumerate(counts) if k > plain]
+    assert rebuilt == [s for s in range(len(counts)) if s % 3 == 0], counts
+    ctx.close()
+
+
 def test_md_is_deterministic(goldens):
     from pd_gb300 import ffi
     d = goldens["water_c1"]
