@@ -123,45 +123,77 @@ __global__ void k_keys(DevView v, const int* atom_sys, const int* lo, const int*
   atomicAdd(&count[b], 1);
 }
 
-// --- exclusive scan (three-phase, 1024 elements per block) -----------------
-__global__ void k_scan_block(const int* in, int* out, int* block_sums, int n) {
-  __shared__ int sh[1024];
-  int tid = threadIdx.x;
-  int i = blockIdx.x * 1024 + tid;
-  int x = i < n ? in[i] : 0;
-  sh[tid] = x;
-  __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    int y = tid >= o ? sh[tid - o] : 0;
-    __syncthreads();
-    sh[tid] += y;
-    __syncthreads();
+// --- exclusive scans --------------------------------------------------------
+__device__ __forceinline__ int warp_inclusive_scan(int x, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
-  if (i < n) out[i] = sh[tid] - x;
-  if (tid == 1023) block_sums[blockIdx.x] = sh[1023];
+  return x;
 }
 
-__global__ void k_scan_sums(int* sums, int nb) {
-  // single block: sequential chunks, inclusive -> exclusive
-  __shared__ int sh[1024];
-  __shared__ int carry;
-  if (threadIdx.x == 0) carry = 0;
+// 1024 threads: the exclusive prefix of each thread's value within the CTA
+// (warp scans, then a scan of the 32 warp totals); *total gets the CTA's sum
+__device__ __forceinline__ int cta_exclusive_scan(int x, int* wsum, int* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int inc = warp_inclusive_scan(x, lane);
+  if (lane == 31) wsum[wid] = inc;
   __syncthreads();
+  if (wid == 0) {
+    const int t = wsum[lane];
+    const int ti = warp_inclusive_scan(t, lane);
+    wsum[lane] = ti - t;
+    if (lane == 31) wsum[32] = ti;
+  }
+  __syncthreads();
+  *total = wsum[32];
+  return wsum[wid] + inc - x;
+}
+
+// three-phase scan, 1024 elements per CTA
+__global__ void __launch_bounds__(1024) k_scan_block(const int* in, int* out, int* block_sums, int n) {
+  __shared__ int wsum[33];
+  const int i = blockIdx.x * 1024 + threadIdx.x;
+  const int x = i < n ? in[i] : 0;
+  int total;
+  const int e = cta_exclusive_scan(x, wsum, &total);
+  if (i < n) out[i] = e;
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(int* sums, int nb) {
+  // single CTA: 1024-element chunks in order, carrying the running total
+  __shared__ int wsum[33];
+  int carry = 0;
   for (int base = 0; base < nb; base += 1024) {
-    int i = base + threadIdx.x;
-    int x = i < nb ? sums[i] : 0;
-    sh[threadIdx.x] = x;
+    const int i = base + threadIdx.x;
+    const int x = i < nb ? sums[i] : 0;
+    int total;
+    const int e = cta_exclusive_scan(x, wsum, &total);
+    if (i < nb) sums[i] = e + carry;
+    carry += total;
     __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-      int y = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
-      __syncthreads();
-      sh[threadIdx.x] += y;
-      __syncthreads();
-    }
-    if (i < nb) sums[i] = sh[threadIdx.x] - x + carry;
-    __syncthreads();
-    if (threadIdx.x == 1023) carry += sh[1023];
-    __syncthreads();
+  }
+}
+
+// one CTA for n <= kScanOne: 8 consecutive elements per thread
+constexpr int kScanOne = 8192;
+__global__ void __launch_bounds__(1024) k_scan_one(const int* in, int* out, int n) {
+  __shared__ int wsum[33];
+  const int base = threadIdx.x * 8;
+  int x[8], s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    x[k] = base + k < n ? in[base + k] : 0;
+    s += x[k];
+  }
+  int total;
+  int run = cta_exclusive_scan(s, wsum, &total);
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    if (base + k < n) out[base + k] = run;
+    run += x[k];
   }
 }
 
@@ -391,6 +423,21 @@ __global__ void k_bgrid_scatter(int nblocks, const int* bcell, const int* offset
   blocks[offset[cell] + atomicAdd(&cursor[cell], 1)] = b;
 }
 
+// position of the n-th (from 0) set bit of m (m holds more than n set bits)
+__device__ __forceinline__ int nth_set_bit(unsigned m, int n) {
+  int pos = 0;
+#pragma unroll
+  for (int b = 16; b > 0; b >>= 1) {
+    const int c = __popc(m & ((1u << b) - 1u));
+    if (n >= c) {
+      n -= c;
+      m >>= b;
+      pos += b;
+    }
+  }
+  return pos;
+}
+
 // one warp per row bi, 4 warps per CTA, `words` bitmap words per warp in
 // dynamic shared memory.  COUNT: tiles of the row -> row_cnt.  WRITE: the row's
 // tiles from row_start[bi] (positions past `cap` are dropped; the last row
@@ -507,7 +554,7 @@ __global__ void __launch_bounds__(128) k_tile_rows(DevView v, const BlockGrid* g
     __syncwarp();
     for (int w0 = 0; w0 < nw; w0 += 32) {
       const int w = w0 + lane;
-      unsigned word = w < nw ? bits[w] : 0u;
+      const unsigned word = w < nw ? bits[w] : 0u;
       const int k = __popc(word);
       int inc = k;
 #pragma unroll
@@ -515,18 +562,27 @@ __global__ void __launch_bounds__(128) k_tile_rows(DevView v, const BlockGrid* g
         const int t = __shfl_up_sync(0xffffffffu, inc, o);
         if (lane >= o) inc += t;
       }
+      const int tot = __shfl_sync(0xffffffffu, inc, 31);
       if (WRITE) {
-        long long t = base + n + inc - k;
-        while (word) {
-          const int bit = __ffs(word) - 1;
-          word &= word - 1u;
-          const int bj = bi + 32 * w + bit;
-          int fl = 0;
-          tile_test(v, S, bi, bj, R, margin, full_R, full_margin, fl);
-          write_tile(v, S, bi, bj, fl, t++, cap);
+        // the hits of these 32 words dealt over the lanes, in column order
+        const int excl = inc - k;
+        for (int t0 = 0; t0 < tot; t0 += 32) {
+          const int t = t0 + lane;
+          int L = 0;
+#pragma unroll
+          for (int b = 16; b > 0; b >>= 1)
+            if (__shfl_sync(0xffffffffu, excl, L + b) <= t) L += b;
+          const unsigned wl = __shfl_sync(0xffffffffu, word, L);
+          const int nth = t - __shfl_sync(0xffffffffu, excl, L);
+          if (t < tot) {
+            const int bj = bi + 32 * (w0 + L) + nth_set_bit(wl, nth);
+            int fl = 0;
+            tile_test(v, S, bi, bj, R, margin, full_R, full_margin, fl);
+            write_tile(v, S, bi, bj, fl, base + n + t, cap);
+          }
         }
       }
-      n += __shfl_sync(0xffffffffu, inc, 31);
+      n += tot;
     }
   }
   if (lane == 0) {
@@ -566,8 +622,12 @@ __global__ void k_mask_mark(DevView v, const int* slot_of, const int* row_start,
   const int fs = v.far_start[a], fe = v.far_start[a + 1];
   if (!w && fs == fe) return;
   const int ga = slot_of[a] >> 5;
+  int last = ga;
   auto mark = [&](int b) {
     const int gb = slot_of[b] >> 5;
+    // (diagonal tiles get their masks anyway; partners of one block come in runs)
+    if (gb == last || gb == ga) return;
+    last = gb;
     const int t = tile_index(v, row_start, row_cnt, ga < gb ? ga : gb, ga < gb ? gb : ga);
     if (t >= 0) need[t] = 1;
   };
@@ -808,8 +868,13 @@ static int list_tile_grid(const Context& c) {
   return (int)(want < g ? (want > 0 ? want : 1) : g);
 }
 
-// exclusive scan of n ints (n <= 2^20) with the three-kernel scan
-static void scan_ints(const int* in, int* out, int* tmp, long long n, cudaStream_t st) {
+// exclusive scan of n ints (n <= 2^20): one CTA up to kScanOne, else three phases
+static void scan_ints(Context& c, const int* in, int* out, int* tmp, long long n, cudaStream_t st) {
+  c.kernel_launches += n <= kScanOne ? 1 : 3;
+  if (n <= kScanOne) {
+    k_scan_one<<<1, 1024, 0, st>>>(in, out, (int)n);
+    return;
+  }
   const int nb = nblk(n, 1024);
   k_scan_block<<<nb, 1024, 0, st>>>(in, out, tmp, (int)n);
   k_scan_sums<<<1, 1024, 0, st>>>(tmp, nb);
@@ -817,7 +882,7 @@ static void scan_ints(const int* in, int* out, int* tmp, long long n, cudaStream
 }
 
 static void launch_cull(Context& c, float list_radius) {
-  c.kernel_launches += 10;
+  c.kernel_launches += 4;   // and two scans
   DevView v = c.view();
   cudaStream_t st = c.stream;
   const int nb = c.nblocks;
@@ -828,9 +893,9 @@ static void launch_cull(Context& c, float list_radius) {
   // the kept counts and their scan reuse the tile-compaction arrays
   cudaMemsetAsync(c.d_tile_flag.p, 0, sizeof(int) * c.tile_cap, st);
   k_cull_mask<<<list_tile_grid(c), 256, 0, st>>>(v, R * R, c.d_cull_mask.p, c.d_tile_flag.p, row);
-  scan_ints(c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, c.tile_cap, st);
+  scan_ints(c, c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, c.tile_cap, st);
   k_cull_groups<<<nblk(nb, 256), 256, 0, st>>>(nb, row);
-  scan_ints(row + 2 * nb, row + 3 * nb, c.d_cull_scan_tmp.p, nb, st);
+  scan_ints(c, row + 2 * nb, row + 3 * nb, c.d_cull_scan_tmp.p, nb, st);
   k_cull_write<<<list_tile_grid(c), 256, 0, st>>>(v, c.d_cull_mask.p, c.d_tile_pos.p, row);
   k_cull_rows<<<nblk((long long)nb * 32, 256), 256, 0, st>>>(v, row);
 }
@@ -853,7 +918,7 @@ static void launch_rows(Context& c, bool write, float R, float full_radius) {
 }
 
 int launch_list_build(Context& c, float list_radius, float full_radius, ListSizing sizing) {
-  c.kernel_launches += 25;
+  c.kernel_launches += 16;   // and three scans
   DevView v = c.view();
   cudaStream_t st = c.stream;
   int ncells = c.nsys * kCellsPerSystem;
@@ -865,7 +930,7 @@ int launch_list_build(Context& c, float list_radius, float full_radius, ListSizi
   cudaMemsetAsync(c.d_count.p, 0, sizeof(int) * ncells, st);
   cudaMemsetAsync(c.d_cursor.p, 0, sizeof(int) * ncells, st);
   k_keys<<<nblk(c.natom, 256), 256, 0, st>>>(v, c.d_atom_sys.p, lo, hi, c.d_bucket.p, c.d_count.p);
-  scan_ints(c.d_count.p, c.d_offset.p, c.d_scan_tmp.p, ncells, st);
+  scan_ints(c, c.d_count.p, c.d_offset.p, c.d_scan_tmp.p, ncells, st);
   k_scatter<<<nblk(c.natom, 256), 256, 0, st>>>(c.natom, c.d_bucket.p, c.d_offset.p, c.d_cursor.p,
                                                  c.d_tmp_sorted.p);
   k_cell_sort<<<nblk(ncells, 256), 256, 0, st>>>(ncells, c.d_offset.p, c.d_count.p, c.d_tmp_sorted.p);
@@ -883,11 +948,11 @@ int launch_list_build(Context& c, float list_radius, float full_radius, ListSizi
   cudaMemsetAsync(c.d_bcell_count.p, 0, sizeof(int) * c.nblocks, st);
   cudaMemsetAsync(c.d_bcell_cursor.p, 0, sizeof(int) * c.nblocks, st);
   k_bgrid_count<<<nblk(c.nblocks, 256), 256, 0, st>>>(v, c.d_bgrid.p, c.d_bcell.p, c.d_bcell_count.p);
-  scan_ints(c.d_bcell_count.p, c.d_bcell_off.p, c.d_bcell_scan_tmp.p, c.nblocks, st);
+  scan_ints(c, c.d_bcell_count.p, c.d_bcell_off.p, c.d_bcell_scan_tmp.p, c.nblocks, st);
   k_bgrid_scatter<<<nblk(c.nblocks, 256), 256, 0, st>>>(c.nblocks, c.d_bcell.p, c.d_bcell_off.p,
                                                          c.d_bcell_cursor.p, c.d_bcell_blocks.p);
   launch_rows(c, false, list_radius, full_radius);
-  scan_ints(c.d_row_cnt.p, c.d_row_start.p, c.d_row_scan_tmp.p, c.nblocks, st);
+  scan_ints(c, c.d_row_cnt.p, c.d_row_start.p, c.d_row_scan_tmp.p, c.nblocks, st);
   if (sizing != kListDevice) {
     // the tile count (last row's start + count) against the capacity
     int last[2] = {0, 0};
@@ -912,10 +977,10 @@ int launch_list_build(Context& c, float list_radius, float full_radius, ListSizi
                                                    c.d_tile_need.p);
   k_masks<<<list_tile_grid(c), 256, 0, st>>>(v, c.d_tile_need.p);
   if (c.has_gb) {
-    c.kernel_launches += 5;
+    c.kernel_launches += 2;   // and a scan
     const int pairs = c.gb_item_tiles == 2 ? 1 : 0;
     k_item_flags<<<nblk(c.tile_cap, 256), 256, 0, st>>>(v, c.tile_cap, pairs, c.d_tile_flag.p);
-    scan_ints(c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, c.tile_cap, st);
+    scan_ints(c, c.d_tile_flag.p, c.d_tile_pos.p, c.d_scan_tmp2.p, c.tile_cap, st);
     k_item_write<<<nblk(c.tile_cap, 256), 256, 0, st>>>(v, c.tile_cap, pairs, c.d_tile_flag.p, c.d_tile_pos.p);
   }
   k_pack<<<nblk(c.nslots, 256), 256, 0, st>>>(v, c.d_charge.p, 0.f, 0.f, 1, c.npairs_all, 0);
