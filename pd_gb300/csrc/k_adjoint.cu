@@ -189,7 +189,7 @@ __device__ __forceinline__ void adj_gb_tile(const DevView& v, const GBConst& k, 
   }
 }
 
-__global__ void __launch_bounds__(256) k_adj_gb_pair(DevView v, GBConst k, const float* born, long long* gq,
+__global__ void __launch_bounds__(256) k_adj_gb_pair(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* born, long long* gq,
                                                       long long* gr, long long* ge) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -263,7 +263,7 @@ __device__ __forceinline__ void adj_born_tile(const DevView& v, const GBConst& k
   }
 }
 
-__global__ void __launch_bounds__(256) k_adj_born(DevView v, GBConst k, const float* w, long long* gR,
+__global__ void __launch_bounds__(256) k_adj_born(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* w, long long* gR,
                                                    long long* gV) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -367,7 +367,7 @@ __device__ __forceinline__ void adj_nb_tile(const DevView& v, const NBConst& k, 
 }
 
 template <int ELEC>
-__global__ void __launch_bounds__(256) k_adj_nb(DevView v, NBConst k, long long* gq, long long* gr, long long* ge) {
+__global__ void __launch_bounds__(256) k_adj_nb(const __grid_constant__ DevView v, const __grid_constant__ NBConst k, long long* gq, long long* gr, long long* ge) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nt = *v.ntiles;

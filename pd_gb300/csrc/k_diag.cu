@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(256) k_fma_probe(float* out, int iters, float 
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float gb_u_census(float r2, float ai, float aj) { return -0.25f * __fdividef(r2, ai * aj); }
 
-__global__ void __launch_bounds__(256) k_census(DevView v, NBConst nk, GBConst gk, int do_nb, int do_gb,
+__global__ void __launch_bounds__(256) k_census(const __grid_constant__ DevView v, const __grid_constant__ NBConst nk, const __grid_constant__ GBConst gk, int do_nb, int do_gb,
                                                 const float* born, unsigned long long* out) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;

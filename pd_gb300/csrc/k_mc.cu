@@ -33,7 +33,7 @@ __device__ __forceinline__ double mc_r2(const double* p, const SystemInfo& S, in
 // one warp per moved atom i, lanes over the atoms j of its system; a pair of two
 // moved atoms is counted once (from its lower index)
 template <int ELEC>
-__global__ void k_mc_delta(DevView v, NBConst k, const double* ref, const int* atom_sys, const unsigned char* moved,
+__global__ void k_mc_delta(const __grid_constant__ DevView v, const __grid_constant__ NBConst k, const double* ref, const int* atom_sys, const unsigned char* moved,
                            const int* list, const int* count, long long* eref) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;

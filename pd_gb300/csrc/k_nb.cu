@@ -182,7 +182,7 @@ __device__ __forceinline__ void nb_flush_energy(const DevView& v, int lane, int 
 // One warp per work item, grid-stride: the tiles left on the tile path, then the
 // j-atom groups (cull: the last list build wrote them and they fit)
 template <int ELEC, bool ENERGY>
-__global__ void __launch_bounds__(256, ENERGY ? 0 : 4) k_nb_tiles(DevView v, NBConst k, int cull) {
+__global__ void __launch_bounds__(256, ENERGY ? 0 : 4) k_nb_tiles(const __grid_constant__ DevView v, const __grid_constant__ NBConst k, int cull) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const bool grouped = cull && v.cull_n[2];
