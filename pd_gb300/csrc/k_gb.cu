@@ -640,12 +640,14 @@ __device__ __forceinline__ void gb_pair_tile2(const DevView& v, const GBConst& k
 // and, above it, the GB term (gbff.cpp:1592-1678) with Coulomb at eps_in in
 // place of eps_out.  akh, akr: Born radii times sqrtK; e1: the pair's eps_out
 // Coulomb energy; ir = 1/r.  Returns what the pair adds to dE/dr / r and to
-// the two atoms' dE/da (by value: the caller's accumulators stay in registers).
+// the two atoms' dE/da.  Inlined under the caller's warp vote: a call (the
+// accumulators saved around it) or outputs through references (accumulators
+// kept in local memory) both cost more than the registers it adds.
 struct GBTerm {
   float g, dah, dar;
 };
-__device__ __noinline__ GBTerm gb_full_term(const DevView& v, const GBConst& k, float r2, float ir, float e1,
-                                            float akh, float akr, int sh, int sr) {
+__device__ __forceinline__ GBTerm gb_full_term(const DevView& v, const GBConst& k, float r2, float ir, float e1,
+                                               float akh, float akr, int sh, int sr) {
   GBTerm t = {0.f, 0.f, 0.f};
   const float ah = akh * k.inv_sqrtK, ar = akr * k.inv_sqrtK;
   const float aiaj = ah * ar;

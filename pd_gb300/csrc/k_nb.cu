@@ -19,10 +19,24 @@ struct NBAcc {
 };
 
 // Force part of the pair law in FP32 (same law as nb_pair): dE/dr divided by r.
-template <int ELEC>
+// SW (energy switch on both terms over the same radii, the common PD setting):
+// one switch factor serves LJ and Coulomb, dE/dr / r = S^2 (gv + ge) +
+// (Ev + Ee) S' / r with S' = -4 u S / w^2.
+template <int ELEC, bool SW = false>
 __device__ __forceinline__ float nb_force_f(const NBConst& k, float r2, float rsum, float eps, float qq) {
   const float invr = rsqrtf(r2), ir2 = invr * invr;
   const float r = r2 * invr;
+  if (SW) {
+    const float t2 = rsum * rsum * ir2;
+    const float B = t2 * t2 * t2, A = B * B;
+    const bool vin = r < k.vdwcut_f;
+    const float ev = vin ? eps * (A - 2.f * B) : 0.f;
+    const float gv = vin ? -12.f * eps * ir2 * (A - B) : 0.f;
+    const float Ee = qq * invr;
+    const float u = fmaxf(r - k.inner_f, 0.f);
+    const float sw = 1.f - u * u * k.invw2_f;
+    return sw * sw * (gv - Ee * ir2) + (ev + Ee) * (-4.f * k.invw2_f * u * sw) * invr;
+  }
   float g = 0.f;
   // switching without a branch: below the inner cutoff u = 0, so sw = 1 and the
   // derivative term is exactly 0 (same value as the unswitched law); a branch
@@ -60,7 +74,7 @@ __device__ __forceinline__ float nb_force_f(const NBConst& k, float r2, float rs
 // lane's j atom already in i's frame.  Tiles: j slot jb + lane, per-pair image
 // when mi.  GROUP: the j atoms of a group (slots in gent[].w, -1 = empty lane,
 // parked far away), never masked, one image.
-template <int ELEC, bool MASKED, bool ENERGY, bool GROUP>
+template <int ELEC, bool MASKED, bool ENERGY, bool GROUP, bool SW>
 __device__ __forceinline__ void nb_rot(const DevView& v, const NBConst& k, const SystemInfo& S, int lane, int si,
                                        int ai, const float4& xi, const float4& pi, float qi, unsigned ex, unsigned m14,
                                        float4 xj, float4 pj, bool mi_tile, int jb, const float4* gent, NBAcc& I,
@@ -93,7 +107,8 @@ __device__ __forceinline__ void nb_rot(const DevView& v, const NBConst& k, const
           in = r2d <= k.cut2_dd;
         }
       }
-    } else if (listed && (fabsf(r2 - k.cut2) <= 2e-6f * k.cut2 || fabsf(r2 - k.vdwcut2) <= 2e-6f * k.vdwcut2)) {
+    } else if (listed && (fabsf(r2 - k.cut2) <= 2e-6f * k.cut2 ||
+                          (!SW && fabsf(r2 - k.vdwcut2) <= 2e-6f * k.vdwcut2))) {
       // at a hard cutoff: decide, and take the distance, in FP64 (FP64 work only on this branch)
       const int sjr = GROUP ? __float_as_int(gent[(lane + kk) & 31].w) : jb + ((lane + kk) & 31);
       const double d2 = nb_r2_fp64(v, S, si, sjr);
@@ -104,7 +119,7 @@ __device__ __forceinline__ void nb_rot(const DevView& v, const NBConst& k, const
       const bool is14 = MASKED && ((m14 >> kk) & 1u);
       const float eps = pi.y * pj.y * (is14 ? k.vdw14 : 1.f);
       const float qq = qi * xj.w * (is14 ? k.elec14 : 1.f);
-      const float fs = nb_force_f<ELEC>(k, r2, pi.x + pj.x, eps, qq);
+      const float fs = nb_force_f<ELEC, SW>(k, r2, pi.x + pj.x, eps, qq);
       if (ENERGY) {
         // energy of this pair in FP64 from FP64 positions and parameters
         const int aj = v.sorted_atom[sj];
@@ -181,7 +196,7 @@ __device__ __forceinline__ void nb_flush_energy(const DevView& v, int lane, int 
 
 // One warp per work item, grid-stride: the tiles left on the tile path, then the
 // j-atom groups (cull: the last list build wrote them and they fit)
-template <int ELEC, bool ENERGY>
+template <int ELEC, bool ENERGY, bool SW = false>
 __global__ void __launch_bounds__(256, ENERGY ? 0 : 4) k_nb_tiles(const __grid_constant__ DevView v, const __grid_constant__ NBConst k, int cull) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -216,10 +231,10 @@ __global__ void __launch_bounds__(256, ENERGY ? 0 : 4) k_nb_tiles(const __grid_c
       xj.z += T.oz;
       const bool mi = T.flags & 1;
       if (tile_masked(T))
-        nb_rot<ELEC, true, ENERGY, false>(v, k, S, lane, si, ai, xi, pi, qi, ex, m14, xj, pj, mi, T.bj * 32,
+        nb_rot<ELEC, true, ENERGY, false, SW>(v, k, S, lane, si, ai, xi, pi, qi, ex, m14, xj, pj, mi, T.bj * 32,
                                           nullptr, I, J, ev, ee, vir);
       else
-        nb_rot<ELEC, false, ENERGY, false>(v, k, S, lane, si, ai, xi, pi, qi, ex, m14, xj, pj, mi, T.bj * 32,
+        nb_rot<ELEC, false, ENERGY, false, SW>(v, k, S, lane, si, ai, xi, pi, qi, ex, m14, xj, pj, mi, T.bj * 32,
                                            nullptr, I, J, ev, ee, vir);
       nb_flush(v, si, I);
     } else {
@@ -241,7 +256,7 @@ __global__ void __launch_bounds__(256, ENERGY ? 0 : 4) k_nb_tiles(const __grid_c
         xj.y += e.y;
         xj.z += e.z;
       }
-      nb_rot<ELEC, false, ENERGY, true>(v, k, S, lane, si, ai, xi, pi, qi, 0u, 0u, xj, pj, false, 0, gent, I, J,
+      nb_rot<ELEC, false, ENERGY, true, SW>(v, k, S, lane, si, ai, xi, pi, qi, 0u, 0u, xj, pj, false, 0, gent, I, J,
                                         ev, ee, vir);
       nb_flush(v, si, I);
     }
@@ -261,7 +276,10 @@ static void launch_nb_mode(Context& c, const NBConst& k, int g) {
   switch (k.elecmode) {
     case 0: k_nb_tiles<0, E><<<g, 256, 0, c.stream>>>(v, k, cull); break;
     case 1: k_nb_tiles<1, E><<<g, 256, 0, c.stream>>>(v, k, cull); break;
-    case 3: k_nb_tiles<3, E><<<g, 256, 0, c.stream>>>(v, k, cull); break;
+    case 3:
+      if (k.samesw && !E) k_nb_tiles<3, false, true><<<g, 256, 0, c.stream>>>(v, k, cull);
+      else k_nb_tiles<3, E><<<g, 256, 0, c.stream>>>(v, k, cull);
+      break;
     default: k_nb_tiles<4, E><<<g, 256, 0, c.stream>>>(v, k, cull); break;
   }
 }

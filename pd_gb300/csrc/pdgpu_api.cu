@@ -136,6 +136,7 @@ NBConst pdgpu::make_nb_const(const pdgpu_nb_params& p) {
   if (p.ForceSwitch) k.elecmode = 4;
   if (!p.DoElec) k.elecmode = 0;
   k.dovdw = p.DoVdw ? 1 : 0;
+  k.samesw = (k.elecmode == 3 && k.dovdw && p.VdwCutoff == p.Cutoff && p.VdwInnerCutoff == p.InnerCutoff) ? 1 : 0;
   return k;
 }
 

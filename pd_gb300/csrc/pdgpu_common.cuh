@@ -95,6 +95,9 @@ struct NBConst {
   float vdwcut_f, vdwinner_f, vdwinvw2_f, inner_f, invw2_f, inner2_f, sA_f, fsw_k;  // fsw_k = cut2 - 3 inner2
   int elecmode;            // 0 none, 1 plain, 3 energy switch, 4 force switch
   int dovdw;
+  // 1: LJ and Coulomb switched over the same radii (Cutoff = VdwCutoff,
+  // InnerCutoff = VdwInnerCutoff, energy switch, LJ on): one switch serves both
+  int samesw;
 };
 
 // Constants for the GB fast path (FF_GeneralizedBorn_Still::calcForcesIncludingVacuo)

@@ -40,6 +40,27 @@ def test_concat_and_subset_roundtrip():
             assert np.array_equal(getattr(sub, t)[1], getattr(ref, t)[1])
 
 
+def test_replicate_tiles_a_periodic_box():
+    """SystemImage.replicate (the replicated C2 boxes of the list-scaling
+    measurement): copies shifted by whole box edges, indices re-based, one
+    system in the enlarged box."""
+    from pd_gb300.workspace import SystemImage
+    w = SystemImage._from_fixture(golden("water_c1"))
+    r = w.replicate((2, 1, 3))
+    n = w.natom
+    assert r.nsystems == 1 and r.natom == 6 * n
+    assert np.allclose(r.box[0], w.box[0] * np.array([2, 1, 3]))
+    L = w.box[0]
+    for c in range(6):
+        i, k = divmod(c, 3)
+        assert np.allclose(r.pos[c * n:(c + 1) * n] - w.pos, L * np.array([i, 0, k]))
+    assert len(r.excl) == 6 * len(w.excl) and r.excl[:, :2].max() < 6 * n
+    assert np.array_equal(r.excl[len(w.excl):2 * len(w.excl), :2], w.excl[:, :2] + n)
+    assert np.array_equal(r.charge, np.tile(w.charge, 6))
+    with pytest.raises(ValueError):
+        SystemImage.concat([w, w]).replicate((2, 1, 1))
+
+
 def test_forcefield_defaults_mirror_pd():
     """Constructor defaults of the components equal PD's (nonbonded.cpp:985-1021, gbff.cpp:33-55, lcpo.h)."""
     import pd_gb300 as pdg
