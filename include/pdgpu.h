@@ -146,6 +146,15 @@ int pdgpu_set_positions(pdgpu_ctx *ctx, const double *xyz, size_t stride_bytes);
 /* Same from device memory already on this context's device (packed xyz). */
 int pdgpu_set_positions_device(pdgpu_ctx *ctx, const double *d_xyz);
 int pdgpu_get_positions(pdgpu_ctx *ctx, double *xyz, size_t stride_bytes);
+/* Asynchronous forms for page-locked host memory (pdgpu_host_alloc), packed
+ * xyz: the copy is queued on the context stream in order with the work around
+ * it and the call returns at once; the caller leaves the buffer alone until
+ * pdgpu_synchronize returns.  A dynamics loop can then move every step's
+ * positions in and out with no host round trip per step (PD's per-step
+ * WorkSpace exchange without the wait).  set: the context's positions must
+ * have been set once with pdgpu_set_positions (that call sizes the list). */
+int pdgpu_set_positions_async(pdgpu_ctx *ctx, const double *xyz);
+int pdgpu_get_positions_async(pdgpu_ctx *ctx, double *xyz);
 
 /* ---- neighbour list ------------------------------------------------------- */
 /* Replaces NeighbourList::calcNewList (neighbourlist.cpp:222-439): cell-grid
@@ -256,6 +265,9 @@ int pdgpu_md_enqueue(pdgpu_ctx *ctx, int nsteps, int energy_on_last);
 int pdgpu_synchronize(pdgpu_ctx *ctx);
 /* Kinetic energy of each system after the last step (J), PD's calcKineticEnergy. */
 int pdgpu_get_kinetic(pdgpu_ctx *ctx, double *ekin);
+/* Same, queued on the context stream into page-locked host memory (see
+ * pdgpu_set_positions_async): valid after pdgpu_synchronize returns. */
+int pdgpu_get_kinetic_async(pdgpu_ctx *ctx, double *ekin);
 /* One REX_Local exchange sweep (remd.cpp:178-215): rungs (parity, parity+1),
  * (parity+2, parity+3)... of the temperature ladder, Metropolis on the last
  * energies (remd.cpp:349-356), accepted swaps exchange the systems' target

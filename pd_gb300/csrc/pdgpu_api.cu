@@ -832,6 +832,23 @@ int pdgpu_set_positions_device(pdgpu_ctx* h, const double* d_xyz) {
   return size_list(c);
 }
 
+int pdgpu_set_positions_async(pdgpu_ctx* h, const double* xyz) {
+  if (!h || !xyz) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.positions_set) return PDGPU_ERR_STATE;
+  CK(cudaSetDevice(c.device));
+  CK(cudaMemcpyAsync(c.d_pos.p, xyz, 24 * (size_t)c.natom, cudaMemcpyHostToDevice, c.stream));
+  return PDGPU_OK;
+}
+
+int pdgpu_get_positions_async(pdgpu_ctx* h, double* xyz) {
+  if (!h || !xyz) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  CK(cudaSetDevice(c.device));
+  CK(cudaMemcpyAsync(xyz, c.d_pos.p, 24 * (size_t)c.natom, cudaMemcpyDeviceToHost, c.stream));
+  return PDGPU_OK;
+}
+
 int pdgpu_get_positions(pdgpu_ctx* h, double* xyz, size_t stride) {
   if (!h || !xyz || stride < 24 || stride % 8) return PDGPU_ERR_ARG;
   Context& c = h->c;

@@ -27,6 +27,7 @@ struct MDState {
   DBuf<double> d_vscale;              // [nsys]
   DBuf<int> d_accepted;               // [nsys]
   DBuf<long long> d_ke;               // [nsys] kinetic energy, fixed point kcal/mol
+  DBuf<double> d_ke_j;                // [nsys] the same in J (asynchronous reads)
   DBuf<long long> d_facc_sa;          // [nslots*3] cached LCPO forces
   DBuf<long long> d_surf_cache;       // [nsys] cached LCPO energy
   DBuf<int> d_mode;                   // [nsys] exchange mode of each rung's lower replica (0 swap, 1 down, 2 up)

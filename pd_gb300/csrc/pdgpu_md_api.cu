@@ -49,6 +49,12 @@ void invalidate_graphs(MDState& md) {
   md.graphs.clear();
 }
 
+// kinetic energies from their fixed-point sums to J (pdgpu_get_kinetic_async)
+__global__ void k_ke_joules(const long long* ke, double* out, int nsys) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) out[s] = (double)ke[s] / kEnergyScale * kKcalMolToJ;
+}
+
 __global__ void k_add_surf(long long* eacc, const long long* cache, int nsys) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s < nsys) eacc[(size_t)s * E_NSLOTS + E_SURF] += cache[s];
@@ -205,7 +211,8 @@ int pdgpu_md_setup(pdgpu_ctx* h, const pdgpu_md_params* p, const double* temps) 
   if (md.d_vel.alloc(3 * N) != cudaSuccess || md.d_temp.alloc(c.nsys) != cudaSuccess ||
       md.d_ladder.alloc(c.nsys) != cudaSuccess || md.d_temp_sys.alloc(c.nsys) != cudaSuccess ||
       md.d_vscale.alloc(c.nsys) != cudaSuccess || md.d_accepted.alloc(c.nsys) != cudaSuccess ||
-      md.d_ke.alloc(c.nsys) != cudaSuccess || md.d_facc_sa.alloc(3 * (size_t)c.nslots) != cudaSuccess ||
+      md.d_ke.alloc(c.nsys) != cudaSuccess || md.d_ke_j.alloc(c.nsys) != cudaSuccess ||
+      md.d_facc_sa.alloc(3 * (size_t)c.nslots) != cudaSuccess ||
       md.d_surf_cache.alloc(c.nsys) != cudaSuccess || md.d_step.alloc(1) != cudaSuccess ||
       md.d_mode.alloc(c.nsys) != cudaSuccess || md.d_copy_src.alloc(c.nsys) != cudaSuccess ||
       md.d_copy_scale.alloc(c.nsys) != cudaSuccess || md.d_bad.alloc(c.nsys) != cudaSuccess)
@@ -324,6 +331,19 @@ int pdgpu_get_kinetic(pdgpu_ctx* h, double* ekin) {
   CK(cudaMemcpyAsync(ke.data(), c.md->d_ke.p, sizeof(long long) * c.nsys, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   for (int s = 0; s < c.nsys; s++) ekin[s] = (double)ke[s] / kEnergyScale * kKcalMolToJ;
+  return PDGPU_OK;
+}
+
+int pdgpu_get_kinetic_async(pdgpu_ctx* h, double* ekin) {
+  if (!h || !ekin) return PDGPU_ERR_ARG;
+  Context& c = h->c;
+  if (!c.md) return PDGPU_ERR_STATE;
+  CK(cudaSetDevice(c.device));
+  MDState& md = *c.md;
+  k_ke_joules<<<(c.nsys + 127) / 128, 128, 0, c.stream>>>(md.d_ke.p, md.d_ke_j.p, c.nsys);
+  c.kernel_launches += 1;
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(ekin, md.d_ke_j.p, sizeof(double) * c.nsys, cudaMemcpyDeviceToHost, c.stream));
   return PDGPU_OK;
 }
 

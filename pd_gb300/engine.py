@@ -267,6 +267,25 @@ class DeviceContext:
         ffi.check(self.lib.pdgpu_get_kinetic(self.h, _pd(out)), "pdgpu_get_kinetic")
         return out
 
+    # asynchronous host copies: `buf` page-locked (ffi.host_array), packed, left
+    # untouched until synchronize() returns
+    def _host_buf(self, buf, shape, what):
+        if buf.dtype != np.float64 or buf.shape != shape or not buf.flags.c_contiguous:
+            raise ValueError("%s: a C-contiguous float64 array of shape %s" % (what, shape))
+        return _pd(buf)
+
+    def set_positions_async(self, buf):
+        ffi.check(self.lib.pdgpu_set_positions_async(self.h, self._host_buf(buf, (self.natom, 3), "set_positions_async")),
+                  "pdgpu_set_positions_async")
+
+    def get_positions_async(self, buf):
+        ffi.check(self.lib.pdgpu_get_positions_async(self.h, self._host_buf(buf, (self.natom, 3), "get_positions_async")),
+                  "pdgpu_get_positions_async")
+
+    def kinetic_async(self, buf):
+        ffi.check(self.lib.pdgpu_get_kinetic_async(self.h, self._host_buf(buf, (self.nsystems,), "kinetic_async")),
+                  "pdgpu_get_kinetic_async")
+
     def remd_exchange(self, parity):
         acc = np.zeros(max(self.nsystems - 1, 1), np.int32)
         temps = np.zeros(self.nsystems)

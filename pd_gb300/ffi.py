@@ -98,6 +98,8 @@ SIGNATURES = {
     "pdgpu_set_positions": ([ctypes.c_void_p, _dp, ctypes.c_size_t], ctypes.c_int),
     "pdgpu_set_positions_device": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "pdgpu_get_positions": ([ctypes.c_void_p, _dp, ctypes.c_size_t], ctypes.c_int),
+    "pdgpu_set_positions_async": ([ctypes.c_void_p, _dp], ctypes.c_int),
+    "pdgpu_get_positions_async": ([ctypes.c_void_p, _dp], ctypes.c_int),
     "pdgpu_rebuild_list": ([ctypes.c_void_p], ctypes.c_int),
     "pdgpu_compute": ([ctypes.c_void_p, ctypes.c_uint, ctypes.POINTER(Energies), _dp, ctypes.c_size_t],
                       ctypes.c_int),
@@ -117,6 +119,7 @@ SIGNATURES = {
     "pdgpu_get_velocities": ([ctypes.c_void_p, _dp, ctypes.c_size_t], ctypes.c_int),
     "pdgpu_md_run": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "pdgpu_get_kinetic": ([ctypes.c_void_p, _dp], ctypes.c_int),
+    "pdgpu_get_kinetic_async": ([ctypes.c_void_p, _dp], ctypes.c_int),
     "pdgpu_remd_exchange": ([ctypes.c_void_p, ctypes.c_int, _ip, _dp], ctypes.c_int),
     "pdgpu_md_autotune": ([ctypes.c_void_p, ctypes.c_int, _ip, _ip], ctypes.c_int),
     "pdgpu_remd_set_modes": ([ctypes.c_void_p, _ip], ctypes.c_int),

@@ -273,6 +273,38 @@ def test_remd_metropolis_decision_matches_pd_criterion(goldens):
     ctx.close()
 
 
+def test_async_host_copies_match_synchronous_calls(goldens):
+    """A dynamics loop through the asynchronous entry points (positions in,
+    one step, kinetic energies and positions out, all queued in stream order
+    into page-locked buffers, one wait at the end) gives bit for bit what the
+    synchronous calls give step by step."""
+    from pd_gb300 import ffi
+    d = goldens["water_c1"]
+    ref = water_ctx(d, 1, ffi.NB | ffi.BONDED)
+    pos = d["pos"].copy()
+    kes = []
+    for _ in range(7):
+        ref.set_positions(pos)
+        ref.md_run(1)
+        kes.append(ref.kinetic())
+        pos = ref.get_positions()
+    ref.close()
+    ctx = water_ctx(d, 1, ffi.NB | ffi.BONDED)
+    pos_h = ffi.host_array(d["pos"].shape)
+    pos_h[...] = d["pos"]
+    ke_h = [ffi.host_array((1,)) for _ in range(7)]
+    for k in range(7):
+        ctx.set_positions_async(pos_h)
+        ctx.md_enqueue(1)
+        ctx.kinetic_async(ke_h[k])
+        ctx.get_positions_async(pos_h)
+    ctx.synchronize()
+    assert np.array_equal(pos_h, pos)
+    for k in range(7):
+        assert np.array_equal(ke_h[k], kes[k])
+    ctx.close()
+
+
 @pytest.mark.parametrize("use_graph", [False, True])
 def test_list_rebuilds_follow_update_nlist(goldens, use_graph):
     """The list is rebuilt on the steps PD's ProtocolBase::refreshNeighborList
