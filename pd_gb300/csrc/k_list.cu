@@ -329,7 +329,11 @@ __device__ __forceinline__ bool tile_test(const DevView& v, const SystemInfo& S,
     if (S.periodic) {
       const float L = (float)S.box[c];
       d -= L * rintf(d * (float)S.ibox[c]);
-      if (fabsf(d) + hs[c] + margin >= 0.5f * L - kSafe) need_mi = true;
+      // a pair of the two blocks inside the cutoff in some other image would
+      // sit at least L - R apart along this axis in the tile's image: below
+      // that every pair inside the cutoff takes the tile's image, and pairs
+      // whose images differ lie beyond the cutoff in both
+      if (fabsf(d) + hs[c] + margin >= L - R - kSafe) need_mi = true;
     }
     const float g = fabsf(d) - hs[c];
     if (g > 0.f) dist2 += g * g;
