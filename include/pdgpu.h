@@ -27,14 +27,17 @@ extern "C" {
 #define PDGPU_OK 0
 #define PDGPU_ERR_ARG (-1)            /* invalid argument (PD: ProcedureException)          */
 #define PDGPU_ERR_CUDA (-2)           /* CUDA runtime error                                  */
-#define PDGPU_ERR_LIST_OVERFLOW (-3)  /* an LCPO overlap list exceeded its capacity          */
+#define PDGPU_ERR_LIST_OVERFLOW (-3)  /* an LCPO overlap list, or the tile list inside a
+                                         captured dynamics step, exceeded its capacity      */
 #define PDGPU_ERR_FIXED_OVERFLOW (-4) /* a fixed-point accumulator left its range            */
 #define PDGPU_ERR_NAN (-5)            /* NaN energy or force (PD: assertStability)           */
 #define PDGPU_ERR_TIMEOUT (-6)        /* a device wait exceeded its iteration limit          */
 #define PDGPU_ERR_UNSUPPORTED (-7)    /* option not supported (e.g. GB in a periodic box)    */
 #define PDGPU_ERR_STALE_LIST (-8)     /* an atom moved more than Padding/2 since the rebuild */
 #define PDGPU_ERR_STATE (-9)          /* call sequence error (e.g. compute before positions) */
-#define PDGPU_ERR_CAPACITY (-10)      /* larger than a fixed-size entry point's static scratch */
+#define PDGPU_ERR_CAPACITY (-10)      /* larger than a fixed-size entry point's static scratch,
+                                         or a list that would need arrays such a call may
+                                         not allocate (pdgpu_param_grad_device_noalloc)     */
 
 /* ---- what to compute ------------------------------------------------------ */
 #define PDGPU_NB 1u      /* FF_NonBonded: LJ + Coulomb with PD's switching     */
@@ -158,7 +161,13 @@ int pdgpu_get_positions_async(pdgpu_ctx *ctx, double *xyz);
 
 /* ---- neighbour list ------------------------------------------------------- */
 /* Replaces NeighbourList::calcNewList (neighbourlist.cpp:222-439): cell-grid
- * sort, block bounding boxes and the tile list at radius max(cutoffs)+Padding. */
+ * sort, block bounding boxes and the tile list at radius max(cutoffs)+Padding,
+ * found through a grid over the block centres.  The tile arrays are sized by
+ * the first build (the first pdgpu_set_positions after the parameters) with a
+ * quarter of headroom and grow at any build outside a captured dynamics step
+ * that finds more tiles; inside a captured step an overflow is reported as
+ * PDGPU_ERR_LIST_OVERFLOW by the step's status, and the next call of this
+ * function grows them. */
 int pdgpu_rebuild_list(pdgpu_ctx *ctx);
 
 /* ---- evaluation ----------------------------------------------------------- */

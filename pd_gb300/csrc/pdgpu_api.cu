@@ -196,14 +196,14 @@ const char* pdgpu_error_string(int status) {
     case PDGPU_OK: return "ok";
     case PDGPU_ERR_ARG: return "invalid argument";
     case PDGPU_ERR_CUDA: return "CUDA runtime error";
-    case PDGPU_ERR_LIST_OVERFLOW: return "LCPO overlap list overflow";
+    case PDGPU_ERR_LIST_OVERFLOW: return "LCPO overlap list or tile list overflow";
     case PDGPU_ERR_FIXED_OVERFLOW: return "fixed-point accumulator overflow";
     case PDGPU_ERR_NAN: return "NaN energy or force";
     case PDGPU_ERR_TIMEOUT: return "device wait timed out";
     case PDGPU_ERR_UNSUPPORTED: return "unsupported option";
     case PDGPU_ERR_STALE_LIST: return "an atom moved more than Padding/2 since the list was built";
     case PDGPU_ERR_STATE: return "call sequence error";
-    case PDGPU_ERR_CAPACITY: return "larger than the static scratch of the allocation-free entry point";
+    case PDGPU_ERR_CAPACITY: return "beyond what the allocation-free entry point holds (static scratch or list arrays)";
     default: return "unknown status";
   }
 }

@@ -13,10 +13,10 @@ _ip = ctypes.POINTER(ctypes.c_int)
 
 OK = 0
 ERRORS = {
-    -1: "invalid argument", -2: "CUDA runtime error", -3: "LCPO overlap list overflow",
+    -1: "invalid argument", -2: "CUDA runtime error", -3: "LCPO overlap list or tile list overflow",
     -4: "fixed-point accumulator overflow", -5: "NaN energy or force", -6: "device wait timed out",
     -7: "unsupported option", -8: "stale neighbour list", -9: "call sequence error",
-    -10: "larger than the static scratch of the allocation-free entry point",
+    -10: "beyond what the allocation-free entry point holds (static scratch or list arrays)",
 }
 ERR_STALE_LIST = -8
 ERR_CAPACITY = -10
