@@ -183,3 +183,44 @@ def test_list_memory_scales_linearly_with_the_box():
     for b, t in per_atom[1:]:
         assert b <= 1.25 * b1, per_atom
         assert abs(t / t1 - 1) < 0.15, per_atom
+
+
+def test_tile_overflow_inside_a_device_sized_build_is_reported_and_recovers():
+    """A build that cannot read the tile count back (as inside a captured
+    dynamics step) and finds more tiles than the arrays hold writes a short
+    list and reports PDGPU_ERR_LIST_OVERFLOW; the next host-side rebuild grows
+    the arrays and the evaluation equals a fresh context's."""
+    from pd_gb300 import ffi
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.workspace import load_workload
+    d = golden("cfg_c4_large")
+    im = load_workload(str(d["image"])).subset(int(d["system"][0]))
+    centre = im.pos.mean(0)
+    ctx = DeviceContext(im)
+    ctx.set_list(2.0)
+    ctx.set_nb(**NB_OPEN)
+    ctx.set_positions(centre + (im.pos - centre) * 2.0)   # sizes the list on a spread copy
+    tiles0, cap0, _ = ctx.list_tiles()
+    ctx.set_positions(im.pos)
+    ctx.time_kernel("list", reps=1, flush_l2=False)        # a build without the host round trip
+    with pytest.raises(ffi.PDGPUError) as err:
+        ctx.synchronize()
+    assert err.value.status == -3                          # PDGPU_ERR_LIST_OVERFLOW
+    tiles, cap, _ = ctx.list_tiles()
+    assert cap == cap0 and len(tiles) == cap0              # the short list fills the arrays
+    ctx.rebuild_list()
+    tiles, cap1, _ = ctx.list_tiles()
+    assert cap1 > cap0 and len(tiles) < cap1
+    f = np.zeros((im.natom, 3))
+    e = ctx.compute(ffi.NB, f)[0]
+    ctx.close()
+    ref = DeviceContext(im)
+    ref.set_list(2.0)
+    ref.set_nb(**NB_OPEN)
+    ref.set_positions(im.pos)
+    f0 = np.zeros((im.natom, 3))
+    e0 = ref.compute(ffi.NB, f0)[0]
+    ref.close()
+    for k in ("vdw", "elec"):
+        assert abs(e[k] - e0[k]) <= 1e-12 * abs(e0[k]), (k, e[k], e0[k])
+    assert np.array_equal(f, f0)
