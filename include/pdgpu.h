@@ -353,8 +353,9 @@ int pdgpu_get_nb_groups(pdgpu_ctx *ctx, int *on, long long *ngroups, long long *
 /* ---- diagnostics ---------------------------------------------------------- */
 /* Tile / pair counts of the current list: ntiles, nmasked tiles, slots. */
 int pdgpu_list_stats(pdgpu_ctx *ctx, long long *ntiles, long long *nmasked, long long *nslots);
-/* The current tile list as (bi, bj, flags) per tile, rows ascending and
- * columns ascending within a row (block b holds sorted slots 32b..32b+31);
+/* The current tile list as (bi, bj, flags) per tile, each row's tiles
+ * together with ascending columns, rows in any order (block b holds sorted
+ * slots 32b..32b+31);
  * at most `cap` tiles are written, *ntiles gets the list length.  Flags: bit 0
  * per-pair minimum image, bit 1 diagonal, bit 2 every pair inside all cutoffs.
  * Also the device memory the list arrays hold (tile capacity, bytes). */

@@ -308,10 +308,12 @@ __global__ void k_slot_params(DevView v, const double* radius, const double* sqe
 // at most one cell per block; row bi visits only the cells within
 // R + h_i + hmax of its centre along each axis (h: half-extents, hmax the
 // system's largest), marks its hits in a per-warp bitmap over its columns
-// bj >= bi, and writes them in ascending bj.  The list is row-major with
-// ascending columns whatever order the cells were visited in, so every build
-// from the same positions writes the same list.  A row whose cell range spans
-// the whole grid (all pairs within reach) walks its columns directly.
+// bj >= bi, takes its place in the list with one atomic on the tile total and
+// writes its tiles there in ascending bj.  Rows land in any order, each
+// contiguous with ascending columns (what the binary searches, the GB tile
+// pairs and the NB groups rely on); every sum over tiles is in fixed point,
+// so the results do not depend on the rows' order.  A row whose cell range
+// spans the whole grid (all pairs within reach) walks its columns directly.
 // ---------------------------------------------------------------------------
 // box test of one block pair; flags as Tile::flags.  FP32 geometry (the FP64
 // pipe is narrow on this GPU), every decision taken 1e-3 A on the safe side:
@@ -442,15 +444,26 @@ __device__ __forceinline__ int nth_set_bit(unsigned m, int n) {
   return pos;
 }
 
+// the tiles that get an exclusion mask whatever their pairs hold (diagonal, and
+// those with a system's padded last block) and the ones k_mask_mark finds with
+// a bonded pair: each tile once (need: one bit per tile), in the mask list
+__device__ __forceinline__ void mask_list_add(unsigned* need, int* mlist, int* nml, int mask_cap, int t) {
+  const unsigned bit = 1u << (t & 31);
+  if (atomicOr(&need[t >> 5], bit) & bit) return;
+  const int k = atomicAdd(nml, 1);
+  if (k < mask_cap) mlist[k] = t;
+}
+
 // one warp per row bi, 4 warps per CTA, `words` bitmap words per warp in
-// dynamic shared memory.  COUNT: tiles of the row -> row_cnt.  WRITE: the row's
-// tiles from row_start[bi] (positions past `cap` are dropped; the last row
-// stores the tile count, clamped to cap, and flags an overflow)
-template <bool WRITE>
+// dynamic shared memory: the row's tiles are found (hits marked in the bitmap),
+// counted, given a place in the list by an atomic on the tile total (rows land
+// in any order, each contiguous with ascending columns) and written there;
+// positions past `cap` are dropped (k_tile_total flags the overflow)
 __global__ void __launch_bounds__(128) k_tile_rows(DevView v, const BlockGrid* grid, const int* cell_off,
                                                    const int* cell_count, const int* cell_blocks, float R,
                                                    float margin, float full_R, float full_margin, int* row_cnt,
-                                                   const int* row_start, long long cap, int words) {
+                                                   int* row_start, long long cap, int words, int* total,
+                                                   unsigned* need, int* mlist, int* nml) {
   extern __shared__ unsigned s_bits[];
   const int lane = threadIdx.x & 31;
   const int bi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -488,17 +501,27 @@ __global__ void __launch_bounds__(128) k_tile_rows(DevView v, const BlockGrid* g
     hi[c] = b;
   }
   const unsigned lt = (1u << lane) - 1u;
-  long long n = 0;   // tiles of the row so far
-  const long long base = WRITE ? (long long)row_start[bi] : 0;
+  long long n = 0;   // tiles of the row
+  long long base = 0;
   if (all) {
+    // count, take the row's place, then write (the test is cheap: no cell walk)
+#pragma unroll 2
+    for (int j0 = bi; j0 < end; j0 += 32) {
+      const int bj = j0 + lane;
+      int fl = 0;
+      n += __popc(__ballot_sync(0xffffffffu, bj < end && tile_test(v, S, bi, bj, R, margin, 0.f, 0.f, fl)));
+    }
+    if (lane == 0) base = atomicAdd(total, (int)n);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    long long w = 0;
 #pragma unroll 2
     for (int j0 = bi; j0 < end; j0 += 32) {
       const int bj = j0 + lane;
       int fl = 0;
       const bool hit = bj < end && tile_test(v, S, bi, bj, R, margin, full_R, full_margin, fl);
       const unsigned m = __ballot_sync(0xffffffffu, hit);
-      if (WRITE && hit) write_tile(v, S, bi, bj, fl, base + n + __popc(m & lt), cap);
-      n += __popc(m);
+      if (hit) write_tile(v, S, bi, bj, fl, base + w + __popc(m & lt), cap);
+      w += __popc(m);
     }
   } else {
     const int nw = (end - bi + 31) >> 5;
@@ -537,9 +560,9 @@ __global__ void __launch_bounds__(128) k_tile_rows(DevView v, const BlockGrid* g
         const int t = __shfl_up_sync(0xffffffffu, inc, o);
         if (lane >= o) inc += t;
       }
-      const int total = __shfl_sync(0xffffffffu, inc, 31);
+      const int cnt = __shfl_sync(0xffffffffu, inc, 31);
       const int excl = inc - len;
-      for (int t0 = 0; t0 < total; t0 += 32) {
+      for (int t0 = 0; t0 < cnt; t0 += 32) {
         const int t = t0 + lane;
         // the run holding entry t: the last lane whose runs start at or before t
         int L = 0;
@@ -547,7 +570,7 @@ __global__ void __launch_bounds__(128) k_tile_rows(DevView v, const BlockGrid* g
         for (int b = 16; b > 0; b >>= 1)
           if (__shfl_sync(0xffffffffu, excl, L + b) <= t) L += b;
         const int p = __shfl_sync(0xffffffffu, p0, L) + t - __shfl_sync(0xffffffffu, excl, L);
-        if (t < total) {
+        if (t < cnt) {
           const int bj = cell_blocks[p];
           int fl;
           if (bj >= bi && tile_test(v, S, bi, bj, R, margin, 0.f, 0.f, fl))
@@ -556,48 +579,65 @@ __global__ void __launch_bounds__(128) k_tile_rows(DevView v, const BlockGrid* g
       }
     }
     __syncwarp();
+    int k = 0;
+    for (int w = lane; w < nw; w += 32) k += __popc(bits[w]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+    n = k;
+    if (lane == 0) base = atomicAdd(total, (int)n);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    long long done = 0;
     for (int w0 = 0; w0 < nw; w0 += 32) {
       const int w = w0 + lane;
       const unsigned word = w < nw ? bits[w] : 0u;
-      const int k = __popc(word);
-      int inc = k;
+      const int kw = __popc(word);
+      int inc = kw;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const int t = __shfl_up_sync(0xffffffffu, inc, o);
         if (lane >= o) inc += t;
       }
       const int tot = __shfl_sync(0xffffffffu, inc, 31);
-      if (WRITE) {
-        // the hits of these 32 words dealt over the lanes, in column order
-        const int excl = inc - k;
-        for (int t0 = 0; t0 < tot; t0 += 32) {
-          const int t = t0 + lane;
-          int L = 0;
+      // the hits of these 32 words dealt over the lanes, in column order
+      const int excl = inc - kw;
+      for (int t0 = 0; t0 < tot; t0 += 32) {
+        const int t = t0 + lane;
+        int L = 0;
 #pragma unroll
-          for (int b = 16; b > 0; b >>= 1)
-            if (__shfl_sync(0xffffffffu, excl, L + b) <= t) L += b;
-          const unsigned wl = __shfl_sync(0xffffffffu, word, L);
-          const int nth = t - __shfl_sync(0xffffffffu, excl, L);
-          if (t < tot) {
-            const int bj = bi + 32 * (w0 + L) + nth_set_bit(wl, nth);
-            int fl = 0;
-            tile_test(v, S, bi, bj, R, margin, full_R, full_margin, fl);
-            write_tile(v, S, bi, bj, fl, base + n + t, cap);
-          }
+        for (int b = 16; b > 0; b >>= 1)
+          if (__shfl_sync(0xffffffffu, excl, L + b) <= t) L += b;
+        const unsigned wl = __shfl_sync(0xffffffffu, word, L);
+        const int nth = t - __shfl_sync(0xffffffffu, excl, L);
+        if (t < tot) {
+          const int bj = bi + 32 * (w0 + L) + nth_set_bit(wl, nth);
+          int fl = 0;
+          tile_test(v, S, bi, bj, R, margin, full_R, full_margin, fl);
+          write_tile(v, S, bi, bj, fl, base + done + t, cap);
         }
       }
-      n += tot;
+      done += tot;
     }
   }
   if (lane == 0) {
-    if (!WRITE) {
-      row_cnt[bi] = (int)n;
-    } else if (bi == v.nblocks - 1) {
-      const long long total = base + n;
-      *v.ntiles = (int)(total < cap ? total : cap);
-      if (total > cap) atomicOr(v.status, (unsigned)ST_TILE_OVERFLOW);
-    }
+    row_start[bi] = (int)base;
+    row_cnt[bi] = (int)n;
+    // the diagonal tile is the row's first; a tile with the system's padded
+    // last block, its last
+    if (base < cap) mask_list_add(need, mlist, nml, v.mask_cap, (int)base);
+    const int last = end - 1;
+    int fl;
+    if (S.natom != S.npad && bi != last && n > 1 && base + n - 1 < cap &&
+        tile_test(v, S, bi, last, R, margin, 0.f, 0.f, fl))
+      mask_list_add(need, mlist, nml, v.mask_cap, (int)(base + n - 1));
   }
+}
+
+// the tile count from the rows' total, clamped to the capacity (an overflow
+// leaves a short list and is flagged)
+__global__ void k_tile_total(DevView v, const int* total, long long cap) {
+  const long long t = *total;
+  *v.ntiles = (int)(t < cap ? t : cap);
+  if (t > cap) atomicOr(v.status, (unsigned)ST_TILE_OVERFLOW);
 }
 
 // index of tile (bi, bj) in the list (rows contiguous, ascending columns), -1 if absent
@@ -615,11 +655,10 @@ __device__ __forceinline__ int tile_index(const DevView& v, const int* row_start
 }
 
 // exclusion masks in rotation order (bit k <-> j slot (lane+k)&31); one warp per tile
-// tiles holding a bonded pair (bond order <= 3: excluded or 1-4), marked from
-// each atom's partners (band words, far list): need[tile] = 1.  Diagonal tiles
-// and tiles with padding slots are recognised in k_masks.
+// tiles holding a bonded pair (bond order <= 3: excluded or 1-4), found from
+// each atom's partners (band words, far list) and added to the mask list
 __global__ void k_mask_mark(DevView v, const int* slot_of, const int* row_start, const int* row_cnt,
-                            unsigned char* need) {
+                            unsigned* need, int* mlist, int* nml) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= v.natom) return;
   const unsigned long long w = v.band_excl[a] | v.band_14[a];
@@ -629,29 +668,29 @@ __global__ void k_mask_mark(DevView v, const int* slot_of, const int* row_start,
   int last = ga;
   auto mark = [&](int b) {
     const int gb = slot_of[b] >> 5;
-    // (diagonal tiles get their masks anyway; partners of one block come in runs)
+    // (diagonal tiles are in the list already; partners of one block come in runs)
     if (gb == last || gb == ga) return;
     last = gb;
     const int t = tile_index(v, row_start, row_cnt, ga < gb ? ga : gb, ga < gb ? gb : ga);
-    if (t >= 0) need[t] = 1;
+    if (t >= 0) mask_list_add(need, mlist, nml, v.mask_cap, t);
   };
   for (unsigned long long m = w; m; m &= m - 1) mark(a + __ffsll((long long)m));
   for (int q = fs; q < fe; q++)
     if (v.far_bo[q] <= 3) mark(v.far_idx[q]);
 }
 
-// grid-stride over the tiles, one warp per tile; tiles without a bonded pair,
-// padding slot or diagonal get no mask and skip the pair loop
-__global__ void k_masks(DevView v, const unsigned char* need) {
+// one warp per tile of the mask list (grid-stride): the tile's exclusion and
+// 1-4 bits, a mask table entry when any is set
+__global__ void k_masks(DevView v, const int* mlist, const int* nml) {
   const int lane = threadIdx.x & 31;
-  const int nt = *v.ntiles;
+  const int n = min(*nml, v.mask_cap);
+  if (*nml > v.mask_cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(v.status, (unsigned)ST_TILE_OVERFLOW);
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < nt; warp += nwarps) {
+  for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += nwarps) {
+    const int warp = mlist[e];
     Tile T = v.tiles[warp];
     int ai = v.sorted_atom[T.bi * 32 + lane];
     int aj0 = v.sorted_atom[T.bj * 32 + lane];
-    bool diag = T.flags & 2;
-    if (!need[warp] && !diag && __all_sync(0xffffffffu, ai >= 0 && aj0 >= 0)) continue;
     // each atom's band words and far-partner range, loaded once per lane (the
     // lower index of a pair holds them, as in pair_bondorder); j's are shuffled in
     unsigned long long exi = 0ull, b14i = 0ull, exj0 = 0ull, b14j0 = 0ull;
@@ -824,8 +863,8 @@ __global__ void k_cull_groups(int nb, int* row) {
   if (b < nb) row[2 * nb + b] = (row[b] + 31) >> 5;
 }
 
-// pos: exclusive scan of the kept counts over the tile list (row-major, so a
-// row's entries keep tile order, then lane order)
+// pos: exclusive scan of the kept counts over the tile list (a row's tiles are
+// contiguous, so its entries keep tile order, then lane order)
 __global__ void k_cull_write(DevView v, const unsigned* jmask, const int* pos, const int* row) {
   const int lane = threadIdx.x & 31;
   const int nt = *v.ntiles;
@@ -905,24 +944,23 @@ static void launch_cull(Context& c, float list_radius) {
 }
 
 // rows of the tile-list build: 4 warps per CTA, a bitmap over each warp's row
-static void launch_rows(Context& c, bool write, float R, float full_radius) {
+// (the row total, the mask list and the need bits zeroed beforehand)
+static void launch_rows(Context& c, float R, float full_radius) {
   const int words = (c.max_sys_blocks + 31) / 32 + 1;
   const size_t smem = (size_t)4 * words * sizeof(unsigned);
   DevView v = c.view();
   const int g = nblk((long long)c.nblocks * 32, 128);
-  const float pad = (float)c.lp.Padding;
-  if (write)
-    k_tile_rows<true><<<g, 128, smem, c.stream>>>(v, c.d_bgrid.p, c.d_bcell_off.p, c.d_bcell_count.p,
-                                                   c.d_bcell_blocks.p, R, pad, full_radius, c.full_margin(),
-                                                   c.d_row_cnt.p, c.d_row_start.p, c.tile_cap, words);
-  else
-    k_tile_rows<false><<<g, 128, smem, c.stream>>>(v, c.d_bgrid.p, c.d_bcell_off.p, c.d_bcell_count.p,
-                                                    c.d_bcell_blocks.p, R, pad, 0.f, 0.f, c.d_row_cnt.p,
-                                                    c.d_row_start.p, c.tile_cap, words);
+  int* cnt = c.d_counters.p;
+  cudaMemsetAsync(cnt + 6, 0, 2 * sizeof(int), c.stream);
+  cudaMemsetAsync(c.d_tile_need.p, 0, sizeof(unsigned) * c.d_tile_need.n, c.stream);
+  k_tile_rows<<<g, 128, smem, c.stream>>>(v, c.d_bgrid.p, c.d_bcell_off.p, c.d_bcell_count.p, c.d_bcell_blocks.p, R,
+                                          (float)c.lp.Padding, full_radius, c.full_margin(), c.d_row_cnt.p,
+                                          c.d_row_start.p, c.tile_cap, words, cnt + 6, c.d_tile_need.p,
+                                          c.d_mlist.p, cnt + 7);
 }
 
 int launch_list_build(Context& c, float list_radius, float full_radius, ListSizing sizing) {
-  c.kernel_launches += 16;   // and three scans
+  c.kernel_launches += 16;   // and two scans
   DevView v = c.view();
   cudaStream_t st = c.stream;
   int ncells = c.nsys * kCellsPerSystem;
@@ -955,31 +993,30 @@ int launch_list_build(Context& c, float list_radius, float full_radius, ListSizi
   scan_ints(c, c.d_bcell_count.p, c.d_bcell_off.p, c.d_bcell_scan_tmp.p, c.nblocks, st);
   k_bgrid_scatter<<<nblk(c.nblocks, 256), 256, 0, st>>>(c.nblocks, c.d_bcell.p, c.d_bcell_off.p,
                                                          c.d_bcell_cursor.p, c.d_bcell_blocks.p);
-  launch_rows(c, false, list_radius, full_radius);
-  scan_ints(c, c.d_row_cnt.p, c.d_row_start.p, c.d_row_scan_tmp.p, c.nblocks, st);
+  launch_rows(c, list_radius, full_radius);
   if (sizing != kListDevice) {
-    // the tile count (last row's start + count) against the capacity
-    int last[2] = {0, 0};
-    if (cudaMemcpyAsync(&last[0], c.d_row_start.p + c.nblocks - 1, sizeof(int), cudaMemcpyDeviceToHost, st) !=
-            cudaSuccess ||
-        cudaMemcpyAsync(&last[1], c.d_row_cnt.p + c.nblocks - 1, sizeof(int), cudaMemcpyDeviceToHost, st) !=
-            cudaSuccess ||
+    // the tile count against the capacity: a list that outgrew the arrays is
+    // rebuilt into grown ones
+    int total = 0;
+    if (cudaMemcpyAsync(&total, c.d_counters.p + 6, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
       return PDGPU_ERR_CUDA;
-    const long long total = (long long)last[0] + last[1];
     if (total > c.tile_cap) {
       if (sizing == kListCheck) return PDGPU_ERR_CAPACITY;
       const int e = alloc_tiles(c, total);
       if (e != PDGPU_OK) return e;
       v = c.view();
+      c.kernel_launches += 1;
+      launch_rows(c, list_radius, full_radius);
     }
   }
   cudaMemsetAsync(c.d_counters.p, 0, sizeof(int) * 6, st);
-  launch_rows(c, true, list_radius, full_radius);
-  cudaMemsetAsync(c.d_tile_need.p, 0, c.tile_cap, st);
+  k_tile_total<<<1, 1, 0, st>>>(v, c.d_counters.p + 6, c.tile_cap);
   k_mask_mark<<<nblk(c.natom, 256), 256, 0, st>>>(v, c.d_slot_of.p, c.d_row_start.p, c.d_row_cnt.p,
-                                                   c.d_tile_need.p);
-  k_masks<<<list_tile_grid(c), 256, 0, st>>>(v, c.d_tile_need.p);
+                                                   c.d_tile_need.p, c.d_mlist.p, c.d_counters.p + 7);
+  k_masks<<<nblk((long long)c.mask_cap * 32, 256) < list_tile_grid(c) ? nblk((long long)c.mask_cap * 32, 256)
+                                                                       : list_tile_grid(c),
+            256, 0, st>>>(v, c.d_mlist.p, c.d_counters.p + 7);
   if (c.has_gb) {
     c.kernel_launches += 2;   // and a scan
     const int pairs = c.gb_item_tiles == 2 ? 1 : 0;

@@ -443,15 +443,15 @@ pdgpu_ctx* pdgpu_create(int device, const pdgpu_system_desc* d, int* status) {
   if (e == cudaSuccess) e = c.d_bcell_blocks.alloc(c.nblocks);
   if (e == cudaSuccess) e = c.d_row_cnt.alloc(c.nblocks);
   if (e == cudaSuccess) e = c.d_row_start.alloc(c.nblocks);
-  if (e == cudaSuccess) e = c.d_row_scan_tmp.alloc((c.nblocks + 1023) / 1024 + 1);
   if (e == cudaSuccess) e = c.d_sorted_atom.alloc(c.nslots);
   if (e == cudaSuccess) e = c.d_slot_of.alloc(N);
   if (e == cudaSuccess) e = c.d_center.alloc(3 * (size_t)c.nblocks);
   if (e == cudaSuccess) e = c.d_half.alloc(c.nblocks);
   // (the tile arrays are sized by the first list build, from its tile count)
-  if (e == cudaSuccess) e = c.d_counters.alloc(6);
-  if (e == cudaSuccess) e = cudaMemset(c.d_counters.p, 0, sizeof(int) * 6);
+  if (e == cudaSuccess) e = c.d_counters.alloc(8);
+  if (e == cudaSuccess) e = cudaMemset(c.d_counters.p, 0, sizeof(int) * 8);
   if (e == cudaSuccess) e = c.d_masks.alloc((size_t)c.mask_cap * 32);
+  if (e == cudaSuccess) e = c.d_mlist.alloc(c.mask_cap);
   if (e == cudaSuccess) e = c.d_xq.alloc(c.nslots);
   if (e == cudaSuccess) e = c.d_par.alloc(c.nslots);
   if (e == cudaSuccess) e = c.d_rel0.alloc(c.nslots);
@@ -571,7 +571,7 @@ int pdgpu::alloc_tiles(Context& c, long long tiles) {
   if (e == cudaSuccess && c.has_gb) e = c.d_items.alloc(cap);
   if (e == cudaSuccess) e = c.d_tile_flag.alloc(cap);
   if (e == cudaSuccess) e = c.d_tile_pos.alloc(cap);
-  if (e == cudaSuccess) e = c.d_tile_need.alloc(cap);
+  if (e == cudaSuccess) e = c.d_tile_need.alloc(cap / 32 + 1);
   if (e == cudaSuccess) e = c.d_scan_tmp2.alloc((cap + 1023) / 1024 + 1);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -1088,7 +1088,7 @@ int pdgpu_list_tiles(pdgpu_ctx* h, int* tiles, long long cap, long long* ntiles,
   if (list_bytes) {
     // the arrays whose size follows the list
     *list_bytes = (long long)(c.d_tiles.n * sizeof(Tile) + c.d_items.n * 4 + c.d_tile_flag.n * 4 +
-                              c.d_tile_pos.n * 4 + c.d_scan_tmp2.n * 4 + c.d_tile_need.n +
+                              c.d_tile_pos.n * 4 + c.d_scan_tmp2.n * 4 + c.d_tile_need.n * 4 + c.d_mlist.n * 4 +
                               c.d_masks.n * sizeof(uint2) + c.d_cull_mask.n * 4 + c.d_cull_rest.n * 4 +
                               c.d_cull_ent.n * sizeof(float4) + c.d_cull_bi.n * 4);
   }

@@ -111,11 +111,14 @@ struct Context {
   DBuf<int> d_bcell;           // [nblocks] cell of each block
   DBuf<int> d_bcell_count, d_bcell_off, d_bcell_cursor, d_bcell_scan_tmp;  // [nblocks] cells
   DBuf<int> d_bcell_blocks;    // [nblocks] blocks in cell order
-  DBuf<int> d_row_cnt, d_row_start, d_row_scan_tmp;  // [nblocks] tiles per row, first tile of each row
-  DBuf<Tile> d_tiles;          // [tile_cap] row-major tile list, ascending columns
+  DBuf<int> d_row_cnt, d_row_start;  // [nblocks] tiles per row, first tile of each row
+  DBuf<Tile> d_tiles;          // [tile_cap] rows contiguous (any order), ascending columns
   DBuf<int> d_tile_flag, d_tile_pos, d_scan_tmp2;  // [tile_cap] compaction scratch (GB items, NB groups)
-  DBuf<unsigned char> d_tile_need;                  // [tile_cap] tile holds a bonded pair (mask build)
-  DBuf<int> d_counters;        // [0] ntiles, [1] nmasks, [2] nitems, [3..5] NB groups (rest tiles, groups, fit)
+  DBuf<unsigned> d_tile_need;  // [tile_cap/32 + 1] one bit per tile: in the mask list
+  DBuf<int> d_mlist;           // [mask_cap] tiles that get their exclusion bits (diagonal, padded, bonded)
+  // [0] ntiles, [1] nmasks, [2] nitems, [3..5] NB groups (rest tiles, groups, fit),
+  // [6] tiles the rows found (before the capacity clamp), [7] mask-list length
+  DBuf<int> d_counters;
   DBuf<unsigned> d_items;      // [tile_cap] GB work items (with GB only)
   DBuf<uint2> d_masks;         // [mask_cap*32]
   DBuf<float4> d_xq, d_par, d_rel0;  // [nslots]

@@ -10,8 +10,8 @@ taken at the minimum image.  The device decides in FP32, 1e-3 A to the safe
 side; the host scan below is in FP64, so it checks that:
   - every pair closer than R - 1e-3 A is a tile (the grid misses nothing);
   - every tile is closer than R + 2e-3 A (nothing stray);
-  - rows come in ascending order, with columns ascending inside a row, and
-    no pair twice.
+  - each row's tiles sit together with ascending columns (rows take their
+    places in the list by an atomic, in any order), and no pair comes twice.
 """
 import numpy as np
 import pytest
@@ -59,9 +59,13 @@ def _check_list(ctx, image, R):
     tiles, cap, _ = ctx.list_tiles()
     centre, half, bsys, _ = _blocks(ctx, image)
     bi, bj = tiles[:, 0].astype(np.int64), tiles[:, 1].astype(np.int64)
-    # order: rows ascending, columns ascending inside a row, each pair once
+    # each row contiguous with ascending columns, each pair once
+    starts = np.flatnonzero(np.r_[True, bi[1:] != bi[:-1]])
+    assert len(starts) == len(np.unique(bi)), "a row's tiles are split"
+    same = bi[1:] == bi[:-1]
+    assert np.all(bj[1:][same] > bj[:-1][same])
     key = bi * len(centre) + bj
-    assert np.all(np.diff(key) > 0)
+    assert len(np.unique(key)) == len(key)
     assert np.all(bj >= bi) and np.all(bsys[bi] == bsys[bj])
     assert len(tiles) <= cap
     got = set(key.tolist())
