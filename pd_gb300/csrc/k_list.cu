@@ -449,7 +449,8 @@ __device__ __forceinline__ int nth_set_bit(unsigned m, int n) {
 // a bonded pair: each tile once (need: one bit per tile), in the mask list
 __device__ __forceinline__ void mask_list_add(unsigned* need, int* mlist, int* nml, int mask_cap, int t) {
   const unsigned bit = 1u << (t & 31);
-  if (atomicOr(&need[t >> 5], bit) & bit) return;
+  // (a plain read first: most marks repeat a tile already in the list)
+  if ((need[t >> 5] & bit) || (atomicOr(&need[t >> 5], bit) & bit)) return;
   const int k = atomicAdd(nml, 1);
   if (k < mask_cap) mlist[k] = t;
 }
