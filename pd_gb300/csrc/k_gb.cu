@@ -788,9 +788,11 @@ __device__ __forceinline__ void gb_pair_items(const DevView& v, const GBConst& k
   }
 }
 
-// the force-only pass (every dynamics step) keeps three CTAs per SM; the energy
-// pass carries FP64 records of its close pairs and gets more registers
-__global__ void __launch_bounds__(256, 3) k_gb_pair(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* born, long long* deda) {
+// the force-only pass (every dynamics step) runs in CTAs of 128 threads, seven
+// per SM (28 warps at 72 registers; 3 CTAs of 256 hold 24 at 80), launched as
+// twice the tile kernels' CTA count; the energy pass carries FP64 records of
+// its close pairs and gets more registers
+__global__ void __launch_bounds__(128, 7) k_gb_pair(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* born, long long* deda) {
   gb_pair_items<0>(v, k, born, deda);
 }
 __global__ void __launch_bounds__(256, 2) k_gb_pair_energy(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* born,
@@ -1084,7 +1086,7 @@ int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset
     if (ke.e64_r2 > 0.f) k_gb_pair_energy<<<g, 256, 0, st>>>(v, ke, c.d_born_f.p, c.d_deda.p);
     else k_gb_pair_energy32<<<g, 256, 0, st>>>(v, ke, c.d_born_f.p, c.d_deda.p);
   } else {
-    k_gb_pair<<<g, 256, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
+    k_gb_pair<<<2 * g, 128, 0, st>>>(v, k, c.d_born_f.p, c.d_deda.p);
   }
   k_gb_self<<<nb, 256, 0, st>>>(v, c.d_charge.p, k, premul, c.d_deda.p, c.d_born_d.p, c.d_chain_f.p,
                                 energy ? 1 : 0);
@@ -1099,7 +1101,7 @@ int launch_gb_stage(Context& c, const GBConst& k, int stage) {
   int g = tile_grid(c);
   c.kernel_launches += 1;
   if (stage == 1) k_gb_born<<<g, 256, 0, c.stream>>>(v, k, c.d_gpol.p);
-  else if (stage == 2) k_gb_pair<<<g, 256, 0, c.stream>>>(v, k, c.d_born_f.p, c.d_deda.p);
+  else if (stage == 2) k_gb_pair<<<2 * g, 128, 0, c.stream>>>(v, k, c.d_born_f.p, c.d_deda.p);
   else k_gb_chain<<<g, 256, 0, c.stream>>>(v, k, c.d_chain_f.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
