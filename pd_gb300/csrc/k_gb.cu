@@ -1021,7 +1021,8 @@ __device__ __forceinline__ void chain_full2(const DevView& v, const GBConst& k, 
   flush_force(v, r0 + lane, FR);
 }
 
-__global__ void __launch_bounds__(256) k_gb_chain(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* chain) {
+// CTAs of 128 threads, nine per SM (36 warps at 56 registers; 4 x 256 hold 32 at 64)
+__global__ void __launch_bounds__(128, 9) k_gb_chain(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* chain) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int ni = *v.nitems;
@@ -1091,7 +1092,7 @@ int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset
   k_gb_self<<<nb, 256, 0, st>>>(v, c.d_charge.p, k, premul, c.d_deda.p, c.d_born_d.p, c.d_chain_f.p,
                                 energy ? 1 : 0);
   if (c.gb_no_chain) c.kernel_launches -= 1;
-  else k_gb_chain<<<g, 256, 0, st>>>(v, k, c.d_chain_f.p);
+  else k_gb_chain<<<2 * g, 128, 0, st>>>(v, k, c.d_chain_f.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 
@@ -1102,7 +1103,7 @@ int launch_gb_stage(Context& c, const GBConst& k, int stage) {
   c.kernel_launches += 1;
   if (stage == 1) k_gb_born<<<g, 256, 0, c.stream>>>(v, k, c.d_gpol.p);
   else if (stage == 2) k_gb_pair<<<2 * g, 128, 0, c.stream>>>(v, k, c.d_born_f.p, c.d_deda.p);
-  else k_gb_chain<<<g, 256, 0, c.stream>>>(v, k, c.d_chain_f.p);
+  else k_gb_chain<<<2 * g, 128, 0, c.stream>>>(v, k, c.d_chain_f.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

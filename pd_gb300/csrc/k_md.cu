@@ -81,7 +81,7 @@ __global__ void k_vv(MDView m, double dt) {
   double tm = 0.0;
   if (valid) {
     atom_force(m, a, f);
-    tm = 0.5 * dt / m.mass[a];
+    tm = 0.5 * dt * m.mterms[a].x;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       v[c] = m.vel[3 * a + c] + f[c] * tm;
@@ -110,11 +110,12 @@ __global__ void k_langevin(MDView m, LangevinCoeffs L, int first_step, int last_
   const bool valid = a < m.natom;
   const unsigned long long step = *m.stepc;
   double f[3] = {0.0, 0.0, 0.0}, v[3] = {0.0, 0.0, 0.0};
-  double inv_mass = 0.0, tm = 0.0;
+  double2 mt = make_double2(0.0, 0.0);
+  double tm = 0.0;
   if (valid) {
     atom_force(m, a, f);
-    inv_mass = 1.0 / m.mass[a];
-    tm = L.dt * inv_mass;
+    mt = m.mterms[a];
+    tm = L.dt * mt.x;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       v[c] = m.vel[3 * a + c];
@@ -124,8 +125,8 @@ __global__ void k_langevin(MDView m, LangevinCoeffs L, int first_step, int last_
   add_ke(m, a, valid, v);
   if (!valid) return;
   if (!last_step) {
-    const double T = m.temp[m.atom_sys[a]];
-    const double s = sqrt(1.38065E-23 * T * inv_mass);
+    // sqrt(k_B T / m): the temperature's root in FP32 (it only scales the noise)
+    const double s = (double)sqrtf((float)m.temp[m.atom_sys[a]]) * mt.y;
     const double sigmav = s * L.sv;
     const double sigmar = s * L.sr;
     // six normals, in PD's draw order n1x n2y | n2x n1z | n1y n2z (md.cpp:1017-1019)

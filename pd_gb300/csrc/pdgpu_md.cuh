@@ -20,6 +20,7 @@ struct MDState {
   unsigned long long exchange_round = 0;
   bool trajectory_started = false;
   DBuf<double> d_vel;                 // [natom*3] m/s
+  DBuf<double2> d_mterms;             // [natom] (1 / mass, sqrt(k_B / mass)), SI
   DBuf<unsigned long long> d_step;    // [1] device copy of the step counter
   DBuf<double> d_temp;                // [nsys] target temperature of each system (K)
   DBuf<double> d_ladder;              // [nsys] temperature of each rung (K)
@@ -51,6 +52,7 @@ struct MDView {
   const int* slot_of;
   const int* atom_sys;
   const double* mass;
+  const double2* mterms;     // (1 / mass, sqrt(k_B / mass)): no FP64 divide or root per step
   double* pos;
   double* vel;
   const double* temp;
@@ -67,6 +69,7 @@ inline MDView md_view(Context& c, MDState& md) {
   m.slot_of = c.d_slot_of.p;
   m.atom_sys = c.d_atom_sys.p;
   m.mass = c.d_mass.p;
+  m.mterms = md.d_mterms.p;
   m.pos = c.d_pos.p;
   m.vel = md.d_vel.p;
   m.temp = md.d_temp.p;

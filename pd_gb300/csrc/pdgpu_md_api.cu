@@ -49,6 +49,12 @@ void invalidate_graphs(MDState& md) {
   md.graphs.clear();
 }
 
+// per-atom mass terms of the integrators: 1 / m and sqrt(k_B / m) (md.cpp:951-960)
+__global__ void k_mass_terms(const double* mass, double2* out, int n) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a < n) out[a] = make_double2(1.0 / mass[a], sqrt(1.38065E-23 / mass[a]));
+}
+
 // kinetic energies from their fixed-point sums to J (pdgpu_get_kinetic_async)
 __global__ void k_ke_joules(const long long* ke, double* out, int nsys) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -208,7 +214,7 @@ int pdgpu_md_setup(pdgpu_ctx* h, const pdgpu_md_params* p, const double* temps) 
   md.p = *p;
   md.L = coeffs(p->FricCoeff, p->Timestep);
   const size_t N = c.natom;
-  if (md.d_vel.alloc(3 * N) != cudaSuccess || md.d_temp.alloc(c.nsys) != cudaSuccess ||
+  if (md.d_vel.alloc(3 * N) != cudaSuccess || md.d_mterms.alloc(N) != cudaSuccess || md.d_temp.alloc(c.nsys) != cudaSuccess ||
       md.d_ladder.alloc(c.nsys) != cudaSuccess || md.d_temp_sys.alloc(c.nsys) != cudaSuccess ||
       md.d_vscale.alloc(c.nsys) != cudaSuccess || md.d_accepted.alloc(c.nsys) != cudaSuccess ||
       md.d_ke.alloc(c.nsys) != cudaSuccess || md.d_ke_j.alloc(c.nsys) != cudaSuccess ||
@@ -221,6 +227,9 @@ int pdgpu_md_setup(pdgpu_ctx* h, const pdgpu_md_params* p, const double* temps) 
   std::vector<int> order(c.nsys);
   for (int s = 0; s < c.nsys; s++) order[s] = s;
   CK(cudaMemsetAsync(md.d_vel.p, 0, sizeof(double) * 3 * N, c.stream));
+  k_mass_terms<<<(c.natom + 255) / 256, 256, 0, c.stream>>>(c.d_mass.p, md.d_mterms.p, c.natom);
+  c.kernel_launches += 1;
+  CK(cudaGetLastError());
   CK(cudaMemcpyAsync(md.d_temp.p, temps, sizeof(double) * c.nsys, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(md.d_ladder.p, temps, sizeof(double) * c.nsys, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(md.d_temp_sys.p, order.data(), sizeof(int) * c.nsys, cudaMemcpyHostToDevice, c.stream));
