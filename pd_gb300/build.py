@@ -17,6 +17,11 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpdgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# FP32 denormals flush to zero: the special-function instructions (rsqrt, rcp,
+# ex2) then run without their denormal fix-up sequences (the three GB passes of
+# the 64-peptide batch: 1.96 -> 1.81 ms); no FP32 quantity of the path comes
+# near 1e-38, and FP64 arithmetic is unaffected.
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-ftz=true"]
 
 
 def nvcc():
@@ -32,7 +37,7 @@ def sources():
 
 def _compile(src, extra):
     obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
+    cmd = [nvcc(), *ARCH, *FLAGS, "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
            "-c", src, "-o", obj, *extra]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -46,6 +51,7 @@ def up_to_date():
     t = os.path.getmtime(LIB)
     deps = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
     deps.append(os.path.join(ROOT, "include", "pdgpu.h"))
+    deps.append(os.path.abspath(__file__))
     return all(os.path.getmtime(d) <= t for d in deps)
 
 

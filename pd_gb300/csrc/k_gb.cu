@@ -153,43 +153,64 @@ __device__ __forceinline__ float pair_contact2(const GBConst& k, float2 RS, floa
   return m * m * k.invP5 * 1.0001f;
 }
 
+// Step-packed lean bodies: lane l holds the rotating block's atoms l + kk and
+// l + kk + 1 as one FP32x2 register pair (and their running sums), so a packed
+// instruction covers two rotation steps of one held atom, whose values are
+// broadcast into both halves once per item.  Each rotation moves the pair two
+// lanes; after 16 of them lane l's pair holds the sums of atoms l and l + 1.
+#define ROT2(p) p.x = __shfl_sync(0xffffffffu, p.x, (lane + 2) & 31); p.y = __shfl_sync(0xffffffffu, p.y, (lane + 2) & 31)
+
+// the CCF of one pair: 1 outside close contact
+__device__ __forceinline__ float born_ccf(const GBConst& k, float r2, float rs) {
+  const float rs2 = rs * rs;
+  if (!gb_contact(k, r2, rs2)) return 1.f;
+  const float h = 0.5f - 0.5f * cospif(__fdividef(r2, rs2) * k.P5);
+  return h * h;
+}
+
 __device__ __forceinline__ void born_full2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B, int lane,
                                            long long* gpol) {
   const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
+  const int l1 = (lane + 1) & 31;
   const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
   const float4 pa = v.par[sa], pb = v.par[sb];
-  const float2 nx = make_float2(-xa.x, -xb.x), ny = make_float2(-xa.y, -xb.y), nz = make_float2(-xa.z, -xb.z);
-  const float2 RS = make_float2(pa.z, pb.z), VP = make_float2(k.P4 * pa.w, k.P4 * pb.w);
-  float4 xr = v.xq[r0 + lane];
-  const float4 pr = v.par[r0 + lane];
-  float Rr = pr.z, VPr = k.P4 * pr.w, gr = 0.f;
-  const float c2 = pair_contact2(k, RS, Rr);
-  float2 G = f2(0.f);
-#pragma unroll 4
-  for (int kk = 0; kk < 32; kk++) {
-    const float2 dx = __fadd2_rn(f2(xr.x), nx), dy = __fadd2_rn(f2(xr.y), ny), dz = __fadd2_rn(f2(xr.z), nz);
-    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
-    const float2 ir2 = make_float2(__fdividef(1.f, r2.x), __fdividef(1.f, r2.y));
-    float2 w = __fmul2_rn(ir2, ir2);
-    if (__any_sync(0xffffffffu, r2.x <= c2 || r2.y <= c2)) {
-      const float2 rs = __fadd2_rn(RS, f2(Rr)), rs2 = __fmul2_rn(rs, rs);
-      if (gb_contact(k, r2.x, rs2.x)) {
-        const float h = 0.5f - 0.5f * cospif(__fdividef(r2.x, rs2.x) * k.P5);
-        w.x *= h * h;
-      }
-      if (gb_contact(k, r2.y, rs2.y)) {
-        const float h = 0.5f - 0.5f * cospif(__fdividef(r2.y, rs2.y) * k.P5);
-        w.y *= h * h;
-      }
+  const float2 AX = f2(-xa.x), AY = f2(-xa.y), AZ = f2(-xa.z), BX = f2(-xb.x), BY = f2(-xb.y), BZ = f2(-xb.z);
+  const float2 VA = f2(k.P4 * pa.w), VB = f2(k.P4 * pb.w);
+  const float4 x0 = v.xq[r0 + lane], x1 = v.xq[r0 + l1];
+  const float4 p0 = v.par[r0 + lane], p1 = v.par[r0 + l1];
+  float2 X = make_float2(x0.x, x1.x), Y = make_float2(x0.y, x1.y), Z = make_float2(x0.z, x1.z);
+  float2 VR = make_float2(k.P4 * p0.w, k.P4 * p1.w);
+  const float c2 = pair_contact2(k, make_float2(pa.z, pb.z), p0.z);
+  float2 GA = f2(0.f), GB = f2(0.f), GR = f2(0.f);
+#pragma unroll 2
+  for (int kk = 0; kk < 32; kk += 2) {
+    const float2 ax = __fadd2_rn(X, AX), ay = __fadd2_rn(Y, AY), az = __fadd2_rn(Z, AZ);
+    const float2 bx = __fadd2_rn(X, BX), by = __fadd2_rn(Y, BY), bz = __fadd2_rn(Z, BZ);
+    const float2 ra = __ffma2_rn(az, az, __ffma2_rn(ay, ay, __fmul2_rn(ax, ax)));
+    const float2 rb = __ffma2_rn(bz, bz, __ffma2_rn(by, by, __fmul2_rn(bx, bx)));
+    const float2 ia = make_float2(__fdividef(1.f, ra.x), __fdividef(1.f, ra.y));
+    const float2 ib = make_float2(__fdividef(1.f, rb.x), __fdividef(1.f, rb.y));
+    float2 wa = __fmul2_rn(ia, ia), wb = __fmul2_rn(ib, ib);
+    if (__any_sync(0xffffffffu, fminf(fminf(ra.x, ra.y), fminf(rb.x, rb.y)) <= c2)) {
+      // rare: the rotating atoms' radii are read here rather than rotated
+      const float R0 = v.par[r0 + ((lane + kk) & 31)].z, R1 = v.par[r0 + ((lane + kk + 1) & 31)].z;
+      wa.x *= born_ccf(k, ra.x, pa.z + R0);
+      wa.y *= born_ccf(k, ra.y, pa.z + R1);
+      wb.x *= born_ccf(k, rb.x, pb.z + R0);
+      wb.y *= born_ccf(k, rb.y, pb.z + R1);
     }
-    G = __ffma2_rn(w, f2(VPr), G);
-    gr = fmaf(w.x, VP.x, gr);
-    gr = fmaf(w.y, VP.y, gr);
-    ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(Rr); ROT(VPr); ROT(gr);
+    GA = __ffma2_rn(wa, VR, GA);
+    GB = __ffma2_rn(wb, VR, GB);
+    GR = __ffma2_rn(wa, VA, GR);
+    GR = __ffma2_rn(wb, VB, GR);
+    ROT2(X); ROT2(Y); ROT2(Z); ROT2(VR); ROT2(GR);
   }
-  fix_range(v.status, fabsf(G.x) + fabsf(G.y) + fabsf(gr));
-  atomic_add_ll(&gpol[sa], fx32(G.x));
-  atomic_add_ll(&gpol[sb], fx32(G.y));
+  // GR.x holds the sum of the rotating atom of this lane, GR.y that of lane + 1
+  const float gr = GR.x + __shfl_sync(0xffffffffu, GR.y, (lane + 31) & 31);
+  const float ga = GA.x + GA.y, gb = GB.x + GB.y;
+  fix_range(v.status, fabsf(ga) + fabsf(gb) + fabsf(gr));
+  atomic_add_ll(&gpol[sa], fx32(ga));
+  atomic_add_ll(&gpol[sb], fx32(gb));
   atomic_add_ll(&gpol[r0 + lane], fx32(gr));
 }
 
