@@ -153,11 +153,14 @@ __device__ __forceinline__ float pair_contact2(const GBConst& k, float2 RS, floa
   return m * m * k.invP5 * 1.0001f;
 }
 
-// Step-packed lean bodies: lane l holds the rotating block's atoms l + kk and
-// l + kk + 1 as one FP32x2 register pair (and their running sums), so a packed
+// Step-packed lean bodies (Born, chain rule): lane l takes the rotating
+// block's atoms l + kk and l + kk + 1 as one FP32x2 register pair, so a packed
 // instruction covers two rotation steps of one held atom, whose values are
-// broadcast into both halves once per item.  Each rotation moves the pair two
-// lanes; after 16 of them lane l's pair holds the sums of atoms l and l + 1.
+// broadcast into both halves once per item.  The rotating block is staged once
+// per item in the warp's own shared-memory rows as step pairs (x_l, x_l+1,
+// y_l, y_l+1) ..., read with one 16-byte load per four values; only its running
+// sums rotate through the warp by shuffles, two lanes per step, so that after
+// 16 rotations lane l's pair holds the sums of atoms l and l + 1.
 #define ROT2(p) p.x = __shfl_sync(0xffffffffu, p.x, (lane + 2) & 31); p.y = __shfl_sync(0xffffffffu, p.y, (lane + 2) & 31)
 
 // the CCF of one pair: 1 outside close contact
@@ -168,8 +171,13 @@ __device__ __forceinline__ float born_ccf(const GBConst& k, float r2, float rs) 
   return h * h;
 }
 
+constexpr int kBornThreads = 256;
+constexpr int kBornWarps = kBornThreads / 32;
+
 __device__ __forceinline__ void born_full2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B, int lane,
                                            long long* gpol) {
+  __shared__ float4 rot_sh[kBornWarps][2][32];   // (x, x', y, y'), (z, z', P4 V, P4 V')
+  float4 (*rs)[32] = rot_sh[threadIdx.x >> 5];
   const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
   const int l1 = (lane + 1) & 31;
   const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
@@ -178,12 +186,18 @@ __device__ __forceinline__ void born_full2(const DevView& v, const GBConst& k, c
   const float2 VA = f2(k.P4 * pa.w), VB = f2(k.P4 * pb.w);
   const float4 x0 = v.xq[r0 + lane], x1 = v.xq[r0 + l1];
   const float4 p0 = v.par[r0 + lane], p1 = v.par[r0 + l1];
-  float2 X = make_float2(x0.x, x1.x), Y = make_float2(x0.y, x1.y), Z = make_float2(x0.z, x1.z);
-  float2 VR = make_float2(k.P4 * p0.w, k.P4 * p1.w);
+  __syncwarp();
+  rs[0][lane] = make_float4(x0.x, x1.x, x0.y, x1.y);
+  rs[1][lane] = make_float4(x0.z, x1.z, k.P4 * p0.w, k.P4 * p1.w);
+  __syncwarp();
   const float c2 = pair_contact2(k, make_float2(pa.z, pb.z), p0.z);
   float2 GA = f2(0.f), GB = f2(0.f), GR = f2(0.f);
 #pragma unroll 2
   for (int kk = 0; kk < 32; kk += 2) {
+    const int j = (lane + kk) & 31;
+    const float4 P = rs[0][j], Q = rs[1][j];
+    const float2 X = make_float2(P.x, P.y), Y = make_float2(P.z, P.w), Z = make_float2(Q.x, Q.y);
+    const float2 VR = make_float2(Q.z, Q.w);
     const float2 ax = __fadd2_rn(X, AX), ay = __fadd2_rn(Y, AY), az = __fadd2_rn(Z, AZ);
     const float2 bx = __fadd2_rn(X, BX), by = __fadd2_rn(Y, BY), bz = __fadd2_rn(Z, BZ);
     const float2 ra = __ffma2_rn(az, az, __ffma2_rn(ay, ay, __fmul2_rn(ax, ax)));
@@ -192,8 +206,8 @@ __device__ __forceinline__ void born_full2(const DevView& v, const GBConst& k, c
     const float2 ib = make_float2(__fdividef(1.f, rb.x), __fdividef(1.f, rb.y));
     float2 wa = __fmul2_rn(ia, ia), wb = __fmul2_rn(ib, ib);
     if (__any_sync(0xffffffffu, fminf(fminf(ra.x, ra.y), fminf(rb.x, rb.y)) <= c2)) {
-      // rare: the rotating atoms' radii are read here rather than rotated
-      const float R0 = v.par[r0 + ((lane + kk) & 31)].z, R1 = v.par[r0 + ((lane + kk + 1) & 31)].z;
+      // rare: the rotating atoms' radii are read here, not staged
+      const float R0 = v.par[r0 + j].z, R1 = v.par[r0 + ((j + 1) & 31)].z;
       wa.x *= born_ccf(k, ra.x, pa.z + R0);
       wa.y *= born_ccf(k, ra.y, pa.z + R1);
       wb.x *= born_ccf(k, rb.x, pb.z + R0);
@@ -203,7 +217,7 @@ __device__ __forceinline__ void born_full2(const DevView& v, const GBConst& k, c
     GB = __ffma2_rn(wb, VR, GB);
     GR = __ffma2_rn(wa, VA, GR);
     GR = __ffma2_rn(wb, VB, GR);
-    ROT2(X); ROT2(Y); ROT2(Z); ROT2(VR); ROT2(GR);
+    ROT2(GR);
   }
   // GR.x holds the sum of the rotating atom of this lane, GR.y that of lane + 1
   const float gr = GR.x + __shfl_sync(0xffffffffu, GR.y, (lane + 31) & 31);
@@ -221,7 +235,7 @@ __device__ __forceinline__ int item_tile(const DevView& v, int it, bool& two) {
   return (int)(code & 0x7fffffffu);
 }
 
-__global__ void __launch_bounds__(256) k_gb_born(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, long long* gpol) {
+__global__ void __launch_bounds__(kBornThreads) k_gb_born(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, long long* gpol) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int ni = *v.nitems;
@@ -988,62 +1002,92 @@ __device__ __forceinline__ void chain_tile2(const DevView& v, const GBConst& k, 
   flush_force(v, r0 + lane, FR);
 }
 
-// Born chain rule of an all-inside tile pair: (c_i V_j + c_j V_i)(4 CCF - dCCF) / r^6
-// along d, with -4 folded into c (w then carries the held atom's sign and the
-// factor 4 of the no-contact case); the CCF branch on the coarse-bound vote.
-__device__ __forceinline__ void chain_full2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B, int lane,
-                                            const float* chain) {
-  const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
-  const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
-  const float4 pa = v.par[sa], pb = v.par[sb];
-  const float2 nx = make_float2(-xa.x, -xb.x), ny = make_float2(-xa.y, -xb.y), nz = make_float2(-xa.z, -xb.z);
-  const float2 RS = make_float2(pa.z, pb.z), VS = make_float2(pa.w, pb.w);
-  const float2 CS = make_float2(-4.f * chain[sa], -4.f * chain[sb]);
-  float4 xr = v.xq[r0 + lane];
-  const float4 pr = v.par[r0 + lane];
-  float Rr = pr.z, Vr = pr.w, Cr = -4.f * chain[r0 + lane];
-  const float c2 = pair_contact2(k, RS, Rr);
-  float2 FX = f2(0.f), FY = f2(0.f), FZ = f2(0.f);
-  PairAcc FR = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 4
-  for (int kk = 0; kk < 32; kk++) {
-    const float2 dx = __fadd2_rn(f2(xr.x), nx), dy = __fadd2_rn(f2(xr.y), ny), dz = __fadd2_rn(f2(xr.z), nz);
-    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
-    const float2 ir2 = make_float2(__fdividef(1.f, r2.x), __fdividef(1.f, r2.y));
-    const float2 ir6 = __fmul2_rn(__fmul2_rn(ir2, ir2), ir2);
-    float2 w = __fmul2_rn(__ffma2_rn(CS, f2(Vr), __fmul2_rn(f2(Cr), VS)), ir6);   // -w of the plain law
-    if (__any_sync(0xffffffffu, r2.x <= c2 || r2.y <= c2)) {
-      const float2 rs = __fadd2_rn(RS, f2(Rr)), rs2 = __fmul2_rn(rs, rs);
-      if (gb_contact(k, r2.x, rs2.x)) {
-        float sn, cs;
-        const float x = __fdividef(r2.x, rs2.x) * k.P5;
-        sincospif(x, &sn, &cs);
-        const float h = 0.5f - 0.5f * cs;
-        w.x *= 0.25f * (4.f * h * h - 2.f * h * sn * (x * 3.14159265358979f));
-      }
-      if (gb_contact(k, r2.y, rs2.y)) {
-        float sn, cs;
-        const float x = __fdividef(r2.y, rs2.y) * k.P5;
-        sincospif(x, &sn, &cs);
-        const float h = 0.5f - 0.5f * cs;
-        w.y *= 0.25f * (4.f * h * h - 2.f * h * sn * (x * 3.14159265358979f));
-      }
-    }
-    FX = __ffma2_rn(w, dx, FX);
-    FY = __ffma2_rn(w, dy, FY);
-    FZ = __ffma2_rn(w, dz, FZ);
-    FR.fx = fmaf(-w.x, dx.x, FR.fx); FR.fx = fmaf(-w.y, dx.y, FR.fx);
-    FR.fy = fmaf(-w.x, dy.x, FR.fy); FR.fy = fmaf(-w.y, dy.y, FR.fy);
-    FR.fz = fmaf(-w.x, dz.x, FR.fz); FR.fz = fmaf(-w.y, dz.y, FR.fz);
-    ROT(xr.x); ROT(xr.y); ROT(xr.z); ROT(Rr); ROT(Vr); ROT(Cr); ROT(FR.fx); ROT(FR.fy); ROT(FR.fz);
-  }
-  flush_force(v, sa, PairAcc{FX.x, FY.x, FZ.x, 0.f});
-  flush_force(v, sb, PairAcc{FX.y, FY.y, FZ.y, 0.f});
-  flush_force(v, r0 + lane, FR);
+// 0.25 (4 CCF - dCCF) of a pair in close contact, 1 otherwise
+__device__ __forceinline__ float chain_fac(const GBConst& k, float r2, float rs) {
+  const float rs2 = rs * rs;
+  if (!gb_contact(k, r2, rs2)) return 1.f;
+  float sn, cs;
+  const float x = __fdividef(r2, rs2) * k.P5;
+  sincospif(x, &sn, &cs);
+  const float h = 0.5f - 0.5f * cs;
+  return 0.25f * (4.f * h * h - 2.f * h * sn * (x * 3.14159265358979f));
 }
 
-// CTAs of 128 threads, nine per SM (36 warps at 56 registers; 4 x 256 hold 32 at 64)
-__global__ void __launch_bounds__(128, 9) k_gb_chain(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* chain) {
+// CTAs of 128 threads, seven per SM (28 warps at 72 registers)
+constexpr int kChainThreads = 128;
+constexpr int kChainWarps = kChainThreads / 32;
+
+// Born chain rule of an all-inside tile pair, step-packed: (c_i V_j + c_j V_i)
+// (4 CCF - dCCF) / r^6 along d, with -4 folded into c (w then carries the held
+// atom's sign and the factor 4 of the no-contact case); the CCF branch on the
+// coarse-bound vote.
+__device__ __forceinline__ void chain_full2(const DevView& v, const GBConst& k, const Tile& A, const Tile& B, int lane,
+                                            const float* chain) {
+  __shared__ float4 rot_sh[kChainWarps][3][32];   // (x, x', y, y'), (z, z', V, V'), (c, c')
+  float4 (*rs)[32] = rot_sh[threadIdx.x >> 5];
+  const int sa = A.bj * 32 + lane, sb = B.bj * 32 + lane, r0 = A.bi * 32;
+  const int l1 = (lane + 1) & 31;
+  const float4 xa = j_in_i_frame(v, A, lane), xb = j_in_i_frame(v, B, lane);
+  const float4 pa = v.par[sa], pb = v.par[sb];
+  const float2 AX = f2(-xa.x), AY = f2(-xa.y), AZ = f2(-xa.z), BX = f2(-xb.x), BY = f2(-xb.y), BZ = f2(-xb.z);
+  const float2 VA = f2(pa.w), VB = f2(pb.w), CA = f2(-4.f * chain[sa]), CB = f2(-4.f * chain[sb]);
+  float c2;
+  {
+    const float4 x0 = v.xq[r0 + lane], p0 = v.par[r0 + lane];
+    const float c0 = -4.f * chain[r0 + lane];
+    const float x1 = __shfl_sync(0xffffffffu, x0.x, l1), y1 = __shfl_sync(0xffffffffu, x0.y, l1);
+    const float z1 = __shfl_sync(0xffffffffu, x0.z, l1), v1 = __shfl_sync(0xffffffffu, p0.w, l1);
+    const float c1 = __shfl_sync(0xffffffffu, c0, l1);
+    c2 = pair_contact2(k, make_float2(pa.z, pb.z), p0.z);
+    __syncwarp();
+    rs[0][lane] = make_float4(x0.x, x1, x0.y, y1);
+    rs[1][lane] = make_float4(x0.z, z1, p0.w, v1);
+    rs[2][lane] = make_float4(c0, c1, 0.f, 0.f);
+    __syncwarp();
+  }
+  float2 FAX = f2(0.f), FAY = f2(0.f), FAZ = f2(0.f), FBX = f2(0.f), FBY = f2(0.f), FBZ = f2(0.f);
+  float2 FRX = f2(0.f), FRY = f2(0.f), FRZ = f2(0.f);   // minus the rotating atoms' sums
+#pragma unroll 2
+  for (int kk = 0; kk < 32; kk += 2) {
+    const int j = (lane + kk) & 31;
+    const float4 P = rs[0][j], Q = rs[1][j];
+    const float2 CR = *reinterpret_cast<const float2*>(&rs[2][j]);
+    const float2 X = make_float2(P.x, P.y), Y = make_float2(P.z, P.w), Z = make_float2(Q.x, Q.y);
+    const float2 VR = make_float2(Q.z, Q.w);
+    const float2 ax = __fadd2_rn(X, AX), ay = __fadd2_rn(Y, AY), az = __fadd2_rn(Z, AZ);
+    const float2 bx = __fadd2_rn(X, BX), by = __fadd2_rn(Y, BY), bz = __fadd2_rn(Z, BZ);
+    const float2 ra = __ffma2_rn(az, az, __ffma2_rn(ay, ay, __fmul2_rn(ax, ax)));
+    const float2 rb = __ffma2_rn(bz, bz, __ffma2_rn(by, by, __fmul2_rn(bx, bx)));
+    const float2 ia = make_float2(__fdividef(1.f, ra.x), __fdividef(1.f, ra.y));
+    const float2 ib = make_float2(__fdividef(1.f, rb.x), __fdividef(1.f, rb.y));
+    // -w of the plain law: (c_held V_rot + c_rot V_held) (-4) / r^6
+    float2 wa = __fmul2_rn(__ffma2_rn(CA, VR, __fmul2_rn(CR, VA)), __fmul2_rn(__fmul2_rn(ia, ia), ia));
+    float2 wb = __fmul2_rn(__ffma2_rn(CB, VR, __fmul2_rn(CR, VB)), __fmul2_rn(__fmul2_rn(ib, ib), ib));
+    if (__any_sync(0xffffffffu, fminf(fminf(ra.x, ra.y), fminf(rb.x, rb.y)) <= c2)) {
+      // rare: the rotating atoms' radii are read here, not staged
+      const float R0 = v.par[r0 + j].z, R1 = v.par[r0 + ((j + 1) & 31)].z;
+      wa.x *= chain_fac(k, ra.x, pa.z + R0);
+      wa.y *= chain_fac(k, ra.y, pa.z + R1);
+      wb.x *= chain_fac(k, rb.x, pb.z + R0);
+      wb.y *= chain_fac(k, rb.y, pb.z + R1);
+    }
+    FAX = __ffma2_rn(wa, ax, FAX); FAY = __ffma2_rn(wa, ay, FAY); FAZ = __ffma2_rn(wa, az, FAZ);
+    FBX = __ffma2_rn(wb, bx, FBX); FBY = __ffma2_rn(wb, by, FBY); FBZ = __ffma2_rn(wb, bz, FBZ);
+    FRX = __ffma2_rn(wa, ax, __ffma2_rn(wb, bx, FRX));
+    FRY = __ffma2_rn(wa, ay, __ffma2_rn(wb, by, FRY));
+    FRZ = __ffma2_rn(wa, az, __ffma2_rn(wb, bz, FRZ));
+    ROT2(FRX); ROT2(FRY); ROT2(FRZ);
+  }
+  const int lm = (lane + 31) & 31;
+  const float frx = FRX.x + __shfl_sync(0xffffffffu, FRX.y, lm);
+  const float fry = FRY.x + __shfl_sync(0xffffffffu, FRY.y, lm);
+  const float frz = FRZ.x + __shfl_sync(0xffffffffu, FRZ.y, lm);
+  flush_force(v, sa, PairAcc{FAX.x + FAX.y, FAY.x + FAY.y, FAZ.x + FAZ.y, 0.f});
+  flush_force(v, sb, PairAcc{FBX.x + FBX.y, FBY.x + FBY.y, FBZ.x + FBZ.y, 0.f});
+  flush_force(v, r0 + lane, PairAcc{-frx, -fry, -frz, 0.f});
+}
+
+__global__ void __launch_bounds__(kChainThreads, 7) k_gb_chain(const __grid_constant__ DevView v, const __grid_constant__ GBConst k, const float* chain) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int ni = *v.nitems;
@@ -1093,7 +1137,7 @@ int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset
   int nb = (c.nslots + 255) / 256;
   cudaMemsetAsync(c.d_gpol.p, 0, sizeof(long long) * c.nslots, st);
   cudaMemsetAsync(c.d_deda.p, 0, sizeof(long long) * c.nslots, st);
-  k_gb_born<<<g, 256, 0, st>>>(v, k, c.d_gpol.p);
+  k_gb_born<<<g, kBornThreads, 0, st>>>(v, k, c.d_gpol.p);
   k_gb_radii<<<nb, 256, 0, st>>>(v, c.d_gbT.p, c.d_gpol.p, halfeconv, born_offset, c.d_born_f.p, c.d_born_d.p);
   GBConst ke = k;
   if (c.gb_no_chain) ke.e64_r2 = 0.f;  // a gradient call's energy pass: FP32 pair energies
@@ -1113,7 +1157,7 @@ int launch_gb(Context& c, const GBConst& k, double halfeconv, double born_offset
   k_gb_self<<<nb, 256, 0, st>>>(v, c.d_charge.p, k, premul, c.d_deda.p, c.d_born_d.p, c.d_chain_f.p,
                                 energy ? 1 : 0);
   if (c.gb_no_chain) c.kernel_launches -= 1;
-  else k_gb_chain<<<2 * g, 128, 0, st>>>(v, k, c.d_chain_f.p);
+  else k_gb_chain<<<2 * g, kChainThreads, 0, st>>>(v, k, c.d_chain_f.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 
@@ -1122,9 +1166,9 @@ int launch_gb_stage(Context& c, const GBConst& k, int stage) {
   DevView v = c.view();
   int g = tile_grid(c);
   c.kernel_launches += 1;
-  if (stage == 1) k_gb_born<<<g, 256, 0, c.stream>>>(v, k, c.d_gpol.p);
+  if (stage == 1) k_gb_born<<<g, kBornThreads, 0, c.stream>>>(v, k, c.d_gpol.p);
   else if (stage == 2) k_gb_pair<<<2 * g, 128, 0, c.stream>>>(v, k, c.d_born_f.p, c.d_deda.p);
-  else k_gb_chain<<<2 * g, 128, 0, c.stream>>>(v, k, c.d_chain_f.p);
+  else k_gb_chain<<<2 * g, kChainThreads, 0, c.stream>>>(v, k, c.d_chain_f.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 
