@@ -20,6 +20,14 @@
 
 namespace pdgpu {
 
+// 1 / x by the special-function unit alone (rcp.approx.ftz, ~1 ulp): the pair
+// terms' reciprocals of r^2 (no multiply by the numerator 1 as __fdividef has)
+__device__ __forceinline__ float rcp_ftz(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // ---------------------------------------------------------------------------
 // pass 1: Born-radius pair sums  Gpol_i += P4 Vj CCF / r^4  (bond order > 2)
 // ---------------------------------------------------------------------------
@@ -51,7 +59,7 @@ __device__ __forceinline__ float born_w(const GBConst& k, float r2, float rs, bo
       ccf = h * h;
     }
   }
-  const float ir2 = __fdividef(1.f, r2);
+  const float ir2 = rcp_ftz(r2);
   return k.P4 * ccf * ir2 * ir2;
 }
 
@@ -116,7 +124,7 @@ __device__ __forceinline__ void born_tile2(const DevView& v, const GBConst& k, c
         ccf.y = h * h;
       }
     }
-    const float2 ir2 = make_float2(__fdividef(1.f, r2.x), __fdividef(1.f, r2.y));
+    const float2 ir2 = make_float2(rcp_ftz(r2.x), rcp_ftz(r2.y));
     float2 w = __fmul2_rn(__fmul2_rn(P4, ccf), __fmul2_rn(ir2, ir2));
     if (!FULL) {
       if (!still_in<false>(v, k, r2.x, sa, sr)) w.x = 0.f;
@@ -192,7 +200,7 @@ __device__ __forceinline__ void born_full2(const DevView& v, const GBConst& k, c
   __syncwarp();
   const float c2 = pair_contact2(k, make_float2(pa.z, pb.z), p0.z);
   float2 GA = f2(0.f), GB = f2(0.f), GR = f2(0.f);
-#pragma unroll 2
+#pragma unroll 4
   for (int kk = 0; kk < 32; kk += 2) {
     const int j = (lane + kk) & 31;
     const float4 P = rs[0][j], Q = rs[1][j];
@@ -202,8 +210,8 @@ __device__ __forceinline__ void born_full2(const DevView& v, const GBConst& k, c
     const float2 bx = __fadd2_rn(X, BX), by = __fadd2_rn(Y, BY), bz = __fadd2_rn(Z, BZ);
     const float2 ra = __ffma2_rn(az, az, __ffma2_rn(ay, ay, __fmul2_rn(ax, ax)));
     const float2 rb = __ffma2_rn(bz, bz, __ffma2_rn(by, by, __fmul2_rn(bx, bx)));
-    const float2 ia = make_float2(__fdividef(1.f, ra.x), __fdividef(1.f, ra.y));
-    const float2 ib = make_float2(__fdividef(1.f, rb.x), __fdividef(1.f, rb.y));
+    const float2 ia = make_float2(rcp_ftz(ra.x), rcp_ftz(ra.y));
+    const float2 ib = make_float2(rcp_ftz(rb.x), rcp_ftz(rb.y));
     float2 wa = __fmul2_rn(ia, ia), wb = __fmul2_rn(ib, ib);
     if (__any_sync(0xffffffffu, fminf(fminf(ra.x, ra.y), fminf(rb.x, rb.y)) <= c2)) {
       // rare: the rotating atoms' radii are read here, not staged
@@ -908,7 +916,7 @@ __device__ __forceinline__ float chain_w(const GBConst& k, float r2, float rs, f
       dccf = 2.f * h * sn * (x * 3.14159265358979f);
     }
   }
-  const float ir2 = __fdividef(1.f, r2);
+  const float ir2 = rcp_ftz(r2);
   return cv * (4.f * ccf - dccf) * ir2 * ir2 * ir2;
 }
 
@@ -981,7 +989,7 @@ __device__ __forceinline__ void chain_tile2(const DevView& v, const GBConst& k, 
         fac.y = 4.f * h * h - 2.f * h * sn * (x * 3.14159265358979f);
       }
     }
-    const float2 ir2 = make_float2(__fdividef(1.f, r2.x), __fdividef(1.f, r2.y));
+    const float2 ir2 = make_float2(rcp_ftz(r2.x), rcp_ftz(r2.y));
     const float2 cvv = __ffma2_rn(CS, f2(pr.w), __fmul2_rn(f2(cr), VS));
     float2 w = __fmul2_rn(__fmul2_rn(cvv, fac), __fmul2_rn(__fmul2_rn(ir2, ir2), ir2));
     if (!FULL) {
@@ -1058,8 +1066,8 @@ __device__ __forceinline__ void chain_full2(const DevView& v, const GBConst& k, 
     const float2 bx = __fadd2_rn(X, BX), by = __fadd2_rn(Y, BY), bz = __fadd2_rn(Z, BZ);
     const float2 ra = __ffma2_rn(az, az, __ffma2_rn(ay, ay, __fmul2_rn(ax, ax)));
     const float2 rb = __ffma2_rn(bz, bz, __ffma2_rn(by, by, __fmul2_rn(bx, bx)));
-    const float2 ia = make_float2(__fdividef(1.f, ra.x), __fdividef(1.f, ra.y));
-    const float2 ib = make_float2(__fdividef(1.f, rb.x), __fdividef(1.f, rb.y));
+    const float2 ia = make_float2(rcp_ftz(ra.x), rcp_ftz(ra.y));
+    const float2 ib = make_float2(rcp_ftz(rb.x), rcp_ftz(rb.y));
     // -w of the plain law: (c_held V_rot + c_rot V_held) (-4) / r^6
     float2 wa = __fmul2_rn(__ffma2_rn(CA, VR, __fmul2_rn(CR, VA)), __fmul2_rn(__fmul2_rn(ia, ia), ia));
     float2 wb = __fmul2_rn(__ffma2_rn(CB, VR, __fmul2_rn(CR, VB)), __fmul2_rn(__fmul2_rn(ib, ib), ib));
