@@ -1055,7 +1055,7 @@ __device__ __forceinline__ void chain_full2(const DevView& v, const GBConst& k, 
   }
   float2 FAX = f2(0.f), FAY = f2(0.f), FAZ = f2(0.f), FBX = f2(0.f), FBY = f2(0.f), FBZ = f2(0.f);
   float2 FRX = f2(0.f), FRY = f2(0.f), FRZ = f2(0.f);   // minus the rotating atoms' sums
-#pragma unroll 2
+#pragma unroll 1
   for (int kk = 0; kk < 32; kk += 2) {
     const int j = (lane + kk) & 31;
     const float4 P = rs[0][j], Q = rs[1][j];
