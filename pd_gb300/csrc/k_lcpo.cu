@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(256) k_lcpo_prep(DevView v, const float4* lc, 
 // candidate overlaps: heavy-atom pairs (use == 1) with r < r_i + r_j.  A tile
 // whose two block boxes lie farther apart than their largest radii can reach
 // holds none and is skipped (warp-uniform test; the margin covers rounding).
+// Candidates land in any order: k_lcpo_sort orders them by atom index.
 __global__ void __launch_bounds__(256) k_lcpo_cand(DevView v, const float4* lc, const float4* box, int* ncand,
                                                    int* cand) {
   const int lane = threadIdx.x & 31;
@@ -78,19 +79,31 @@ __global__ void __launch_bounds__(256) k_lcpo_cand(DevView v, const float4* lc, 
     const unsigned dmask = (T.flags & 2) ? diag_exclusion(lane) : 0u;
     const int si = T.bi * 32 + lane;
     const float4 li = lc[si];
-    int sj = T.bj * 32 + lane;
-    float4 lj = lc[sj];
+    float4 lj = lc[T.bj * 32 + lane];
+    // mi: the steps at which this lane's i atom has a candidate; mj: the i lanes
+    // the rotating j atom has (it rotates with the atom, so after 32 steps each
+    // lane holds its own j atom's mask).  One atomic per lane and side then
+    // reserves the candidates, instead of one per candidate.
+    unsigned mi = 0u, mj = 0u;
     for (int kk = 0; kk < 32; kk++) {
       float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
       float r2 = dx * dx + dy * dy + dz * dz;
       float rr = li.x + lj.x;
-      if (!((dmask >> kk) & 1u) && li.y > 0.f && lj.y > 0.f && r2 < rr * rr) {
-        int p = atomicAdd(&ncand[si], 1);
-        if (p < kLcpoCand) cand[(size_t)si * kLcpoCand + p] = sj;
-        p = atomicAdd(&ncand[sj], 1);
-        if (p < kLcpoCand) cand[(size_t)sj * kLcpoCand + p] = si;
-      }
-      ROT(xj.x); ROT(xj.y); ROT(xj.z); ROT(lj.x); ROT(lj.y); ROT(sj);
+      const bool c = !((dmask >> kk) & 1u) && li.y > 0.f && lj.y > 0.f && r2 < rr * rr;
+      mi |= (unsigned)c << kk;
+      mj |= (unsigned)c << lane;
+      ROT(xj.x); ROT(xj.y); ROT(xj.z); ROT(lj.x); ROT(lj.y); ROT(mj);
+    }
+    if (mi) {
+      int p = atomicAdd(&ncand[si], __popc(mi));
+      for (unsigned m = mi; m; m &= m - 1u, p++)
+        if (p < kLcpoCand) cand[(size_t)si * kLcpoCand + p] = T.bj * 32 + ((lane + __ffs(m) - 1) & 31);
+    }
+    if (mj) {
+      const int sj = T.bj * 32 + lane;
+      int p = atomicAdd(&ncand[sj], __popc(mj));
+      for (unsigned m = mj; m; m &= m - 1u, p++)
+        if (p < kLcpoCand) cand[(size_t)sj * kLcpoCand + p] = T.bi * 32 + (__ffs(m) - 1);
     }
   }
 }
