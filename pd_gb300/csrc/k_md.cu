@@ -73,6 +73,21 @@ __device__ __forceinline__ void add_ke(const MDView& m, int a, bool valid, const
   }
 }
 
+// The device step counter (kept on the device so captured graphs stay valid)
+// advances once per integration step: every block reads it at its start, and the
+// last block to finish (a count of finished blocks) increments it and resets the
+// count for the next launch.  Every thread of the block calls this.
+__device__ __forceinline__ void advance_step(const MDView& m) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(m.done, 1u) == gridDim.x - 1) {
+      *m.stepc += 1;
+      *m.done = 0u;
+    }
+  }
+}
+
 // PD velocity Verlet as written: half kick, (KE), half kick, drift t*(v+dv), kick
 __global__ void k_vv(MDView m, double dt) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -89,16 +104,18 @@ __global__ void k_vv(MDView m, double dt) {
     }
   }
   add_ke(m, a, valid, v);
-  if (!valid) return;
+  if (valid) {
 #pragma unroll
-  for (int c = 0; c < 3; c++) {
-    double dv = f[c] * tm;
-    v[c] += dv;
-    p[c] += dt * (v[c] + dv) * (1.0 / kAngstrom);
-    v[c] += dv;
-    m.vel[3 * a + c] = v[c];
-    m.pos[3 * a + c] = p[c];
+    for (int c = 0; c < 3; c++) {
+      double dv = f[c] * tm;
+      v[c] += dv;
+      p[c] += dt * (v[c] + dv) * (1.0 / kAngstrom);
+      v[c] += dv;
+      m.vel[3 * a + c] = v[c];
+      m.pos[3 * a + c] = p[c];
+    }
   }
+  advance_step(m);
 }
 
 // PD Langevin step (gamma*dt > 1e-5 branch) with per-system target temperature
@@ -123,8 +140,7 @@ __global__ void k_langevin(MDView m, LangevinCoeffs L, int first_step, int last_
     }
   }
   add_ke(m, a, valid, v);
-  if (!valid) return;
-  if (!last_step) {
+  if (valid && !last_step) {
     // sqrt(k_B T / m): the temperature's root in FP32 (it only scales the noise)
     const double s = (double)sqrtf((float)m.temp[m.atom_sys[a]]) * mt.y;
     const double sigmav = s * L.sv;
@@ -148,8 +164,11 @@ __global__ void k_langevin(MDView m, LangevinCoeffs L, int first_step, int last_
       v[c] = v[c] * L.c0 + dv;
     }
   }
+  if (valid) {
 #pragma unroll
-  for (int c = 0; c < 3; c++) m.vel[3 * a + c] = v[c];
+    for (int c = 0; c < 3; c++) m.vel[3 * a + c] = v[c];
+  }
+  advance_step(m);
 }
 
 // REMD: one thread walks the temperature ladder (remd.cpp:178-215, 349-356).
@@ -294,19 +313,13 @@ __global__ void k_zero_ll(long long* p, size_t n) {
   if (i < n) p[i] = 0;
 }
 
-// advance the device-side step counter (kept on the device so captured graphs stay valid)
-__global__ void k_advance(unsigned long long* stepc) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) *stepc += 1;
-}
-
 int launch_integrate(Context& c, MDState& md, bool first, bool last) {
-  c.kernel_launches += 2;
+  c.kernel_launches += 1;
   MDView m = md_view(c, md);
   int nb = (c.natom + 255) / 256;
   cudaMemsetAsync(md.d_ke.p, 0, sizeof(long long) * c.nsys, c.stream);
   if (md.p.Integrator == 0) k_vv<<<nb, 256, 0, c.stream>>>(m, md.p.Timestep);
   else k_langevin<<<nb, 256, 0, c.stream>>>(m, md.L, first ? 1 : 0, last ? 1 : 0);
-  k_advance<<<1, 32, 0, c.stream>>>(md.d_step.p);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
 

@@ -22,6 +22,7 @@ struct MDState {
   DBuf<double> d_vel;                 // [natom*3] m/s
   DBuf<double2> d_mterms;             // [natom] (1 / mass, sqrt(k_B / mass)), SI
   DBuf<unsigned long long> d_step;    // [1] device copy of the step counter
+  DBuf<unsigned> d_done;              // [1] integrator blocks finished in the running launch (0 between launches)
   DBuf<double> d_temp;                // [nsys] target temperature of each system (K)
   DBuf<double> d_ladder;              // [nsys] temperature of each rung (K)
   DBuf<int> d_temp_sys;               // [nsys] system holding each rung
@@ -60,7 +61,8 @@ struct MDView {
   const long long* facc_sa;   // may be null
   long long* ke;
   unsigned long long seed;
-  const unsigned long long* stepc;
+  unsigned long long* stepc;   // read by every block; the last block to finish advances it
+  unsigned* done;
 };
 
 inline MDView md_view(Context& c, MDState& md) {
@@ -78,6 +80,7 @@ inline MDView md_view(Context& c, MDState& md) {
   m.ke = md.d_ke.p;
   m.seed = md.p.seed;
   m.stepc = md.d_step.p;
+  m.done = md.d_done.p;
   return m;
 }
 

@@ -219,7 +219,7 @@ int pdgpu_md_setup(pdgpu_ctx* h, const pdgpu_md_params* p, const double* temps) 
       md.d_vscale.alloc(c.nsys) != cudaSuccess || md.d_accepted.alloc(c.nsys) != cudaSuccess ||
       md.d_ke.alloc(c.nsys) != cudaSuccess || md.d_ke_j.alloc(c.nsys) != cudaSuccess ||
       md.d_facc_sa.alloc(3 * (size_t)c.nslots) != cudaSuccess ||
-      md.d_surf_cache.alloc(c.nsys) != cudaSuccess || md.d_step.alloc(1) != cudaSuccess ||
+      md.d_surf_cache.alloc(c.nsys) != cudaSuccess || md.d_step.alloc(1) != cudaSuccess || md.d_done.alloc(1) != cudaSuccess ||
       md.d_mode.alloc(c.nsys) != cudaSuccess || md.d_copy_src.alloc(c.nsys) != cudaSuccess ||
       md.d_copy_scale.alloc(c.nsys) != cudaSuccess || md.d_bad.alloc(c.nsys) != cudaSuccess)
     return PDGPU_ERR_CUDA;
@@ -237,6 +237,7 @@ int pdgpu_md_setup(pdgpu_ctx* h, const pdgpu_md_params* p, const double* temps) 
   CK(cudaMemsetAsync(md.d_surf_cache.p, 0, sizeof(long long) * c.nsys, c.stream));
   CK(cudaMemsetAsync(md.d_ke.p, 0, sizeof(long long) * c.nsys, c.stream));
   CK(cudaMemsetAsync(md.d_step.p, 0, sizeof(unsigned long long), c.stream));
+  CK(cudaMemsetAsync(md.d_done.p, 0, sizeof(unsigned), c.stream));
   CK(cudaStreamSynchronize(c.stream));
   md.ready = true;
   return PDGPU_OK;
