@@ -155,17 +155,45 @@ __global__ void k_lcpo_sort(DevView v, const float4* lc, const float4* lpos, con
   if (lane == 0) nl_n[s] = keep;
 }
 
+// what one overlap partner j adds to atom i's SA and force, from the sums over
+// the atoms k overlapping both (lcpo.cpp:781-949): n2, a2t along d_ij, s_ji,
+// the k sums n3, n3b, n4b, Si3 (sum of s_jk), Si3ik; P x sigma weights folded in
+__device__ __forceinline__ void lcpo_j_terms(const float4& qi, const float4& qj, float pa2, float pa3, float pa4,
+                                             float Si2_t, float sji, const float n2[3], const float a2t[3],
+                                             const float n3[3], const float n3b[3], const float n4b[3], float Si3_t,
+                                             float Si3ik_t, float& sa, float fl[3]) {
+  // j's weights (P2, P3, P4) sigma_j on the n2, n3, n4 terms; i's P2 sigma_i and
+  // P4 sigma_i on the a2 terms (lcpo.cpp:900-949)
+  const float wa = qi.x + Si3_t * qi.z;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const float n4 = sji * n3[c] + n4b[c] + n2[c] * Si3ik_t;
+    const float n3t = n3[c] + n3b[c];
+    fl[c] += n2[c] * qj.x + n3t * qj.y + n4 * qj.z + a2t[c] * wa;
+  }
+  sa += pa2 * Si2_t + pa3 * Si3_t + pa4 * (Si3_t * Si2_t);
+}
+
 // per atom i (one warp, lanes over i's overlap partners j): SASA_i and the
 // derivative terms collected on atom i (lcpo.cpp:781-949).  Each lane sums its
 // partners' terms in FP32 (already folded with the P x sigma weights, so a lane
 // carries SA and the force only); the lanes combine in 64-bit fixed point.
-// Six CTAs of 256 per SM at 40 registers (four at 64 before): the pass is bound
-// by load latency, not issue, and the C4 batch's LCPO recalculation went from
-// 0.876 to 0.810 ms.
-__global__ void __launch_bounds__(256, 6) k_lcpo_main(DevView v, const float4* lc, const float4* lpos, const float4* psig,
-                                                   const int* nl_n, const int2* nl_e2, const float4* nl_ent,
-                                                   const double* P, const double* sigma, double* sasa_out,
-                                                   long long* facc_out, long long* esurf_out, int esurf_stride) {
+// The atoms k that overlap both i and j are i's own partners that j overlaps:
+// i's partners are staged once in the warp's shared-memory table with their
+// k-only terms (d_ik, the n3 / n3b weights along d_ik, the Si3ik term), and
+// every lane walks the same table (same length, broadcast reads), testing the
+// j-k overlap and recomputing s_jk from the positions.  Where j's own list
+// was cut at 80 partners, a k past j's 80th atom index is not j's partner.
+// An atom i whose own list was cut at 80 walks its partners' lists instead
+// (k need not be among i's first 80 partners there).
+// Six CTAs of 256 per SM at 40 registers: the pass is bound by load latency.
+constexpr int kLcpoWarps = 8;
+__global__ void __launch_bounds__(kLcpoWarps * 32, 6) k_lcpo_main(DevView v, const float4* lc, const float4* lpos,
+                                                   const float4* psig, const int* nl_n, const int2* nl_e2,
+                                                   const float4* nl_ent, const int* ncand, const double* P,
+                                                   const double* sigma, double* sasa_out, long long* facc_out,
+                                                   long long* esurf_out, int esurf_stride) {
+  __shared__ float4 tab_sh[kLcpoWarps][2][kLcpoMax];   // (d_ik, r_k), (w3, w3b, Si3ik term, atom_k)
   const int lane = threadIdx.x & 31;
   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (s >= v.nslots) return;
@@ -182,10 +210,32 @@ __global__ void __launch_bounds__(256, 6) k_lcpo_main(DevView v, const float4* l
   const float pa2 = (float)P[4 * a + 1], pa3 = (float)P[4 * a + 2], pa4 = (float)P[4 * a + 3];
   const float PI = 3.14159265358979f;
   const int n = nl_n[s];
+  const int2* rowi = nl_e2 + (size_t)s * kLcpoMax;
+  const float4* rowix = nl_ent + (size_t)s * kLcpoMax;
+  const bool cut_i = ncand[s] > kLcpoMax;
+  float4 (*T)[kLcpoMax] = tab_sh[threadIdx.x >> 5];
+  if (!cut_i) {
+    for (int t = lane; t < n; t += 32) {
+      const float4 xk = rowix[t];
+      const float rk = xk.w;
+      const float dx = xk.x - xi.x, dy = xk.y - xi.y, dz = xk.z - xi.z;
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      const float inv = rsqrtf(d2);
+      const float dk = d2 * inv;
+      const float rrk = (ri * ri - rk * rk) * inv * inv;
+      // a k that does not overlap i at these positions (the candidate test's
+      // rounding) is marked with the largest atom index and skipped
+      const int atom_k = ((ri + rk) * (ri + rk) < d2) ? 0x7fffffff : v.sorted_atom[rowi[t].x];
+      T[0][t] = make_float4(dx, dy, dz, rk);
+      T[1][t] = make_float4(PI * ri * (rrk - 1.f) * inv, PI * rk * (-rrk - 1.f) * inv,
+                            PI * ri * (2.f * ri - dk - dk * rrk), __int_as_float(atom_k));
+    }
+  }
+  __syncwarp();
   float sa = 0.f, fl[3] = {0.f, 0.f, 0.f};
   for (int jj = lane; jj < n; jj += 32) {
-    const int2 ej = nl_e2[(size_t)s * kLcpoMax + jj];
-    const float4 xj = nl_ent[(size_t)s * kLcpoMax + jj];
+    const int2 ej = rowi[jj];
+    const float4 xj = rowix[jj];
     const int sj = ej.x;
     const float Si2_t = __int_as_float(ej.y);
     const float4 qj = psig[sj];
@@ -203,40 +253,56 @@ __global__ void __launch_bounds__(256, 6) k_lcpo_main(DevView v, const float4* l
     float a2t[3] = {dAdd * ddd[0], dAdd * ddd[1], dAdd * ddd[2]};
     float n3[3] = {0, 0, 0}, n3b[3] = {0, 0, 0}, n4b[3] = {0, 0, 0};
     float Si3_t = 0.f, Si3ik_t = 0.f;
-    const int nk = nl_n[sj];
-    const int2* rowe = nl_e2 + (size_t)sj * kLcpoMax;
-    const float4* rowx = nl_ent + (size_t)sj * kLcpoMax;
-    for (int kk = 0; kk < nk; kk++) {
-      const int2 ek = rowe[kk];
-      if (ek.x == s) continue;
-      const float4 xk = rowx[kk];
-      const float rk = xk.w;
-      const float3 dik = make_float3(xk.x - xi.x, xk.y - xi.y, xk.z - xi.z);
-      float dik2 = dik.x * dik.x + dik.y * dik.y + dik.z * dik.z;
-      if ((ri + rk) * (ri + rk) < dik2) continue;
-      float invdik = rsqrtf(dik2);
-      float dk = dik2 * invdik;
-      float rrk = (ri * ri - rk * rk) * invdik * invdik;
-      float dA = PI * ri * (rrk - 1.f);
-      float u0 = dik.x * invdik, u1 = dik.y * invdik, u2 = dik.z * invdik;
-      float sjk = __int_as_float(ek.y);
-      n3[0] += dA * u0; n3[1] += dA * u1; n3[2] += dA * u2;
-      dA = PI * rk * (-rrk - 1.f);
-      Si3ik_t += PI * ri * (2.f * ri - dk - dk * rrk);
-      n3b[0] += dA * u0; n3b[1] += dA * u1; n3b[2] += dA * u2;
-      n4b[0] += sjk * dA * u0; n4b[1] += sjk * dA * u1; n4b[2] += sjk * dA * u2;
-      Si3_t += sjk;
+    if (!cut_i) {
+      // j's list cut at 80: its partners are the overlapping atoms up to its 80th atom index
+      const int cap_j = ncand[sj] > kLcpoMax ? v.sorted_atom[nl_e2[(size_t)sj * kLcpoMax + kLcpoMax - 1].x]
+                                             : 0x7ffffffe;
+      const float rj2 = rj * rj;
+      for (int t = 0; t < n; t++) {
+        const float4 K = T[0][t];
+        const float ex = K.x - dij.x, ey = K.y - dij.y, ez = K.z - dij.z;   // k - j
+        const float d2 = ex * ex + ey * ey + ez * ez;
+        const float rjk = rj + K.w;
+        if (t == jj || !(d2 < rjk * rjk)) continue;
+        const float4 W = T[1][t];
+        if (__float_as_int(W.w) > cap_j) continue;
+        const float inv = rsqrtf(d2);
+        // overlap of j's sphere by k: 2 pi rj (rj - d/2 - (rj^2 - rk^2)/(2d))  (lcpo.cpp:731-733)
+        const float sjk = 6.283185307179586f * rj * (rj - 0.5f * d2 * inv - 0.5f * (rj2 - K.w * K.w) * inv);
+        const float w4 = sjk * W.y;
+        n3[0] += W.x * K.x; n3[1] += W.x * K.y; n3[2] += W.x * K.z;
+        n3b[0] += W.y * K.x; n3b[1] += W.y * K.y; n3b[2] += W.y * K.z;
+        n4b[0] += w4 * K.x; n4b[1] += w4 * K.y; n4b[2] += w4 * K.z;
+        Si3_t += sjk;
+        Si3ik_t += W.z;
+      }
+    } else {
+      const int nk = nl_n[sj];
+      const int2* rowe = nl_e2 + (size_t)sj * kLcpoMax;
+      const float4* rowx = nl_ent + (size_t)sj * kLcpoMax;
+      for (int kk = 0; kk < nk; kk++) {
+        const int2 ek = rowe[kk];
+        if (ek.x == s) continue;
+        const float4 xk = rowx[kk];
+        const float rk = xk.w;
+        const float3 dik = make_float3(xk.x - xi.x, xk.y - xi.y, xk.z - xi.z);
+        float dik2 = dik.x * dik.x + dik.y * dik.y + dik.z * dik.z;
+        if ((ri + rk) * (ri + rk) < dik2) continue;
+        float invdik = rsqrtf(dik2);
+        float dk = dik2 * invdik;
+        float rrk = (ri * ri - rk * rk) * invdik * invdik;
+        float dA = PI * ri * (rrk - 1.f);
+        float u0 = dik.x * invdik, u1 = dik.y * invdik, u2 = dik.z * invdik;
+        float sjk = __int_as_float(ek.y);
+        n3[0] += dA * u0; n3[1] += dA * u1; n3[2] += dA * u2;
+        dA = PI * rk * (-rrk - 1.f);
+        Si3ik_t += PI * ri * (2.f * ri - dk - dk * rrk);
+        n3b[0] += dA * u0; n3b[1] += dA * u1; n3b[2] += dA * u2;
+        n4b[0] += sjk * dA * u0; n4b[1] += sjk * dA * u1; n4b[2] += sjk * dA * u2;
+        Si3_t += sjk;
+      }
     }
-    // j's weights (P2, P3, P4) sigma_j on the n2, n3, n4 terms; i's P2 sigma_i and
-    // P4 sigma_i on the a2 terms (lcpo.cpp:900-949)
-    const float wa = qi.x + Si3_t * qi.z;
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const float n4 = sji * n3[c] + n4b[c] + n2[c] * Si3ik_t;
-      const float n3t = n3[c] + n3b[c];
-      fl[c] += n2[c] * qj.x + n3t * qj.y + n4 * qj.z + a2t[c] * wa;
-    }
-    sa += pa2 * Si2_t + pa3 * Si3_t + pa4 * (Si3_t * Si2_t);
+    lcpo_j_terms(qi, qj, pa2, pa3, pa4, Si2_t, sji, n2, a2t, n3, n3b, n4b, Si3_t, Si3ik_t, sa, fl);
   }
   // the lanes combine in 64-bit fixed point (2^32 per unit, exact integer sums;
   // the force scale is the accumulators' own)
@@ -272,8 +338,8 @@ int launch_lcpo(Context& c, long long* facc_out, long long* esurf_out, int esurf
   int nw = (int)(((long long)c.nslots * 32 + 255) / 256);
   k_lcpo_sort<<<nw, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_pos.p, c.d_lc_ncand.p, c.d_lc_cand.p, c.d_lc_n.p,
                                    c.d_lc_e2.p, c.d_lc_ent.p);
-  k_lcpo_main<<<nw, 256, 0, st>>>(v, c.d_lc_par.p, c.d_lc_pos.p, c.d_lc_psig.p, c.d_lc_n.p, c.d_lc_e2.p,
-                                   c.d_lc_ent.p, c.d_lcpoP.p, c.d_lcpoSig.p, c.d_sasa.p, facc_out, esurf_out,
+  k_lcpo_main<<<(int)(((long long)c.nslots * 32 + kLcpoWarps * 32 - 1) / (kLcpoWarps * 32)), kLcpoWarps * 32, 0, st>>>(
+      v, c.d_lc_par.p, c.d_lc_pos.p, c.d_lc_psig.p, c.d_lc_n.p, c.d_lc_e2.p, c.d_lc_ent.p, c.d_lc_ncand.p, c.d_lcpoP.p, c.d_lcpoSig.p, c.d_sasa.p, facc_out, esurf_out,
                                    esurf_stride);
   return cudaGetLastError() == cudaSuccess ? PDGPU_OK : PDGPU_ERR_CUDA;
 }
