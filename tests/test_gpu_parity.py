@@ -172,6 +172,64 @@ def test_lcpo_matches_pd(goldens, name):
     assert rel_rms(f, d["sasa_f"]) <= F_TOL
 
 
+def _dense_lcpo_lattice(a=2.1, r=3.1, seed=4, n=10, gap=2e-3):
+    """A jittered 10^3 lattice, 2.1 A apart, of atoms with LCPO radius 3.1 A:
+    407 atoms overlap more than 80 others (up to 105; none beyond the 160
+    candidates kept), so both an atom's own list and its partners' lists are
+    cut at 80 as PD cuts them (lcpo.h:24).  Atoms are moved until no pair lies
+    within `gap` of the overlap distance, where FP32 and FP64 could decide a
+    pair differently."""
+    from scipy.spatial import cKDTree
+    rng = np.random.default_rng(seed)
+    g = np.arange(n)
+    pos = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3) * a
+    pos = pos + rng.uniform(-0.15, 0.15, pos.shape)
+    for _ in range(50):
+        p = cKDTree(pos).query_pairs(2 * r + gap, output_type="ndarray")
+        d = np.linalg.norm(pos[p[:, 0]] - pos[p[:, 1]], axis=1)
+        bad = np.unique(p[np.abs(d - 2 * r) < gap][:, 1])
+        if len(bad) == 0:
+            return pos
+        pos[bad] += rng.uniform(-0.15, 0.15, (len(bad), 3))
+    raise RuntimeError("no lattice without near-boundary pairs")
+
+
+def test_lcpo_cut_lists_match_oracle():
+    """LCPO where lists are cut at 80 partners (PD's first 80 by atom index):
+    the device against the oracle's FP64 restatement of lcpo.cpp on the same
+    positions.  P2-P4 are positive here so no atom's SA is clamped at zero; a k
+    counted past a cut list would move SA by ~1e-2 of it.  Tolerances: SA and
+    the energy are sums of positive FP32 terms (1e-4 of the largest SA, 1e-5
+    of the energy); the forces of the dense lattice are small differences of
+    ~1e4 FP32 terms per atom (force relative RMS 1e-3)."""
+    pytest.importorskip("scipy")
+    from oracle import pdoracle as O
+    from pd_gb300 import ffi
+    from pd_gb300.engine import DeviceContext
+    from pd_gb300.workspace import SystemImage
+    pos = _dense_lcpo_lattice()
+    n = len(pos)
+    P = np.array([0.5, 1e-3, 1e-3, 1e-5])
+    sigma = 3.47e-23
+    kw = dict(lcpo_radius=np.full(n, 3.1), lcpo_p=np.tile(P, (n, 1)), lcpo_sigma=np.full(n, sigma),
+              lcpo_use=np.ones(n, np.int32))
+    im = SystemImage([n], np.zeros(3), np.zeros(n), np.full(n, 1.5), np.zeros(n), np.full(n, 2e-26),
+                     np.zeros((0, 3), np.int32), pos=pos, **kw)
+    ctx = DeviceContext(im)
+    ctx.set_list(2.0)
+    ctx.set_positions(pos)
+    f = np.zeros((n, 3))
+    e = ctx.compute(ffi.SA, f)[0]
+    sa = ctx.sasa()
+    ctx.close()
+    s = O.OracleSystem(pos, np.zeros(n), np.full(n, 1.5), np.zeros(n), np.zeros((0, 3), np.int32))
+    ref_e, ref_f, ref_sa = O.lcpo_forces(s, 2 * 3.1 + 2.0, np.full(n, 3.1), np.tile(P, (n, 1)), np.full(n, sigma),
+                                         np.ones(n, np.int32))
+    assert np.max(np.abs(sa - ref_sa)) <= 1e-4 * np.max(ref_sa)
+    assert rel_err(e["surf"], ref_e[6]) <= 1e-5
+    assert rel_rms(f, ref_f) <= 1e-3
+
+
 @pytest.mark.parametrize("name", ["water_c1", "peptide30", "peptide120"])
 def test_bonded_matches_pd(goldens, name):
     from pd_gb300 import ffi
