@@ -162,3 +162,26 @@ def test_oracle_matches_pd_on_the_gb_workloads(name):
     assert rel_err(e[6], ref_energy(d, "sasa", "surf")) < 1e-12
     assert np.max(np.abs(sa - d["lcpo_sasa"])) <= 1e-4
     assert rel_rms(f, d["sasa_f"]) < 1e-7
+
+
+def test_dense_lcpo_lattice_cuts_lists_and_the_cut_matters():
+    """The premise of the device test of cut LCPO lists (test_gpu_parity.py::
+    test_lcpo_cut_lists_match_oracle): atoms beyond PD's 80 partners and none
+    beyond the 160 candidates, no pair near the overlap distance, and the
+    triple terms (the sums the cut decides) a large share of each SA."""
+    pytest.importorskip("scipy")
+    from scipy.spatial import cKDTree
+    from test_gpu_parity import _dense_lcpo_lattice
+    pos = _dense_lcpo_lattice()
+    n = len(pos)
+    p = cKDTree(pos).query_pairs(2 * 3.1, output_type="ndarray")
+    count = np.bincount(p.ravel(), minlength=n)
+    assert (count > 80).sum() > 300 and count.max() <= 160
+    q = cKDTree(pos).query_pairs(2 * 3.1 + 2e-3, output_type="ndarray")
+    d = np.linalg.norm(pos[q[:, 0]] - pos[q[:, 1]], axis=1)
+    assert np.min(np.abs(d - 2 * 3.1)) >= 2e-3
+    s = O.OracleSystem(pos, np.zeros(n), np.full(n, 1.5), np.zeros(n), np.zeros((0, 3), np.int32))
+    radius, sigma, use = np.full(n, 3.1), np.full(n, 3.47e-23), np.ones(n, np.int32)
+    _, _, sa = O.lcpo_forces(s, 8.2, radius, np.tile([0.5, 1e-3, 1e-3, 1e-5], (n, 1)), sigma, use)
+    _, _, sa_pairs = O.lcpo_forces(s, 8.2, radius, np.tile([0.5, 1e-3, 0.0, 0.0], (n, 1)), sigma, use)
+    assert np.all(sa > 0) and np.mean(sa - sa_pairs) > 0.3 * np.mean(sa)
